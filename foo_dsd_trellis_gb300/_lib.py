@@ -1,0 +1,101 @@
+"""ctypes binding of libdsdgpu.so (include/dsdgpu.h).
+
+The library is built in-tree by foo_dsd_trellis_gb300/build.py.  Loading fails
+loudly when it is missing: there is no CPU fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libdsdgpu.so")
+
+OK = 0
+ERR_ARG = -1
+ERR_CUDA = -2
+ERR_NOMEM = -3
+ERR_STATE = -4
+ERR_DEVICE = -5
+ERR_UNSUPPORTED = -6
+
+_ERR_NAMES = {ERR_ARG: "ERR_ARG", ERR_CUDA: "ERR_CUDA", ERR_NOMEM: "ERR_NOMEM",
+              ERR_STATE: "ERR_STATE", ERR_DEVICE: "ERR_DEVICE",
+              ERR_UNSUPPORTED: "ERR_UNSUPPORTED"}
+
+
+class DsdGpuError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{_ERR_NAMES.get(code, code)}: {message}")
+        self.code = code
+
+
+class SdmParams(C.Structure):
+    _fields_ = [("order", C.c_int), ("a", C.c_double * 10), ("g", C.c_double * 10),
+                ("depth", C.c_int), ("cands", C.c_int), ("lat", C.c_int),
+                ("state_limit", C.c_double)]
+
+
+class Segment(C.Structure):
+    _fields_ = [("d_in", C.c_void_p), ("d_out", C.c_void_p), ("count", C.c_int64),
+                ("discard", C.c_int64), ("channel", C.c_int), ("seed_from", C.c_int),
+                ("d_seed_state", C.c_void_p), ("out_count", C.c_int64)]
+
+
+class FirParams(C.Structure):
+    _fields_ = [("fs_in", C.c_uint), ("fs_out", C.c_uint), ("boxcar_taps", C.c_int),
+                ("soft_clip", C.c_int), ("gain_start", C.c_double), ("gain_end", C.c_double)]
+
+
+class DasParams(C.Structure):
+    _fields_ = [("seg_len", C.c_int64), ("nsegs", C.c_int), ("seed_mode", C.c_int),
+                ("reposition", C.c_int), ("fs_out", C.c_uint)]
+
+
+_vp = C.c_void_p
+_sz = C.c_size_t
+_szp = C.POINTER(C.c_size_t)
+
+# name -> (restype, argtypes); the exported surface of include/dsdgpu.h
+SIGNATURES = {
+    "dsdgpu_create": (C.c_int, [C.c_int, C.POINTER(_vp)]),
+    "dsdgpu_destroy": (None, [_vp]),
+    "dsdgpu_last_error": (C.c_char_p, [_vp]),
+    "dsdgpu_synchronize": (C.c_int, [_vp]),
+    "dsdgpu_sdm_setup": (C.c_int, [_vp, C.POINTER(SdmParams), C.c_int]),
+    "dsdgpu_sdm_reset": (C.c_int, [_vp, C.c_int]),
+    "dsdgpu_sdm_process": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp, _sz, _szp]),
+    "dsdgpu_sdm_process_host": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _vp, _szp]),
+    "dsdgpu_sdm_drain": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _szp]),
+    "dsdgpu_sdm_copy_state": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "dsdgpu_sdm_segments": (C.c_int, [_vp, C.POINTER(Segment), C.c_int]),
+    "dsdgpu_sdm_query": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_double),
+                                   C.POINTER(C.c_uint64)]),
+}
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Load libdsdgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run __graft_entry__.build() first "
+                           "(there is no CPU fallback)")
+    lib = C.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(ctx, rc: int) -> None:
+    if rc != OK:
+        msg = load().dsdgpu_last_error(ctx) if ctx else b""
+        raise DsdGpuError(rc, (msg or b"").decode(errors="replace"))

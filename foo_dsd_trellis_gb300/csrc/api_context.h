@@ -1,0 +1,52 @@
+// The opaque dsdgpu_context of include/dsdgpu.h, shared by the host-side
+// translation units of libdsdgpu.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/dsdgpu.h"
+#include "sdm_internal.h"
+
+struct dsdgpu_context {
+  int device = 0;
+  int num_sms = 0;
+  int max_blocks = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+
+  int* d_counter = nullptr;   // persistent-kernel job counter
+  int* d_status = nullptr;    // device status word (bounded walks/waits)
+
+  // trellis SDM
+  bool sdm_ready = false;
+  dsdgpu::SdmParams sdm{};
+  int nctx = 0;
+  dsdgpu::SdmCtx* d_ctx = nullptr;
+  std::vector<int64_t> pending;   // latency fill per context (host mirror)
+  std::vector<int> draining;
+  dsdgpu::SdmJob* d_jobs = nullptr;
+  int jobs_cap = 0;
+
+  // reusable device scratch for the host-buffer entry points
+  void* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+
+  int fail(int code, const char* what);
+  int cuda_fail(cudaError_t e, const char* what);
+  int ensure_scratch(size_t bytes);
+  int check_status();
+  int run_jobs(const std::vector<dsdgpu::SdmJob>& jobs);
+  void plan_steps(int64_t pend, int64_t count, int64_t discard, int64_t* skip, int64_t* out,
+                  int64_t* new_pend) const;
+  void release_all() {
+    if (d_ctx) cudaFree(d_ctx);
+    if (d_jobs) cudaFree(d_jobs);
+    if (d_scratch) cudaFree(d_scratch);
+    d_ctx = nullptr;
+    d_jobs = nullptr;
+    d_scratch = nullptr;
+  }
+};

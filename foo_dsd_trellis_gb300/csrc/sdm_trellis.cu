@@ -1,0 +1,418 @@
+// Trellis (Viterbi look-ahead) 1-bit sigma-delta modulator for sm_103a.
+//
+// One warp runs one SDM job (a channel block or a DAS segment); a persistent
+// grid pulls jobs from an atomic counter, so one launch covers any mix of
+// channels, segments and streams.  Lane i owns the candidate at rank i
+// (K <= 32): its NTF state, cost, path, traceback bit and a lat-bit traceback
+// ring live in registers.  Each input sample:
+//
+//   1. expansion   every live lane advances its NTF (FP64, reference order,
+//                  no contraction: __dadd_rn/__dmul_rn) and forms both
+//                  children: slots 2i (bit 0, state[0] + 1) and 2i + 1
+//                  (bit 1, state[0] - 1)          (reference src/trellis.c:37-191)
+//   2. selection   warp argmin over the 2n children by int64 cost bits,
+//                  majority vote on the traceback bit with the 1.1x override,
+//                  then the reference's ordered insertion with path-hash
+//                  dedup, emulated warp-cooperatively: the sorted act list is
+//                  held one entry per lane and every insertion is a ballot +
+//                  shuffle; the hash chains are walked in shared memory
+//                                                  (src/trellis.c:582-731)
+//   3. commit      survivors pull their parent's state, path, traceback bit
+//                  and ring with shuffles, normalise cost by the new minimum
+//                  and write their decision bit into the ring
+//                                                  (src/trellis.c:938-972)
+//
+// The shared-memory slot arrays (path, cost bits, chain link for both banks)
+// reproduce the reference's slot memory, including the K = 32 store one past
+// act[] that lands on path_hash[0] while bank 1 is sorted (src/trellis.c:668-673).
+#include "sdm_internal.h"
+
+#include <climits>
+
+namespace dsdgpu {
+
+constexpr int kWarpsPerBlock = 4;
+constexpr int kRegRingWords = 8;      // rings held in registers: lat <= 256
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ long long key_of(double c) { return __double_as_longlong(c); }
+
+__device__ __forceinline__ double clampd(double v, double lim) {
+  if (v > lim) return lim;
+  if (v < -lim) return -lim;
+  return v;
+}
+
+__device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int src) {
+  return (unsigned long long)__shfl_sync(kFull, (long long)v, src);
+}
+
+// NTF advance with y = 0 (src/trellis.c:104-118 for order 7; every order has
+// the same shape): d[0] = (s0 - g0 s1) + x; d[i] = (s[i] + s[i-1]) - g[i] s[i+1];
+// d[N-1] = s[N-1] + s[N-2]; v = ((x + a0 d0) + a1 d1) + ...
+template <int N>
+__device__ __forceinline__ double ntf_advance(const SdmParams& P, const double (&s)[N],
+                                              double (&d)[N], double x) {
+  d[0] = __dadd_rn(__dsub_rn(s[0], __dmul_rn(P.g[0], s[1])), x);
+  double v = __dadd_rn(x, __dmul_rn(P.a[0], d[0]));
+#pragma unroll
+  for (int i = 1; i < N - 1; i++) {
+    d[i] = __dsub_rn(__dadd_rn(s[i], s[i - 1]), __dmul_rn(P.g[i], s[i + 1]));
+    v = __dadd_rn(v, __dmul_rn(P.a[i], d[i]));
+  }
+  d[N - 1] = __dadd_rn(s[N - 1], s[N - 2]);
+  v = __dadd_rn(v, __dmul_rn(P.a[N - 1], d[N - 1]));
+  return v;
+}
+
+struct WarpSmem {
+  unsigned long long path[2][kSlots];
+  long long key[2][kSlots];
+  int8_t link[2][kSlots];
+  int8_t heads[kBuckets];
+};
+
+template <int N>
+__device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restrict__ ctxs,
+                        WarpSmem& sm, int* __restrict__ status) {
+  const int lane = threadIdx.x & 31;
+  const SdmCtx* src = &ctxs[job.copy_from >= 0 ? job.copy_from : job.ctx];
+  SdmCtx* dst = &ctxs[job.ctx];
+  const int K = P.cands;
+  const int W = (P.lat + 31) >> 5;
+  const unsigned long long mask = P.mask;
+
+  int n = src->n, bank = src->bank, pos = src->pos;
+  double s[N];
+  double cost = 0.0;
+  unsigned long long path = 0;
+  uint32_t ring[kRegRingWords];
+  int nxt = 0, slot = 0;
+#pragma unroll
+  for (int k = 0; k < N; k++) s[k] = 0.0;
+#pragma unroll
+  for (int w = 0; w < kRegRingWords; w++) ring[w] = 0;
+  if (lane < n) {
+#pragma unroll
+    for (int k = 0; k < N; k++) s[k] = src->s[lane][k];
+    cost = src->cost[lane];
+    path = src->path[lane];
+    nxt = src->next[lane];
+    slot = src->slot[lane];
+#pragma unroll
+    for (int w = 0; w < kRegRingWords; w++)
+      if (w < W) ring[w] = src->ring[lane][w];
+  }
+  for (int i = lane; i < 2 * kSlots; i += 32) {
+    const int b = i / kSlots, j = i % kSlots;
+    sm.path[b][j] = src->spath[b][j];
+    sm.key[b][j] = (long long)src->skey[b][j];
+    sm.link[b][j] = src->slink[b][j];
+  }
+  unsigned long long c_conv = 0, c_coll = 0, c_drop = 0, c_tot = 0;
+  if (job.copy_from < 0) {
+    c_conv = src->conv_fail;
+    c_coll = src->cands_collapse;
+    c_drop = src->next_filter_drops;
+    c_tot = src->total_children;
+  }
+  __syncwarp();
+  if (job.seed_state) {
+    // DAS temp seeding: every live candidate gets the estimated state, cost 0.
+    if (lane < n) {
+#pragma unroll
+      for (int k = 0; k < N; k++) s[k] = job.seed_state[k];
+      cost = 0.0;
+      sm.key[bank][slot] = key_of(0.0);
+    }
+    __syncwarp();
+  }
+
+  const long long n_in = job.n_in;
+  const double* __restrict__ in = job.in;
+  double x_cur = 0.0, x_nxt = 0.0;
+  if (in) {
+    if (lane < n_in) x_cur = in[lane];
+    if (32 + lane < n_in) x_nxt = in[32 + lane];
+  }
+  uint8_t obit = 0;
+  int err = 0;
+
+  for (long long t = 0; t < n_in; t++) {
+    const int tl = (int)(t & 31);
+    if (tl == 0 && t > 0) {
+      x_cur = x_nxt;
+      x_nxt = (in && t + 32 + lane < n_in) ? in[t + 32 + lane] : 0.0;
+    }
+    const double x = __shfl_sync(kFull, x_cur, tl);
+    const int nb = bank ^ 1;
+    int next_pos = pos + 1;
+    if (next_pos == P.lat) next_pos = 0;
+    const bool live = lane < n;
+
+    // ---- 1. expansion ----
+    double d[N];
+#pragma unroll
+    for (int k = 0; k < N; k++) d[k] = 0.0;
+    double s00 = 0.0, s01 = 0.0;
+    long long key0 = LLONG_MAX, key1 = LLONG_MAX;
+    unsigned long long q = 0;
+    int new_next = 0;
+    const int old_next = nxt;
+    if (live) {
+      const double v = ntf_advance<N>(P, s, d, x);
+      s00 = __dadd_rn(d[0], 1.0);
+      s01 = __dsub_rn(d[0], 1.0);
+      if (P.state_limit > 0.0) {
+#pragma unroll
+        for (int k = 1; k < N; k++) d[k] = clampd(d[k], P.state_limit);
+        s00 = clampd(s00, P.state_limit);
+        s01 = clampd(s01, P.state_limit);
+      }
+      const double e0 = __dadd_rn(v, P.a[0]);
+      const double e1 = __dsub_rn(v, P.a[0]);
+      key0 = key_of(__dadd_rn(cost, __dmul_rn(e0, e0)));
+      key1 = key_of(__dadd_rn(cost, __dmul_rn(e1, e1)));
+      q = (path << 1) & mask;
+      uint32_t wv = 0;
+#pragma unroll
+      for (int w = 0; w < kRegRingWords; w++)
+        if (w == (next_pos >> 5)) wv = ring[w];
+      new_next = (int)((wv >> (next_pos & 31)) & 1u);
+      sm.path[nb][2 * lane] = q;
+      sm.path[nb][2 * lane + 1] = q | 1ull;
+      sm.key[nb][2 * lane] = key0;
+      sm.key[nb][2 * lane + 1] = key1;
+      sm.heads[q & (kBuckets - 1)] = -1;
+      sm.heads[(q | 1ull) & (kBuckets - 1)] = -1;
+    }
+    __syncwarp();
+
+    // ---- 2. selection ----
+    long long mk = key0;
+    int mi = 2 * lane;
+    if (key1 < key0) { mk = key1; mi = 2 * lane + 1; }
+    if (!live) mi = 1 << 20;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const long long ok = __shfl_xor_sync(kFull, mk, off);
+      const int oi = __shfl_xor_sync(kFull, mi, off);
+      if (ok < mk || (ok == mk && oi < mi)) { mk = ok; mi = oi; }
+    }
+    const unsigned nx1 = __ballot_sync(kFull, live && old_next);
+    const int votes1 = 2 * __popc(nx1);
+    const int majority = (votes1 > 2 * n - votes1) ? 1 : 0;
+    const int min_next = __shfl_sync(kFull, old_next, mi >> 1);
+    if (min_next != majority) {
+      const bool cand = live && old_next == majority;
+      long long bk = key0;
+      int bi = 2 * lane;
+      if (key1 < key0) { bk = key1; bi = 2 * lane + 1; }
+      if (!cand) { bk = LLONG_MAX; bi = 1 << 20; }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const long long ok = __shfl_xor_sync(kFull, bk, off);
+        const int oi = __shfl_xor_sync(kFull, bi, off);
+        if (ok < bk || (ok == bk && oi < bi)) { bk = ok; bi = oi; }
+      }
+      if (bi < (1 << 20)) {
+        const double cmin = __longlong_as_double(mk);
+        const double cbm = __longlong_as_double(bk);
+        if (cbm < __dmul_rn(cmin, 1.1)) { mk = bk; mi = bi; }
+      }
+    }
+    const int want = __shfl_sync(kFull, old_next, mi >> 1);
+    unsigned elig = __ballot_sync(kFull, live && old_next == want);
+    c_drop += 2ull * (unsigned)(n - __popc(elig));
+    c_tot += 2ull * (unsigned)n;
+
+    int cnt = 0;
+    long long Lk = LLONG_MAX;
+    int Ls = -1;
+    long long worst = LLONG_MAX;
+    while (elig) {
+      const int p = __ffs(elig) - 1;
+      elig &= elig - 1;
+      const unsigned long long qp = shfl64(q, p);
+      const long long kp0 = __shfl_sync(kFull, key0, p);
+      const long long kp1 = __shfl_sync(kFull, key1, p);
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int c = 2 * p + h;
+        const long long sk = h ? kp1 : kp0;
+        const unsigned long long sp = h ? (qp | 1ull) : qp;
+        if (cnt == K && worst <= sk) continue;
+        const int b = (int)(sp & (kBuckets - 1));
+        int t = sm.heads[b];
+        int hops = 0;
+        while (t >= 0) {
+          if (sm.path[nb][t] == sp) break;
+          t = sm.link[nb][t];
+          if (++hops > 4 * kSlots) { err = kStatusChainLimit; t = -1; break; }
+        }
+        bool do_insert;
+        bool removed = false;
+        if (t < 0) {
+          __syncwarp();
+          if (lane == 0) {
+            sm.link[nb][c] = sm.heads[b];
+            sm.heads[b] = (int8_t)c;
+          }
+          __syncwarp();
+          if (cnt == K && K == kMaxCands && nb == 1) {
+            // the store to act[32] hits path_hash[0] in the reference layout
+            const int ev = __shfl_sync(kFull, Ls, K - 1);
+            if (lane == 0) sm.heads[0] = (int8_t)ev;
+            __syncwarp();
+          }
+          do_insert = true;
+        } else {
+          const long long tk = sm.key[nb][t];
+          if (tk <= sk) continue;
+          const unsigned tm = __ballot_sync(kFull, lane < cnt && Ls == t);
+          if (tm) {
+            const int tp = __ffs(tm) - 1;
+            const long long dk = __shfl_down_sync(kFull, Lk, 1);
+            const int ds = __shfl_down_sync(kFull, Ls, 1);
+            if (lane >= tp && lane < cnt - 1) { Lk = dk; Ls = ds; }
+            cnt--;
+            removed = true;
+          }
+          do_insert = true;
+        }
+        if (do_insert) {
+          const int ip = __popc(__ballot_sync(kFull, lane < cnt && Lk <= sk));
+          const long long uk = __shfl_up_sync(kFull, Lk, 1);
+          const int us = __shfl_up_sync(kFull, Ls, 1);
+          if (lane > ip) { Lk = uk; Ls = us; }
+          if (lane == ip) { Lk = sk; Ls = c; }
+          if (removed || cnt < K) cnt++;
+          worst = __shfl_sync(kFull, Lk, cnt - 1);
+        }
+      }
+    }
+
+    // ---- 3. commit ----
+    const int n_old = n;
+    const int n_new = cnt;
+    const double min_cost = __longlong_as_double(__shfl_sync(kFull, Lk, 0));
+    const bool surv = lane < n_new;
+    const int pp = surv ? (Ls >> 1) : lane;
+    const int hh = surv ? (Ls & 1) : 0;
+    const double f00 = __shfl_sync(kFull, s00, pp);
+    const double f01 = __shfl_sync(kFull, s01, pp);
+    double ns[N];
+    ns[0] = hh ? f01 : f00;
+#pragma unroll
+    for (int k = 1; k < N; k++) ns[k] = __shfl_sync(kFull, d[k], pp);
+    const unsigned long long npath = shfl64(q, pp) | (unsigned long long)hh;
+    const int nnext = __shfl_sync(kFull, new_next, pp);
+    uint32_t nring[kRegRingWords];
+#pragma unroll
+    for (int w = 0; w < kRegRingWords; w++)
+      nring[w] = (w < W) ? __shfl_sync(kFull, ring[w], pp) : 0u;
+    if (surv) {
+#pragma unroll
+      for (int k = 0; k < N; k++) s[k] = ns[k];
+      cost = __dsub_rn(__longlong_as_double(Lk), min_cost);
+      path = npath;
+      nxt = nnext;
+      slot = Ls;
+#pragma unroll
+      for (int w = 0; w < kRegRingWords; w++) {
+        uint32_t v = nring[w];
+        if (w == (pos >> 5)) v = (v & ~(1u << (pos & 31))) | ((uint32_t)hh << (pos & 31));
+        ring[w] = v;
+      }
+      sm.key[nb][Ls] = key_of(cost);
+    }
+    __syncwarp();
+    if (n_new < n_old) { c_conv++; c_coll++; }
+    n = n_new;
+    bank = nb;
+    pos = next_pos;
+
+    // ---- output ----
+    if (t >= job.skip_out) {
+      const long long o = t - job.skip_out;
+      const int ol = (int)(o & 31);
+      if (lane == ol) obit = (uint8_t)want;
+      if (ol == 31 || t == n_in - 1) {
+        if (lane <= ol) job.out[o - ol + lane] = obit;
+      }
+    }
+  }
+
+  // ---- store the context ----
+  if (lane < n) {
+#pragma unroll
+    for (int k = 0; k < N; k++) dst->s[lane][k] = s[k];
+    dst->cost[lane] = cost;
+    dst->path[lane] = path;
+    dst->next[lane] = (uint8_t)nxt;
+    dst->slot[lane] = (uint8_t)slot;
+#pragma unroll
+    for (int w = 0; w < kRegRingWords; w++)
+      if (w < W) dst->ring[lane][w] = ring[w];
+  }
+  __syncwarp();
+  for (int i = lane; i < 2 * kSlots; i += 32) {
+    const int b = i / kSlots, j = i % kSlots;
+    dst->spath[b][j] = sm.path[b][j];
+    dst->skey[b][j] = (unsigned long long)sm.key[b][j];
+    dst->slink[b][j] = sm.link[b][j];
+  }
+  if (lane == 0) {
+    dst->n = n;
+    dst->bank = bank;
+    dst->pos = pos;
+    dst->conv_fail = c_conv;
+    dst->cands_collapse = c_coll;
+    dst->next_filter_drops = c_drop;
+    dst->total_children = c_tot;
+  }
+  err = __reduce_max_sync(kFull, err);
+  if (err && lane == 0) atomicMax(status, err);
+}
+
+template <int N>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+sdm_jobs_kernel(SdmParams P, const SdmJob* __restrict__ jobs, int njobs,
+                int* __restrict__ job_counter, SdmCtx* __restrict__ ctxs,
+                int* __restrict__ status) {
+  __shared__ WarpSmem smem[kWarpsPerBlock];
+  WarpSmem& sm = smem[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int j = 0;
+    if (lane == 0) j = atomicAdd(job_counter, 1);
+    j = __shfl_sync(kFull, j, 0);
+    if (j >= njobs) break;
+    const SdmJob job = jobs[j];
+    run_job<N>(P, job, ctxs, sm, status);
+    __syncwarp();
+  }
+}
+
+// Host-side launcher: grid = min(jobs, resident warps) / warps per block.
+int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_counter,
+                    SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream) {
+  if (njobs <= 0) return 0;
+  int blocks = (njobs + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  if (max_blocks > 0 && blocks > max_blocks) blocks = max_blocks;
+  cudaMemsetAsync(d_counter, 0, sizeof(int), stream);
+  const dim3 grid(blocks), block(kWarpsPerBlock * 32);
+  switch (P.order) {
+#define DSD_CASE(NN) \
+  case NN: sdm_jobs_kernel<NN><<<grid, block, 0, stream>>>(P, d_jobs, njobs, d_counter, d_ctxs, d_status); break;
+    DSD_CASE(2) DSD_CASE(3) DSD_CASE(4) DSD_CASE(5) DSD_CASE(6)
+    DSD_CASE(7) DSD_CASE(8) DSD_CASE(9) DSD_CASE(10)
+#undef DSD_CASE
+    default: return -1;
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int sdm_max_lat_in_registers() { return 32 * kRegRingWords; }
+
+}  // namespace dsdgpu

@@ -1,0 +1,132 @@
+/*
+ * dsdgpu — GB300 (sm_103a) implementation of the foo_dsd_trellis PCM/DSD -> DSD
+ * hot path behind a C ABI: FIR upsampling chain with the engine glue, the
+ * trellis sigma-delta modulator, Density-Aligned Stitching of parallel
+ * segments, and bit packing / DoP framing.
+ *
+ * Conventions (those of the reference's include/gpu_compute.h:1-9):
+ *   - every call returns an int status: 0 (DSDGPU_OK) on success, a negative
+ *     DSDGPU_ERR_* code on failure; the caller decides what to do next;
+ *   - an opaque context owns the device, a CUDA stream and all device state;
+ *     it is not thread-safe: drive one context from one thread;
+ *   - setup calls are separate from per-block calls;
+ *   - buffers named d_* are device pointers owned by the caller; buffers named
+ *     h_* are host pointers (pinned or pageable).
+ * Decisions are exchanged as one byte per DSD sample (1 = +1.0, 0 = -1.0)
+ * unless a function says otherwise.
+ */
+#ifndef DSDGPU_H
+#define DSDGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DSDGPU_OK                0
+#define DSDGPU_ERR_ARG          (-1)  /* invalid argument; the reference's -1 */
+#define DSDGPU_ERR_CUDA         (-2)  /* a CUDA runtime call failed */
+#define DSDGPU_ERR_NOMEM        (-3)  /* device or host allocation failed */
+#define DSDGPU_ERR_STATE        (-4)  /* call out of order (not set up, ...) */
+#define DSDGPU_ERR_DEVICE       (-5)  /* a kernel reported a bounded-wait or
+                                         bounded-walk failure in its status word */
+#define DSDGPU_ERR_UNSUPPORTED  (-6)  /* parameters valid for the reference but
+                                         not built in this library */
+
+typedef struct dsdgpu_context dsdgpu_context_t;
+
+/* Trellis SDM parameters: the arguments of sdm_context_init plus the NTF
+ * coefficients of the ntf_filter_t it is given and the state limiter
+ * (reference include/trellis.h:62-63, include/ntf.h:14-20,
+ * include/trellis.h:57). */
+typedef struct {
+    int    order;        /* NTF order, 2..10 */
+    double a[10];        /* ntf_filter_t.a (first `order` used) */
+    double g[10];        /* ntf_filter_t.g */
+    int    depth;        /* path-dedup mask width, 1..64 (the reference
+                            accepts 1..32; 33..64 follow its arithmetic with a
+                            64-bit path) */
+    int    cands;        /* candidates kept per sample K, 1..32 */
+    int    lat;          /* traceback latency in samples, 1..2048 */
+    double state_limit;  /* integrator clamp, 0 = off */
+} dsdgpu_sdm_params_t;
+
+/* One segment of work for dsdgpu_sdm_segments: sdm_segment_process
+ * (reference src/engine.c:915-938) on context `channel`, optionally after
+ * sdm_context_copy_state from `seed_from` (src/trellis.c:1064) and seeding of
+ * the live candidates with `d_seed_state` and zero cost
+ * (src/dsp_plugin.c:2316-2326). */
+typedef struct {
+    const double *d_in;          /* device, `count` doubles */
+    uint8_t      *d_out;         /* device, room for `count` decision bytes */
+    int64_t       count;         /* input samples */
+    int64_t       discard;       /* warm-up decisions to drop after latency fill */
+    int           channel;       /* context the segment runs on and leaves its state in */
+    int           seed_from;     /* context to copy first, or -1 */
+    const double *d_seed_state;  /* device, `order` doubles, or NULL */
+    int64_t       out_count;     /* written: decisions produced */
+} dsdgpu_segment_t;
+
+/* ---- lifecycle (replaces gpu_create / gpu_destroy, include/gpu_compute.h:52-55) ---- */
+
+/* Create a context on CUDA device `device`.  *out is NULL on failure. */
+int  dsdgpu_create(int device, dsdgpu_context_t **out);
+void dsdgpu_destroy(dsdgpu_context_t *ctx);
+/* Human-readable description of the last failure on this context. */
+const char *dsdgpu_last_error(const dsdgpu_context_t *ctx);
+/* Wait for all work queued on the context's stream. */
+int  dsdgpu_synchronize(dsdgpu_context_t *ctx);
+
+/* ---- trellis SDM (replaces sdm_context_init / sdm_process_block /
+ *      sdm_drain / sdm_context_copy_state / sdm_context_reset,
+ *      include/trellis.h:62-88; and gpu_cuda_trellis_setup / gpu_cuda_trellis,
+ *      include/gpu_compute.h:246-256) ---- */
+
+/* Allocate and initialise `num_contexts` device SDM contexts with one
+ * parameter set (sdm_context_init on each).  Replaces any previous setup. */
+int dsdgpu_sdm_setup(dsdgpu_context_t *ctx, const dsdgpu_sdm_params_t *p, int num_contexts);
+
+/* sdm_context_reset on context `channel`, or on all contexts when -1. */
+int dsdgpu_sdm_reset(dsdgpu_context_t *ctx, int channel);
+
+/* sdm_process_block on contexts [first, first + nch): channel c reads
+ * d_in[c * in_stride ...] (count doubles) and writes its decisions to
+ * d_out[c * out_stride ...].  out_counts[c] receives the decisions of channel
+ * c (count minus what is still filling the latency); may be NULL. */
+int dsdgpu_sdm_process(dsdgpu_context_t *ctx, int first, int nch,
+                       const double *d_in, size_t in_stride, size_t count,
+                       uint8_t *d_out, size_t out_stride, size_t *out_counts);
+
+/* Host-buffer form with the reference's float +-1.0 output: h_in is
+ * [nch][count] doubles, h_out [nch][count] floats.  Copies in, runs, copies
+ * out (sdm_process_block's own signature, per channel). */
+int dsdgpu_sdm_process_host(dsdgpu_context_t *ctx, int first, int nch,
+                            const double *h_in, size_t count, float *h_out,
+                            size_t *out_counts);
+
+/* sdm_drain on contexts [first, first + nch). */
+int dsdgpu_sdm_drain(dsdgpu_context_t *ctx, int first, int nch, uint8_t *d_out,
+                     size_t out_stride, size_t max_out, size_t *out_counts);
+
+/* sdm_context_copy_state(dst, src). */
+int dsdgpu_sdm_copy_state(dsdgpu_context_t *ctx, int dst, int src);
+
+/* Run many segments in one persistent launch (the batched form).  Segments
+ * whose `channel` is the same must not appear twice in one call, and no
+ * segment may name as `seed_from` a context another segment of the call runs
+ * on (copy it beforehand with dsdgpu_sdm_copy_state). */
+int dsdgpu_sdm_segments(dsdgpu_context_t *ctx, dsdgpu_segment_t *segs, int nseg);
+
+/* Best candidate's integrator state (sdm_state_distance's input,
+ * src/trellis.c:1094-1109) and the counters conv_fail, cands_collapse,
+ * next_filter_drops, total_children (include/trellis.h:53-56), plus
+ * num_cands, pending.  best_state may be NULL; info may be NULL (6 values). */
+int dsdgpu_sdm_query(dsdgpu_context_t *ctx, int channel, double *best_state, uint64_t *info);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DSDGPU_H */

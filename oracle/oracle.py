@@ -1,0 +1,255 @@
+"""ORACLE — test infrastructure only.
+
+ctypes bindings for oracle/liboracle.so (the C restatement) and, where it was
+built, oracle/_ref/libref.so / libref_wide.so (the reference's own trellis.c,
+ntf.c and dop.c).  Only tests/, __graft_entry__.smoke() and bench.py's CPU
+legs import this module; the product package never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.path.join(HERE, "_ref")
+
+_dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
+_u8p = C.POINTER(C.c_uint8)
+_u64p = C.POINTER(C.c_uint64)
+
+
+def build(ref: bool = False) -> None:
+    """Compile liboracle.so (and the reference libraries when `ref`)."""
+    subprocess.check_call(["make", "-s", "-C", HERE] + (["ref"] if ref else []),
+                          stdout=subprocess.DEVNULL)
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(t)
+
+
+class _SdmLib:
+    """Common wrapper: `prefix` is 'ora' (restatement) or 'ref' (reference)."""
+
+    def __init__(self, path: str, prefix: str):
+        self.lib = C.CDLL(path)
+        self.p = prefix
+        L, p = self.lib, prefix
+        f = getattr(L, f"{p}_sdm_new")
+        f.restype = C.c_void_p
+        f.argtypes = [C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double]
+        for name, res, args in [
+            ("sdm_free", None, [C.c_void_p]),
+            ("sdm_process", C.c_size_t, [C.c_void_p, _dp, _fp, C.c_size_t]),
+            ("sdm_drain", C.c_size_t, [C.c_void_p, _fp, C.c_size_t]),
+            ("sdm_reset", None, [C.c_void_p]),
+            ("sdm_copy", None, [C.c_void_p, C.c_void_p]),
+            ("sdm_segment", C.c_size_t, [C.c_void_p, _dp, _fp, C.c_size_t, C.c_size_t]),
+            ("sdm_seed", None, [C.c_void_p, _dp]),
+            ("sdm_best_state", None, [C.c_void_p, _dp]),
+            ("sdm_info", None, [C.c_void_p, _u64p]),
+            ("estimate_state", None, [C.c_int, _dp, _dp, _dp, _dp, C.c_size_t,
+                                      C.c_double, C.c_int, _dp]),
+            ("dop_pack_i24", C.c_int, [_fp, _u8p, C.c_size_t, C.c_int]),
+            ("bits_pack", None, [_fp, _u8p, C.c_size_t]),
+        ]:
+            fn = getattr(L, f"{p}_{name}")
+            fn.restype = res
+            fn.argtypes = args
+        self.lib.__dict__  # keep reference alive
+
+    def fn(self, name):
+        return getattr(self.lib, f"{self.p}_{name}")
+
+
+class Sdm:
+    """One trellis SDM context (the reference's sdm_context_t)."""
+
+    def __init__(self, lib: _SdmLib, order, a, g, depth, cands, lat, state_limit=0.0):
+        self.L = lib
+        self.order = order
+        self.a = np.zeros(10, np.float64)
+        self.g = np.zeros(10, np.float64)
+        self.a[:order] = a[:order]
+        self.g[:order] = g[:order]
+        self.h = lib.fn("sdm_new")(order, _ptr(self.a, _dp), _ptr(self.g, _dp), depth,
+                                  cands, lat, float(state_limit))
+        if not self.h:
+            raise ValueError("sdm init rejected the parameters")
+        self.lat = lat
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            self.L.fn("sdm_free")(h)
+            self.h = None
+
+    def process(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.float64)
+        out = np.empty(max(len(x), 1), np.float32)
+        n = self.L.fn("sdm_process")(self.h, _ptr(x, _dp), _ptr(out, _fp), len(x))
+        return out[:n]
+
+    def segment(self, x: np.ndarray, discard: int) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.float64)
+        out = np.empty(max(len(x), 1), np.float32)
+        n = self.L.fn("sdm_segment")(self.h, _ptr(x, _dp), _ptr(out, _fp), len(x), discard)
+        return out[:n]
+
+    def drain(self, max_out: int) -> np.ndarray:
+        out = np.empty(max(max_out, 1), np.float32)
+        n = self.L.fn("sdm_drain")(self.h, _ptr(out, _fp), max_out)
+        return out[:n]
+
+    def reset(self):
+        self.L.fn("sdm_reset")(self.h)
+
+    def copy_from(self, other: "Sdm"):
+        self.L.fn("sdm_copy")(self.h, other.h)
+
+    def seed(self, state):
+        s = np.zeros(10, np.float64)
+        s[: self.order] = state[: self.order]
+        self.L.fn("sdm_seed")(self.h, _ptr(s, _dp))
+
+    def best_state(self) -> np.ndarray:
+        s = np.zeros(10, np.float64)
+        self.L.fn("sdm_best_state")(self.h, _ptr(s, _dp))
+        return s[: self.order]
+
+    def info(self) -> dict:
+        v = np.zeros(9, np.uint64)
+        self.L.fn("sdm_info")(self.h, _ptr(v, _u64p))
+        keys = ["num_cands", "pos", "pending", "idx", "draining", "conv_fail",
+                "cands_collapse", "next_filter_drops", "total_children"]
+        return {k: int(x) for k, x in zip(keys, v)}
+
+
+_cache: dict = {}
+
+
+def oracle_lib() -> _SdmLib:
+    if "ora" not in _cache:
+        path = os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        lib = _SdmLib(path, "ora")
+        _bind_oracle_extras(lib.lib)
+        _cache["ora"] = lib
+    return _cache["ora"]
+
+
+def ref_lib(wide: bool = False):
+    """The reference's own SDM, or None when oracle/_ref was not built."""
+    key = "wide" if wide else "ref"
+    if key not in _cache:
+        path = os.path.join(REF_DIR, "libref_wide.so" if wide else "libref.so")
+        if not os.path.exists(path):
+            _cache[key] = None
+        else:
+            lib = _SdmLib(path, "ref")
+            L = lib.lib
+            L.ref_ntf_count.restype = C.c_int
+            L.ref_ntf_entry.argtypes = [C.c_int, _dp, _dp, C.POINTER(C.c_int),
+                                        C.POINTER(C.c_uint), C.c_char_p, C.c_int]
+            L.ref_ntf_lookup.argtypes = [C.c_int, C.c_uint]
+            L.ref_ntf_auto.argtypes = [C.c_uint]
+            L.ref_path_bits.restype = C.c_int
+            _cache[key] = lib
+    return _cache[key]
+
+
+def _bind_oracle_extras(L):
+    L.ora_sdm_process_bits.restype = C.c_size_t
+    L.ora_sdm_process_bits.argtypes = [C.c_void_p, _dp, _u8p, C.c_size_t]
+    L.ora_sdm_segment_bits.restype = C.c_size_t
+    L.ora_sdm_segment_bits.argtypes = [C.c_void_p, _dp, _u8p, C.c_size_t, C.c_size_t]
+    L.ora_dop_pack_u8.restype = C.c_int
+    L.ora_dop_pack_u8.argtypes = [_u8p, _u8p, C.c_size_t, C.c_int]
+    L.ora_bits_pack_u8.argtypes = [_u8p, _u8p, C.c_size_t]
+    L.ora_fir_design.argtypes = [C.c_int, C.c_int, _dp]
+    L.ora_fir_plan.argtypes = [C.c_uint, C.c_uint, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.ora_fir_upsample.restype = C.c_size_t
+    L.ora_fir_upsample.argtypes = [C.c_uint, C.c_uint, _dp, C.c_size_t, _dp]
+    L.ora_engine_fir.restype = C.c_size_t
+    L.ora_engine_fir.argtypes = [C.c_uint, C.c_uint, _fp, C.c_size_t, C.c_int,
+                                 C.c_double, C.c_double, C.c_int, _dp]
+    L.ora_sdm_run_jobs.restype = C.c_int
+
+
+def sdm(order, a, g, depth, cands, lat, state_limit=0.0) -> Sdm:
+    return Sdm(oracle_lib(), order, a, g, depth, cands, lat, state_limit)
+
+
+def sdm_bits(ctx: Sdm, x: np.ndarray) -> np.ndarray:
+    """Run the oracle context over x and return 0/1 decision bytes."""
+    x = np.ascontiguousarray(x, np.float64)
+    out = np.empty(max(len(x), 1), np.uint8)
+    n = ctx.L.lib.ora_sdm_process_bits(ctx.h, _ptr(x, _dp), _ptr(out, _u8p), len(x))
+    return out[:n]
+
+
+def segment_bits(ctx: Sdm, x: np.ndarray, discard: int) -> np.ndarray:
+    x = np.ascontiguousarray(x, np.float64)
+    out = np.empty(max(len(x), 1), np.uint8)
+    n = ctx.L.lib.ora_sdm_segment_bits(ctx.h, _ptr(x, _dp), _ptr(out, _u8p), len(x), discard)
+    return out[:n]
+
+
+def fir_design(ntaps: int, quarter: bool = False) -> np.ndarray:
+    h = np.zeros(ntaps, np.float64)
+    rc = oracle_lib().lib.ora_fir_design(ntaps, int(quarter), _ptr(h, _dp))
+    if rc != 0:
+        raise ValueError("bad tap count")
+    return h
+
+
+def fir_plan(fs_in: int, fs_out: int):
+    fac = (C.c_int * 9)()
+    nt = (C.c_int * 9)()
+    s = oracle_lib().lib.ora_fir_plan(fs_in, fs_out, fac, nt)
+    if s < 0:
+        raise ValueError("unsupported rate pair")
+    return [(fac[i], nt[i]) for i in range(s)]
+
+
+def engine_fir(fs_in, fs_out, x: np.ndarray, boxcar_taps=8, g_start=1.0, g_end=1.0,
+               soft_clip=True) -> np.ndarray:
+    """FP64 boxcar -> FIR chain -> gain ramp -> soft clip (engine rate-conversion path)."""
+    x = np.ascontiguousarray(x, np.float32)
+    ratio = fs_out // fs_in
+    out = np.empty(max(len(x) * ratio, 1), np.float64)
+    n = oracle_lib().lib.ora_engine_fir(fs_in, fs_out, _ptr(x, _fp), len(x), boxcar_taps,
+                                        g_start, g_end, int(soft_clip), _ptr(out, _dp))
+    return out[:n]
+
+
+def estimate_state(order, a, g, init, x, state_limit=0.0, levels=16, lib=None):
+    L = lib or oracle_lib()
+    aa = np.zeros(10); aa[:order] = a[:order]
+    gg = np.zeros(10); gg[:order] = g[:order]
+    ii = np.zeros(10); ii[:order] = init[:order]
+    x = np.ascontiguousarray(x, np.float64)
+    out = np.zeros(10)
+    L.fn("estimate_state")(order, _ptr(aa, _dp), _ptr(gg, _dp), _ptr(ii, _dp),
+                           _ptr(x, _dp), len(x), float(state_limit), levels, _ptr(out, _dp))
+    return out[:order]
+
+
+def dop_pack_bits(bits: np.ndarray, phase: int = 0):
+    """DoP i24 frames from 0/1 decision bytes; returns (bytes, next_phase)."""
+    bits = np.ascontiguousarray(bits, np.uint8)
+    out = np.zeros(max(len(bits) // 16 * 3, 1), np.uint8)
+    ph = oracle_lib().lib.ora_dop_pack_u8(_ptr(bits, _u8p), _ptr(out, _u8p), len(bits), phase)
+    return out[: len(bits) // 16 * 3], ph
+
+
+def bits_pack(bits: np.ndarray) -> np.ndarray:
+    bits = np.ascontiguousarray(bits, np.uint8)
+    out = np.zeros(max((len(bits) + 7) // 8, 1), np.uint8)
+    oracle_lib().lib.ora_bits_pack_u8(_ptr(bits, _u8p), _ptr(out, _u8p), len(bits))
+    return out[: (len(bits) + 7) // 8]

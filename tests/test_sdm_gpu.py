@@ -1,0 +1,139 @@
+"""GPU trellis SDM vs the oracle (bit-exact): the CUDA path is called through
+the C ABI (libdsdgpu.so via foo_dsd_trellis_gb300.sdm) and compared decision
+by decision with the CPU restatement of src/trellis.c."""
+import zlib
+
+import numpy as np
+import pytest
+
+from signals import multitone, sdm_input
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _ntf(name, rate):
+    from foo_dsd_trellis_gb300 import ntf
+    return ntf.get_filter(name, rate)
+
+
+def _gpu_sdm(f, depth, K, lat, lim=0.0, nctx=1):
+    from foo_dsd_trellis_gb300.sdm import TrellisSdm
+    return TrellisSdm(f.order, f.a, f.g, depth, K, lat, lim, num_contexts=nctx)
+
+
+def _ora(oracle, f, depth, K, lat, lim=0.0):
+    return oracle.sdm(f.order, np.array(f.a), np.array(f.g), depth, K, lat, lim)
+
+
+CASES = [
+    # (ntf name, rate, depth, K, lat, limit)
+    ("clans-5", 2822400, 32, 16, 32, 0.0),     # the plain DSD64 configuration
+    ("clans-7", 6144000, 64, 32, 128, 0.0),    # the DSD128 DAS configuration
+    ("clans-6", 5644800, 32, 32, 128, 0.0),
+    ("clans-8", 11289600, 48, 16, 32, 0.0),
+    ("sdm-6", 22579200, 16, 2, 32, 10.0),
+    ("clans-4", 2822400, 8, 32, 64, 4.0),
+    ("sdm-8", 5644800, 4, 8, 16, 0.0),
+    ("clans-6", 2822400, 1, 3, 7, 0.0),
+    ("sdm-5", 11289600, 33, 31, 100, 2.0),
+    ("clans-6", 2822400, 32, 1, 256, 0.0),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}-d{c[2]}-K{c[3]}-lat{c[4]}" for c in CASES])
+def test_process_block_bit_exact(oracle, case):
+    name, rate, depth, K, lat, lim = case
+    f = _ntf(name, rate)
+    n = 20000
+    x = sdm_input(n, seed=zlib.crc32(repr(case).encode()) & 0xffff, amp=0.45)
+    ref = _ora(oracle, f, depth, K, lat, lim)
+    want = oracle.sdm_bits(ref, x)
+    g = _gpu_sdm(f, depth, K, lat, lim)
+    got = g.process_block(torch.from_numpy(x).cuda())[0].cpu().numpy()
+    assert len(got) == len(want) == n - lat
+    bad = np.nonzero(got != want)[0]
+    assert bad.size == 0, f"first mismatch at {bad[:5]} of {len(want)}"
+    q = g.query(0)
+    info = ref.info()
+    assert q["num_cands"] == info["num_cands"]
+    assert q["total_children"] == info["total_children"]
+    assert q["next_filter_drops"] == info["next_filter_drops"]
+    assert q["conv_fail"] == info["conv_fail"]
+    np.testing.assert_array_equal(q["best_state"], ref.best_state())
+
+
+def test_streaming_blocks_and_drain(oracle):
+    f = _ntf("clans-7", 6144000)
+    x = multitone(30000, seed=5)
+    ref = _ora(oracle, f, 64, 32, 128)
+    g = _gpu_sdm(f, 64, 32, 128)
+    rng = np.random.default_rng(3)
+    pos = 0
+    while pos < len(x):
+        b = int(rng.integers(1, 5000))
+        blk = x[pos:pos + b]
+        pos += b
+        want = oracle.sdm_bits(ref, blk)
+        got = g.process_block(torch.from_numpy(blk).cuda())[0].cpu().numpy()
+        np.testing.assert_array_equal(got, want)
+    want = (ref.drain(500) > 0).astype(np.uint8)
+    got = g.drain(500)[0].cpu().numpy()
+    np.testing.assert_array_equal(got, want)
+
+
+def test_short_block_then_drain(oracle):
+    """Fewer samples than the latency, then drain (test/test_trellis.c:122-140)."""
+    f = _ntf("clans-5", 2822400)
+    ref = _ora(oracle, f, 8, 16, 64)
+    g = _gpu_sdm(f, 8, 16, 64)
+    x = np.zeros(40)
+    assert len(oracle.sdm_bits(ref, x)) == 0
+    assert g.process_block(torch.from_numpy(x).cuda())[0].numel() == 0
+    want = (ref.drain(256) > 0).astype(np.uint8)
+    got = g.drain(256)[0].cpu().numpy()
+    assert len(want) == 40
+    np.testing.assert_array_equal(got, want)
+
+
+def test_multichannel_and_host_form(oracle):
+    f = _ntf("clans-6", 5644800)
+    xs = np.stack([sdm_input(8000, seed=s) for s in (1, 2, 3)])
+    g = _gpu_sdm(f, 32, 32, 128, nctx=3)
+    got = g.process_block_host(xs)
+    for c in range(3):
+        ref = _ora(oracle, f, 32, 32, 128)
+        want = ref.process(xs[c])
+        np.testing.assert_array_equal(got[c], want)
+
+
+def test_segments_copy_seed_discard(oracle):
+    """DAS-style segments: copy a warmed context, seed the candidates with a
+    state, run with warm-up discard (src/engine.c:915-938)."""
+    f = _ntf("clans-7", 6144000)
+    K, depth, lat = 32, 64, 128
+    x = multitone(60000, seed=11)
+    base = _ora(oracle, f, depth, K, lat)
+    oracle.sdm_bits(base, x[:5000])
+    g = _gpu_sdm(f, depth, K, lat, nctx=5)
+    g.process_block(torch.from_numpy(x[:5000]).cuda(), first=0)
+    g.copy_state(4, 0)          # snapshot: segments must not read a context that runs
+    seed = np.array(base.best_state())
+    from foo_dsd_trellis_gb300.sdm import SegmentSpec
+    specs, wants = [], []
+    for i, (a, b, disc, sd) in enumerate([(5000, 20000, 0, False), (15000, 32000, 3000, True),
+                                          (28000, 45000, 8192 - lat, True),
+                                          (40000, 60000, 100000, False)]):
+        ctxo = oracle.sdm(f.order, np.array(f.a), np.array(f.g), depth, K, lat)
+        ctxo.copy_from(base)
+        if sd:
+            ctxo.seed(seed)
+        wants.append(oracle.segment_bits(ctxo, x[a:b], disc))
+        specs.append(SegmentSpec(torch.from_numpy(x[a:b].copy()).cuda(), channel=i,
+                                 discard=disc, seed_from=4,
+                                 seed_state=torch.from_numpy(seed).cuda() if sd else None))
+    # channel 0 is also a target: copy_state of 4 onto 0 is the seeding source
+    outs = g.segments(specs)
+    for got, want in zip(outs, wants):
+        np.testing.assert_array_equal(got.cpu().numpy(), want)
