@@ -44,7 +44,7 @@ class Segment(C.Structure):
 
 class FirParams(C.Structure):
     _fields_ = [("fs_in", C.c_uint), ("fs_out", C.c_uint), ("boxcar_taps", C.c_int),
-                ("soft_clip", C.c_int), ("gain_start", C.c_double), ("gain_end", C.c_double)]
+                ("soft_clip", C.c_int)]
 
 
 class DasParams(C.Structure):
@@ -71,6 +71,12 @@ SIGNATURES = {
     "dsdgpu_sdm_segments": (C.c_int, [_vp, C.POINTER(Segment), C.c_int]),
     "dsdgpu_sdm_query": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_double),
                                    C.POINTER(C.c_uint64)]),
+    "dsdgpu_fir_setup": (C.c_int, [_vp, C.POINTER(FirParams), C.c_int]),
+    "dsdgpu_fir_reset": (C.c_int, [_vp]),
+    "dsdgpu_fir_process": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp, _sz,
+                                     C.c_double, C.c_double, _szp]),
+    "dsdgpu_fir_process_async": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp, _sz,
+                                           C.c_double, C.c_double, _szp]),
 }
 
 _lib = None

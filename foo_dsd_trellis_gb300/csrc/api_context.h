@@ -9,6 +9,7 @@
 
 #include "../../include/dsdgpu.h"
 #include "sdm_internal.h"
+#include "fir_internal.h"
 
 struct dsdgpu_context {
   int device = 0;
@@ -30,6 +31,14 @@ struct dsdgpu_context {
   dsdgpu::SdmJob* d_jobs = nullptr;
   int jobs_cap = 0;
 
+  // FIR chain
+  bool fir_ready = false;
+  dsdgpu::FirChainConst fir{};
+  dsdgpu_fir_params_t fir_params{};
+  int fir_channels = 0;
+  size_t fir_smem = 0;
+  float* d_fir_hist = nullptr;   // last PCM samples per channel
+
   // reusable device scratch for the host-buffer entry points
   void* d_scratch = nullptr;
   size_t scratch_bytes = 0;
@@ -45,6 +54,8 @@ struct dsdgpu_context {
     if (d_ctx) cudaFree(d_ctx);
     if (d_jobs) cudaFree(d_jobs);
     if (d_scratch) cudaFree(d_scratch);
+    if (d_fir_hist) cudaFree(d_fir_hist);
+    d_fir_hist = nullptr;
     d_ctx = nullptr;
     d_jobs = nullptr;
     d_scratch = nullptr;

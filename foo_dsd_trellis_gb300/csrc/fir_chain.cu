@@ -1,0 +1,335 @@
+// Fused multi-stage polyphase upsampling FIR for sm_103a, with the engine glue
+// around it (reference src/engine.c:608-717, src/fir.c:523-725):
+//
+//   PCM float  -> boxcar running mean over `taps` samples (optional)
+//              -> S upsampling stages (2x half-band 63/127 taps, or a 4x
+//                 quarter-band 127-tap stage), FP32 FMA polyphase
+//              -> FP64 gain ramp g_start + step * i
+//              -> FP64 tanh soft clip above +-0.95 (optional)
+//              -> double output for the trellis SDM
+//
+// One CTA produces a tile of final output samples for one channel.  It walks
+// the chain backwards to find the input range each stage needs, stages the
+// PCM window (with its history halo) and every intermediate signal in shared
+// memory, and writes only the final double tile to HBM: the chain's HBM
+// traffic is one read of the PCM input and one write of the output.
+//
+// Stream continuity: a call may be one block of a longer stream.  The last
+// kHistory PCM samples of the previous block are kept per channel and stand in
+// for negative input indices, so the chain is the same LTI system as one long
+// run (the delay lines of ippsFIRMR, src/fir.c:319-329).
+//
+// Half-band taps at even offsets from the centre are sin(k pi)/(k pi) ~ 1e-17
+// in the FP64 design; they are dropped from the FP32 polyphase because their
+// products are below FP32 resolution of any output.
+#include "api_context.h"
+#include "fir_internal.h"
+
+#include <cmath>
+#include <cstring>
+
+namespace dsdgpu {
+
+__constant__ FirChainConst c_fir;
+
+// floor division for possibly negative numerators
+__device__ __forceinline__ long long fdiv(long long a, int b) {
+  return a >= 0 ? a / b : -((-a + b - 1) / b);
+}
+
+__global__ void __launch_bounds__(kFirThreads)
+fir_chain_kernel(const float* __restrict__ pcm, size_t pcm_stride, long long count,
+                 const float* __restrict__ hist, double* __restrict__ out, size_t out_stride,
+                 double g_start, double g_step, int apply_gain, int soft_clip) {
+  extern __shared__ float sm[];
+  const FirChainConst& F = c_fir;
+  const int ch = blockIdx.y;
+  const long long total_out = count * F.ratio;
+  const long long o_lo = (long long)blockIdx.x * F.tile;
+  if (o_lo >= total_out) return;
+  const long long o_hi = min(o_lo + (long long)F.tile, total_out);
+
+  // ranges of every signal: sig[S] is the output, sig[0] the boxcar output
+  long long lo[kMaxStages + 1], hi[kMaxStages + 1];
+  lo[F.S] = o_lo;
+  hi[F.S] = o_hi;
+  for (int k = F.S - 1; k >= 0; k--) {
+    lo[k] = fdiv(lo[k + 1] - (F.L[k] - 1), F.U[k]);
+    hi[k] = fdiv(hi[k + 1] - 1, F.U[k]) + 1;
+  }
+  const int bt = F.boxcar;
+  const long long p_lo = lo[0] - (bt > 0 ? bt - 1 : 0);
+
+  // shared layout: [pcm window][sig 0][sig 1]...[sig S-1]
+  float* buf[kMaxStages + 1];
+  float* pw = sm;
+  int off = (int)(hi[0] - p_lo);
+  for (int k = 0; k < F.S; k++) {
+    buf[k] = sm + off;
+    off += (int)(hi[k] - lo[k]);
+  }
+
+  const float* x = pcm + (size_t)ch * pcm_stride;
+  const float* hx = hist + (size_t)ch * kHistory;
+  for (long long i = p_lo + threadIdx.x; i < hi[0]; i += blockDim.x) {
+    float v;
+    if (i >= 0) v = x[i];
+    else if (i >= -kHistory) v = hx[kHistory + i];
+    else v = 0.0f;
+    pw[i - p_lo] = v;
+  }
+  __syncthreads();
+
+  // boxcar: mean of the last `bt` samples (the reference keeps a running FP64
+  // sum; the direct sum differs only in rounding)
+  for (long long i = lo[0] + threadIdx.x; i < hi[0]; i += blockDim.x) {
+    float v;
+    if (bt > 0) {
+      float s = 0.0f;
+      for (int j = 0; j < bt; j++) s += pw[i - j - p_lo];
+      v = s * F.inv_boxcar;
+    } else {
+      v = pw[i - p_lo];
+    }
+    buf[0][i - lo[0]] = v;
+  }
+  __syncthreads();
+
+  for (int k = 0; k < F.S; k++) {
+    const int U = F.U[k];
+    const float* in = buf[k];
+    const long long ilo = lo[k];
+    const long long mlo = lo[k + 1], mhi = hi[k + 1];
+    const bool last = (k == F.S - 1);
+    // one thread per input index i: outputs U*i + r, r = 0..U-1
+    const long long i0 = fdiv(mlo, U), i1 = fdiv(mhi - 1, U) + 1;
+    for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      for (int r = 0; r < U; r++) {
+        const long long m = (long long)U * i + r;
+        if (m < mlo || m >= mhi) continue;
+        const int nt = F.nphase[k][r];
+        const int toff = F.phase_off[k][r];
+        float acc0 = 0.0f, acc1 = 0.0f;
+        int t = 0;
+        for (; t + 1 < nt; t += 2) {
+          acc0 = fmaf(F.taps[toff + t], in[i - F.lag[toff + t] - ilo], acc0);
+          acc1 = fmaf(F.taps[toff + t + 1], in[i - F.lag[toff + t + 1] - ilo], acc1);
+        }
+        if (t < nt) acc0 = fmaf(F.taps[toff + t], in[i - F.lag[toff + t] - ilo], acc0);
+        if (!last) {
+          buf[k + 1][m - mlo] = acc0 + acc1;
+        } else {
+          double y = (double)acc0 + (double)acc1;
+          if (apply_gain) y = __dmul_rn(y, __dadd_rn(g_start, __dmul_rn(g_step, (double)m)));
+          if (soft_clip) {
+            if (y > 0.95) y = 0.95 + 0.05 * tanh((y - 0.95) * 20.0);
+            else if (y < -0.95) y = -0.95 - 0.05 * tanh((-y - 0.95) * 20.0);
+          }
+          out[(size_t)ch * out_stride + m] = y;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Keep the last kHistory PCM samples of this block (for the next one).
+__global__ void fir_history_kernel(const float* __restrict__ pcm, size_t pcm_stride,
+                                   long long count, float* __restrict__ hist) {
+  const int ch = blockIdx.x;
+  float* h = hist + (size_t)ch * kHistory;
+  const float* x = pcm + (size_t)ch * pcm_stride;
+  // new history = last kHistory samples of (old history ++ block)
+  __shared__ float tmp[kHistory];
+  for (int j = threadIdx.x; j < kHistory; j += blockDim.x) {
+    const long long src = count - kHistory + j;   // index into the block
+    tmp[j] = src >= 0 ? x[src] : h[kHistory + src];
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < kHistory; j += blockDim.x) h[j] = tmp[j];
+}
+
+// FP64 design of the reference's half-band / quarter-band taps (src/fir.c:65-121).
+static double bessel_i0(double x) {
+  double sum = 1.0, term = 1.0;
+  const double q = (x / 2.0) * (x / 2.0);
+  for (int k = 1; k <= 25; k++) {
+    term *= q / ((double)k * (double)k);
+    sum += term;
+    if (term < 1e-20 * sum) break;
+  }
+  return sum;
+}
+
+void design_taps(int ntaps, bool quarter, double* h) {
+  const int c = (ntaps - 1) / 2;
+  const double beta = 12.0, pi = 3.14159265358979323846;
+  const double i0b = bessel_i0(beta);
+  double sum = 0.0;
+  for (int n = 0; n < ntaps; n++) {
+    const double x = quarter ? (double)(n - c) * 0.25 : (double)(n - c) / 2.0;
+    const double sinc = (std::fabs(x) < 1e-15) ? 1.0 : std::sin(pi * x) / (pi * x);
+    const double t = (double)(n - c) / c;
+    const double arg = 1.0 - t * t;
+    const double w = bessel_i0(beta * std::sqrt(arg > 0.0 ? arg : 0.0)) / i0b;
+    h[n] = quarter ? 0.25 * sinc * w : sinc * w;
+    sum += h[n];
+  }
+  for (int n = 0; n < ntaps; n++) h[n] /= sum;
+}
+
+// Stage plan of fir_chain_init_ex for upsampling (src/fir.c:523-611, 131-150).
+int plan_chain(unsigned fs_in, unsigned fs_out, int* U, int* L) {
+  if (fs_in == 0 || fs_out < fs_in || fs_out % fs_in) return -1;
+  const unsigned ratio = fs_out / fs_in;
+  if (ratio & (ratio - 1)) return -1;
+  int S = 0;
+  for (unsigned r = ratio; r > 1; r >>= 1) S++;
+  if (S > kMaxStages) return -1;
+  const bool to512 = (fs_out == 22579200u || fs_out == 24576000u);
+  if (ratio == 8 && to512) {
+    U[0] = 4; L[0] = 127;
+    U[1] = 2; L[1] = 63;
+    return 2;
+  }
+  for (int i = 0; i < S; i++) {
+    U[i] = 2;
+    L[i] = (S >= 2 && i == 0 && to512) ? 127 : 63;
+  }
+  return S;
+}
+
+int build_chain_const(unsigned fs_in, unsigned fs_out, int boxcar, FirChainConst* F) {
+  memset(F, 0, sizeof *F);
+  int U[kMaxStages], L[kMaxStages];
+  const int S = plan_chain(fs_in, fs_out, U, L);
+  if (S < 0) return -1;
+  F->S = S;
+  F->ratio = (int)(fs_out / fs_in);
+  F->boxcar = boxcar;
+  F->inv_boxcar = boxcar > 0 ? (float)(1.0 / boxcar) : 1.0f;
+  int toff = 0;
+  int rows = 1;
+  for (int k = 0; k < S; k++) {
+    F->U[k] = U[k];
+    F->L[k] = L[k];
+    double h[255];
+    design_taps(L[k], U[k] == 4, h);
+    for (int r = 0; r < U[k]; r++) {
+      F->phase_off[k][r] = toff;
+      int n = 0;
+      for (int j = 0; U[k] * j + r < L[k]; j++) {
+        const int tap = U[k] * j + r;
+        const double hv = h[tap] * (double)U[k];
+        if (std::fabs(hv) < 1e-12) continue;     // half-band zero taps
+        if (toff + n >= kMaxChainTaps) return -1;
+        F->taps[toff + n] = (float)hv;
+        F->lag[toff + n] = j;
+        n++;
+      }
+      F->nphase[k][r] = n;
+      toff += n;
+    }
+    rows *= U[k];
+  }
+  // output tile: a few thousand final samples per CTA
+  F->tile = 4096;
+  return 0;
+}
+
+size_t chain_smem_bytes(const FirChainConst& F) {
+  // worst-case extents of every signal for a tile, plus the PCM window
+  long long lo[kMaxStages + 1], hi[kMaxStages + 1];
+  size_t best = 0;
+  for (int phase = 0; phase < 4; phase++) {
+    lo[F.S] = (long long)phase * F.tile + 1000003LL * F.ratio;   // a generic offset
+    hi[F.S] = lo[F.S] + F.tile;
+    for (int k = F.S - 1; k >= 0; k--) {
+      auto fd = [](long long a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); };
+      lo[k] = fd(lo[k + 1] - (F.L[k] - 1), F.U[k]);
+      hi[k] = fd(hi[k + 1] - 1, F.U[k]) + 1;
+    }
+    size_t tot = (size_t)(hi[0] - lo[0] + (F.boxcar > 0 ? F.boxcar - 1 : 0));
+    for (int k = 0; k < F.S; k++) tot += (size_t)(hi[k] - lo[k]);
+    if (tot > best) best = tot;
+  }
+  return (best + 16) * sizeof(float);
+}
+
+}  // namespace dsdgpu
+
+using namespace dsdgpu;
+
+extern "C" {
+
+int dsdgpu_fir_setup(dsdgpu_context_t* c, const dsdgpu_fir_params_t* p, int num_channels) {
+  if (!c || !p || num_channels < 1) return DSDGPU_ERR_ARG;
+  if (p->boxcar_taps < 0 || p->boxcar_taps > 64) return c->fail(DSDGPU_ERR_ARG, "boxcar taps out of range");
+  cudaSetDevice(c->device);
+  FirChainConst F;
+  if (build_chain_const(p->fs_in, p->fs_out, p->boxcar_taps, &F) != 0)
+    return c->fail(DSDGPU_ERR_ARG, "unsupported rate pair (upsampling by a power of two only)");
+  if (c->d_fir_hist) cudaFree(c->d_fir_hist);
+  c->d_fir_hist = nullptr;
+  cudaError_t e = cudaMalloc(&c->d_fir_hist, sizeof(float) * kHistory * (size_t)num_channels);
+  if (e != cudaSuccess) return c->cuda_fail(e, "fir history allocation");
+  cudaMemsetAsync(c->d_fir_hist, 0, sizeof(float) * kHistory * (size_t)num_channels, c->stream);
+  c->fir = F;
+  c->fir_params = *p;
+  c->fir_channels = num_channels;
+  c->fir_smem = chain_smem_bytes(F);
+  if (c->fir_smem > 200 * 1024) return c->fail(DSDGPU_ERR_UNSUPPORTED, "fir tile does not fit shared memory");
+  cudaFuncSetAttribute(fir_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->fir_smem);
+  c->fir_ready = true;
+  return c->check_status();
+}
+
+int dsdgpu_fir_reset(dsdgpu_context_t* c) {
+  if (!c) return DSDGPU_ERR_ARG;
+  if (!c->fir_ready) return c->fail(DSDGPU_ERR_STATE, "fir not set up");
+  cudaSetDevice(c->device);
+  cudaMemsetAsync(c->d_fir_hist, 0, sizeof(float) * kHistory * (size_t)c->fir_channels, c->stream);
+  return c->check_status();
+}
+
+int dsdgpu_fir_process_async(dsdgpu_context_t* c, int first, int nch, const float* d_in,
+                             size_t in_stride, size_t count, double* d_out, size_t out_stride,
+                             double gain_start, double gain_end, size_t* out_count) {
+  if (!c) return DSDGPU_ERR_ARG;
+  if (!c->fir_ready) return c->fail(DSDGPU_ERR_STATE, "fir not set up");
+  if (first < 0 || nch < 1 || first + nch > c->fir_channels) return c->fail(DSDGPU_ERR_ARG, "bad channel range");
+  const size_t n_out = count * (size_t)c->fir.ratio;
+  if (out_count) *out_count = n_out;
+  if (count == 0) return DSDGPU_OK;
+  if (!d_in || !d_out) return c->fail(DSDGPU_ERR_ARG, "null buffer");
+  if (out_stride < n_out) return c->fail(DSDGPU_ERR_ARG, "output stride too small");
+  cudaSetDevice(c->device);
+  // gain ramp of engine_process_block (src/engine.c:609-651)
+  double gs = gain_start, ge = gain_end;
+  if (gs == 0.0) gs = ge;
+  const int apply = (gs != 1.0 || ge != 1.0) ? 1 : 0;
+  const double step = (n_out > 1) ? (ge - gs) / (double)(n_out - 1) : 0.0;
+  cudaError_t e = cudaMemcpyToSymbolAsync(c_fir, &c->fir, sizeof(FirChainConst), 0,
+                                          cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return c->cuda_fail(e, "fir constants");
+  const dim3 grid((unsigned)((n_out + c->fir.tile - 1) / c->fir.tile), (unsigned)nch);
+  float* hist = c->d_fir_hist + (size_t)first * kHistory;
+  fir_chain_kernel<<<grid, kFirThreads, c->fir_smem, c->stream>>>(
+      d_in, in_stride, (long long)count, hist, d_out, out_stride, gs, step, apply,
+      c->fir_params.soft_clip);
+  fir_history_kernel<<<nch, 128, 0, c->stream>>>(d_in, in_stride, (long long)count, hist);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return c->cuda_fail(e, "fir launch");
+  return DSDGPU_OK;
+}
+
+int dsdgpu_fir_process(dsdgpu_context_t* c, int first, int nch, const float* d_in,
+                       size_t in_stride, size_t count, double* d_out, size_t out_stride,
+                       double gain_start, double gain_end, size_t* out_count) {
+  int rc = dsdgpu_fir_process_async(c, first, nch, d_in, in_stride, count, d_out, out_stride,
+                                    gain_start, gain_end, out_count);
+  if (rc) return rc;
+  return c->check_status();
+}
+
+}  // extern "C"

@@ -69,6 +69,17 @@ typedef struct {
     int64_t       out_count;     /* written: decisions produced */
 } dsdgpu_segment_t;
 
+/* FIR chain + engine glue parameters: fir_chain_init_ex(fs_in, fs_out) for an
+ * upsampling power-of-two ratio (reference src/fir.c:523-611) and the
+ * engine's per-channel pre/post processing around it (src/engine.c:608-717). */
+typedef struct {
+    unsigned fs_in;       /* input rate (PCM or DSD), Hz */
+    unsigned fs_out;      /* output DSD rate, fs_in * 2^k, k = 1..9 */
+    int      boxcar_taps; /* running-mean pre-smooth at the input rate: 8 on the
+                             rate-conversion path, 0 = off (DAS FIR phase) */
+    int      soft_clip;   /* 1: tanh knee above +-0.95 before the SDM */
+} dsdgpu_fir_params_t;
+
 /* ---- lifecycle (replaces gpu_create / gpu_destroy, include/gpu_compute.h:52-55) ---- */
 
 /* Create a context on CUDA device `device`.  *out is NULL on failure. */
@@ -118,6 +129,29 @@ int dsdgpu_sdm_copy_state(dsdgpu_context_t *ctx, int dst, int src);
  * segment may name as `seed_from` a context another segment of the call runs
  * on (copy it beforehand with dsdgpu_sdm_copy_state). */
 int dsdgpu_sdm_segments(dsdgpu_context_t *ctx, dsdgpu_segment_t *segs, int nseg);
+
+/* ---- FIR chain (replaces fir_chain_init_ex / fir_chain_process_d /
+ *      fir_chain_reset, include/fir.h:178-203, and gpu_cuda_fir_chain_f64,
+ *      include/gpu_compute.h) ---- */
+
+/* Plan the chain and allocate per-channel history for `num_channels`. */
+int dsdgpu_fir_setup(dsdgpu_context_t *ctx, const dsdgpu_fir_params_t *p, int num_channels);
+/* Clear the per-channel history (fir_chain_reset plus the boxcar reset). */
+int dsdgpu_fir_reset(dsdgpu_context_t *ctx);
+/* One block per channel: d_in[c * in_stride ...] holds `count` float PCM
+ * samples; d_out[c * out_stride ...] receives count * fs_out / fs_in doubles:
+ * boxcar, FIR chain, gain ramp from gain_start to gain_end over the block
+ * (a gain_start of 0 means gain_end; no ramp when both are 1), soft clip.
+ * History carries over to the next call, as the reference's delay lines do. */
+int dsdgpu_fir_process(dsdgpu_context_t *ctx, int first, int nch,
+                       const float *d_in, size_t in_stride, size_t count,
+                       double *d_out, size_t out_stride,
+                       double gain_start, double gain_end, size_t *out_count);
+/* Same, queued on the context's stream without waiting. */
+int dsdgpu_fir_process_async(dsdgpu_context_t *ctx, int first, int nch,
+                             const float *d_in, size_t in_stride, size_t count,
+                             double *d_out, size_t out_stride,
+                             double gain_start, double gain_end, size_t *out_count);
 
 /* Best candidate's integrator state (sdm_state_distance's input,
  * src/trellis.c:1094-1109) and the counters conv_fail, cands_collapse,
