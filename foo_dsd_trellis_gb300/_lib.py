@@ -49,7 +49,11 @@ class FirParams(C.Structure):
 
 class DasParams(C.Structure):
     _fields_ = [("seg_len", C.c_int64), ("nsegs", C.c_int), ("seed_mode", C.c_int),
-                ("reposition", C.c_int), ("fs_out", C.c_uint)]
+                ("reposition", C.c_int)]
+
+
+DAS_FULL_PARALLEL = 0
+DAS_SEG0_FIRST = 1
 
 
 _vp = C.c_void_p
@@ -71,6 +75,8 @@ SIGNATURES = {
     "dsdgpu_sdm_segments": (C.c_int, [_vp, C.POINTER(Segment), C.c_int]),
     "dsdgpu_sdm_query": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_double),
                                    C.POINTER(C.c_uint64)]),
+    "dsdgpu_das_process": (C.c_int, [_vp, C.POINTER(DasParams), C.c_int, _vp, _sz, _sz, _vp,
+                                     _sz, _szp, C.POINTER(C.c_int), C.c_int]),
     "dsdgpu_fir_setup": (C.c_int, [_vp, C.POINTER(FirParams), C.c_int]),
     "dsdgpu_fir_reset": (C.c_int, [_vp]),
     "dsdgpu_fir_process": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp, _sz,

@@ -10,6 +10,7 @@
 #include "../../include/dsdgpu.h"
 #include "sdm_internal.h"
 #include "fir_internal.h"
+#include "das_internal.h"
 
 struct dsdgpu_context {
   int device = 0;
@@ -39,6 +40,20 @@ struct dsdgpu_context {
   size_t fir_smem = 0;
   float* d_fir_hist = nullptr;   // last PCM samples per channel
 
+  // DAS (device plan buffers, grown on demand)
+  int das_persistent = 0;          // contexts [0, das_persistent) are the channels' own
+  int das_last_segments = 0;
+  uint8_t* d_das_bits = nullptr;   size_t das_bits_cap = 0;
+  double* d_das_est = nullptr;     size_t das_est_cap = 0;
+  long long* d_das_i64 = nullptr;  size_t das_i64_cap = 0;
+  double* d_das_f64 = nullptr;     size_t das_f64_cap = 0;
+  int* d_das_bp = nullptr;         size_t das_bp_cap = 0;
+  dsdgpu::SeamTask* d_das_tasks = nullptr;        size_t das_tasks_cap = 0;
+  dsdgpu::AssemblePiece* d_das_pieces = nullptr;  size_t das_pieces_cap = 0;
+  dsdgpu::SegBuf* d_das_segbuf = nullptr;         size_t das_segbuf_cap = 0;
+  double* d_das_qfir = nullptr;    size_t das_qfir_cap = 0;
+  bool das_qfir_ready = false;
+
   // reusable device scratch for the host-buffer entry points
   void* d_scratch = nullptr;
   size_t scratch_bytes = 0;
@@ -56,6 +71,16 @@ struct dsdgpu_context {
     if (d_scratch) cudaFree(d_scratch);
     if (d_fir_hist) cudaFree(d_fir_hist);
     d_fir_hist = nullptr;
+    void* das[] = {d_das_bits, d_das_est, d_das_i64, d_das_f64, d_das_bp, d_das_tasks,
+                   d_das_pieces, d_das_segbuf, d_das_qfir};
+    for (void* p : das)
+      if (p) cudaFree(p);
+    d_das_bits = nullptr; d_das_est = nullptr; d_das_i64 = nullptr; d_das_f64 = nullptr;
+    d_das_bp = nullptr; d_das_tasks = nullptr; d_das_pieces = nullptr; d_das_segbuf = nullptr;
+    d_das_qfir = nullptr;
+    das_bits_cap = das_est_cap = das_i64_cap = das_f64_cap = das_bp_cap = 0;
+    das_tasks_cap = das_pieces_cap = das_segbuf_cap = das_qfir_cap = 0;
+    das_qfir_ready = false;
     d_ctx = nullptr;
     d_jobs = nullptr;
     d_scratch = nullptr;

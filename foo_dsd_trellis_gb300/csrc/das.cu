@@ -1,0 +1,771 @@
+// Density-Aligned Stitching on sm_103a (reference src/dsp_plugin.c:1283-2762).
+//
+// One chunk per call.  The host plans the segment layout (and the RMS-driven
+// reposition of quiet boundaries, whose window RMS values come from a kernel);
+// the segments run as one persistent SDM launch; then
+//
+//   das_seam_kernel     one CTA per boundary: match density by block prefix
+//                       sum, the reference's candidate scan, the run nearest
+//                       the density peak, and the 255-tap FP64 pop metric for
+//                       every candidate (threads over (candidate, offset);
+//                       each dot product keeps the reference's tap order);
+//   das_assemble_kernel gathers the final stream for every channel.
+//
+// The stitch search of a boundary only reads the last `overlap` decisions of
+// the previous segment's copied region and the first `overlap` decisions of
+// the new segment, and the write positions do not depend on the chosen seams
+// (the stitch point moves only which side of the overlap a sample comes from),
+// so every boundary is searched in parallel and the assembly is a gather.
+#include "api_context.h"
+#include "das_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace dsdgpu {
+
+int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_counter,
+                    SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream);
+
+constexpr int kSeamThreads = 512;
+constexpr int kMaxQ = 32;
+
+// ---- window RMS (src/dsp_plugin.c:1975-1978): serial FP64 sum of squares ----
+__global__ void das_rms_kernel(const double* __restrict__ x, const long long* __restrict__ centers,
+                               int n, int win, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const long long c = centers[i];
+  double s = 0.0;
+  for (long long k = c - win / 2; k < c + win / 2; k++) s = __dadd_rn(s, __dmul_rn(x[k], x[k]));
+  out[i] = sqrt(__ddiv_rn(s, (double)win));
+}
+
+// ---- 16-level greedy state estimator (src/trellis.c:1125-1187), serial ----
+// One thread per channel walks the chunk from seg1's start and records the
+// state at every later segment start.
+__global__ void das_estimate_kernel(SdmParams P, const double* __restrict__ fir, size_t fir_stride,
+                                    const SdmCtx* __restrict__ pers, int pers_first,
+                                    const long long* __restrict__ starts, int S, long long count,
+                                    double* __restrict__ est /* [nch][S][kMaxOrder] */, int nch) {
+  const int ch = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ch >= nch) return;
+  const int N = P.order;
+  double st[kMaxOrder], ns[kMaxOrder];
+  const SdmCtx* c = &pers[pers_first + ch];
+  for (int k = 0; k < N; k++) st[k] = c->s[0][k];
+  const double* x = fir + (size_t)ch * fir_stride;
+  const long long est_start = starts[1];
+  const double step = 2.0 / 15.0;
+  long long pos = 0;
+  for (int s = 1; s < S; s++) {
+    const long long bnd = s >= 2 ? starts[s] - est_start : 0;
+    if (bnd > pos && bnd <= count - est_start) {
+      for (long long t = pos; t < bnd; t++) {
+        const double xv = x[est_start + t];
+        ns[0] = __dadd_rn(__dsub_rn(st[0], __dmul_rn(P.g[0], st[1])), xv);
+        double v = __dadd_rn(xv, __dmul_rn(P.a[0], ns[0]));
+        for (int i = 1; i < N - 1; i++) {
+          ns[i] = __dsub_rn(__dadd_rn(st[i], st[i - 1]), __dmul_rn(P.g[i], st[i + 1]));
+          v = __dadd_rn(v, __dmul_rn(P.a[i], ns[i]));
+        }
+        ns[N - 1] = __dadd_rn(st[N - 1], st[N - 2]);
+        v = __dadd_rn(v, __dmul_rn(P.a[N - 1], ns[N - 1]));
+        const double yi = __ddiv_rn(v, P.a[0]);
+        int idx = __double2int_rz(__dadd_rn(__ddiv_rn(__dadd_rn(yi, 1.0), step), 0.5));
+        if (idx < 0) idx = 0;
+        if (idx > 15) idx = 15;
+        const double y = __dadd_rn(-1.0, __dmul_rn((double)idx, step));
+        ns[0] = __dsub_rn(ns[0], y);
+        if (P.state_limit > 0.0)
+          for (int i = 0; i < N; i++) {
+            if (ns[i] > P.state_limit) ns[i] = P.state_limit;
+            else if (ns[i] < -P.state_limit) ns[i] = -P.state_limit;
+          }
+        for (int i = 0; i < N; i++) st[i] = ns[i];
+      }
+      pos = bnd;
+    }
+    for (int k = 0; k < kMaxOrder; k++) est[((size_t)ch * S + s) * kMaxOrder + k] = k < N ? st[k] : 0.0;
+  }
+}
+
+// Best-candidate state of the persistent contexts, replicated per segment
+// (full-parallel seeding, src/dsp_plugin.c:2268-2283).
+__global__ void das_seed_from_best_kernel(const SdmCtx* __restrict__ ctxs, int first, int S,
+                                          double* __restrict__ est, int nch, int order) {
+  const int ch = blockIdx.x;
+  const SdmCtx* c = &ctxs[first + ch];
+  for (int i = threadIdx.x; i < S * kMaxOrder; i += blockDim.x) {
+    const int k = i % kMaxOrder;
+    est[(size_t)ch * S * kMaxOrder + i] = k < order ? c->s[0][k] : 0.0;
+  }
+}
+
+// ---- seam search, one CTA per boundary (src/dsp_plugin.c:2455-2652) ----
+__global__ void __launch_bounds__(kSeamThreads)
+das_seam_kernel(const SeamTask* __restrict__ tasks, int ntasks, const double* __restrict__ qfir2,
+                int lat, int* __restrict__ bp_out) {
+  const int ti = blockIdx.x;
+  if (ti >= ntasks) return;
+  const SeamTask T = tasks[ti];
+  const int L = T.ovl_len;
+  extern __shared__ unsigned char smraw[];
+  int8_t* dif = (int8_t*)smraw;                       // next - prev in {-1, 0, 1} (x2 later)
+  int* dmap = (int*)(smraw + ((L + 15) & ~15));       // density map, L + 1 ints
+  __shared__ int red[32];
+  __shared__ int s_peak, s_pp, s_nq, s_best;
+  __shared__ int qpos[kMaxQ + 1], qden[kMaxQ + 1];
+  __shared__ double qmax[kMaxQ + 1];
+  __shared__ double s_q2[255];
+
+  for (int k = threadIdx.x; k < 255; k += blockDim.x) s_q2[k] = qfir2[k];
+  // match flags: prev = T.prev[0..L), next = T.next[0..L)
+  for (int i = threadIdx.x; i < L; i += blockDim.x) {
+    const int a = T.prev[i], b = T.next[i];
+    dif[i] = (int8_t)(b - a);          // bits 0/1: diff of the +-1 samples is 2 * (b - a)
+  }
+  __syncthreads();
+
+  int half_w = lat;
+  if (half_w > L / 2) half_w = L / 2;
+  if (half_w < 4) half_w = 4;
+
+  // prefix sum of matches -> dmap[p] = matches in [max(0, p - hw), min(L, p + hw))
+  // (the reference's incremental window, src/dsp_plugin.c:2483-2501)
+  // inclusive scan into dmap[1..L], dmap[0] = 0
+  {
+    const int per = (L + blockDim.x - 1) / blockDim.x;
+    const int b0 = threadIdx.x * per, b1 = min(L, b0 + per);
+    int loc = 0;
+    for (int i = b0; i < b1; i++) loc += (dif[i] == 0);
+    // exclusive scan of loc over threads
+    int v = loc;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int n = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += n;
+    }
+    if (lane == 31) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+      int x = lane < (int)(blockDim.x >> 5) ? red[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int n = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += n;
+      }
+      red[lane] = x;
+    }
+    __syncthreads();
+    int run = v - loc + (w > 0 ? red[w - 1] : 0);
+    if (threadIdx.x == 0) dmap[0] = 0;
+    for (int i = b0; i < b1; i++) {
+      run += (dif[i] == 0);
+      dmap[i + 1] = run;
+    }
+  }
+  __syncthreads();
+  // convert the prefix into window counts in place, via registers
+  int* pref = dmap;
+  int myv[32];
+  {
+    int cnt = 0;
+    for (int p = threadIdx.x; p < L && cnt < 32; p += blockDim.x, cnt++) {
+      const int hi = min(L, p + half_w), lo = max(0, p - half_w);
+      myv[cnt] = pref[hi] - pref[lo];
+    }
+    __syncthreads();
+    cnt = 0;
+    for (int p = threadIdx.x; p < L && cnt < 32; p += blockDim.x, cnt++) dmap[p] = myv[cnt];
+  }
+  __syncthreads();
+
+  // peak and its first position
+  {
+    int best = -1, bi = 0x7fffffff;
+    for (int p = threadIdx.x; p < L; p += blockDim.x) {
+      const int v = dmap[p];
+      if (v > best || (v == best && p < bi)) { best = v; bi = p; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const int ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    __shared__ int wb[32], wi[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) { wb[w] = best; wi[w] = bi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int B = -1, I = 0;
+      for (int i = 0; i < (int)(blockDim.x >> 5); i++)
+        if (wb[i] > B || (wb[i] == B && wi[i] < I)) { B = wb[i]; I = wi[i]; }
+      s_peak = L > 0 ? (B > 0 ? B : 0) : 0;
+      s_pp = L > 0 ? I : 0;
+    }
+    __syncthreads();
+  }
+
+  // candidate scan and the peak-run candidate (serial, as the reference)
+  if (threadIdx.x == 0) {
+    const int peak = s_peak;
+    const int floor_d = peak * 9 / 10;
+    const int min_spacing = half_w;
+    int nq = 0;
+    for (int p = 0; p < L - 3 && nq < kMaxQ;) {
+      if (dif[p] != 0 || dmap[p] < floor_d) { p++; continue; }
+      const int rs = p;
+      int rl = 0;
+      while (p < L && dif[p] == 0) { rl++; p++; }
+      if (rl < 4) continue;
+      if (nq > 0 && rs - qpos[nq - 1] < min_spacing) continue;
+      qpos[nq] = rs;
+      qden[nq] = dmap[rs];
+      nq++;
+    }
+    const int pp = s_pp;
+    int prp = pp, prl = 1;
+    for (int mr = 8; mr >= 1 && prl < 4; mr >>= 1) {
+      for (int r = 0; r <= half_w && prl < 4; r++) {
+        for (int t = 0; t < 2 && prl < 4; t++) {
+          const int tp = t == 0 ? pp - r : pp + r;
+          if (tp < 0 || tp + mr > L) continue;
+          int rl = 0;
+          for (int k = 0; k < mr; k++) {
+            if (dif[tp + k] == 0) rl++;
+            else break;
+          }
+          if (rl >= mr) { prp = tp; prl = mr; }
+        }
+      }
+    }
+    int dup = 0;
+    for (int ci = 0; ci < nq; ci++)
+      if (abs(qpos[ci] - prp) < min_spacing) { dup = 1; break; }
+    if (!dup && nq < kMaxQ) {
+      qpos[nq] = prp;
+      qden[nq] = L > 0 ? dmap[prp] : 0;
+      nq++;
+    }
+    if (nq == 0) { qpos[0] = 0; qden[0] = 0; nq = 1; }
+    for (int ci = 0; ci < nq; ci++) qmax[ci] = 0.0;
+    s_nq = nq;
+  }
+  __syncthreads();
+  const int nq = s_nq;
+
+  // pop metric: |255-tap FIR of the stitched-minus-unstitched difference| over
+  // j in [-512, 512); terms with idx < sp (before the stitch) or with equal
+  // bits are zero and are skipped (adding +-0 leaves the magnitude unchanged)
+  if (nq > 1) {
+    // offsets j < -127 see no term at all (k >= 127 - j > 254): value 0
+    const int jlo = -127, jhi = 512, nj = jhi - jlo;
+    for (int it = threadIdx.x; it < nq * nj; it += blockDim.x) {
+      const int ci = it / nj;
+      const int j = jlo + it % nj;
+      const int sp = qpos[ci];
+      double val = 0.0;
+      int k0 = 127 - j;
+      if (k0 < 0) k0 = 0;
+      for (int k = k0; k < 255; k++) {
+        const int idx = sp + j - 127 + k;
+        if (idx >= L) break;
+        const int d = dif[idx];
+        if (d) val = __dadd_rn(val, d > 0 ? s_q2[k] : -s_q2[k]);
+      }
+      const double ad = fabs(val);
+      // max over j: atomicMax on the bit pattern of a non-negative double
+      atomicMax((unsigned long long*)&qmax[ci], (unsigned long long)__double_as_longlong(ad));
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double q[kMaxQ + 1];
+    const int peak = s_peak;
+    for (int ci = 0; ci < nq; ci++) {
+      if (nq == 1) { q[ci] = 0.0; continue; }
+      double dr = __ddiv_rn((double)qden[ci], (double)(peak > 0 ? peak : 1));
+      if (dr < 0.5) dr = 0.5;
+      q[ci] = __ddiv_rn(qmax[ci], dr);
+    }
+    int best = 0;
+    for (int ci = 1; ci < nq; ci++) {
+      const double ratio = __ddiv_rn(q[ci], __dadd_rn(q[best], 1e-15));
+      if (ratio < 0.8) best = ci;
+      else if (ratio < 1.2 && qden[ci] > qden[best]) best = ci;
+    }
+    s_best = qpos[best];
+    bp_out[T.boundary] = s_best;
+  }
+}
+
+// ---- assembly: gather every channel's stream (src/dsp_plugin.c:2420-2714) ----
+__global__ void das_assemble_kernel(const AssemblePiece* __restrict__ pieces, int npieces,
+                                    const int* __restrict__ bp, uint8_t* __restrict__ out,
+                                    size_t out_stride, int nch, int S, const SegBuf* __restrict__ segbuf) {
+  const int pi = blockIdx.y;
+  if (pi >= npieces) return;
+  const AssemblePiece P = pieces[pi];
+  // this piece covers stream [begin, end) taken from segment P.seg, whose
+  // decision i sits at stream position P.base + i
+  const long long begin = P.base + (P.stitched ? bp[P.seg] : 0);
+  long long end = P.end_base;
+  if (P.next_stitched) end = P.next_base + bp[P.next_seg];
+  for (int ch = 0; ch < nch; ch++) {
+    const uint8_t* src = segbuf[ch * S + P.seg].ptr;
+    uint8_t* dst = out + (size_t)ch * out_stride;
+    for (long long p = begin + blockIdx.x * (long long)blockDim.x + threadIdx.x; p < end;
+         p += (long long)gridDim.x * blockDim.x)
+      dst[p] = src[p - P.base];
+  }
+}
+
+// The pop-metric low-pass, host side (src/dsp_plugin.c:2568-2600), times two:
+// the difference of two +-1 samples is +-2, and doubling is exact.
+void pop_fir_times_two(double* q2) {
+  const int N = 255;
+  const double fc = 20000.0 / (5644800.0 / 2.0);
+  double q[255];
+  double sum = 0;
+  for (int i = 0; i < N; i++) {
+    const double n = i - 127.0;
+    if (n > -0.001 && n < 0.001) q[i] = 2.0 * fc;
+    else q[i] = std::sin(2.0 * 3.14159265358979 * fc * n) / (3.14159265358979 * n);
+    const double x = 2.0 * i / (N - 1) - 1.0;
+    const double kb = 8.0;
+    const double arg = kb * std::sqrt(1.0 - x * x > 0 ? 1.0 - x * x : 0);
+    double i0a = 1.0, term = 1.0;
+    for (int m = 1; m <= 20; m++) {
+      term *= (arg / 2.0 / m) * (arg / 2.0 / m);
+      i0a += term;
+    }
+    double i0k = 1.0;
+    term = 1.0;
+    for (int m = 1; m <= 20; m++) {
+      term *= (kb / 2.0 / m) * (kb / 2.0 / m);
+      i0k += term;
+    }
+    q[i] *= i0a / i0k;
+    sum += q[i];
+  }
+  for (int i = 0; i < N; i++) q2[i] = 2.0 * (q[i] / sum);
+}
+
+}  // namespace dsdgpu
+
+using namespace dsdgpu;
+
+namespace {
+
+template <typename T>
+int ensure_dev(dsdgpu_context* c, T** p, size_t* cap, size_t n, const char* what) {
+  if (*cap >= n) return DSDGPU_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (n ? n : 1));
+  if (e != cudaSuccess) return c->cuda_fail(e, what);
+  *cap = n;
+  return DSDGPU_OK;
+}
+
+// Grow the SDM context bank to `need` contexts, keeping the existing ones.
+int ensure_ctx_capacity(dsdgpu_context* c, int need) {
+  if (c->nctx >= need) return DSDGPU_OK;
+  SdmCtx* nd = nullptr;
+  cudaError_t e = cudaMalloc(&nd, sizeof(SdmCtx) * (size_t)need);
+  if (e != cudaSuccess) return c->cuda_fail(e, "context bank growth");
+  if (c->nctx > 0) cudaMemcpyAsync(nd, c->d_ctx, sizeof(SdmCtx) * (size_t)c->nctx,
+                                   cudaMemcpyDeviceToDevice, c->stream);
+  cudaStreamSynchronize(c->stream);
+  if (c->d_ctx) cudaFree(c->d_ctx);
+  c->d_ctx = nd;
+  c->pending.resize(need, 0);
+  c->draining.resize(need, 0);
+  c->nctx = need;
+  return DSDGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int nch,
+                       const double* d_fir, size_t fir_stride, size_t count, uint8_t* d_out,
+                       size_t out_stride, size_t* out_count, int* h_stitch_pos, int max_segs) {
+  if (!c || !dp || nch < 1) return DSDGPU_ERR_ARG;
+  if (!c->sdm_ready) return c->fail(DSDGPU_ERR_STATE, "sdm not set up");
+  if (nch > c->das_persistent) {
+    if (c->das_persistent == 0 && c->nctx >= nch) c->das_persistent = nch;
+    else return c->fail(DSDGPU_ERR_STATE, "persistent contexts: call dsdgpu_sdm_setup with num_contexts >= channels");
+  }
+  if (count > 0 && (!d_fir || !d_out)) return c->fail(DSDGPU_ERR_ARG, "null buffer");
+  cudaSetDevice(c->device);
+  const int lat = c->sdm.lat;
+  const size_t overlap = 64 * (size_t)lat;
+
+  // ---- layout (src/dsp_plugin.c:1343-1366, 1936-1957) ----
+  int S = dp->seg_len > 0 ? (int)(count / (size_t)dp->seg_len) : dp->nsegs;
+  if (S < 1) S = 1;
+  size_t min_seg = overlap * 4;
+  if (min_seg < 256) min_seg = 256;
+  while (S > 1 && count / (size_t)S < min_seg) S--;
+  std::vector<long long> start(S), size(S);
+  {
+    size_t base = count / (size_t)S, rem = count % (size_t)S, pos = 0;
+    for (int s = 0; s < S; s++) {
+      start[s] = (long long)pos;
+      size[s] = (long long)((s == S - 1) ? count - pos : base + ((size_t)s < rem ? 1 : 0));
+      pos += (size_t)size[s];
+    }
+  }
+  int rc;
+  // ---- reposition of quiet boundaries (src/dsp_plugin.c:1959-2024) ----
+  if (dp->reposition && S > 2) {
+    const long long win = 2048;
+    std::vector<long long> centers;
+    std::vector<int> which;
+    for (int s = 2; s < S; s++) {
+      const long long b = start[s];
+      if (b < win || b + win >= (long long)count) continue;
+      centers.push_back(b);
+      which.push_back(s);
+    }
+    if (!centers.empty()) {
+      rc = ensure_dev(c, &c->d_das_i64, &c->das_i64_cap, centers.size(), "rms centers");
+      if (rc) return rc;
+      rc = ensure_dev(c, &c->d_das_f64, &c->das_f64_cap, centers.size(), "rms values");
+      if (rc) return rc;
+      cudaMemcpyAsync(c->d_das_i64, centers.data(), sizeof(long long) * centers.size(),
+                      cudaMemcpyHostToDevice, c->stream);
+      das_rms_kernel<<<(unsigned)((centers.size() + 127) / 128), 128, 0, c->stream>>>(
+          d_fir, c->d_das_i64, (int)centers.size(), (int)win, c->d_das_f64);
+      std::vector<double> cur(centers.size());
+      cudaMemcpyAsync(cur.data(), c->d_das_f64, sizeof(double) * cur.size(), cudaMemcpyDeviceToHost, c->stream);
+      rc = c->check_status();
+      if (rc) return rc;
+      const size_t base = count / (size_t)S;
+      long long max_shift = (long long)(base * 2 / 5);
+      if (max_shift > 200000) max_shift = 200000;
+      const long long step = win / 2;
+      for (size_t wi = 0; wi < which.size(); wi++) {
+        if (cur[wi] > 0.005) continue;
+        const int s = which[wi];
+        // RMS at every offset this boundary could try; the constraints below
+        // depend on the neighbours' (possibly moved) starts, the RMS does not
+        std::vector<long long> cand;
+        const long long b = start[s];
+        for (long long off = step; off <= max_shift; off += step)
+          for (int dir = -1; dir <= 1; dir += 2) {
+            const long long cc = dir < 0 ? (b > off ? b - off : 0) : b + off;
+            if (cc < win / 2 || cc + win / 2 >= (long long)count) continue;
+            cand.push_back(cc);
+          }
+        std::vector<double> rms(cand.size());
+        if (!cand.empty()) {
+          rc = ensure_dev(c, &c->d_das_i64, &c->das_i64_cap, cand.size(), "rms centers");
+          if (rc) return rc;
+          rc = ensure_dev(c, &c->d_das_f64, &c->das_f64_cap, cand.size(), "rms values");
+          if (rc) return rc;
+          cudaMemcpyAsync(c->d_das_i64, cand.data(), sizeof(long long) * cand.size(),
+                          cudaMemcpyHostToDevice, c->stream);
+          das_rms_kernel<<<(unsigned)((cand.size() + 127) / 128), 128, 0, c->stream>>>(
+              d_fir, c->d_das_i64, (int)cand.size(), (int)win, c->d_das_f64);
+          cudaMemcpyAsync(rms.data(), c->d_das_f64, sizeof(double) * rms.size(), cudaMemcpyDeviceToHost, c->stream);
+          rc = c->check_status();
+          if (rc) return rc;
+        }
+        long long best_pos = b;
+        double best_rms = cur[wi];
+        size_t ci = 0;
+        for (long long off = step; off <= max_shift; off += step) {
+          for (int dir = -1; dir <= 1; dir += 2) {
+            const long long cc = dir < 0 ? (b > off ? b - off : 0) : b + off;
+            if (cc < win / 2 || cc + win / 2 >= (long long)count) continue;
+            const double r = rms[ci++];
+            if (s > 0 && cc <= start[s - 1] + (long long)overlap * 2) continue;
+            if (s < S - 1 && start[s + 1] >= (long long)overlap * 2 &&
+                cc >= start[s + 1] - (long long)overlap * 2)
+              continue;
+            if (r > best_rms) { best_rms = r; best_pos = cc; }
+          }
+          if (best_rms > 0.005) break;
+        }
+        if (best_pos != b) {
+          start[s] = best_pos;
+          size[s - 1] = best_pos - start[s - 1];
+          size[s] = (s < S - 1) ? start[s + 1] - best_pos : (long long)count - best_pos;
+        }
+      }
+    }
+  }
+
+  const bool seg0_first = dp->seed_mode == DSDGPU_DAS_SEG0_FIRST;
+  // context bank: [0, P) persistent, then per channel S temps, then P snapshots
+  const int P = c->das_persistent;
+  const int temp0 = P;
+  const int snap0 = P + nch * S;
+  rc = ensure_ctx_capacity(c, snap0 + nch);
+  if (rc) return rc;
+
+  // segment output buffers
+  std::vector<long long> seg_in_start(S), seg_in_count(S), seg_discard(S);
+  size_t buf_total = 0;
+  std::vector<size_t> seg_off(S);
+  for (int s = 0; s < S; s++) {
+    const bool ext = s < S - 1;
+    long long in_start, in_cnt, disc = 0;
+    if (s == 0) {
+      in_start = 0;
+      in_cnt = size[0];
+      if (seg0_first) {
+        // no extension
+      } else if (ext && size[0] + (long long)overlap <= (long long)count) {
+        in_cnt += (long long)overlap;
+      }
+    } else if (s == 1 && seg0_first) {
+      in_start = start[1];
+      in_cnt = size[1];
+      if (S > 2 && start[1] + size[1] + (long long)overlap <= (long long)count) in_cnt += (long long)overlap;
+    } else {
+      in_start = start[s] >= (long long)overlap ? start[s] - (long long)overlap : 0;
+      in_cnt = start[s] + size[s] - in_start;
+      if (ext && start[s] + size[s] + (long long)overlap <= (long long)count) in_cnt += (long long)overlap;
+      disc = start[s] >= (long long)overlap ? (long long)overlap - lat : 0;
+    }
+    seg_in_start[s] = in_start;
+    seg_in_count[s] = in_cnt;
+    seg_discard[s] = disc;
+    seg_off[s] = buf_total;
+    buf_total += ((size_t)in_cnt + 255) & ~(size_t)255;
+  }
+  rc = ensure_dev(c, &c->d_das_bits, &c->das_bits_cap, buf_total * (size_t)nch + 256, "segment buffers");
+  if (rc) return rc;
+  rc = ensure_dev(c, &c->d_das_est, &c->das_est_cap, (size_t)nch * S * kMaxOrder, "seed states");
+  if (rc) return rc;
+
+  // ---- segment SDM runs ----
+  std::vector<int64_t> seg_out((size_t)nch * S, 0);
+  auto seg_ptr = [&](int ch, int s) { return c->d_das_bits + (size_t)ch * buf_total + seg_off[s]; };
+  auto add_job = [&](std::vector<SdmJob>& jobs, int ch, int s, int ctx, int copy_from, bool seed,
+                     int pend_from) {
+    int64_t skip, out, np;
+    c->plan_steps(c->pending[pend_from], seg_in_count[s], seg_discard[s], &skip, &out, &np);
+    c->pending[ctx] = np;
+    c->draining[ctx] = c->draining[pend_from];
+    seg_out[(size_t)ch * S + s] = out;
+    if (seg_in_count[s] == 0) return;
+    SdmJob j;
+    j.in = d_fir + (size_t)ch * fir_stride + seg_in_start[s];
+    j.out = seg_ptr(ch, s);
+    j.n_in = seg_in_count[s];
+    j.skip_out = skip;
+    j.ctx = ctx;
+    j.copy_from = copy_from;
+    j.seed_state = seed ? c->d_das_est + ((size_t)ch * S + s) * kMaxOrder : nullptr;
+    j.pad = 0;
+    jobs.push_back(j);
+  };
+  int first_par = 0;
+  if (seg0_first) {
+    std::vector<SdmJob> j0;
+    for (int ch = 0; ch < nch; ch++) add_job(j0, ch, 0, ch, -1, false, ch);
+    rc = c->run_jobs(j0);
+    if (rc) return rc;
+    if (S > 1) {
+      std::vector<SdmJob> j1;
+      for (int ch = 0; ch < nch; ch++) add_job(j1, ch, 1, temp0 + ch * S + 1, ch, false, ch);
+      rc = c->run_jobs(j1);
+      if (rc) return rc;
+    }
+    if (S > 2) {
+      std::vector<long long> st(start.begin(), start.end());
+      rc = ensure_dev(c, &c->d_das_i64, &c->das_i64_cap, (size_t)S, "starts");
+      if (rc) return rc;
+      cudaMemcpyAsync(c->d_das_i64, st.data(), sizeof(long long) * S, cudaMemcpyHostToDevice, c->stream);
+      das_estimate_kernel<<<(nch + 31) / 32, 32, 0, c->stream>>>(
+          c->sdm, d_fir, fir_stride, c->d_ctx, 0, c->d_das_i64, S, (long long)count,
+          c->d_das_est, nch);
+    }
+    // seg2+ copy the persistent context after seg0: snapshot it so the
+    // parallel launch reads a context nothing writes
+    for (int ch = 0; ch < nch; ch++) {
+      cudaMemcpyAsync(c->d_ctx + snap0 + ch, c->d_ctx + ch, sizeof(SdmCtx), cudaMemcpyDeviceToDevice, c->stream);
+      c->pending[snap0 + ch] = c->pending[ch];
+      c->draining[snap0 + ch] = c->draining[ch];
+    }
+    first_par = 2;
+  } else {
+    for (int ch = 0; ch < nch; ch++) {
+      cudaMemcpyAsync(c->d_ctx + snap0 + ch, c->d_ctx + ch, sizeof(SdmCtx), cudaMemcpyDeviceToDevice, c->stream);
+      c->pending[snap0 + ch] = c->pending[ch];
+      c->draining[snap0 + ch] = c->draining[ch];
+    }
+    das_seed_from_best_kernel<<<nch, 128, 0, c->stream>>>(c->d_ctx, snap0, S, c->d_das_est, nch,
+                                                         c->sdm.order);
+  }
+  {
+    std::vector<SdmJob> jp;
+    for (int ch = 0; ch < nch; ch++)
+      for (int s = first_par; s < S; s++) {
+        if (s == 0) add_job(jp, ch, 0, ch, -1, false, ch);
+        else add_job(jp, ch, s, temp0 + ch * S + s, snap0 + ch, true, snap0 + ch);
+      }
+    rc = c->run_jobs(jp);
+    if (rc) return rc;
+  }
+
+  // ---- stream plan: write positions do not depend on the seams ----
+  std::vector<long long> cnt(S), ps(S, 0), wp(S, 0);
+  std::vector<int> stitched(S, 0), used(S, 0);
+  for (int s = 0; s < S; s++) cnt[s] = seg_out[s];
+  if (!seg0_first && cnt[0] > size[0]) cnt[0] = size[0];
+  long long w = cnt[0];
+  wp[0] = w;
+  used[0] = 1;
+  std::vector<SeamTask> tasks;
+  int last_used = 0;
+  for (int s = 1; s < S; s++) {
+    const long long so = seg_out[s];
+    if (so == 0) continue;
+    used[s] = 1;
+    if (s == 1 && seg0_first) {
+      ps[s] = w;                  // DIRECT: appended as is
+      w += so;
+      wp[s] = w;
+      last_used = s;
+      continue;
+    }
+    if (w < (long long)overlap)
+      return c->fail(DSDGPU_ERR_UNSUPPORTED, "stream shorter than the overlap before a seam");
+    const long long pstart = w - (long long)overlap;
+    long long ol = w - pstart;
+    if (ol > so) ol = so;
+    if (ol > (long long)overlap) ol = (long long)overlap;
+    // the previous `overlap` stream decisions must all come from segment
+    // last_used: its copied part starts at base (+ its seam, < overlap)
+    const bool prev_stitched = stitched[last_used] != 0;
+    const long long base_last = last_used == 0 ? 0 : ps[last_used];
+    const long long prev_len = prev_stitched ? seg_out[last_used] : cnt[last_used];
+    if (prev_stitched ? (prev_len < 2 * (long long)overlap) : (prev_len < (long long)overlap))
+      return c->fail(DSDGPU_ERR_UNSUPPORTED, "segment shorter than the overlap");
+    SeamTask t;
+    t.boundary = s;
+    t.ovl_len = (int)ol;
+    t.prev_seg = last_used;
+    t.prev_off = pstart - base_last;
+    t.prev = nullptr;
+    t.next = nullptr;
+    tasks.push_back(t);
+    ps[s] = pstart;
+    stitched[s] = 1;
+    w = pstart + so;
+    wp[s] = w;
+    last_used = s;
+  }
+  const long long final_count = w;
+  if (out_count) *out_count = (size_t)final_count;
+  if (out_stride < (size_t)final_count) return c->fail(DSDGPU_ERR_ARG, "output stride too small");
+
+  // ---- seams (channel 0) ----
+  rc = ensure_dev(c, &c->d_das_bp, &c->das_bp_cap, (size_t)S, "seam positions");
+  if (rc) return rc;
+  cudaMemsetAsync(c->d_das_bp, 0, sizeof(int) * S, c->stream);
+  if (!tasks.empty()) {
+    for (auto& t : tasks) {
+      t.prev = seg_ptr(0, t.prev_seg) + t.prev_off;
+      t.next = seg_ptr(0, t.boundary);
+    }
+    rc = ensure_dev(c, &c->d_das_tasks, &c->das_tasks_cap, tasks.size(), "seam tasks");
+    if (rc) return rc;
+    if (!c->das_qfir_ready) {
+      double q2[255];
+      pop_fir_times_two(q2);
+      rc = ensure_dev(c, &c->d_das_qfir, &c->das_qfir_cap, 255, "pop filter");
+      if (rc) return rc;
+      cudaMemcpyAsync(c->d_das_qfir, q2, sizeof q2, cudaMemcpyHostToDevice, c->stream);
+      cudaStreamSynchronize(c->stream);
+      c->das_qfir_ready = true;
+    }
+    cudaMemcpyAsync(c->d_das_tasks, tasks.data(), sizeof(SeamTask) * tasks.size(),
+                    cudaMemcpyHostToDevice, c->stream);
+    int maxL = 0;
+    for (auto& t : tasks) maxL = std::max(maxL, t.ovl_len);
+    const size_t smem = ((size_t)(maxL + 15) & ~(size_t)15) + sizeof(int) * (size_t)(maxL + 1) + 64;
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(das_seam_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (maxL > 32 * kSeamThreads) return c->fail(DSDGPU_ERR_UNSUPPORTED, "overlap too long for the seam kernel");
+    das_seam_kernel<<<(unsigned)tasks.size(), kSeamThreads, smem, c->stream>>>(
+        c->d_das_tasks, (int)tasks.size(), c->d_das_qfir, lat, c->d_das_bp);
+  }
+
+  // ---- assembly ----
+  std::vector<AssemblePiece> pieces;
+  std::vector<int> order_used;
+  for (int s = 0; s < S; s++)
+    if (used[s]) order_used.push_back(s);
+  for (size_t i = 0; i < order_used.size(); i++) {
+    const int s = order_used[i];
+    AssemblePiece p;
+    p.seg = s;
+    p.base = (s == 0) ? 0 : ps[s];
+    p.stitched = stitched[s];
+    p.end_base = wp[s];
+    p.next_stitched = 0;
+    p.next_seg = 0;
+    p.next_base = 0;
+    if (i + 1 < order_used.size()) {
+      const int n = order_used[i + 1];
+      if (stitched[n]) {
+        p.next_stitched = 1;
+        p.next_seg = n;
+        p.next_base = ps[n];
+      } else {
+        p.end_base = ps[n];   // DIRECT follower starts at our end
+      }
+    }
+    pieces.push_back(p);
+  }
+  std::vector<SegBuf> sb((size_t)nch * S);
+  for (int ch = 0; ch < nch; ch++)
+    for (int s = 0; s < S; s++) sb[(size_t)ch * S + s].ptr = seg_ptr(ch, s);
+  rc = ensure_dev(c, &c->d_das_pieces, &c->das_pieces_cap, pieces.size(), "assembly plan");
+  if (rc) return rc;
+  rc = ensure_dev(c, &c->d_das_segbuf, &c->das_segbuf_cap, sb.size(), "segment table");
+  if (rc) return rc;
+  cudaMemcpyAsync(c->d_das_pieces, pieces.data(), sizeof(AssemblePiece) * pieces.size(),
+                  cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(c->d_das_segbuf, sb.data(), sizeof(SegBuf) * sb.size(), cudaMemcpyHostToDevice,
+                  c->stream);
+  if (!pieces.empty()) {
+    const dim3 grid(64, (unsigned)pieces.size());
+    das_assemble_kernel<<<grid, 256, 0, c->stream>>>(c->d_das_pieces, (int)pieces.size(),
+                                                      c->d_das_bp, d_out, out_stride, nch, S,
+                                                      c->d_das_segbuf);
+  }
+
+  // ---- state carry: persistent <- last temp (src/dsp_plugin.c:2715-2725) ----
+  if (S > 1) {
+    for (int ch = 0; ch < nch; ch++) {
+      const int last = temp0 + ch * S + (S - 1);
+      cudaMemcpyAsync(c->d_ctx + ch, c->d_ctx + last, sizeof(SdmCtx), cudaMemcpyDeviceToDevice, c->stream);
+      c->pending[ch] = c->pending[last];
+      c->draining[ch] = c->draining[last];
+    }
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return c->cuda_fail(e, "das launch");
+  rc = c->check_status();
+  if (rc) return rc;
+  if (h_stitch_pos) {
+    std::vector<int> bp(S);
+    cudaMemcpy(bp.data(), c->d_das_bp, sizeof(int) * S, cudaMemcpyDeviceToHost);
+    for (int s = 0; s < S && s < max_segs; s++) h_stitch_pos[s] = bp[s];
+  }
+  c->das_last_segments = S;
+  return DSDGPU_OK;
+}
+
+}  // extern "C"

@@ -226,6 +226,7 @@ int dsdgpu_sdm_setup(dsdgpu_context_t* c, const dsdgpu_sdm_params_t* p, int num_
   if (e != cudaSuccess) return c->cuda_fail(e, "context allocation");
   c->sdm = P;
   c->nctx = num_contexts;
+  c->das_persistent = 0;
   c->pending.assign(num_contexts, 0);
   c->draining.assign(num_contexts, 0);
   sdm_ctx_init_kernel<<<num_contexts, 256, 0, c->stream>>>(c->d_ctx, 0, num_contexts, 0);

@@ -80,6 +80,22 @@ typedef struct {
     int      soft_clip;   /* 1: tanh knee above +-0.95 before the SDM */
 } dsdgpu_fir_params_t;
 
+/* DAS seeding modes (reference src/dsp_plugin.c:2185-2283). */
+#define DSDGPU_DAS_FULL_PARALLEL 0  /* every segment from the chunk-start state
+                                       (the reference's mode at DSD512 and up) */
+#define DSDGPU_DAS_SEG0_FIRST    1  /* seg0 on the channel's context, seg1 DIRECT
+                                       from its end state, seg2+ seeded by the
+                                       16-level greedy estimate (below DSD512) */
+
+/* Density-Aligned Stitching parameters for one chunk.  The overlap is
+ * 64 * lat of the SDM setup (src/dsp_plugin.c:1343). */
+typedef struct {
+    int64_t seg_len;     /* nominal segment length in FIR samples; 0: use nsegs */
+    int     nsegs;       /* segment count when seg_len is 0 */
+    int     seed_mode;   /* DSDGPU_DAS_FULL_PARALLEL or DSDGPU_DAS_SEG0_FIRST */
+    int     reposition;  /* 1: move quiet boundaries of seg >= 2 (RMS search) */
+} dsdgpu_das_params_t;
+
 /* ---- lifecycle (replaces gpu_create / gpu_destroy, include/gpu_compute.h:52-55) ---- */
 
 /* Create a context on CUDA device `device`.  *out is NULL on failure. */
@@ -152,6 +168,23 @@ int dsdgpu_fir_process_async(dsdgpu_context_t *ctx, int first, int nch,
                              const float *d_in, size_t in_stride, size_t count,
                              double *d_out, size_t out_stride,
                              double gain_start, double gain_end, size_t *out_count);
+
+/* ---- Density-Aligned Stitching (replaces the DAS block of plugin_process,
+ *      src/dsp_plugin.c:1283-2762, and gpu_cuda_trellis_das,
+ *      include/gpu_compute.h) ---- */
+
+/* One chunk of `nch` channels through segment-parallel SDM and stitching.
+ * Requires dsdgpu_sdm_setup with num_contexts >= nch: contexts [0, nch) are
+ * the channels' persistent SDM states, used and carried like the reference's
+ * (the last segment's state is copied back).  d_fir[c * fir_stride ...] holds
+ * `count` doubles of channel c; the stitched decisions go to
+ * d_out[c * out_stride ...] and *out_count receives their number.  When
+ * h_stitch_pos is not NULL it receives up to max_segs seam offsets (entry s
+ * for boundary s; 0 where there is none). */
+int dsdgpu_das_process(dsdgpu_context_t *ctx, const dsdgpu_das_params_t *p, int nch,
+                       const double *d_fir, size_t fir_stride, size_t count,
+                       uint8_t *d_out, size_t out_stride, size_t *out_count,
+                       int *h_stitch_pos, int max_segs);
 
 /* Best candidate's integrator state (sdm_state_distance's input,
  * src/trellis.c:1094-1109) and the counters conv_fail, cands_collapse,

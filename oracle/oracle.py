@@ -163,6 +163,32 @@ def ref_lib(wide: bool = False):
     return _cache[key]
 
 
+class DasCfg(C.Structure):
+    _fields_ = [("seg_len", C.c_int), ("nsegs", C.c_int), ("seed_mode", C.c_int),
+                ("reposition", C.c_int)]
+
+
+def das_run(order, a, g, depth, cands, lat, state_limit, fir: np.ndarray, seg_len=0, nsegs=0,
+            seed_mode=0, reposition=True, nthreads=None):
+    """DAS over one chunk; fir is [nch, count] float64.  Returns (bits [nch, n],
+    stitch positions per segment, segment starts)."""
+    L = oracle_lib().lib
+    fir = np.ascontiguousarray(np.atleast_2d(fir), np.float64)
+    nch, count = fir.shape
+    aa = np.zeros(10); aa[:order] = a[:order]
+    gg = np.zeros(10); gg[:order] = g[:order]
+    cfg = DasCfg(seg_len, nsegs, seed_mode, int(reposition))
+    outs = [np.zeros(count + 16, np.uint8) for _ in range(nch)]
+    fps = (_dp * nch)(*[fir[c].ctypes.data_as(_dp) for c in range(nch)])
+    ops = (_u8p * nch)(*[o.ctypes.data_as(_u8p) for o in outs])
+    smax = max(1, (count // seg_len) if seg_len > 0 else nsegs)
+    sp = (C.c_int * smax)()
+    ss = (C.c_size_t * smax)()
+    n = L.ora_das_run(order, _ptr(aa, _dp), _ptr(gg, _dp), depth, cands, lat, float(state_limit),
+                      C.byref(cfg), fps, count, nch, ops, sp, ss, nthreads or os.cpu_count() or 1)
+    return np.stack([o[:n] for o in outs]), list(sp), list(ss)
+
+
 def _bind_oracle_extras(L):
     L.ora_sdm_process_bits.restype = C.c_size_t
     L.ora_sdm_process_bits.argtypes = [C.c_void_p, _dp, _u8p, C.c_size_t]
@@ -179,6 +205,11 @@ def _bind_oracle_extras(L):
     L.ora_engine_fir.argtypes = [C.c_uint, C.c_uint, _fp, C.c_size_t, C.c_int,
                                  C.c_double, C.c_double, C.c_int, _dp]
     L.ora_sdm_run_jobs.restype = C.c_int
+    L.ora_das_run.restype = C.c_size_t
+    L.ora_das_run.argtypes = [C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double,
+                              C.POINTER(DasCfg), C.POINTER(_dp), C.c_size_t, C.c_int,
+                              C.POINTER(_u8p), C.POINTER(C.c_int), C.POINTER(C.c_size_t),
+                              C.c_int]
 
 
 def sdm(order, a, g, depth, cands, lat, state_limit=0.0) -> Sdm:

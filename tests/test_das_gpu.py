@@ -1,0 +1,69 @@
+"""GPU Density-Aligned Stitching vs the oracle's restatement: the stitched
+decision streams and the chosen seams must be identical (bit-exact), for both
+seeding modes, several channels, and a quiet boundary that triggers the RMS
+reposition."""
+import numpy as np
+import pytest
+
+from signals import multitone, uniform_noise
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _run(oracle, f, depth, K, lat, fir, **kw):
+    from foo_dsd_trellis_gb300.das import DasChannels
+    want, wseams, _ = oracle.das_run(f.order, np.array(f.a), np.array(f.g), depth, K, lat, 0.0,
+                                     fir, **kw)
+    d = DasChannels(f.order, f.a, f.g, depth, K, lat, num_channels=fir.shape[0])
+    got, seams = d.process_chunk(torch.from_numpy(np.ascontiguousarray(fir)).cuda(), **kw)
+    got = got.cpu().numpy()
+    return want, wseams, got, seams
+
+
+def _ntf(name, rate):
+    from foo_dsd_trellis_gb300 import ntf
+    return ntf.get_filter(name, rate)
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["full_parallel", "seg0_first"])
+def test_das_small(oracle, mode):
+    f = _ntf("clans-6", 5644800)
+    x = np.stack([multitone(80000, 3) * 2.0, multitone(80000, 4) * 1.5])
+    want, ws, got, gs = _run(oracle, f, 16, 8, 16, x, nsegs=7, seed_mode=mode)
+    assert got.shape == want.shape
+    assert list(gs) == list(ws)
+    bad = np.nonzero(got != want)
+    assert bad[0].size == 0, f"mismatch at {list(zip(*bad))[:5]}"
+
+
+def test_das_k32_depth64_lat128(oracle):
+    """The DSD128 configuration's trellis (K=32, depth 64, lat 128), overlap
+    8192, 32768-sample nominal segments."""
+    f = _ntf("clans-7", 6144000)
+    x = np.stack([multitone(32768 * 6 + 1234, 8), multitone(32768 * 6 + 1234, 9)])
+    want, ws, got, gs = _run(oracle, f, 64, 32, 128, x, seg_len=32768, seed_mode=0)
+    assert got.shape == want.shape
+    assert list(gs) == list(ws)
+    assert np.array_equal(got, want)
+
+
+def test_das_quiet_boundary_reposition(oracle):
+    """A near-silent stretch around a seg>=2 boundary moves it (RMS search)."""
+    f = _ntf("clans-5", 2822400)
+    n = 120000
+    x = multitone(n, 12) * 2.0
+    x[55000:65000] = uniform_noise(10000, 5, 1e-4)    # quiet around the boundary at 60000
+    want, ws, got, gs = _run(oracle, f, 16, 4, 16, x[None, :], nsegs=6, seed_mode=1)
+    assert list(gs) == list(ws)
+    assert np.array_equal(got, want)
+
+
+def test_das_single_segment_is_plain_sdm(oracle):
+    f = _ntf("clans-6", 5644800)
+    x = multitone(30000, 21)[None, :]
+    want, ws, got, gs = _run(oracle, f, 32, 16, 32, x, nsegs=1, seed_mode=0)
+    ref = oracle.sdm(f.order, np.array(f.a), np.array(f.g), 32, 16, 32)
+    plain = oracle.sdm_bits(ref, x[0])
+    assert np.array_equal(got[0], plain)
+    assert np.array_equal(want[0], plain)
