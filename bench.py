@@ -1,0 +1,333 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 PCM -> DSD hot path on its headline workload.
+
+Workload (one step): DSD128 stereo, 10 s of 48 kHz float32 PCM (31 log-spaced
+tones at -20 dBFS plus pink noise at -30 dBFS, seeded) -> boxcar + 7-stage
+half-band FIR chain to 6.144 MHz with the PCM gain and soft clip -> trellis
+SDM (CLANS-7 order-7 NTF, K = 32, depth 64, lat 128) over 65,536-sample DAS
+segments (overlap 8192, full-parallel seeding) -> density-aligned stitching
+-> DoP framing.  The metric is output DSD samples per second over both
+channels (and x realtime).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+`--impl reference` times the reference's CPU algorithm for this path (the
+oracle's C port on this host's cores; the reference's own trellis.c is built
+from source only where its tree is present, and never on an aarch64 GPU host)
+on a bounded slice of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "trellis SDM DSD Msamples/s & xRT at DSD128 bit-exact; batched vs plain; adjoint ms"
+UNIT = "DSD Msamples/s"
+WL = dict(workload="dsd128_das_stereo_10s_multitone_pink", fs_in=48000, fs_out=6144000,
+          channels=2, seconds=10.0, ntf="clans-7", ntf_order=7, cands=32, depth=64, lat=128,
+          das_seg_len=65536, das_overlap=64 * 128, seed_mode="full_parallel", output="dop",
+          boxcar_taps=8, soft_clip=True, seed=1001)
+FP64_OPS_PER_CAND_SAMPLE = 5 * WL["ntf_order"] + 6   # (2N+1) mul + (3N+5) add
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--seconds", type=float, default=WL["seconds"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(pcm, seconds_sample: float, nthreads: int | None = None) -> dict:
+    """The oracle's C port of the same path (FP64 FIR restatement, trellis SDM
+    port bit-identical to the reference's trellis.c, DAS restatement, DoP) on a
+    leading slice of the workload, on this host's cores."""
+    import numpy as np
+    from oracle import oracle as O
+    from foo_dsd_trellis_gb300 import ntf
+    O.build()
+    f = ntf.get_filter(WL["ntf"], WL["fs_out"])
+    frames = int(seconds_sample * WL["fs_in"])
+    x = pcm[:, :frames]
+    from foo_dsd_trellis_gb300.pipeline import PCM_FIR_GAIN
+    nthreads = nthreads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    fir = np.stack([O.engine_fir(WL["fs_in"], WL["fs_out"], x[c], boxcar_taps=WL["boxcar_taps"],
+                                 g_start=PCM_FIR_GAIN, g_end=PCM_FIR_GAIN, soft_clip=True)
+                    for c in range(x.shape[0])])
+    bits, _, _ = O.das_run(f.order, np.array(f.a), np.array(f.g), WL["depth"], WL["cands"],
+                           WL["lat"], 0.0, fir, seg_len=WL["das_seg_len"], seed_mode=0,
+                           reposition=True, nthreads=nthreads)
+    for c in range(bits.shape[0]):
+        O.dop_pack_bits(bits[c], 0)
+    dt = time.perf_counter() - t0
+    n_out = bits.shape[0] * bits.shape[1]
+    return {"value": n_out / dt / 1e6, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"first {seconds_sample:g} s of the workload ({x.shape[0]} ch, "
+                      f"{n_out} DSD samples): FP64 FIR restatement + trellis SDM port + DAS + DoP",
+            "seconds": dt}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+    from foo_dsd_trellis_gb300 import signals
+    pcm = signals.dsd128_multitone_pink(args.seconds, WL["fs_in"], WL["channels"], WL["seed"])
+    sample_s = 0.5
+    for _ in range(args.warmup):
+        cpu_baseline(pcm, 0.05)
+    vals, secs = [], []
+    info = None
+    for _ in range(args.steps):
+        info = cpu_baseline(pcm, sample_s)
+        vals.append(info["value"])
+        secs.append(info["seconds"])
+    v = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * float(np.mean(secs)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": dict(WL, cpu_sample_seconds=sample_s),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": "port",
+                             "sample": info["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def plain_form(f, x_dev, seg_in, overlap, lat, nseg=2):
+    """The one-segment-per-launch form: the same SDM kernel, one DAS segment
+    per launch, launched back to back."""
+    import torch
+    from foo_dsd_trellis_gb300.sdm import SegmentSpec, TrellisSdm
+    g = TrellisSdm(f.order, f.a, f.g, WL["depth"], WL["cands"], lat, num_contexts=nseg + 1)
+    specs = [SegmentSpec(x_dev[i * seg_in:(i + 1) * seg_in].contiguous(), channel=i,
+                         discard=overlap - lat, seed_from=nseg) for i in range(nseg)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in specs:
+        g.segments([s])
+    dt = time.perf_counter() - t0
+    g.close()
+    return nseg * seg_in / dt
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    from foo_dsd_trellis_gb300 import ntf, signals
+    from foo_dsd_trellis_gb300.pipeline import OUT_DOP, PCM_FIR_GAIN, Encoder, FULL_PARALLEL
+
+    f = ntf.get_filter(WL["ntf"], WL["fs_out"])
+    # weak scaling: every rank converts its own stereo stream (own seed)
+    pcm = signals.dsd128_multitone_pink(args.seconds, WL["fs_in"], WL["channels"],
+                                        WL["seed"] + 2 * rank)
+    nch, frames = pcm.shape
+    enc = Encoder(WL["fs_in"], WL["fs_out"], nch, f, WL["depth"], WL["cands"], WL["lat"],
+                  seg_len=WL["das_seg_len"], seed_mode=FULL_PARALLEL, reposition=True,
+                  boxcar_taps=WL["boxcar_taps"], soft_clip=WL["soft_clip"],
+                  output_format=OUT_DOP, device=local)
+    d_pcm = torch.from_numpy(pcm).cuda()
+    d_out = torch.empty(enc.out_capacity(frames) + 64, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")   # > L2 (129 MB)
+    lib_stream = torch.cuda.ExternalStream(enc.stream_ptr)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        enc.process(d_pcm, d_out)
+    torch.cuda.synchronize()
+
+    fp64_peak = enc.probe_fp64_gops()
+    clocks = ClockSampler(local)
+    launches0 = enc.launches()
+    sdm0, _ = enc.sdm_work()
+    step_ms, sdm_ms = [], []
+    n_out = nbytes = 0
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    for _ in range(args.steps):
+        flush.fill_(1)                      # evict L2 between steps (outside the events)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(lib_stream)
+        n_out, nbytes = enc.process(d_pcm, d_out)
+        e1.record(lib_stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        sdm_ms.append(enc.stage_ms()["sdm"])
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier()
+    launches = enc.launches() - launches0
+    sdm_samples = (enc.sdm_work()[0] - sdm0) / args.steps
+    stages = enc.stage_ms()
+
+    total_s = sum(step_ms) / 1000.0
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    out_samples_step = n_out * nch                 # both channels
+    value = out_samples_step * args.steps * world / total_s / 1e6
+    xrt = (n_out / WL["fs_out"]) * args.steps / total_s
+
+    # end to end through the host-buffer C-ABI call (pinned host memory)
+    h_pcm = torch.from_numpy(pcm).pin_memory().numpy()
+    h_out = torch.empty(enc.out_capacity(frames) + 64, dtype=torch.uint8).pin_memory().numpy()
+    enc.process_host(h_pcm, h_out)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ns, nb = enc.process_host(h_pcm, h_out)
+    e2e_s = time.perf_counter() - t0
+    e2e_value = ns * nch * args.steps * world / e2e_s / 1e6
+
+    # roofline of the dominant kernel: the persistent trellis SDM launch
+    sdm_s = statistics.mean(sdm_ms) / 1000.0
+    flops = sdm_samples * WL["cands"] * FP64_OPS_PER_CAND_SAMPLE
+    achieved = flops / sdm_s / 1e12
+    peak = fp64_peak / 1000.0
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None, "kernel": "sdm_jobs_kernel<7>",
+                "peak_source": "DADD/DMUL issue rate measured in this run (dsdgpu_probe_fp64); "
+                               "MEASURED_PEAKS.json has no FP64 entry",
+                "algorithmic_flops_per_launch": flops,
+                "sdm_input_samples_per_launch": sdm_samples,
+                "flops_per_sample": WL["cands"] * FP64_OPS_PER_CAND_SAMPLE}
+    prof = os.path.join(ROOT, "profiles", "sdm_dram_traffic.json")
+    if os.path.exists(prof):
+        try:
+            with open(prof) as fh:
+                roofline["traffic"] = json.load(fh).get("bytes_per_launch_scaled")
+        except (OSError, ValueError):
+            pass
+
+    plain = None
+    if not args.no_plain and rank == 0:
+        seg_in = WL["das_seg_len"] + 2 * WL["das_overlap"]
+        t = torch.arange(2 * seg_in, dtype=torch.float64, device="cuda")
+        gen = torch.Generator(device="cuda").manual_seed(7)
+        x_dev = 0.3 * torch.sin(t * 0.0013) + 0.05 * torch.rand(2 * seg_in, dtype=torch.float64,
+                                                                 device="cuda", generator=gen)
+        plain_sps = plain_form(f, x_dev, seg_in, WL["das_overlap"], WL["lat"])
+        batched_sps = sdm_samples / sdm_s
+        plain = {"msamples_per_s": plain_sps / 1e6, "batched_msamples_per_s": batched_sps / 1e6,
+                 "batched_over_plain": batched_sps / plain_sps,
+                 "note": "SDM input samples/s; plain = one 81,920-sample DAS segment per launch"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(pcm, 2.0)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1000 * total_s / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": dict(WL, l2="512 MiB written between timed steps (outside the events)",
+                               fir_gain=PCM_FIR_GAIN),
+                "xrt": xrt,
+                "e2e": {"value": e2e_value, "unit": UNIT,
+                        "h2d_bytes_per_step": int(pcm.nbytes), "d2h_bytes_per_step": int(nb)},
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+                "gpu_launches": int(launches), "stages_ms": stages, "plain": plain,
+                "fp64_peak_gops": fp64_peak}
+        print(json.dumps(line), flush=True)
+    enc.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -52,6 +52,15 @@ class DasParams(C.Structure):
                 ("reposition", C.c_int)]
 
 
+class PipelineParams(C.Structure):
+    _fields_ = [("fir", FirParams), ("sdm", SdmParams), ("das", DasParams),
+                ("output_format", C.c_int)]
+
+
+OUT_BITS = 0
+OUT_DOP = 1
+OUT_NATIVE = 2
+
 DAS_FULL_PARALLEL = 0
 DAS_SEG0_FIRST = 1
 
@@ -66,6 +75,8 @@ SIGNATURES = {
     "dsdgpu_destroy": (None, [_vp]),
     "dsdgpu_last_error": (C.c_char_p, [_vp]),
     "dsdgpu_synchronize": (C.c_int, [_vp]),
+    "dsdgpu_launch_count": (C.c_int, [_vp, C.POINTER(C.c_uint64)]),
+    "dsdgpu_sdm_work": (C.c_int, [_vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "dsdgpu_sdm_setup": (C.c_int, [_vp, C.POINTER(SdmParams), C.c_int]),
     "dsdgpu_sdm_reset": (C.c_int, [_vp, C.c_int]),
     "dsdgpu_sdm_process": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp, _sz, _szp]),
@@ -77,6 +88,17 @@ SIGNATURES = {
                                    C.POINTER(C.c_uint64)]),
     "dsdgpu_das_process": (C.c_int, [_vp, C.POINTER(DasParams), C.c_int, _vp, _sz, _sz, _vp,
                                      _sz, _szp, C.POINTER(C.c_int), C.c_int]),
+    "dsdgpu_pack_dop": (C.c_int, [_vp, C.c_int, _vp, _sz, _sz, _vp, C.c_int,
+                                  C.POINTER(C.c_int)]),
+    "dsdgpu_pack_native": (C.c_int, [_vp, C.c_int, _vp, _sz, _sz, _vp, _sz]),
+    "dsdgpu_pipeline_setup": (C.c_int, [_vp, C.POINTER(PipelineParams), C.c_int]),
+    "dsdgpu_pipeline_process": (C.c_int, [_vp, _vp, _sz, _sz, C.c_double, C.c_double, _vp, _sz,
+                                          _szp, _szp]),
+    "dsdgpu_pipeline_process_host": (C.c_int, [_vp, _vp, _sz, C.c_double, C.c_double, _vp, _sz,
+                                               _szp, _szp]),
+    "dsdgpu_stage_times": (C.c_int, [_vp, C.POINTER(C.c_float)]),
+    "dsdgpu_get_stream": (C.c_int, [_vp, C.POINTER(_vp)]),
+    "dsdgpu_probe_fp64": (C.c_int, [_vp, C.POINTER(C.c_double)]),
     "dsdgpu_fir_setup": (C.c_int, [_vp, C.POINTER(FirParams), C.c_int]),
     "dsdgpu_fir_reset": (C.c_int, [_vp]),
     "dsdgpu_fir_process": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp, _sz,

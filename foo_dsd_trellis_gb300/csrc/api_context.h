@@ -18,6 +18,9 @@ struct dsdgpu_context {
   int max_blocks = 0;
   cudaStream_t stream = nullptr;
   std::string last_error;
+  unsigned long long launches = 0;   // kernels this context has launched
+  unsigned long long sdm_samples = 0;       // SDM input samples run so far
+  unsigned long long sdm_last_samples = 0;  // ... by the last SDM launch
 
   int* d_counter = nullptr;   // persistent-kernel job counter
   int* d_status = nullptr;    // device status word (bounded walks/waits)
@@ -54,6 +57,19 @@ struct dsdgpu_context {
   double* d_das_qfir = nullptr;    size_t das_qfir_cap = 0;
   bool das_qfir_ready = false;
 
+  // whole-path pipeline
+  bool pipe_ready = false;
+  dsdgpu_pipeline_params_t pipe{};
+  int pipe_nch = 0;
+  int dop_phase = 0;
+  static constexpr int kEvents = 6;
+  cudaEvent_t ev[kEvents] = {};
+  bool ev_ready = false;
+  bool timing_das = false;        // record events around the segment SDM launch
+  float stage_ms[5] = {0, 0, 0, 0, 0};
+  void* d_io = nullptr;           // device staging of the host-buffer entry point
+  size_t io_bytes = 0;
+
   // reusable device scratch for the host-buffer entry points
   void* d_scratch = nullptr;
   size_t scratch_bytes = 0;
@@ -71,6 +87,12 @@ struct dsdgpu_context {
     if (d_scratch) cudaFree(d_scratch);
     if (d_fir_hist) cudaFree(d_fir_hist);
     d_fir_hist = nullptr;
+    if (d_io) cudaFree(d_io);
+    d_io = nullptr;
+    io_bytes = 0;
+    if (ev_ready)
+      for (int i = 0; i < kEvents; i++) cudaEventDestroy(ev[i]);
+    ev_ready = false;
     void* das[] = {d_das_bits, d_das_est, d_das_i64, d_das_f64, d_das_bp, d_das_tasks,
                    d_das_pieces, d_das_segbuf, d_das_qfir};
     for (void* p : das)

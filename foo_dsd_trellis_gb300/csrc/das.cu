@@ -441,7 +441,7 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
       cudaMemcpyAsync(c->d_das_i64, centers.data(), sizeof(long long) * centers.size(),
                       cudaMemcpyHostToDevice, c->stream);
       das_rms_kernel<<<(unsigned)((centers.size() + 127) / 128), 128, 0, c->stream>>>(
-          d_fir, c->d_das_i64, (int)centers.size(), (int)win, c->d_das_f64);
+          d_fir, c->d_das_i64, (int)centers.size(), (int)win, c->d_das_f64); c->launches++;
       std::vector<double> cur(centers.size());
       cudaMemcpyAsync(cur.data(), c->d_das_f64, sizeof(double) * cur.size(), cudaMemcpyDeviceToHost, c->stream);
       rc = c->check_status();
@@ -472,7 +472,7 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
           cudaMemcpyAsync(c->d_das_i64, cand.data(), sizeof(long long) * cand.size(),
                           cudaMemcpyHostToDevice, c->stream);
           das_rms_kernel<<<(unsigned)((cand.size() + 127) / 128), 128, 0, c->stream>>>(
-              d_fir, c->d_das_i64, (int)cand.size(), (int)win, c->d_das_f64);
+              d_fir, c->d_das_i64, (int)cand.size(), (int)win, c->d_das_f64); c->launches++;
           cudaMemcpyAsync(rms.data(), c->d_das_f64, sizeof(double) * rms.size(), cudaMemcpyDeviceToHost, c->stream);
           rc = c->check_status();
           if (rc) return rc;
@@ -587,7 +587,7 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
       cudaMemcpyAsync(c->d_das_i64, st.data(), sizeof(long long) * S, cudaMemcpyHostToDevice, c->stream);
       das_estimate_kernel<<<(nch + 31) / 32, 32, 0, c->stream>>>(
           c->sdm, d_fir, fir_stride, c->d_ctx, 0, c->d_das_i64, S, (long long)count,
-          c->d_das_est, nch);
+          c->d_das_est, nch); c->launches++;
     }
     // seg2+ copy the persistent context after seg0: snapshot it so the
     // parallel launch reads a context nothing writes
@@ -604,7 +604,7 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
       c->draining[snap0 + ch] = c->draining[ch];
     }
     das_seed_from_best_kernel<<<nch, 128, 0, c->stream>>>(c->d_ctx, snap0, S, c->d_das_est, nch,
-                                                         c->sdm.order);
+                                                         c->sdm.order); c->launches++;
   }
   {
     std::vector<SdmJob> jp;
@@ -613,7 +613,9 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
         if (s == 0) add_job(jp, ch, 0, ch, -1, false, ch);
         else add_job(jp, ch, s, temp0 + ch * S + s, snap0 + ch, true, snap0 + ch);
       }
+    if (c->timing_das) cudaEventRecord(c->ev[2], c->stream);
     rc = c->run_jobs(jp);
+    if (c->timing_das) cudaEventRecord(c->ev[3], c->stream);
     if (rc) return rc;
   }
 
@@ -698,7 +700,7 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
       cudaFuncSetAttribute(das_seam_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (maxL > 32 * kSeamThreads) return c->fail(DSDGPU_ERR_UNSUPPORTED, "overlap too long for the seam kernel");
     das_seam_kernel<<<(unsigned)tasks.size(), kSeamThreads, smem, c->stream>>>(
-        c->d_das_tasks, (int)tasks.size(), c->d_das_qfir, lat, c->d_das_bp);
+        c->d_das_tasks, (int)tasks.size(), c->d_das_qfir, lat, c->d_das_bp); c->launches++;
   }
 
   // ---- assembly ----
@@ -743,7 +745,7 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
     const dim3 grid(64, (unsigned)pieces.size());
     das_assemble_kernel<<<grid, 256, 0, c->stream>>>(c->d_das_pieces, (int)pieces.size(),
                                                       c->d_das_bp, d_out, out_stride, nch, S,
-                                                      c->d_das_segbuf);
+                                                      c->d_das_segbuf); c->launches++;
   }
 
   // ---- state carry: persistent <- last temp (src/dsp_plugin.c:2715-2725) ----

@@ -118,11 +118,16 @@ int dsdgpu_context::run_jobs(const std::vector<SdmJob>& jobs) {
     if (e != cudaSuccess) return cuda_fail(e, "job table allocation");
     jobs_cap = n;
   }
+  unsigned long long steps = 0;
+  for (const SdmJob& j : jobs) steps += (unsigned long long)j.n_in;
+  sdm_samples += steps;
+  sdm_last_samples = steps;
   cudaError_t e = cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(SdmJob) * (size_t)n,
                                   cudaMemcpyHostToDevice, stream);
   if (e != cudaSuccess) return cuda_fail(e, "job table upload");
   if (launch_sdm_jobs(sdm, d_jobs, n, d_counter, d_ctx, d_status, max_blocks, stream) != 0)
     return cuda_fail(cudaGetLastError(), "sdm kernel launch");
+  launches++;
   return check_status();
 }
 
@@ -191,6 +196,19 @@ void dsdgpu_destroy(dsdgpu_context_t* c) {
   delete c;
 }
 
+int dsdgpu_sdm_work(const dsdgpu_context_t* c, uint64_t* total_samples, uint64_t* last_launch) {
+  if (!c) return DSDGPU_ERR_ARG;
+  if (total_samples) *total_samples = c->sdm_samples;
+  if (last_launch) *last_launch = c->sdm_last_samples;
+  return DSDGPU_OK;
+}
+
+int dsdgpu_launch_count(const dsdgpu_context_t* c, uint64_t* count) {
+  if (!c || !count) return DSDGPU_ERR_ARG;
+  *count = c->launches;
+  return DSDGPU_OK;
+}
+
 const char* dsdgpu_last_error(const dsdgpu_context_t* c) {
   return c ? c->last_error.c_str() : "no context";
 }
@@ -229,7 +247,7 @@ int dsdgpu_sdm_setup(dsdgpu_context_t* c, const dsdgpu_sdm_params_t* p, int num_
   c->das_persistent = 0;
   c->pending.assign(num_contexts, 0);
   c->draining.assign(num_contexts, 0);
-  sdm_ctx_init_kernel<<<num_contexts, 256, 0, c->stream>>>(c->d_ctx, 0, num_contexts, 0);
+  sdm_ctx_init_kernel<<<num_contexts, 256, 0, c->stream>>>(c->d_ctx, 0, num_contexts, 0); c->launches++;
   e = cudaGetLastError();
   if (e != cudaSuccess) return c->cuda_fail(e, "context init launch");
   c->sdm_ready = true;
@@ -243,7 +261,7 @@ int dsdgpu_sdm_reset(dsdgpu_context_t* c, int channel) {
   cudaSetDevice(c->device);
   const int first = channel < 0 ? 0 : channel;
   const int count = channel < 0 ? c->nctx : 1;
-  sdm_ctx_init_kernel<<<count, 256, 0, c->stream>>>(c->d_ctx, first, count, 1);
+  sdm_ctx_init_kernel<<<count, 256, 0, c->stream>>>(c->d_ctx, first, count, 1); c->launches++;
   for (int i = first; i < first + count; i++) { c->pending[i] = 0; c->draining[i] = 0; }
   return c->check_status();
 }
@@ -298,7 +316,7 @@ int dsdgpu_sdm_process_host(dsdgpu_context_t* c, int first, int nch, const doubl
   rc = dsdgpu_sdm_process(c, first, nch, d_in, count, count, d_bits, count, oc.data());
   if (rc) return rc;
   // decisions are written at the start of each channel's row
-  bits_to_float_kernel<<<256, 256, 0, c->stream>>>(d_bits, d_f, tot);
+  bits_to_float_kernel<<<256, 256, 0, c->stream>>>(d_bits, d_f, tot); c->launches++;
   for (int ch = 0; ch < nch; ch++) {
     if (out_counts) out_counts[ch] = oc[ch];
     if (oc[ch] == 0) continue;
@@ -350,7 +368,7 @@ int dsdgpu_sdm_copy_state(dsdgpu_context_t* c, int dst, int src) {
   cudaError_t e = cudaMemcpyAsync(c->d_ctx + dst, c->d_ctx + src, sizeof(SdmCtx),
                                   cudaMemcpyDeviceToDevice, c->stream);
   if (e != cudaSuccess) return c->cuda_fail(e, "context copy");
-  zero_counters_kernel<<<1, 1, 0, c->stream>>>(c->d_ctx, dst);
+  zero_counters_kernel<<<1, 1, 0, c->stream>>>(c->d_ctx, dst); c->launches++;
   c->pending[dst] = c->pending[src];
   c->draining[dst] = c->draining[src];
   return c->check_status();

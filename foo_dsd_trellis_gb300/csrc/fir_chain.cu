@@ -316,8 +316,8 @@ int dsdgpu_fir_process_async(dsdgpu_context_t* c, int first, int nch, const floa
   float* hist = c->d_fir_hist + (size_t)first * kHistory;
   fir_chain_kernel<<<grid, kFirThreads, c->fir_smem, c->stream>>>(
       d_in, in_stride, (long long)count, hist, d_out, out_stride, gs, step, apply,
-      c->fir_params.soft_clip);
-  fir_history_kernel<<<nch, 128, 0, c->stream>>>(d_in, in_stride, (long long)count, hist);
+      c->fir_params.soft_clip); c->launches++;
+  fir_history_kernel<<<nch, 128, 0, c->stream>>>(d_in, in_stride, (long long)count, hist); c->launches++;
   e = cudaGetLastError();
   if (e != cudaSuccess) return c->cuda_fail(e, "fir launch");
   return DSDGPU_OK;

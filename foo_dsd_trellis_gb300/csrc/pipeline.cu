@@ -1,0 +1,156 @@
+// Whole-path entry points: PCM -> FIR chain + engine glue -> segment-parallel
+// trellis SDM with Density-Aligned Stitching -> DoP / native / decision bytes.
+// This is the GPU counterpart of the plugin's PCM path with DAS (reference
+// src/dsp_plugin.c:2990-3216 for PCM in / DoP out, src/dsp_plugin.c:1283-2945
+// for the DAS phases), one chunk per call.  Stage timings are taken with CUDA
+// events on the context's stream.
+#include "api_context.h"
+
+#include <cstring>
+
+extern "C" {
+
+int dsdgpu_pipeline_setup(dsdgpu_context_t* c, const dsdgpu_pipeline_params_t* p, int nch) {
+  if (!c || !p || nch < 1) return DSDGPU_ERR_ARG;
+  if (p->output_format < DSDGPU_OUT_BITS || p->output_format > DSDGPU_OUT_NATIVE)
+    return c->fail(DSDGPU_ERR_ARG, "bad output format");
+  int rc = dsdgpu_sdm_setup(c, &p->sdm, nch);
+  if (rc) return rc;
+  rc = dsdgpu_fir_setup(c, &p->fir, nch);
+  if (rc) return rc;
+  c->pipe = *p;
+  c->pipe_nch = nch;
+  c->pipe_ready = true;
+  c->dop_phase = 0;
+  if (!c->ev_ready) {
+    for (int i = 0; i < dsdgpu_context::kEvents; i++) cudaEventCreate(&c->ev[i]);
+    c->ev_ready = true;
+  }
+  return DSDGPU_OK;
+}
+
+int dsdgpu_pipeline_process(dsdgpu_context_t* c, const float* d_pcm, size_t pcm_stride,
+                            size_t frames, double gain_start, double gain_end, uint8_t* d_out,
+                            size_t out_stride, size_t* out_samples, size_t* out_bytes) {
+  if (!c) return DSDGPU_ERR_ARG;
+  if (!c->pipe_ready) return c->fail(DSDGPU_ERR_STATE, "pipeline not set up");
+  if (frames > 0 && (!d_pcm || !d_out)) return c->fail(DSDGPU_ERR_ARG, "null buffer");
+  cudaSetDevice(c->device);
+  const int nch = c->pipe_nch;
+  const size_t n_fir = frames * (size_t)c->fir.ratio;
+  // device work buffers: FIR output (double) and stitched decisions
+  const size_t fir_bytes = (n_fir * sizeof(double) + 255) & ~(size_t)255;
+  const size_t bit_row = (n_fir + 255) & ~(size_t)255;
+  int rc = c->ensure_scratch(fir_bytes * (size_t)nch + bit_row * (size_t)nch + 256);
+  if (rc) return rc;
+  double* d_fir = (double*)c->d_scratch;
+  uint8_t* d_bits = (uint8_t*)c->d_scratch + fir_bytes * (size_t)nch;
+  const size_t fir_stride = fir_bytes / sizeof(double);
+
+  cudaEventRecord(c->ev[0], c->stream);
+  size_t fo = 0;
+  rc = dsdgpu_fir_process_async(c, 0, nch, d_pcm, pcm_stride, frames, d_fir, fir_stride,
+                                gain_start, gain_end, &fo);
+  if (rc) return rc;
+  cudaEventRecord(c->ev[1], c->stream);
+  size_t n = 0;
+  c->timing_das = true;
+  rc = dsdgpu_das_process(c, &c->pipe.das, nch, d_fir, fir_stride, fo, d_bits, bit_row, &n,
+                          nullptr, 0);
+  c->timing_das = false;
+  if (rc) return rc;
+  cudaEventRecord(c->ev[4], c->stream);
+  size_t nbytes = 0;
+  if (c->pipe.output_format == DSDGPU_OUT_DOP) {
+    int next = 0;
+    rc = dsdgpu_pack_dop(c, nch, d_bits, bit_row, n, d_out, c->dop_phase, &next);
+    if (rc) return rc;
+    c->dop_phase = next;
+    nbytes = (n / 16) * 3 * (size_t)nch;
+  } else if (c->pipe.output_format == DSDGPU_OUT_NATIVE) {
+    rc = dsdgpu_pack_native(c, nch, d_bits, bit_row, n, d_out, out_stride);
+    if (rc) return rc;
+    nbytes = ((n + 7) / 8) * (size_t)nch;
+  } else {
+    if (out_stride < n) return c->fail(DSDGPU_ERR_ARG, "output stride too small");
+    cudaMemcpy2DAsync(d_out, out_stride, d_bits, bit_row, n, (size_t)nch,
+                      cudaMemcpyDeviceToDevice, c->stream);
+    nbytes = n * (size_t)nch;
+  }
+  cudaEventRecord(c->ev[5], c->stream);
+  rc = c->check_status();
+  if (rc) return rc;
+  float ms[5] = {0, 0, 0, 0, 0};
+  cudaEventElapsedTime(&ms[0], c->ev[0], c->ev[1]);   // FIR
+  cudaEventElapsedTime(&ms[1], c->ev[2], c->ev[3]);   // segment SDM (last launch)
+  cudaEventElapsedTime(&ms[2], c->ev[1], c->ev[4]);   // DAS total
+  cudaEventElapsedTime(&ms[3], c->ev[4], c->ev[5]);   // pack
+  cudaEventElapsedTime(&ms[4], c->ev[0], c->ev[5]);   // whole step
+  memcpy(c->stage_ms, ms, sizeof ms);
+  if (out_samples) *out_samples = n;
+  if (out_bytes) *out_bytes = nbytes;
+  return DSDGPU_OK;
+}
+
+int dsdgpu_pipeline_process_host(dsdgpu_context_t* c, const float* h_pcm, size_t frames,
+                                 double gain_start, double gain_end, uint8_t* h_out,
+                                 size_t out_capacity, size_t* out_samples, size_t* out_bytes) {
+  if (!c) return DSDGPU_ERR_ARG;
+  if (!c->pipe_ready) return c->fail(DSDGPU_ERR_STATE, "pipeline not set up");
+  if (frames > 0 && (!h_pcm || !h_out)) return c->fail(DSDGPU_ERR_ARG, "null buffer");
+  cudaSetDevice(c->device);
+  const int nch = c->pipe_nch;
+  const size_t n_fir = frames * (size_t)c->fir.ratio;
+  // staging for the input and output on the device, kept across calls
+  const size_t in_bytes = (frames * (size_t)nch * sizeof(float) + 255) & ~(size_t)255;
+  const size_t out_row = (n_fir + 255) & ~(size_t)255;
+  const size_t need = in_bytes + out_row * (size_t)nch;
+  if (c->io_bytes < need) {
+    if (c->d_io) cudaFree(c->d_io);
+    c->d_io = nullptr;
+    c->io_bytes = 0;
+    cudaError_t e = cudaMalloc(&c->d_io, need);
+    if (e != cudaSuccess) return c->cuda_fail(e, "io staging allocation");
+    c->io_bytes = need;
+  }
+  float* d_pcm = (float*)c->d_io;
+  uint8_t* d_out = (uint8_t*)c->d_io + in_bytes;
+  cudaError_t e = cudaMemcpyAsync(d_pcm, h_pcm, frames * (size_t)nch * sizeof(float),
+                                  cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return c->cuda_fail(e, "pcm upload");
+  size_t n = 0, nb = 0;
+  int rc = dsdgpu_pipeline_process(c, d_pcm, frames, frames, gain_start, gain_end, d_out, out_row,
+                                   &n, &nb);
+  if (rc) return rc;
+  if (nb > out_capacity) return c->fail(DSDGPU_ERR_ARG, "host output buffer too small");
+  if (c->pipe.output_format == DSDGPU_OUT_NATIVE) {
+    const size_t rowb = (n + 7) / 8;
+    e = cudaMemcpy2DAsync(h_out, rowb, d_out, out_row, rowb, (size_t)nch, cudaMemcpyDeviceToHost,
+                          c->stream);
+  } else if (c->pipe.output_format == DSDGPU_OUT_BITS) {
+    e = cudaMemcpy2DAsync(h_out, n, d_out, out_row, n, (size_t)nch, cudaMemcpyDeviceToHost,
+                          c->stream);
+  } else {
+    e = cudaMemcpyAsync(h_out, d_out, nb, cudaMemcpyDeviceToHost, c->stream);
+  }
+  if (e != cudaSuccess) return c->cuda_fail(e, "output download");
+  rc = c->check_status();
+  if (rc) return rc;
+  if (out_samples) *out_samples = n;
+  if (out_bytes) *out_bytes = nb;
+  return DSDGPU_OK;
+}
+
+int dsdgpu_stage_times(const dsdgpu_context_t* c, float* ms5) {
+  if (!c || !ms5) return DSDGPU_ERR_ARG;
+  memcpy(ms5, c->stage_ms, sizeof c->stage_ms);
+  return DSDGPU_OK;
+}
+
+int dsdgpu_get_stream(const dsdgpu_context_t* c, void** stream) {
+  if (!c || !stream) return DSDGPU_ERR_ARG;
+  *stream = (void*)c->stream;
+  return DSDGPU_OK;
+}
+
+}  // extern "C"

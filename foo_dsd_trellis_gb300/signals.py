@@ -1,0 +1,62 @@
+"""Seeded synthetic PCM signals with the shapes of the conversion workloads:
+multitone (log-spaced tones at a fixed level with random phases), pink noise
+at a fixed RMS, a sine with TPDF dither, band-limited Gaussian noise.  The
+generator is numpy's PCG64 with seed 1000 + workload index, offset by the
+channel index."""
+from __future__ import annotations
+
+import numpy as np
+
+
+def db_to_amp(db: float) -> float:
+    return float(10.0 ** (db / 20.0))
+
+
+def pink_noise(n: int, rng: np.random.Generator, rms: float) -> np.ndarray:
+    """White Gaussian noise shaped to a 1/f power spectrum in the FFT domain."""
+    w = rng.standard_normal(n)
+    spec = np.fft.rfft(w)
+    f = np.arange(len(spec), dtype=np.float64)
+    f[0] = 1.0
+    spec /= np.sqrt(f)
+    spec[0] = 0.0
+    x = np.fft.irfft(spec, n)
+    return x * (rms / np.sqrt(np.mean(x * x)))
+
+
+def multitone(n: int, fs: float, rng: np.random.Generator, ntones: int = 31, f_lo: float = 20.0,
+              f_hi: float = 20000.0, level_db: float = -20.0) -> np.ndarray:
+    freqs = np.geomspace(f_lo, f_hi, ntones)
+    ph = rng.random(ntones) * 2 * np.pi
+    t = np.arange(n) / fs
+    amp = db_to_amp(level_db)
+    x = np.zeros(n)
+    for f, p in zip(freqs, ph):
+        x += amp * np.sin(2 * np.pi * f * t + p)
+    return x
+
+
+def dsd128_multitone_pink(seconds: float, fs: int = 48000, channels: int = 2,
+                          seed: int = 1001) -> np.ndarray:
+    """31 log-spaced tones 20 Hz-20 kHz at -20 dBFS each with random phases plus
+    pink noise at -30 dBFS: the DSD128 DAS workload's input, float32 [ch, n]."""
+    n = int(round(seconds * fs))
+    out = np.empty((channels, n), np.float32)
+    for c in range(channels):
+        rng = np.random.Generator(np.random.PCG64(seed + c))
+        out[c] = (multitone(n, fs, rng) + pink_noise(n, rng, db_to_amp(-30.0))).astype(np.float32)
+    return out
+
+
+def sine_tpdf(seconds: float, fs: int = 44100, channels: int = 2, f0: float = 997.0,
+              level_db: float = -6.0, dither_db: float = -110.0, seed: int = 1000) -> np.ndarray:
+    """A sine at level_db plus TPDF dither at dither_db RMS, float32 [ch, n]."""
+    n = int(round(seconds * fs))
+    t = np.arange(n) / fs
+    out = np.empty((channels, n), np.float32)
+    for c in range(channels):
+        rng = np.random.Generator(np.random.PCG64(seed + c))
+        tpdf = rng.random(n) - rng.random(n)                  # RMS 1/sqrt(6)
+        d = tpdf * db_to_amp(dither_db) * np.sqrt(6.0)
+        out[c] = (db_to_amp(level_db) * np.sin(2 * np.pi * f0 * t) + d).astype(np.float32)
+    return out

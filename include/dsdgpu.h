@@ -96,6 +96,20 @@ typedef struct {
     int     reposition;  /* 1: move quiet boundaries of seg >= 2 (RMS search) */
 } dsdgpu_das_params_t;
 
+/* Output formats of the whole-path pipeline. */
+#define DSDGPU_OUT_BITS    0   /* one byte per decision, [channel][sample] */
+#define DSDGPU_OUT_DOP     1   /* DoP 24-bit frames, [frame][channel][3] */
+#define DSDGPU_OUT_NATIVE  2   /* MSB-first DSD bytes, [channel][byte] */
+
+/* Whole-path parameters: the FIR chain with its glue, the trellis SDM, DAS,
+ * and the output format. */
+typedef struct {
+    dsdgpu_fir_params_t fir;
+    dsdgpu_sdm_params_t sdm;
+    dsdgpu_das_params_t das;
+    int                 output_format;   /* DSDGPU_OUT_* */
+} dsdgpu_pipeline_params_t;
+
 /* ---- lifecycle (replaces gpu_create / gpu_destroy, include/gpu_compute.h:52-55) ---- */
 
 /* Create a context on CUDA device `device`.  *out is NULL on failure. */
@@ -103,6 +117,11 @@ int  dsdgpu_create(int device, dsdgpu_context_t **out);
 void dsdgpu_destroy(dsdgpu_context_t *ctx);
 /* Human-readable description of the last failure on this context. */
 const char *dsdgpu_last_error(const dsdgpu_context_t *ctx);
+/* Number of kernels this context has launched so far. */
+int  dsdgpu_launch_count(const dsdgpu_context_t *ctx, uint64_t *count);
+/* Input samples the trellis SDM has stepped through: in total, and in the
+ * last SDM launch (warm-up and overlap samples of DAS segments included). */
+int  dsdgpu_sdm_work(const dsdgpu_context_t *ctx, uint64_t *total_samples, uint64_t *last_launch);
 /* Wait for all work queued on the context's stream. */
 int  dsdgpu_synchronize(dsdgpu_context_t *ctx);
 
@@ -185,6 +204,52 @@ int dsdgpu_das_process(dsdgpu_context_t *ctx, const dsdgpu_das_params_t *p, int 
                        const double *d_fir, size_t fir_stride, size_t count,
                        uint8_t *d_out, size_t out_stride, size_t *out_count,
                        int *h_stitch_pos, int max_segs);
+
+/* ---- bit packing (replaces dop_pack_i24 / bits_pack, include/dop.h:38-46) ---- */
+
+/* DoP: `n` decisions per channel (d_bits[c * bits_stride ...]) become n / 16
+ * frames of 3 bytes [bits 7..0, bits 15..8, marker] per channel, channels
+ * interleaved frame by frame in d_out ([frame][channel][3], the plugin's
+ * output layout); the marker starts at 0x05 for phase 0, 0xFA for phase 1.
+ * *next_phase receives the phase for the following block. */
+int dsdgpu_pack_dop(dsdgpu_context_t *ctx, int nch, const uint8_t *d_bits, size_t bits_stride,
+                    size_t n, uint8_t *d_out, int phase, int *next_phase);
+
+/* Native DSD bytes, MSB first: d_out[c * out_stride ...] receives (n + 7) / 8
+ * bytes per channel. */
+int dsdgpu_pack_native(dsdgpu_context_t *ctx, int nch, const uint8_t *d_bits, size_t bits_stride,
+                       size_t n, uint8_t *d_out, size_t out_stride);
+
+/* ---- whole path: PCM -> FIR + glue -> segment SDM + DAS -> pack (the PCM
+ *      conversion of plugin_process_pcm with the DAS phases of
+ *      plugin_process, src/dsp_plugin.c:2990-3216, 1283-2945) ---- */
+
+/* Set up the FIR chain, `nch` persistent SDM contexts and the packer. */
+int dsdgpu_pipeline_setup(dsdgpu_context_t *ctx, const dsdgpu_pipeline_params_t *p, int nch);
+/* One chunk from device buffers: d_pcm[c * pcm_stride ...] holds `frames`
+ * float samples of channel c.  The output layout follows the format (rows of
+ * out_stride bytes for BITS and NATIVE).  The DoP marker phase carries over
+ * between calls.  *out_samples receives the decisions per channel,
+ * *out_bytes the bytes written. */
+int dsdgpu_pipeline_process(dsdgpu_context_t *ctx, const float *d_pcm, size_t pcm_stride,
+                            size_t frames, double gain_start, double gain_end,
+                            uint8_t *d_out, size_t out_stride,
+                            size_t *out_samples, size_t *out_bytes);
+/* The same from host buffers: h_pcm is planar [nch][frames]; h_out receives
+ * the packed output (rows of (n + 7) / 8 bytes for NATIVE, n for BITS).
+ * Includes the host<->device copies. */
+int dsdgpu_pipeline_process_host(dsdgpu_context_t *ctx, const float *h_pcm, size_t frames,
+                                 double gain_start, double gain_end, uint8_t *h_out,
+                                 size_t out_capacity, size_t *out_samples, size_t *out_bytes);
+/* Milliseconds of the last pipeline call, measured with CUDA events on the
+ * context's stream: [FIR, segment SDM launch, DAS total, pack, whole call]. */
+int dsdgpu_stage_times(const dsdgpu_context_t *ctx, float *ms5);
+/* The CUDA stream (cudaStream_t) the context queues its work on. */
+int dsdgpu_get_stream(const dsdgpu_context_t *ctx, void **stream);
+
+/* Measured FP64 add/multiply issue rate of the device in Gop/s (separate
+ * DADD and DMUL, the operations the trellis SDM is made of). */
+int dsdgpu_probe_fp64(dsdgpu_context_t *ctx, double *gops);
 
 /* Best candidate's integrator state (sdm_state_distance's input,
  * src/trellis.c:1094-1109) and the counters conv_fail, cands_collapse,
