@@ -18,10 +18,11 @@ ERR_NOMEM = -3
 ERR_STATE = -4
 ERR_DEVICE = -5
 ERR_UNSUPPORTED = -6
+ERR_TOO_LARGE = -7
 
 _ERR_NAMES = {ERR_ARG: "ERR_ARG", ERR_CUDA: "ERR_CUDA", ERR_NOMEM: "ERR_NOMEM",
               ERR_STATE: "ERR_STATE", ERR_DEVICE: "ERR_DEVICE",
-              ERR_UNSUPPORTED: "ERR_UNSUPPORTED"}
+              ERR_UNSUPPORTED: "ERR_UNSUPPORTED", ERR_TOO_LARGE: "ERR_TOO_LARGE"}
 
 
 class DsdGpuError(RuntimeError):
@@ -98,6 +99,8 @@ SIGNATURES = {
                                                _szp, _szp]),
     "dsdgpu_stage_times": (C.c_int, [_vp, C.POINTER(C.c_float)]),
     "dsdgpu_get_stream": (C.c_int, [_vp, C.POINTER(_vp)]),
+    "dsdgpu_sdm_process_noalloc": (C.c_int, [C.POINTER(SdmParams), C.c_int, _vp, _sz, _sz,
+                                             _vp, _sz, _szp, _vp]),
     "dsdgpu_probe_fp64": (C.c_int, [_vp, C.POINTER(C.c_double)]),
     "dsdgpu_fir_setup": (C.c_int, [_vp, C.POINTER(FirParams), C.c_int]),
     "dsdgpu_fir_reset": (C.c_int, [_vp]),

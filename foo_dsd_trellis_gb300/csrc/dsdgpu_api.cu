@@ -51,6 +51,12 @@ __global__ void sdm_ctx_init_kernel(SdmCtx* ctxs, int first, int count, int keep
   }
 }
 
+int init_contexts(SdmCtx* d_ctxs, int first, int count, int keep_counters, cudaStream_t stream) {
+  if (count <= 0) return 0;
+  sdm_ctx_init_kernel<<<count, 256, 0, stream>>>(d_ctxs, first, count, keep_counters);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 __global__ void zero_counters_kernel(SdmCtx* ctxs, int idx) {
   SdmCtx* c = &ctxs[idx];
   c->conv_fail = c->cands_collapse = c->next_filter_drops = c->total_children = 0;

@@ -34,6 +34,8 @@ extern "C" {
                                          bounded-walk failure in its status word */
 #define DSDGPU_ERR_UNSUPPORTED  (-6)  /* parameters valid for the reference but
                                          not built in this library */
+#define DSDGPU_ERR_TOO_LARGE    (-7)  /* request exceeds the fixed scratch of the
+                                         allocation-free entry point */
 
 typedef struct dsdgpu_context dsdgpu_context_t;
 
@@ -246,6 +248,24 @@ int dsdgpu_pipeline_process_host(dsdgpu_context_t *ctx, const float *h_pcm, size
 int dsdgpu_stage_times(const dsdgpu_context_t *ctx, float *ms5);
 /* The CUDA stream (cudaStream_t) the context queues its work on. */
 int dsdgpu_get_stream(const dsdgpu_context_t *ctx, void **stream);
+
+/* Allocation-free trellis SDM (no counterpart in the reference; added for
+ * callers that cannot allocate device memory, such as a player's real-time
+ * audio callback, where an allocation can block and cause a dropout, or a host
+ * that grants a fixed device-memory budget).  It runs sdm_context_init and
+ * then sdm_process_block on up to 8 channels from fresh contexts, with all of
+ * its scratch (context bank, job table, counter, status word) in a fixed
+ * device array of about 110 KB that every GPU which loads the library keeps
+ * until exit; it calls no cudaMalloc, cudaFree or allocating library routine.
+ * More than 8 channels is rejected with DSDGPU_ERR_TOO_LARGE; lat must be
+ * <= 256.  The first call on a device looks up the array's device address
+ * (make it before any stream capture).  Calls share the array: two calls whose
+ * work overlaps on the GPU race and must not be issued.  Work is queued on
+ * `stream` (a cudaStream_t, NULL for the default stream) and the call waits
+ * for it.  Inputs, outputs and out_counts are as for dsdgpu_sdm_process. */
+int dsdgpu_sdm_process_noalloc(const dsdgpu_sdm_params_t *p, int nch, const double *d_in,
+                               size_t in_stride, size_t count, uint8_t *d_out,
+                               size_t out_stride, size_t *out_counts, void *stream);
 
 /* Measured FP64 add/multiply issue rate of the device in Gop/s (separate
  * DADD and DMUL, the operations the trellis SDM is made of). */
