@@ -62,6 +62,9 @@ OUT_BITS = 0
 OUT_DOP = 1
 OUT_NATIVE = 2
 
+OPT_SDM_SELECT = 1
+SELECT_FAST, SELECT_EXACT, SELECT_VERIFY = 0, 1, 2
+
 DAS_FULL_PARALLEL = 0
 DAS_SEG0_FIRST = 1
 
@@ -77,6 +80,7 @@ SIGNATURES = {
     "dsdgpu_last_error": (C.c_char_p, [_vp]),
     "dsdgpu_synchronize": (C.c_int, [_vp]),
     "dsdgpu_launch_count": (C.c_int, [_vp, C.POINTER(C.c_uint64)]),
+    "dsdgpu_set_option": (C.c_int, [_vp, C.c_int, C.c_int]),
     "dsdgpu_sdm_work": (C.c_int, [_vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "dsdgpu_sdm_setup": (C.c_int, [_vp, C.POINTER(SdmParams), C.c_int]),
     "dsdgpu_sdm_reset": (C.c_int, [_vp, C.c_int]),

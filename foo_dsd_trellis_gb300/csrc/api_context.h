@@ -28,6 +28,7 @@ struct dsdgpu_context {
   // trellis SDM
   bool sdm_ready = false;
   dsdgpu::SdmParams sdm{};
+  int sdm_mode = 0;               // selection strategy (DSDGPU_OPT_SDM_SELECT)
   int nctx = 0;
   dsdgpu::SdmCtx* d_ctx = nullptr;
   std::vector<int64_t> pending;   // latency fill per context (host mirror)

@@ -131,7 +131,9 @@ int dsdgpu_context::run_jobs(const std::vector<SdmJob>& jobs) {
   cudaError_t e = cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(SdmJob) * (size_t)n,
                                   cudaMemcpyHostToDevice, stream);
   if (e != cudaSuccess) return cuda_fail(e, "job table upload");
-  if (launch_sdm_jobs(sdm, d_jobs, n, d_counter, d_ctx, d_status, max_blocks, stream) != 0)
+  SdmParams P = sdm;
+  P.mode = sdm_mode;
+  if (launch_sdm_jobs(P, d_jobs, n, d_counter, d_ctx, d_status, max_blocks, stream) != 0)
     return cuda_fail(cudaGetLastError(), "sdm kernel launch");
   launches++;
   return check_status();
@@ -207,6 +209,19 @@ int dsdgpu_sdm_work(const dsdgpu_context_t* c, uint64_t* total_samples, uint64_t
   if (total_samples) *total_samples = c->sdm_samples;
   if (last_launch) *last_launch = c->sdm_last_samples;
   return DSDGPU_OK;
+}
+
+int dsdgpu_set_option(dsdgpu_context_t* c, int option, int value) {
+  if (!c) return DSDGPU_ERR_ARG;
+  switch (option) {
+    case DSDGPU_OPT_SDM_SELECT:
+      if (value < DSDGPU_SELECT_FAST || value > DSDGPU_SELECT_VERIFY)
+        return c->fail(DSDGPU_ERR_ARG, "bad selection mode");
+      c->sdm_mode = value;
+      return DSDGPU_OK;
+    default:
+      return c->fail(DSDGPU_ERR_ARG, "unknown option");
+  }
 }
 
 int dsdgpu_launch_count(const dsdgpu_context_t* c, uint64_t* count) {

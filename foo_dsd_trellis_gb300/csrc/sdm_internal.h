@@ -22,6 +22,14 @@ struct SdmParams {
   int cands;              // K
   int lat;
   int depth;
+  int mode;               // kModeFast, kModeExact or kModeVerify
+};
+
+// Survivor selection strategy of the SDM kernel.
+enum : int {
+  kModeFast = 0,     // parallel rank selection where it is provably equal, serial otherwise
+  kModeExact = 1,    // always the serial (reference-order) selection
+  kModeVerify = 2,   // serial selection, with the fast one computed and compared
 };
 
 // Device-resident SDM context: the state of one reference sdm_context_t that
@@ -67,6 +75,7 @@ struct SdmJob {
 enum : int {
   kStatusOk = 0,
   kStatusChainLimit = 1,   // a path-hash chain walk exceeded its bound
+  kStatusVerifyMismatch = 2,  // verify mode: the fast selection disagreed with the serial one
 };
 
 }  // namespace dsdgpu

@@ -70,6 +70,8 @@ struct WarpSmem {
   long long key[2][kSlots];
   int8_t link[2][kSlots];
   int8_t heads[kBuckets];
+  int8_t act[kMaxCands];       // scatter target of the fast selection
+  uint8_t hashmark[kSlots];    // children the serial path hashed (verify mode)
 };
 
 template <int N>
@@ -226,13 +228,85 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     c_drop += 2ull * (unsigned)(n - __popc(elig));
     c_tot += 2ull * (unsigned)n;
 
+    // ---- 2b. fast selection ----
+    // With no two eligible children on the same path and no two equal costs,
+    // the reference's ordered insertion with path-hash dedup keeps exactly the
+    // K smallest eligible children in (cost bits, index) order: every insert
+    // is new to the hash, evictions drop the largest, skips are children that
+    // would not be among the K smallest.  So ranks replace the serial
+    // insertion.  A child is hashed iff fewer than K earlier eligible children
+    // cost no more; only at K = 32 while bank 1 is sorted can the stored chain
+    // links be read in a later sample (through the act[32] store onto
+    // path_hash[0]), so only then are they written, as "previous hashed child
+    // of the same bucket".  Anything else (duplicate paths, ties, a bucket-0
+    // child after the list is full at K = 32 in bank 1) takes the serial path.
+    const bool me = live && old_next == want;
+    const int m2 = 2 * __popc(elig);
+    const bool links_matter = (K == kMaxCands && nb == 1);
+    bool fast_ok = (P.mode != kModeExact);
+    int f_cnt = 0, f_Ls = -1, f_link0 = -1, f_link1 = -1;
+    long long f_Lk = LLONG_MAX;
+    bool f_h0 = false, f_h1 = false;
+    if (fast_ok) {
+      const unsigned mm = __match_any_sync(kFull, q);
+      if (__any_sync(kFull, me && __popc(mm & elig) > 1)) fast_ok = false;
+      if (links_matter && m2 > K && __any_sync(kFull, me && (q & (kBuckets - 1)) == 0))
+        fast_ok = false;
+    }
+    if (fast_ok) {
+      int r0 = 0, r1 = 0, lo0 = 0, lo1 = 0;
+      unsigned ee = elig;
+      while (ee) {
+        const int qq = __ffs(ee) - 1;
+        ee &= ee - 1;
+        const longlong2 kk = *reinterpret_cast<const longlong2*>(&sm.key[nb][2 * qq]);
+        const int a0 = (kk.x < key0) + (kk.y < key0);
+        const int a1 = (kk.x < key1) + (kk.y < key1);
+        r0 += a0;
+        r1 += a1;
+        if (qq < lane) { lo0 += a0; lo1 += a1; }
+        else if (qq == lane) { lo1 += (kk.x < key1); }
+      }
+      // distinct costs <=> the ranks are a permutation of 0 .. m2-1
+      const int rsum = __reduce_add_sync(kFull, me ? r0 + r1 : 0);
+      if (rsum != m2 * (m2 - 1) / 2) fast_ok = false;
+      if (fast_ok) {
+        if (me && r0 < K) sm.act[r0] = (int8_t)(2 * lane);
+        if (me && r1 < K) sm.act[r1] = (int8_t)(2 * lane + 1);
+        __syncwarp();
+        f_cnt = m2 < K ? m2 : K;
+        if (lane < f_cnt) {
+          f_Ls = sm.act[lane];
+          f_Lk = sm.key[nb][f_Ls];
+        }
+        if (links_matter) {
+          f_h0 = me && lo0 < K;
+          f_h1 = me && lo1 < K;
+          const unsigned H0 = __ballot_sync(kFull, f_h0), H1 = __ballot_sync(kFull, f_h1);
+          const unsigned below = (1u << lane) - 1u;
+          const unsigned s0 = __match_any_sync(kFull, (unsigned)(q & (kBuckets - 1))) & H0 & below;
+          const unsigned s1 = __match_any_sync(kFull, (unsigned)((q | 1ull) & (kBuckets - 1))) & H1 & below;
+          f_link0 = s0 ? 2 * (31 - __clz(s0)) : -1;
+          f_link1 = s1 ? 2 * (31 - __clz(s1)) + 1 : -1;
+        }
+        __syncwarp();
+      }
+    }
+
+    // ---- 2c. serial selection (exact reference order) ----
     int cnt = 0;
     long long Lk = LLONG_MAX;
     int Ls = -1;
+    if (!fast_ok || P.mode == kModeVerify) {
     long long worst = LLONG_MAX;
-    while (elig) {
-      const int p = __ffs(elig) - 1;
-      elig &= elig - 1;
+    unsigned el = elig;
+    if (P.mode == kModeVerify) {
+      if (live) { sm.hashmark[2 * lane] = 0; sm.hashmark[2 * lane + 1] = 0; }
+      __syncwarp();
+    }
+    while (el) {
+      const int p = __ffs(el) - 1;
+      el &= el - 1;
       const unsigned long long qp = shfl64(q, p);
       const long long kp0 = __shfl_sync(kFull, key0, p);
       const long long kp1 = __shfl_sync(kFull, key1, p);
@@ -257,6 +331,7 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
           if (lane == 0) {
             sm.link[nb][c] = sm.heads[b];
             sm.heads[b] = (int8_t)c;
+            sm.hashmark[c] = 1;
           }
           __syncwarp();
           if (cnt == K && K == kMaxCands && nb == 1) {
@@ -289,6 +364,29 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
           if (removed || cnt < K) cnt++;
           worst = __shfl_sync(kFull, Lk, cnt - 1);
         }
+      }
+    }
+    }
+
+    if (fast_ok) {
+      if (P.mode == kModeVerify) {
+        bool bad = (cnt != f_cnt) || (lane < cnt && (Ls != f_Ls || Lk != f_Lk));
+        if (links_matter) {
+          if (live && (sm.hashmark[2 * lane] != 0) != f_h0) bad = true;
+          if (live && (sm.hashmark[2 * lane + 1] != 0) != f_h1) bad = true;
+          if (f_h0 && sm.link[nb][2 * lane] != f_link0) bad = true;
+          if (f_h1 && sm.link[nb][2 * lane + 1] != f_link1) bad = true;
+        }
+        if (__any_sync(kFull, bad)) err = max(err, (int)kStatusVerifyMismatch);
+      } else {
+        cnt = f_cnt;
+        Ls = f_Ls;
+        Lk = f_Lk;
+        if (links_matter) {
+          if (f_h0) sm.link[nb][2 * lane] = (int8_t)f_link0;
+          if (f_h1) sm.link[nb][2 * lane + 1] = (int8_t)f_link1;
+        }
+        __syncwarp();
       }
     }
 

@@ -36,6 +36,9 @@ class DasChannels:
         self.lat = lat
         self.device = device
 
+    def set_select(self, mode: int) -> None:
+        _lib.check(self.h, self.L.dsdgpu_set_option(self.h, _lib.OPT_SDM_SELECT, mode))
+
     def close(self):
         if getattr(self, "h", None):
             self.L.dsdgpu_destroy(self.h)

@@ -53,6 +53,10 @@ class TrellisSdm:
         self.order, self.depth, self.cands, self.lat = order, depth, cands, lat
         self.num_contexts = num_contexts
 
+    def set_select(self, mode: int) -> None:
+        """Survivor selection: _lib.SELECT_FAST (default), SELECT_EXACT, SELECT_VERIFY."""
+        _lib.check(self.h, self.L.dsdgpu_set_option(self.h, _lib.OPT_SDM_SELECT, mode))
+
     def close(self):
         if getattr(self, "h", None):
             self.L.dsdgpu_destroy(self.h)

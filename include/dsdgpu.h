@@ -119,6 +119,17 @@ int  dsdgpu_create(int device, dsdgpu_context_t **out);
 void dsdgpu_destroy(dsdgpu_context_t *ctx);
 /* Human-readable description of the last failure on this context. */
 const char *dsdgpu_last_error(const dsdgpu_context_t *ctx);
+/* Options (dsdgpu_set_option). */
+#define DSDGPU_OPT_SDM_SELECT   1   /* survivor selection of the trellis SDM: */
+#define DSDGPU_SELECT_FAST      0   /*   parallel ranks where provably equal to the
+                                         reference's serial order, serial otherwise
+                                         (default) */
+#define DSDGPU_SELECT_EXACT     1   /*   always the serial reference order */
+#define DSDGPU_SELECT_VERIFY    2   /*   serial, and the parallel result is checked
+                                         against it every sample (a disagreement
+                                         returns DSDGPU_ERR_DEVICE) */
+int  dsdgpu_set_option(dsdgpu_context_t *ctx, int option, int value);
+
 /* Number of kernels this context has launched so far. */
 int  dsdgpu_launch_count(const dsdgpu_context_t *ctx, uint64_t *count);
 /* Input samples the trellis SDM has stepped through: in total, and in the

@@ -137,3 +137,45 @@ def test_segments_copy_seed_discard(oracle):
     outs = g.segments(specs)
     for got, want in zip(outs, wants):
         np.testing.assert_array_equal(got.cpu().numpy(), want)
+
+
+VERIFY_CASES = CASES + [
+    ("clans-7", 6144000, 64, 32, 128, 0.0),
+    ("clans-7", 6144000, 32, 32, 64, 0.0),
+    ("clans-6", 5644800, 16, 32, 32, 0.0),
+    ("sdm-7", 5644800, 8, 32, 128, 3.0),
+]
+
+
+@pytest.mark.parametrize("case", VERIFY_CASES,
+                         ids=[f"v-{c[0]}-d{c[2]}-K{c[3]}-lat{c[4]}-{i}" for i, c in enumerate(VERIFY_CASES)])
+def test_fast_selection_verified_against_serial(oracle, case):
+    """Verify mode runs the serial (reference-order) selection every sample
+    and checks the parallel one against it: any disagreement in survivors,
+    order, costs, hashed set or stored chain links fails the call."""
+    from foo_dsd_trellis_gb300 import _lib
+    name, rate, depth, K, lat, lim = case
+    f = _ntf(name, rate)
+    x = multitone(40000, seed=zlib.crc32(repr(case).encode()) & 0xffff) * 1.5
+    g = _gpu_sdm(f, depth, K, lat, lim, nctx=2)
+    g.set_select(_lib.SELECT_VERIFY)
+    got = g.process_block(torch.from_numpy(x).cuda())[0].cpu().numpy()
+    want = oracle.sdm_bits(_ora(oracle, f, depth, K, lat, lim), x)
+    assert np.array_equal(got, want)
+    # seeded segments start with equal costs everywhere (ties)
+    from foo_dsd_trellis_gb300.sdm import SegmentSpec
+    seed = torch.from_numpy(np.array(g.query(0)["best_state"])).cuda()
+    g.segments([SegmentSpec(torch.from_numpy(x[:20000].copy()).cuda(), channel=1, discard=300,
+                            seed_from=0, seed_state=seed)])
+
+
+def test_exact_and_fast_modes_agree(oracle):
+    from foo_dsd_trellis_gb300 import _lib
+    f = _ntf("clans-7", 6144000)
+    x = multitone(30000, seed=77)
+    outs = []
+    for mode in (_lib.SELECT_FAST, _lib.SELECT_EXACT):
+        g = _gpu_sdm(f, 64, 32, 128)
+        g.set_select(mode)
+        outs.append(g.process_block(torch.from_numpy(x).cuda())[0].cpu().numpy())
+    assert np.array_equal(outs[0], outs[1])
