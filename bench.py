@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--seconds", type=float, default=WL["seconds"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--das-seg-len", type=int, default=WL["das_seg_len"],
+                    help="nominal DAS segment length (profiling of small cases only)")
     return ap.parse_args()
 
 
@@ -199,6 +201,8 @@ def run_ours(args):
     pcm = signals.dsd128_multitone_pink(args.seconds, WL["fs_in"], WL["channels"],
                                         WL["seed"] + 2 * rank)
     nch, frames = pcm.shape
+    if args.das_seg_len != WL["das_seg_len"]:
+        WL["das_seg_len"] = args.das_seg_len
     enc = Encoder(WL["fs_in"], WL["fs_out"], nch, f, WL["depth"], WL["cands"], WL["lat"],
                   seg_len=WL["das_seg_len"], seed_mode=FULL_PARALLEL, reposition=True,
                   boxcar_taps=WL["boxcar_taps"], soft_clip=WL["soft_clip"],

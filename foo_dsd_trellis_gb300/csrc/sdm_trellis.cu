@@ -31,7 +31,7 @@
 
 namespace dsdgpu {
 
-constexpr int kWarpsPerBlock = 4;
+constexpr int kMaxWarpsPerBlock = 4;
 constexpr int kRegRingWords = 8;      // rings held in registers: lat <= 256
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -72,7 +72,42 @@ struct WarpSmem {
   int8_t heads[kBuckets];
   int8_t act[kMaxCands];       // scatter target of the fast selection
   uint8_t hashmark[kSlots];    // children the serial path hashed (verify mode)
+  uint8_t hashmark2[kSlots];   // children the fast path deems hashed
 };
+
+// (key, index) order of the survivor selection: cost bits as int64, then slot.
+__device__ __forceinline__ bool key_less(long long ka, int ia, long long kb, int ib) {
+  return ka < kb || (ka == kb && ia < ib);
+}
+
+// Bitonic sort of the 64 (key, index) pairs held two per lane (sorted
+// positions 2*lane and 2*lane + 1), ascending.
+__device__ __forceinline__ void bitonic64(long long& kA, int& iA, long long& kB, int& iB,
+                                          int lane) {
+#pragma unroll
+  for (int k = 2; k <= 64; k <<= 1) {
+    const bool asc = ((2 * lane) & k) == 0;
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j == 1) {
+        const bool sw = asc ? key_less(kB, iB, kA, iA) : key_less(kA, iA, kB, iB);
+        if (sw) {
+          const long long tk = kA; kA = kB; kB = tk;
+          const int ti = iA; iA = iB; iB = ti;
+        }
+      } else {
+        const int lj = j >> 1;
+        const bool keep_min = (((lane & lj) == 0) == asc);
+        long long pk = __shfl_xor_sync(kFull, kA, lj);
+        int pi = __shfl_xor_sync(kFull, iA, lj);
+        if (keep_min == key_less(pk, pi, kA, iA)) { kA = pk; iA = pi; }
+        pk = __shfl_xor_sync(kFull, kB, lj);
+        pi = __shfl_xor_sync(kFull, iB, lj);
+        if (keep_min == key_less(pk, pi, kB, iB)) { kB = pk; iB = pi; }
+      }
+    }
+  }
+}
 
 template <int N>
 __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restrict__ ctxs,
@@ -191,57 +226,54 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     __syncwarp();
 
     // ---- 2. selection ----
-    long long mk = key0;
-    int mi = 2 * lane;
-    if (key1 < key0) { mk = key1; mi = 2 * lane + 1; }
-    if (!live) mi = 1 << 20;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const long long ok = __shfl_xor_sync(kFull, mk, off);
-      const int oi = __shfl_xor_sync(kFull, mi, off);
-      if (ok < mk || (ok == mk && oi < mi)) { mk = ok; mi = oi; }
-    }
+    // All 2n children sorted by (cost bits as int64, slot index): position 0
+    // is the reference's minimum (first index among equal costs), the first
+    // sorted child carrying the majority bit is its best_maj, and the
+    // eligible children keep their (cost, index) order (src/trellis.c:628-652).
+    long long sk0 = live ? key0 : LLONG_MAX, sk1 = live ? key1 : LLONG_MAX;
+    int si0 = 2 * lane, si1 = 2 * lane + 1;
+    bitonic64(sk0, si0, sk1, si1, lane);
+    const int sn0 = __shfl_sync(kFull, old_next, si0 >> 1);   // traceback bit of each sorted child
+    const int sn1 = __shfl_sync(kFull, old_next, si1 >> 1);
+    const bool sl0 = (si0 >> 1) < n, sl1 = (si1 >> 1) < n;
     const unsigned nx1 = __ballot_sync(kFull, live && old_next);
     const int votes1 = 2 * __popc(nx1);
     const int majority = (votes1 > 2 * n - votes1) ? 1 : 0;
-    const int min_next = __shfl_sync(kFull, old_next, mi >> 1);
-    if (min_next != majority) {
-      const bool cand = live && old_next == majority;
-      long long bk = key0;
-      int bi = 2 * lane;
-      if (key1 < key0) { bk = key1; bi = 2 * lane + 1; }
-      if (!cand) { bk = LLONG_MAX; bi = 1 << 20; }
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const long long ok = __shfl_xor_sync(kFull, bk, off);
-        const int oi = __shfl_xor_sync(kFull, bi, off);
-        if (ok < bk || (ok == bk && oi < bi)) { bk = ok; bi = oi; }
-      }
-      if (bi < (1 << 20)) {
-        const double cmin = __longlong_as_double(mk);
-        const double cbm = __longlong_as_double(bk);
-        if (cbm < __dmul_rn(cmin, 1.1)) { mk = bk; mi = bi; }
+    const long long mk = __shfl_sync(kFull, sk0, 0);
+    int want = __shfl_sync(kFull, sn0, 0);
+    if (want != majority) {
+      const unsigned mA = __ballot_sync(kFull, sl0 && sn0 == majority);
+      const unsigned mB = __ballot_sync(kFull, sl1 && sn1 == majority);
+      int pos = 1 << 20;
+      if (mA) pos = 2 * (__ffs(mA) - 1);
+      if (mB) pos = min(pos, 2 * (__ffs(mB) - 1) + 1);
+      if (pos < (1 << 20)) {
+        const long long bA = __shfl_sync(kFull, sk0, pos >> 1);
+        const long long bB = __shfl_sync(kFull, sk1, pos >> 1);
+        const double cbm = __longlong_as_double((pos & 1) ? bB : bA);
+        if (cbm < __dmul_rn(__longlong_as_double(mk), 1.1)) want = majority;
       }
     }
-    const int want = __shfl_sync(kFull, old_next, mi >> 1);
     unsigned elig = __ballot_sync(kFull, live && old_next == want);
     c_drop += 2ull * (unsigned)(n - __popc(elig));
     c_tot += 2ull * (unsigned)n;
 
     // ---- 2b. fast selection ----
-    // With no two eligible children on the same path and no two equal costs,
-    // the reference's ordered insertion with path-hash dedup keeps exactly the
-    // K smallest eligible children in (cost bits, index) order: every insert
-    // is new to the hash, evictions drop the largest, skips are children that
-    // would not be among the K smallest.  So ranks replace the serial
-    // insertion.  A child is hashed iff fewer than K earlier eligible children
-    // cost no more; only at K = 32 while bank 1 is sorted can the stored chain
-    // links be read in a later sample (through the act[32] store onto
-    // path_hash[0]), so only then are they written, as "previous hashed child
-    // of the same bucket".  Anything else (duplicate paths, ties, a bucket-0
-    // child after the list is full at K = 32 in bank 1) takes the serial path.
+    // With no two eligible children on the same path, the reference's ordered
+    // insertion with path-hash dedup keeps exactly the first K eligible
+    // children of the (cost, index) order: every insert is new to the hash,
+    // evictions drop the largest, ties keep insertion (index) order, skips are
+    // children that would not be among the K smallest.  A child is hashed iff
+    // fewer than K eligible children with a lower index precede it in that
+    // order; only at K = 32 while bank 1 is sorted can the stored chain links
+    // be read in a later sample (through the act[32] store onto path_hash[0]),
+    // so only then are they written, as "previous hashed child of the same
+    // bucket".  Duplicate paths, or a bucket-0 child once the list can be full
+    // at K = 32 in bank 1, take the serial path.
     const bool me = live && old_next == want;
-    const int m2 = 2 * __popc(elig);
+    const bool e0 = sl0 && sn0 == want, e1 = sl1 && sn1 == want;
+    const unsigned EA = __ballot_sync(kFull, e0), EB = __ballot_sync(kFull, e1);
+    const int m2 = __popc(EA) + __popc(EB);
     const bool links_matter = (K == kMaxCands && nb == 1);
     bool fast_ok = (P.mode != kModeExact);
     int f_cnt = 0, f_Ls = -1, f_link0 = -1, f_link1 = -1;
@@ -254,43 +286,44 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
         fast_ok = false;
     }
     if (fast_ok) {
-      int r0 = 0, r1 = 0, lo0 = 0, lo1 = 0;
-      unsigned ee = elig;
-      while (ee) {
-        const int qq = __ffs(ee) - 1;
-        ee &= ee - 1;
-        const longlong2 kk = *reinterpret_cast<const longlong2*>(&sm.key[nb][2 * qq]);
-        const int a0 = (kk.x < key0) + (kk.y < key0);
-        const int a1 = (kk.x < key1) + (kk.y < key1);
-        r0 += a0;
-        r1 += a1;
-        if (qq < lane) { lo0 += a0; lo1 += a1; }
-        else if (qq == lane) { lo1 += (kk.x < key1); }
-      }
-      // distinct costs <=> the ranks are a permutation of 0 .. m2-1
-      const int rsum = __reduce_add_sync(kFull, me ? r0 + r1 : 0);
-      if (rsum != m2 * (m2 - 1) / 2) fast_ok = false;
-      if (fast_ok) {
-        if (me && r0 < K) sm.act[r0] = (int8_t)(2 * lane);
-        if (me && r1 < K) sm.act[r1] = (int8_t)(2 * lane + 1);
-        __syncwarp();
-        f_cnt = m2 < K ? m2 : K;
-        if (lane < f_cnt) {
-          f_Ls = sm.act[lane];
-          f_Lk = sm.key[nb][f_Ls];
+      const unsigned below = (1u << lane) - 1u;
+      const int r0 = __popc(EA & below) + __popc(EB & below);
+      const int r1 = r0 + (e0 ? 1 : 0);
+      if (e0 && r0 < K) sm.act[r0] = (int8_t)si0;
+      if (e1 && r1 < K) sm.act[r1] = (int8_t)si1;
+      if (links_matter) {
+        // eligible children sorted before, with a lower index: OR-scan of
+        // one-hot index masks over the sorted positions
+        const unsigned long long mine = (e0 ? (1ull << si0) : 0ull) | (e1 ? (1ull << si1) : 0ull);
+        unsigned long long inc = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const unsigned long long v = (unsigned long long)__shfl_up_sync(kFull, (long long)inc, o);
+          if (lane >= o) inc |= v;
         }
-        if (links_matter) {
-          f_h0 = me && lo0 < K;
-          f_h1 = me && lo1 < K;
-          const unsigned H0 = __ballot_sync(kFull, f_h0), H1 = __ballot_sync(kFull, f_h1);
-          const unsigned below = (1u << lane) - 1u;
-          const unsigned s0 = __match_any_sync(kFull, (unsigned)(q & (kBuckets - 1))) & H0 & below;
-          const unsigned s1 = __match_any_sync(kFull, (unsigned)((q | 1ull) & (kBuckets - 1))) & H1 & below;
-          f_link0 = s0 ? 2 * (31 - __clz(s0)) : -1;
-          f_link1 = s1 ? 2 * (31 - __clz(s1)) + 1 : -1;
-        }
-        __syncwarp();
+        const unsigned long long before0 = inc & ~mine;
+        const unsigned long long before1 = before0 | (e0 ? (1ull << si0) : 0ull);
+        const int p0 = __popcll(before0 & ((1ull << si0) - 1ull));
+        const int p1 = __popcll(before1 & ((1ull << si1) - 1ull));
+        sm.hashmark2[si0] = (uint8_t)(e0 && p0 < K);
+        sm.hashmark2[si1] = (uint8_t)(e1 && p1 < K);
       }
+      __syncwarp();
+      f_cnt = m2 < K ? m2 : K;
+      if (lane < f_cnt) {
+        f_Ls = sm.act[lane];
+        f_Lk = sm.key[nb][f_Ls];
+      }
+      if (links_matter) {
+        f_h0 = live && sm.hashmark2[2 * lane] != 0;
+        f_h1 = live && sm.hashmark2[2 * lane + 1] != 0;
+        const unsigned H0 = __ballot_sync(kFull, f_h0), H1 = __ballot_sync(kFull, f_h1);
+        const unsigned s0 = __match_any_sync(kFull, (unsigned)(q & (kBuckets - 1))) & H0 & below;
+        const unsigned s1 = __match_any_sync(kFull, (unsigned)((q | 1ull) & (kBuckets - 1))) & H1 & below;
+        f_link0 = s0 ? 2 * (31 - __clz(s0)) : -1;
+        f_link1 = s1 ? 2 * (31 - __clz(s1)) + 1 : -1;
+      }
+      __syncwarp();
     }
 
     // ---- 2c. serial selection (exact reference order) ----
@@ -474,12 +507,12 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
 }
 
 template <int N>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+__global__ void __launch_bounds__(kMaxWarpsPerBlock * 32)
 sdm_jobs_kernel(SdmParams P, const SdmJob* __restrict__ jobs, int njobs,
                 int* __restrict__ job_counter, SdmCtx* __restrict__ ctxs,
                 int* __restrict__ status) {
-  __shared__ WarpSmem smem[kWarpsPerBlock];
-  WarpSmem& sm = smem[threadIdx.x >> 5];
+  extern __shared__ __align__(16) unsigned char sdm_smem_raw[];
+  WarpSmem& sm = reinterpret_cast<WarpSmem*>(sdm_smem_raw)[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
   for (;;) {
     int j = 0;
@@ -492,17 +525,21 @@ sdm_jobs_kernel(SdmParams P, const SdmJob* __restrict__ jobs, int njobs,
   }
 }
 
-// Host-side launcher: grid = min(jobs, resident warps) / warps per block.
+// Host-side launcher: one warp per job, `warps_per_block` warps per CTA (1..4;
+// small CTAs spread a few thousand long-running jobs evenly over the SMs).
 int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_counter,
-                    SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream) {
+                    SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream,
+                    int warps_per_block) {
   if (njobs <= 0) return 0;
-  int blocks = (njobs + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  int wpb = warps_per_block < 1 ? 1 : (warps_per_block > kMaxWarpsPerBlock ? kMaxWarpsPerBlock : warps_per_block);
+  int blocks = (njobs + wpb - 1) / wpb;
   if (max_blocks > 0 && blocks > max_blocks) blocks = max_blocks;
   cudaMemsetAsync(d_counter, 0, sizeof(int), stream);
-  const dim3 grid(blocks), block(kWarpsPerBlock * 32);
+  const dim3 grid(blocks), block(wpb * 32);
+  const size_t smem = sizeof(WarpSmem) * (size_t)wpb;
   switch (P.order) {
 #define DSD_CASE(NN) \
-  case NN: sdm_jobs_kernel<NN><<<grid, block, 0, stream>>>(P, d_jobs, njobs, d_counter, d_ctxs, d_status); break;
+  case NN: sdm_jobs_kernel<NN><<<grid, block, smem, stream>>>(P, d_jobs, njobs, d_counter, d_ctxs, d_status); break;
     DSD_CASE(2) DSD_CASE(3) DSD_CASE(4) DSD_CASE(5) DSD_CASE(6)
     DSD_CASE(7) DSD_CASE(8) DSD_CASE(9) DSD_CASE(10)
 #undef DSD_CASE

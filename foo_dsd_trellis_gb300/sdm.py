@@ -57,6 +57,9 @@ class TrellisSdm:
         """Survivor selection: _lib.SELECT_FAST (default), SELECT_EXACT, SELECT_VERIFY."""
         _lib.check(self.h, self.L.dsdgpu_set_option(self.h, _lib.OPT_SDM_SELECT, mode))
 
+    def set_option(self, option: int, value: int) -> None:
+        _lib.check(self.h, self.L.dsdgpu_set_option(self.h, option, value))
+
     def close(self):
         if getattr(self, "h", None):
             self.L.dsdgpu_destroy(self.h)
