@@ -63,7 +63,6 @@ OUT_DOP = 1
 OUT_NATIVE = 2
 
 OPT_SDM_SELECT = 1
-OPT_SDM_WARPS_PER_BLOCK = 2
 SELECT_FAST, SELECT_EXACT, SELECT_VERIFY = 0, 1, 2
 
 DAS_FULL_PARALLEL = 0

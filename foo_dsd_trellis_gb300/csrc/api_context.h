@@ -29,7 +29,6 @@ struct dsdgpu_context {
   bool sdm_ready = false;
   dsdgpu::SdmParams sdm{};
   int sdm_mode = 0;               // selection strategy (DSDGPU_OPT_SDM_SELECT)
-  int sdm_wpb = 1;                // warps per CTA of the SDM launch
   int nctx = 0;
   dsdgpu::SdmCtx* d_ctx = nullptr;
   std::vector<int64_t> pending;   // latency fill per context (host mirror)

@@ -27,8 +27,7 @@
 namespace dsdgpu {
 
 int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_counter,
-                    SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream,
-                    int warps_per_block);
+                    SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream);
 
 constexpr int kSeamThreads = 512;
 constexpr int kMaxQ = 32;

@@ -11,8 +11,7 @@
 namespace dsdgpu {
 
 int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_counter,
-                    SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream,
-                    int warps_per_block);
+                    SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream);
 int sdm_max_lat_in_registers();
 
 // (Re)initialise contexts [first, first + count) to the state sdm_context_init
@@ -134,7 +133,7 @@ int dsdgpu_context::run_jobs(const std::vector<SdmJob>& jobs) {
   if (e != cudaSuccess) return cuda_fail(e, "job table upload");
   SdmParams P = sdm;
   P.mode = sdm_mode;
-  if (launch_sdm_jobs(P, d_jobs, n, d_counter, d_ctx, d_status, max_blocks, stream, sdm_wpb) != 0)
+  if (launch_sdm_jobs(P, d_jobs, n, d_counter, d_ctx, d_status, max_blocks, stream) != 0)
     return cuda_fail(cudaGetLastError(), "sdm kernel launch");
   launches++;
   return check_status();
@@ -219,10 +218,6 @@ int dsdgpu_set_option(dsdgpu_context_t* c, int option, int value) {
       if (value < DSDGPU_SELECT_FAST || value > DSDGPU_SELECT_VERIFY)
         return c->fail(DSDGPU_ERR_ARG, "bad selection mode");
       c->sdm_mode = value;
-      return DSDGPU_OK;
-    case DSDGPU_OPT_SDM_WARPS_PER_BLOCK:
-      if (value < 1 || value > 4) return c->fail(DSDGPU_ERR_ARG, "warps per block: 1..4");
-      c->sdm_wpb = value;
       return DSDGPU_OK;
     default:
       return c->fail(DSDGPU_ERR_ARG, "unknown option");

@@ -28,8 +28,7 @@
 namespace dsdgpu {
 
 int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_counter,
-                    SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream,
-                    int warps_per_block);
+                    SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream);
 int init_contexts(SdmCtx* d_ctxs, int first, int count, int keep_counters, cudaStream_t stream);
 int sdm_max_lat_in_registers();
 
@@ -107,7 +106,7 @@ extern "C" int dsdgpu_sdm_process_noalloc(const dsdgpu_sdm_params_t* p, int nch,
   if (cudaMemcpyAsync(d_jobs, jobs, sizeof(SdmJob) * (size_t)nch, cudaMemcpyHostToDevice, s) !=
       cudaSuccess)
     return DSDGPU_ERR_CUDA;
-  if (launch_sdm_jobs(P, d_jobs, nch, d_counter, d_ctx, d_status, 0, s, 1) != 0) return DSDGPU_ERR_CUDA;
+  if (launch_sdm_jobs(P, d_jobs, nch, d_counter, d_ctx, d_status, 0, s) != 0) return DSDGPU_ERR_CUDA;
   int st = 0;
   if (cudaMemcpyAsync(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)

@@ -31,7 +31,10 @@
 
 namespace dsdgpu {
 
-constexpr int kMaxWarpsPerBlock = 4;
+// One warp (one job) per CTA: a few thousand long-running jobs spread evenly
+// over the SMs.  The launch bound (32 threads, 13 CTAs per SM) holds the kernel
+// at 128 registers; a 152-register build measured 50 % slower on the DSD128
+// DAS workload.
 constexpr int kRegRingWords = 8;      // rings held in registers: lat <= 256
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -47,22 +50,56 @@ __device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int s
   return (unsigned long long)__shfl_sync(kFull, (long long)v, src);
 }
 
-// NTF advance with y = 0 (src/trellis.c:104-118 for order 7; every order has
-// the same shape): d[0] = (s0 - g0 s1) + x; d[i] = (s[i] + s[i-1]) - g[i] s[i+1];
-// d[N-1] = s[N-1] + s[N-2]; v = ((x + a0 d0) + a1 d1) + ...
+// The NTF advance with y = 0 (src/trellis.c:37-151; every order has the
+// same shape): d[0] = (s0 - g0 s1) + x; d[i] = (s[i] + s[i-1]) - g[i] s[i+1];
+// d[N-1] = s[N-1] + s[N-2]; v = ((x + a0 d0) + a1 d1) + ...  The two children
+// of a candidate share s[1..N-1], so everything that does not involve s[0]
+// (g0 s1, g1 s2, d[2..N-1] and a[i] d[i] for i >= 2) is the same for both
+// siblings: it is computed once per parent, while the next selection runs,
+// and handed to the surviving children as a Pack.  Each sample then keeps only
+// the s[0]-dependent operations on its critical path.  Every operation is the
+// reference's, in the reference's order, rounded separately (no contraction).
 template <int N>
-__device__ __forceinline__ double ntf_advance(const SdmParams& P, const double (&s)[N],
-                                              double (&d)[N], double x) {
-  d[0] = __dadd_rn(__dsub_rn(s[0], __dmul_rn(P.g[0], s[1])), x);
-  double v = __dadd_rn(x, __dmul_rn(P.a[0], d[0]));
-#pragma unroll
-  for (int i = 1; i < N - 1; i++) {
-    d[i] = __dsub_rn(__dadd_rn(s[i], s[i - 1]), __dmul_rn(P.g[i], s[i + 1]));
-    v = __dadd_rn(v, __dmul_rn(P.a[i], d[i]));
+struct Pack {
+  double G0;      // g0 * s1
+  double G1;      // g1 * s2          (N >= 3)
+  double D[N];    // d[i], i = 2..N-1
+  double A[N];    // a[i] * d[i], i = 2..N-1
+};
+
+template <int N>
+__host__ __device__ constexpr int shared_ops() { return N >= 3 ? 4 * N - 8 : 1; }
+
+// Operation k of the shared part, inputs S[1..N-1] (a child's state), into
+// np (with scratch tg/tu).  Orders respect the dependencies when k runs
+// 0, 1, 2, ...
+template <int N>
+__device__ __forceinline__ void shared_op(int k, const SdmParams& P, const double (&S)[N],
+                                          Pack<N>& np, double (&tg)[N], double (&tu)[N]) {
+  if (N < 3) {
+    if (k == 0) np.G0 = __dmul_rn(P.g[0], S[1]);
+    return;
   }
-  d[N - 1] = __dadd_rn(s[N - 1], s[N - 2]);
-  v = __dadd_rn(v, __dmul_rn(P.a[N - 1], d[N - 1]));
-  return v;
+  constexpr int M = N - 3;   // middle indices i = 2..N-2
+  if (k == 0) { np.G0 = __dmul_rn(P.g[0], S[1]); return; }
+  if (k == 1) { np.G1 = __dmul_rn(P.g[1], S[2]); return; }
+  k -= 2;
+  if (k < M) { const int i = 2 + k; tg[i] = __dmul_rn(P.g[i], S[i + 1]); return; }
+  k -= M;
+  if (k < M) { const int i = 2 + k; tu[i] = __dadd_rn(S[i], S[i - 1]); return; }
+  k -= M;
+  if (k == 0) { np.D[N - 1] = __dadd_rn(S[N - 1], S[N - 2]); return; }
+  k -= 1;
+  if (k < M) { const int i = 2 + k; np.D[i] = __dsub_rn(tu[i], tg[i]); return; }
+  k -= M;
+  if (k < N - 2) { const int i = 2 + k; np.A[i] = __dmul_rn(P.a[i], np.D[i]); return; }
+}
+
+template <int N>
+__device__ __forceinline__ void shared_all(const SdmParams& P, const double (&S)[N], Pack<N>& np) {
+  double tg[N], tu[N];
+#pragma unroll
+  for (int k = 0; k < shared_ops<N>(); k++) shared_op<N>(k, P, S, np, tg, tu);
 }
 
 struct WarpSmem {
@@ -73,6 +110,8 @@ struct WarpSmem {
   int8_t act[kMaxCands];       // scatter target of the fast selection
   uint8_t hashmark[kSlots];    // children the serial path hashed (verify mode)
   uint8_t hashmark2[kSlots];   // children the fast path deems hashed
+  int8_t pos[kSlots];          // sorted position of each child (serial path)
+  int8_t idx_at[kSlots];       // child at each sorted position (serial path)
 };
 
 // (key, index) order of the survivor selection: cost bits as int64, then slot.
@@ -82,13 +121,16 @@ __device__ __forceinline__ bool key_less(long long ka, int ia, long long kb, int
 
 // Bitonic sort of the 64 (key, index) pairs held two per lane (sorted
 // positions 2*lane and 2*lane + 1), ascending.
+template <typename Hook>
 __device__ __forceinline__ void bitonic64(long long& kA, int& iA, long long& kB, int& iB,
-                                          int lane) {
+                                          int lane, Hook&& hook) {
+  int stage = 0;
 #pragma unroll
   for (int k = 2; k <= 64; k <<= 1) {
     const bool asc = ((2 * lane) & k) == 0;
 #pragma unroll
     for (int j = k >> 1; j > 0; j >>= 1) {
+      hook(stage++);
       if (j == 1) {
         const bool sw = asc ? key_less(kB, iB, kA, iA) : key_less(kA, iA, kB, iB);
         if (sw) {
@@ -164,6 +206,10 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     }
     __syncwarp();
   }
+  // the candidate as (s0, s1, shared part of its next advance)
+  double cs0 = s[0], cs1 = s[1];
+  Pack<N> pk;
+  shared_all<N>(P, s, pk);
 
   const long long n_in = job.n_in;
   const double* __restrict__ in = job.in;
@@ -174,6 +220,7 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
   }
   uint8_t obit = 0;
   int err = 0;
+  const bool lim_on = P.state_limit > 0.0;
 
   for (long long t = 0; t < n_in; t++) {
     const int tl = (int)(t & 31);
@@ -187,22 +234,30 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     if (next_pos == P.lat) next_pos = 0;
     const bool live = lane < n;
 
-    // ---- 1. expansion ----
-    double d[N];
+    // ---- 1. expansion: the s0-dependent part of the advance ----
+    double S[N];          // the children's shared state s[1..N-1] (clamped)
 #pragma unroll
-    for (int k = 0; k < N; k++) d[k] = 0.0;
+    for (int k = 0; k < N; k++) S[k] = 0.0;
     double s00 = 0.0, s01 = 0.0;
     long long key0 = LLONG_MAX, key1 = LLONG_MAX;
     unsigned long long q = 0;
     int new_next = 0;
     const int old_next = nxt;
     if (live) {
-      const double v = ntf_advance<N>(P, s, d, x);
-      s00 = __dadd_rn(d[0], 1.0);
-      s01 = __dsub_rn(d[0], 1.0);
-      if (P.state_limit > 0.0) {
+      const double d0 = __dadd_rn(__dsub_rn(cs0, pk.G0), x);
+      const double d1 = (N >= 3) ? __dsub_rn(__dadd_rn(cs1, cs0), pk.G1) : __dadd_rn(cs1, cs0);
+      double v = __dadd_rn(x, __dmul_rn(P.a[0], d0));
+      v = __dadd_rn(v, __dmul_rn(P.a[1], d1));
 #pragma unroll
-        for (int k = 1; k < N; k++) d[k] = clampd(d[k], P.state_limit);
+      for (int i = 2; i < N; i++) v = __dadd_rn(v, pk.A[i]);
+      s00 = __dadd_rn(d0, 1.0);
+      s01 = __dsub_rn(d0, 1.0);
+      S[1] = d1;
+#pragma unroll
+      for (int i = 2; i < N; i++) S[i] = pk.D[i];
+      if (lim_on) {
+#pragma unroll
+        for (int k = 1; k < N; k++) S[k] = clampd(S[k], P.state_limit);
         s00 = clampd(s00, P.state_limit);
         s01 = clampd(s01, P.state_limit);
       }
@@ -225,6 +280,9 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     }
     __syncwarp();
 
+    // the children's shared part, one operation per stage of the sort below
+    Pack<N> npk;
+    double tg[N], tu[N];
     // ---- 2. selection ----
     // All 2n children sorted by (cost bits as int64, slot index): position 0
     // is the reference's minimum (first index among equal costs), the first
@@ -232,7 +290,11 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     // eligible children keep their (cost, index) order (src/trellis.c:628-652).
     long long sk0 = live ? key0 : LLONG_MAX, sk1 = live ? key1 : LLONG_MAX;
     int si0 = 2 * lane, si1 = 2 * lane + 1;
-    bitonic64(sk0, si0, sk1, si1, lane);
+    bitonic64(sk0, si0, sk1, si1, lane, [&](int st) {
+      if (st < shared_ops<N>()) shared_op<N>(st, P, S, npk, tg, tu);
+    });
+#pragma unroll
+    for (int k = 21; k < shared_ops<N>(); k++) shared_op<N>(k, P, S, npk, tg, tu);
     const int sn0 = __shfl_sync(kFull, old_next, si0 >> 1);   // traceback bit of each sorted child
     const int sn1 = __shfl_sync(kFull, old_next, si1 >> 1);
     const bool sl0 = (si0 >> 1) < n, sl1 = (si1 >> 1) < n;
@@ -327,78 +389,87 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     }
 
     // ---- 2c. serial selection (exact reference order) ----
+    // The reference's act list is always ordered by (cost, index) (children are
+    // inserted in index order, after every element of equal cost), so it is
+    // held as a set of sorted positions: insertion, eviction of the worst,
+    // replacement and the "list full and worst <= s" skip are bit operations.
+    // Children are visited in index order and the path hash is walked in
+    // shared memory exactly as sdm_check_path does, stale links included.
     int cnt = 0;
     long long Lk = LLONG_MAX;
     int Ls = -1;
     if (!fast_ok || P.mode == kModeVerify) {
-    long long worst = LLONG_MAX;
-    unsigned el = elig;
-    if (P.mode == kModeVerify) {
-      if (live) { sm.hashmark[2 * lane] = 0; sm.hashmark[2 * lane + 1] = 0; }
+      sm.pos[si0] = (int8_t)(2 * lane);
+      sm.pos[si1] = (int8_t)(2 * lane + 1);
+      sm.idx_at[2 * lane] = (int8_t)si0;
+      sm.idx_at[2 * lane + 1] = (int8_t)si1;
+      if (P.mode == kModeVerify && live) { sm.hashmark[2 * lane] = 0; sm.hashmark[2 * lane + 1] = 0; }
       __syncwarp();
-    }
-    while (el) {
-      const int p = __ffs(el) - 1;
-      el &= el - 1;
-      const unsigned long long qp = shfl64(q, p);
-      const long long kp0 = __shfl_sync(kFull, key0, p);
-      const long long kp1 = __shfl_sync(kFull, key1, p);
+      const int nch = 2 * n;
+      unsigned long long Lm = 0ull;   // the act list, as sorted positions
+      unsigned el = elig;
+      while (el) {
+        const int p = __ffs(el) - 1;
+        el &= el - 1;
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int c = 2 * p + h;
-        const long long sk = h ? kp1 : kp0;
-        const unsigned long long sp = h ? (qp | 1ull) : qp;
-        if (cnt == K && worst <= sk) continue;
-        const int b = (int)(sp & (kBuckets - 1));
-        int t = sm.heads[b];
-        int hops = 0;
-        while (t >= 0) {
-          if (sm.path[nb][t] == sp) break;
-          t = sm.link[nb][t];
-          if (++hops > 4 * kSlots) { err = kStatusChainLimit; t = -1; break; }
-        }
-        bool do_insert;
-        bool removed = false;
-        if (t < 0) {
-          __syncwarp();
-          if (lane == 0) {
-            sm.link[nb][c] = sm.heads[b];
-            sm.heads[b] = (int8_t)c;
-            sm.hashmark[c] = 1;
+        for (int h = 0; h < 2; h++) {
+          const int c = 2 * p + h;
+          const int ps = sm.pos[c];
+          const long long sk = sm.key[nb][c];
+          const unsigned long long sp = sm.path[nb][c];
+          if (cnt == K && (63 - __clzll((long long)Lm)) < ps) continue;
+          const int b = (int)(sp & (kBuckets - 1));
+          int t = sm.heads[b];
+          int hops = 0;
+          while (t >= 0) {
+            if (sm.path[nb][t] == sp) break;
+            t = sm.link[nb][t];
+            if (++hops > 4 * kSlots) { err = kStatusChainLimit; t = -1; break; }
           }
-          __syncwarp();
-          if (cnt == K && K == kMaxCands && nb == 1) {
-            // the store to act[32] hits path_hash[0] in the reference layout
-            const int ev = __shfl_sync(kFull, Ls, K - 1);
-            if (lane == 0) sm.heads[0] = (int8_t)ev;
+          if (t < 0) {
             __syncwarp();
+            if (lane == 0) {
+              sm.link[nb][c] = sm.heads[b];
+              sm.heads[b] = (int8_t)c;
+              sm.hashmark[c] = 1;
+            }
+            __syncwarp();
+            if (cnt == K) {
+              const int wp = 63 - __clzll((long long)Lm);
+              if (K == kMaxCands && nb == 1) {
+                // the store to act[32] hits path_hash[0] in the reference layout
+                if (lane == 0) sm.heads[0] = sm.idx_at[wp];
+                __syncwarp();
+              }
+              Lm = (Lm & ~(1ull << wp)) | (1ull << ps);
+            } else {
+              Lm |= 1ull << ps;
+              cnt++;
+            }
+            continue;
           }
-          do_insert = true;
-        } else {
-          const long long tk = sm.key[nb][t];
-          if (tk <= sk) continue;
-          const unsigned tm = __ballot_sync(kFull, lane < cnt && Ls == t);
-          if (tm) {
-            const int tp = __ffs(tm) - 1;
-            const long long dk = __shfl_down_sync(kFull, Lk, 1);
-            const int ds = __shfl_down_sync(kFull, Ls, 1);
-            if (lane >= tp && lane < cnt - 1) { Lk = dk; Ls = ds; }
-            cnt--;
-            removed = true;
+          if (sm.key[nb][t] <= sk) continue;
+          const bool t_in = t < nch && ((Lm >> sm.pos[t]) & 1ull);
+          if (t_in) {
+            Lm = (Lm & ~(1ull << sm.pos[t])) | (1ull << ps);      // replace t by s
+          } else if (cnt == K) {
+            Lm = (Lm & ~(1ull << (63 - __clzll((long long)Lm)))) | (1ull << ps);
+          } else {
+            Lm |= 1ull << ps;
+            cnt++;
           }
-          do_insert = true;
-        }
-        if (do_insert) {
-          const int ip = __popc(__ballot_sync(kFull, lane < cnt && Lk <= sk));
-          const long long uk = __shfl_up_sync(kFull, Lk, 1);
-          const int us = __shfl_up_sync(kFull, Ls, 1);
-          if (lane > ip) { Lk = uk; Ls = us; }
-          if (lane == ip) { Lk = sk; Ls = c; }
-          if (removed || cnt < K) cnt++;
-          worst = __shfl_sync(kFull, Lk, cnt - 1);
         }
       }
-    }
+      // act[rank] = the child at the rank-th set position
+      const unsigned long long lowA = (1ull << (2 * lane)) - 1ull;
+      if ((Lm >> (2 * lane)) & 1ull) sm.act[__popcll(Lm & lowA)] = (int8_t)si0;
+      if ((Lm >> (2 * lane + 1)) & 1ull) sm.act[__popcll(Lm & (lowA | (1ull << (2 * lane))))] = (int8_t)si1;
+      __syncwarp();
+      if (lane < cnt) {
+        Ls = sm.act[lane];
+        Lk = sm.key[nb][Ls];
+      }
+      __syncwarp();
     }
 
     if (fast_ok) {
@@ -432,10 +503,22 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     const int hh = surv ? (Ls & 1) : 0;
     const double f00 = __shfl_sync(kFull, s00, pp);
     const double f01 = __shfl_sync(kFull, s01, pp);
-    double ns[N];
-    ns[0] = hh ? f01 : f00;
+    const double fS1 = __shfl_sync(kFull, S[1], pp);
+    Pack<N> fp;
+    fp.G0 = __shfl_sync(kFull, npk.G0, pp);
+    if (N >= 3) fp.G1 = __shfl_sync(kFull, npk.G1, pp);
 #pragma unroll
-    for (int k = 1; k < N; k++) ns[k] = __shfl_sync(kFull, d[k], pp);
+    for (int i = 2; i < N; i++) {
+      fp.D[i] = __shfl_sync(kFull, npk.D[i], pp);
+      fp.A[i] = __shfl_sync(kFull, npk.A[i], pp);
+    }
+    const bool last = (t == n_in - 1);
+    double fs[N];
+    if (last) {
+      // the full child state is only needed when the context is stored
+#pragma unroll
+      for (int i = 2; i < N; i++) fs[i] = __shfl_sync(kFull, S[i], pp);
+    }
     const unsigned long long npath = shfl64(q, pp) | (unsigned long long)hh;
     const int nnext = __shfl_sync(kFull, new_next, pp);
     uint32_t nring[kRegRingWords];
@@ -443,8 +526,19 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     for (int w = 0; w < kRegRingWords; w++)
       nring[w] = (w < W) ? __shfl_sync(kFull, ring[w], pp) : 0u;
     if (surv) {
+      cs0 = hh ? f01 : f00;
+      cs1 = fS1;
+      pk.G0 = fp.G0;
+      if (N >= 3) pk.G1 = fp.G1;
 #pragma unroll
-      for (int k = 0; k < N; k++) s[k] = ns[k];
+      for (int i = 2; i < N; i++) { pk.D[i] = fp.D[i]; pk.A[i] = fp.A[i]; }
+      if (last) {
+        // the child state, stored now so no register holds it through the loop
+        dst->s[lane][0] = cs0;
+        dst->s[lane][1] = cs1;
+#pragma unroll
+        for (int i = 2; i < N; i++) dst->s[lane][i] = fs[i];
+      }
       cost = __dsub_rn(__longlong_as_double(Lk), min_cost);
       path = npath;
       nxt = nnext;
@@ -474,10 +568,8 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     }
   }
 
-  // ---- store the context ----
+  // ---- store the context (the states were stored at the last sample) ----
   if (lane < n) {
-#pragma unroll
-    for (int k = 0; k < N; k++) dst->s[lane][k] = s[k];
     dst->cost[lane] = cost;
     dst->path[lane] = path;
     dst->next[lane] = (uint8_t)nxt;
@@ -507,7 +599,7 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
 }
 
 template <int N>
-__global__ void __launch_bounds__(kMaxWarpsPerBlock * 32)
+__global__ void __launch_bounds__(32, 13)
 sdm_jobs_kernel(SdmParams P, const SdmJob* __restrict__ jobs, int njobs,
                 int* __restrict__ job_counter, SdmCtx* __restrict__ ctxs,
                 int* __restrict__ status) {
@@ -525,14 +617,12 @@ sdm_jobs_kernel(SdmParams P, const SdmJob* __restrict__ jobs, int njobs,
   }
 }
 
-// Host-side launcher: one warp per job, `warps_per_block` warps per CTA (1..4;
-// small CTAs spread a few thousand long-running jobs evenly over the SMs).
+// Host-side launcher: one warp-sized CTA per job.
 int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_counter,
-                    SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream,
-                    int warps_per_block) {
+                    SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream) {
   if (njobs <= 0) return 0;
-  int wpb = warps_per_block < 1 ? 1 : (warps_per_block > kMaxWarpsPerBlock ? kMaxWarpsPerBlock : warps_per_block);
-  int blocks = (njobs + wpb - 1) / wpb;
+  const int wpb = 1;
+  int blocks = njobs;
   if (max_blocks > 0 && blocks > max_blocks) blocks = max_blocks;
   cudaMemsetAsync(d_counter, 0, sizeof(int), stream);
   const dim3 grid(blocks), block(wpb * 32);

@@ -128,8 +128,6 @@ const char *dsdgpu_last_error(const dsdgpu_context_t *ctx);
 #define DSDGPU_SELECT_VERIFY    2   /*   serial, and the parallel result is checked
                                          against it every sample (a disagreement
                                          returns DSDGPU_ERR_DEVICE) */
-#define DSDGPU_OPT_SDM_WARPS_PER_BLOCK 2  /* SDM launch shape: warps (jobs) per CTA,
-                                              1..4, default 1 */
 int  dsdgpu_set_option(dsdgpu_context_t *ctx, int option, int value);
 
 /* Number of kernels this context has launched so far. */
