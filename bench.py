@@ -38,6 +38,7 @@ WL = dict(workload="dsd128_das_stereo_10s_multitone_pink", fs_in=48000, fs_out=6
           das_seg_len=65536, das_overlap=64 * 128, seed_mode="full_parallel", output="dop",
           boxcar_taps=8, soft_clip=True, seed=1001)
 FP64_OPS_PER_CAND_SAMPLE = 5 * WL["ntf_order"] + 6   # (2N+1) mul + (3N+5) add
+SDM_DRAM_BYTES_PER_SAMPLE = 9.04                      # measured, see the traffic note below
 
 
 def parse():
@@ -59,6 +60,25 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", str(rank)))
     return rank, world, local
+
+
+def max_over_ranks(seconds: float) -> float:
+    """The job's time: the slowest rank's timed region (all-reduce MAX).
+    Works on whatever process group is initialised (NCCL on GPUs, gloo on CPU)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(seconds)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(samples_per_rank_step: int, steps: int, world: int, job_seconds: float) -> float:
+    """Whole-job DSD Msamples/s: every rank converts its own stream (weak
+    scaling), so the job's samples are world x the per-rank count."""
+    return samples_per_rank_step * steps * world / job_seconds / 1e6
 
 
 class ClockSampler:
@@ -161,7 +181,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * float(np.mean(secs)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": dict(WL, cpu_sample_seconds=sample_s),
+            "data": "synthetic", "config": dict(WL, seconds=args.seconds, cpu_sample_seconds=sample_s),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": "port",
                              "sample": info["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -248,14 +268,9 @@ def run_ours(args):
     sdm_samples = (enc.sdm_work()[0] - sdm0) / args.steps
     stages = enc.stage_ms()
 
-    total_s = sum(step_ms) / 1000.0
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
+    total_s = max_over_ranks(sum(step_ms) / 1000.0)
     out_samples_step = n_out * nch                 # both channels
-    value = out_samples_step * args.steps * world / total_s / 1e6
+    value = job_throughput(out_samples_step, args.steps, world, total_s)
     xrt = (n_out / WL["fs_out"]) * args.steps / total_s
 
     # end to end through the host-buffer C-ABI call (pinned host memory)
@@ -265,8 +280,8 @@ def run_ours(args):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         ns, nb = enc.process_host(h_pcm, h_out)
-    e2e_s = time.perf_counter() - t0
-    e2e_value = ns * nch * args.steps * world / e2e_s / 1e6
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_value = job_throughput(ns * nch, args.steps, world, e2e_s)
 
     # roofline of the dominant kernel: the persistent trellis SDM launch
     sdm_s = statistics.mean(sdm_ms) / 1000.0
@@ -280,13 +295,12 @@ def run_ours(args):
                 "algorithmic_flops_per_launch": flops,
                 "sdm_input_samples_per_launch": sdm_samples,
                 "flops_per_sample": WL["cands"] * FP64_OPS_PER_CAND_SAMPLE}
-    prof = os.path.join(ROOT, "profiles", "sdm_dram_traffic.json")
-    if os.path.exists(prof):
-        try:
-            with open(prof) as fh:
-                roofline["traffic"] = json.load(fh).get("bytes_per_launch_scaled")
-        except (OSError, ValueError):
-            pass
+    # DRAM bytes per launch: ncu's dram__bytes for the SDM kernel on the 4 s,
+    # 32,768-segment case (profiles/sdm_jobs_kernel_dsd128_das_4s.md) gave
+    # 9.04 B per SDM input sample; the traffic grows with the samples processed.
+    roofline["traffic"] = SDM_DRAM_BYTES_PER_SAMPLE * sdm_samples
+    roofline["traffic_source"] = ("ncu dram__bytes of a 73.7 M-sample launch, "
+                                  "scaled by SDM input samples")
 
     plain = None
     if not args.no_plain and rank == 0:
@@ -310,7 +324,7 @@ def run_ours(args):
                 "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": 1000 * total_s / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": dict(WL, l2="512 MiB written between timed steps (outside the events)",
+                "config": dict(WL, seconds=args.seconds, l2="512 MiB written between timed steps (outside the events)",
                                fir_gain=PCM_FIR_GAIN),
                 "xrt": xrt,
                 "e2e": {"value": e2e_value, "unit": UNIT,
