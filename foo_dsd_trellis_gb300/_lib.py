@@ -58,6 +58,19 @@ class PipelineParams(C.Structure):
                 ("output_format", C.c_int)]
 
 
+class StreamDesc(C.Structure):
+    _fields_ = [("fs_in", C.c_int32), ("fs_out", C.c_int32), ("channels", C.c_int32),
+                ("boxcar_taps", C.c_int32), ("frames", C.c_int64), ("gain", C.c_double),
+                ("soft_clip", C.c_int32), ("reposition", C.c_int32), ("sdm", SdmParams)]
+
+
+class PlanInfo(C.Structure):
+    _fields_ = [("seg_len", C.c_int64), ("jobs", C.c_int64), ("sdm_samples", C.c_int64),
+                ("out_samples", C.c_int64), ("device_bytes", C.c_int64),
+                ("classes", C.c_int32), ("blocks_per_sm", C.c_int32),
+                ("predicted_ms", C.c_double)]
+
+
 OUT_BITS = 0
 OUT_DOP = 1
 OUT_NATIVE = 2
@@ -106,6 +119,17 @@ SIGNATURES = {
     "dsdgpu_sdm_process_noalloc": (C.c_int, [C.POINTER(SdmParams), C.c_int, _vp, _sz, _sz,
                                              _vp, _sz, _szp, _vp]),
     "dsdgpu_probe_fp64": (C.c_int, [_vp, C.POINTER(C.c_double)]),
+    "dsdgpu_plan_create": (C.c_int, [_vp, C.POINTER(StreamDesc), C.c_int, C.c_int64, C.c_int,
+                                     C.c_uint64, C.POINTER(_vp)]),
+    "dsdgpu_plan_destroy": (None, [_vp]),
+    "dsdgpu_plan_info": (C.c_int, [_vp, C.POINTER(PlanInfo)]),
+    "dsdgpu_plan_stream": (C.c_int, [_vp, C.c_int, C.POINTER(_vp), _szp, C.POINTER(_vp), _szp,
+                                     _szp, _szp]),
+    "dsdgpu_plan_run": (C.c_int, [_vp]),
+    "dsdgpu_plan_run_host": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp)]),
+    "dsdgpu_plan_times": (C.c_int, [_vp, C.POINTER(C.c_float)]),
+    "dsdgpu_plan_time_plain": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int64),
+                                         C.POINTER(C.c_double)]),
     "dsdgpu_fir_setup": (C.c_int, [_vp, C.POINTER(FirParams), C.c_int]),
     "dsdgpu_fir_reset": (C.c_int, [_vp]),
     "dsdgpu_fir_process": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp, _sz,

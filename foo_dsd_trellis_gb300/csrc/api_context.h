@@ -12,6 +12,21 @@
 #include "fir_internal.h"
 #include "das_internal.h"
 
+// Validated copy of the ABI's trellis parameters (sdm_context_init's limits,
+// src/trellis.c:977-1011, plus this build's register-ring latency bound).
+int sdm_params_from_abi(const dsdgpu_sdm_params_t* p, dsdgpu::SdmParams* P, const char** err);
+
+namespace dsdgpu {
+int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_counter,
+                    SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream);
+int init_contexts(SdmCtx* d_ctxs, int first, int count, int keep_counters, cudaStream_t stream);
+int sdm_max_lat_in_registers();
+int launch_pack_dop(const uint8_t* bits, size_t stride, int nch, size_t frames, int phase,
+                    uint8_t* out, int num_sms, cudaStream_t stream);
+int launch_pack_native(const uint8_t* bits, size_t stride, int nch, size_t n, uint8_t* out,
+                       size_t out_stride, int num_sms, cudaStream_t stream);
+}  // namespace dsdgpu
+
 struct dsdgpu_context {
   int device = 0;
   int num_sms = 0;

@@ -18,6 +18,7 @@
 // so every boundary is searched in parallel and the assembly is a gather.
 #include "api_context.h"
 #include "das_internal.h"
+#include "das_plan.h"
 
 #include <algorithm>
 #include <cmath>
@@ -29,14 +30,14 @@ namespace dsdgpu {
 int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_counter,
                     SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream);
 
-constexpr int kSeamThreads = 512;
 constexpr int kMaxQ = 32;
 
 // ---- window RMS (src/dsp_plugin.c:1975-1978): serial FP64 sum of squares ----
 __global__ void das_rms_kernel(const double* __restrict__ x, const long long* __restrict__ centers,
-                               int n, int win, double* __restrict__ out) {
+                               int n, double* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const long long win = kRmsWindow;
   const long long c = centers[i];
   double s = 0.0;
   for (long long k = c - win / 2; k < c + win / 2; k++) s = __dadd_rn(s, __dmul_rn(x[k], x[k]));
@@ -107,10 +108,11 @@ __global__ void das_seed_from_best_kernel(const SdmCtx* __restrict__ ctxs, int f
 // ---- seam search, one CTA per boundary (src/dsp_plugin.c:2455-2652) ----
 __global__ void __launch_bounds__(kSeamThreads)
 das_seam_kernel(const SeamTask* __restrict__ tasks, int ntasks, const double* __restrict__ qfir2,
-                int lat, int* __restrict__ bp_out) {
+                int* __restrict__ bp_out) {
   const int ti = blockIdx.x;
   if (ti >= ntasks) return;
   const SeamTask T = tasks[ti];
+  const int lat = T.lat;
   const int L = T.ovl_len;
   extern __shared__ unsigned char smraw[];
   int8_t* dif = (int8_t*)smraw;                       // next - prev in {-1, 0, 1} (x2 later)
@@ -353,6 +355,43 @@ void pop_fir_times_two(double* q2) {
   for (int i = 0; i < N; i++) q2[i] = 2.0 * (q[i] / sum);
 }
 
+int launch_das_rms(const double* x, const long long* d_centers, int n, double* d_out,
+                   cudaStream_t stream) {
+  if (n <= 0) return 0;
+  das_rms_kernel<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(x, d_centers, n, d_out);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+size_t das_seam_smem(int max_ovl) {
+  return ((size_t)(max_ovl + 15) & ~(size_t)15) + sizeof(int) * (size_t)(max_ovl + 1) + 64;
+}
+
+int das_seam_prepare(int max_ovl) {
+  const size_t smem = das_seam_smem(max_ovl);
+  if (smem <= 48 * 1024) return 0;
+  return cudaFuncSetAttribute(das_seam_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)smem) == cudaSuccess ? 0 : -1;
+}
+
+int launch_das_seams(const SeamTask* d_tasks, int ntasks, int max_ovl, const double* d_qfir2,
+                     int* d_bp, cudaStream_t stream) {
+  if (ntasks <= 0) return 0;
+  if (max_ovl > kMaxSeamOverlap) return -2;
+  const size_t smem = das_seam_smem(max_ovl);
+  das_seam_kernel<<<(unsigned)ntasks, kSeamThreads, smem, stream>>>(d_tasks, ntasks, d_qfir2, d_bp);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_das_assemble(const AssemblePiece* d_pieces, int npieces, const int* d_bp, uint8_t* out,
+                        size_t out_stride, int nch, int S, const SegBuf* d_segbuf,
+                        cudaStream_t stream) {
+  if (npieces <= 0) return 0;
+  const dim3 grid(64, (unsigned)npieces);
+  das_assemble_kernel<<<grid, 256, 0, stream>>>(d_pieces, npieces, d_bp, out, out_stride, nch, S,
+                                                d_segbuf);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 }  // namespace dsdgpu
 
 using namespace dsdgpu;
@@ -407,98 +446,35 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
   const size_t overlap = 64 * (size_t)lat;
 
   // ---- layout (src/dsp_plugin.c:1343-1366, 1936-1957) ----
-  int S = dp->seg_len > 0 ? (int)(count / (size_t)dp->seg_len) : dp->nsegs;
-  if (S < 1) S = 1;
-  size_t min_seg = overlap * 4;
-  if (min_seg < 256) min_seg = 256;
-  while (S > 1 && count / (size_t)S < min_seg) S--;
-  std::vector<long long> start(S), size(S);
-  {
-    size_t base = count / (size_t)S, rem = count % (size_t)S, pos = 0;
-    for (int s = 0; s < S; s++) {
-      start[s] = (long long)pos;
-      size[s] = (long long)((s == S - 1) ? count - pos : base + ((size_t)s < rem ? 1 : 0));
-      pos += (size_t)size[s];
-    }
-  }
+  std::vector<long long> start, size;
+  const int S = das_nominal_layout(count, dp->seg_len, dp->nsegs, overlap, start, size);
   int rc;
   // ---- reposition of quiet boundaries (src/dsp_plugin.c:1959-2024) ----
   if (dp->reposition && S > 2) {
-    const long long win = 2048;
-    std::vector<long long> centers;
-    std::vector<int> which;
-    for (int s = 2; s < S; s++) {
-      const long long b = start[s];
-      if (b < win || b + win >= (long long)count) continue;
-      centers.push_back(b);
-      which.push_back(s);
-    }
-    if (!centers.empty()) {
-      rc = ensure_dev(c, &c->d_das_i64, &c->das_i64_cap, centers.size(), "rms centers");
-      if (rc) return rc;
-      rc = ensure_dev(c, &c->d_das_f64, &c->das_f64_cap, centers.size(), "rms values");
-      if (rc) return rc;
+    RmsEval rms = [&](const std::vector<long long>& centers, std::vector<double>& out) -> int {
+      int r = ensure_dev(c, &c->d_das_i64, &c->das_i64_cap, centers.size(), "rms centers");
+      if (r) return r;
+      r = ensure_dev(c, &c->d_das_f64, &c->das_f64_cap, centers.size(), "rms values");
+      if (r) return r;
       cudaMemcpyAsync(c->d_das_i64, centers.data(), sizeof(long long) * centers.size(),
                       cudaMemcpyHostToDevice, c->stream);
-      das_rms_kernel<<<(unsigned)((centers.size() + 127) / 128), 128, 0, c->stream>>>(
-          d_fir, c->d_das_i64, (int)centers.size(), (int)win, c->d_das_f64); c->launches++;
-      std::vector<double> cur(centers.size());
-      cudaMemcpyAsync(cur.data(), c->d_das_f64, sizeof(double) * cur.size(), cudaMemcpyDeviceToHost, c->stream);
-      rc = c->check_status();
+      if (launch_das_rms(d_fir, c->d_das_i64, (int)centers.size(), c->d_das_f64, c->stream) != 0)
+        return c->cuda_fail(cudaGetLastError(), "rms launch");
+      c->launches++;
+      out.resize(centers.size());
+      cudaMemcpyAsync(out.data(), c->d_das_f64, sizeof(double) * out.size(), cudaMemcpyDeviceToHost,
+                      c->stream);
+      return c->check_status();
+    };
+    std::vector<long long> centers;
+    std::vector<int> which;
+    das_reposition_centers(start, count, centers, which);
+    if (!centers.empty()) {
+      std::vector<double> cur;
+      rc = rms(centers, cur);
       if (rc) return rc;
-      const size_t base = count / (size_t)S;
-      long long max_shift = (long long)(base * 2 / 5);
-      if (max_shift > 200000) max_shift = 200000;
-      const long long step = win / 2;
-      for (size_t wi = 0; wi < which.size(); wi++) {
-        if (cur[wi] > 0.005) continue;
-        const int s = which[wi];
-        // RMS at every offset this boundary could try; the constraints below
-        // depend on the neighbours' (possibly moved) starts, the RMS does not
-        std::vector<long long> cand;
-        const long long b = start[s];
-        for (long long off = step; off <= max_shift; off += step)
-          for (int dir = -1; dir <= 1; dir += 2) {
-            const long long cc = dir < 0 ? (b > off ? b - off : 0) : b + off;
-            if (cc < win / 2 || cc + win / 2 >= (long long)count) continue;
-            cand.push_back(cc);
-          }
-        std::vector<double> rms(cand.size());
-        if (!cand.empty()) {
-          rc = ensure_dev(c, &c->d_das_i64, &c->das_i64_cap, cand.size(), "rms centers");
-          if (rc) return rc;
-          rc = ensure_dev(c, &c->d_das_f64, &c->das_f64_cap, cand.size(), "rms values");
-          if (rc) return rc;
-          cudaMemcpyAsync(c->d_das_i64, cand.data(), sizeof(long long) * cand.size(),
-                          cudaMemcpyHostToDevice, c->stream);
-          das_rms_kernel<<<(unsigned)((cand.size() + 127) / 128), 128, 0, c->stream>>>(
-              d_fir, c->d_das_i64, (int)cand.size(), (int)win, c->d_das_f64); c->launches++;
-          cudaMemcpyAsync(rms.data(), c->d_das_f64, sizeof(double) * rms.size(), cudaMemcpyDeviceToHost, c->stream);
-          rc = c->check_status();
-          if (rc) return rc;
-        }
-        long long best_pos = b;
-        double best_rms = cur[wi];
-        size_t ci = 0;
-        for (long long off = step; off <= max_shift; off += step) {
-          for (int dir = -1; dir <= 1; dir += 2) {
-            const long long cc = dir < 0 ? (b > off ? b - off : 0) : b + off;
-            if (cc < win / 2 || cc + win / 2 >= (long long)count) continue;
-            const double r = rms[ci++];
-            if (s > 0 && cc <= start[s - 1] + (long long)overlap * 2) continue;
-            if (s < S - 1 && start[s + 1] >= (long long)overlap * 2 &&
-                cc >= start[s + 1] - (long long)overlap * 2)
-              continue;
-            if (r > best_rms) { best_rms = r; best_pos = cc; }
-          }
-          if (best_rms > 0.005) break;
-        }
-        if (best_pos != b) {
-          start[s] = best_pos;
-          size[s - 1] = best_pos - start[s - 1];
-          size[s] = (s < S - 1) ? start[s + 1] - best_pos : (long long)count - best_pos;
-        }
-      }
+      rc = das_reposition_apply(start, size, count, overlap, which, cur, rms);
+      if (rc) return rc;
     }
   }
 
@@ -511,35 +487,14 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
   if (rc) return rc;
 
   // segment output buffers
-  std::vector<long long> seg_in_start(S), seg_in_count(S), seg_discard(S);
+  std::vector<long long> seg_in_start, seg_in_count, seg_discard;
+  das_segment_io(start, size, count, overlap, lat, seg0_first, seg_in_start, seg_in_count,
+                 seg_discard);
   size_t buf_total = 0;
   std::vector<size_t> seg_off(S);
   for (int s = 0; s < S; s++) {
-    const bool ext = s < S - 1;
-    long long in_start, in_cnt, disc = 0;
-    if (s == 0) {
-      in_start = 0;
-      in_cnt = size[0];
-      if (seg0_first) {
-        // no extension
-      } else if (ext && size[0] + (long long)overlap <= (long long)count) {
-        in_cnt += (long long)overlap;
-      }
-    } else if (s == 1 && seg0_first) {
-      in_start = start[1];
-      in_cnt = size[1];
-      if (S > 2 && start[1] + size[1] + (long long)overlap <= (long long)count) in_cnt += (long long)overlap;
-    } else {
-      in_start = start[s] >= (long long)overlap ? start[s] - (long long)overlap : 0;
-      in_cnt = start[s] + size[s] - in_start;
-      if (ext && start[s] + size[s] + (long long)overlap <= (long long)count) in_cnt += (long long)overlap;
-      disc = start[s] >= (long long)overlap ? (long long)overlap - lat : 0;
-    }
-    seg_in_start[s] = in_start;
-    seg_in_count[s] = in_cnt;
-    seg_discard[s] = disc;
     seg_off[s] = buf_total;
-    buf_total += ((size_t)in_cnt + 255) & ~(size_t)255;
+    buf_total += ((size_t)seg_in_count[s] + 255) & ~(size_t)255;
   }
   rc = ensure_dev(c, &c->d_das_bits, &c->das_bits_cap, buf_total * (size_t)nch + 256, "segment buffers");
   if (rc) return rc;
@@ -552,7 +507,7 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
   auto add_job = [&](std::vector<SdmJob>& jobs, int ch, int s, int ctx, int copy_from, bool seed,
                      int pend_from) {
     int64_t skip, out, np;
-    c->plan_steps(c->pending[pend_from], seg_in_count[s], seg_discard[s], &skip, &out, &np);
+    sdm_plan_steps(lat, c->pending[pend_from], seg_in_count[s], seg_discard[s], &skip, &out, &np);
     c->pending[ctx] = np;
     c->draining[ctx] = c->draining[pend_from];
     seg_out[(size_t)ch * S + s] = out;
@@ -565,7 +520,7 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
     j.ctx = ctx;
     j.copy_from = copy_from;
     j.seed_state = seed ? c->d_das_est + ((size_t)ch * S + s) * kMaxOrder : nullptr;
-    j.pad = 0;
+    j.flags = 0;
     jobs.push_back(j);
   };
   int first_par = 0;
@@ -620,54 +575,27 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
   }
 
   // ---- stream plan: write positions do not depend on the seams ----
-  std::vector<long long> cnt(S), ps(S, 0), wp(S, 0);
-  std::vector<int> stitched(S, 0), used(S, 0);
-  for (int s = 0; s < S; s++) cnt[s] = seg_out[s];
-  if (!seg0_first && cnt[0] > size[0]) cnt[0] = size[0];
-  long long w = cnt[0];
-  wp[0] = w;
-  used[0] = 1;
+  std::vector<SeamPlan> splan;
+  std::vector<AssemblePiece> pieces;
+  long long final_count = 0;
+  {
+    const char* err = nullptr;
+    if (das_stream_plan(S, seg_out.data(), size, overlap, seg0_first, splan, pieces, &final_count,
+                        &err) != 0)
+      return c->fail(DSDGPU_ERR_UNSUPPORTED, err);
+  }
   std::vector<SeamTask> tasks;
-  int last_used = 0;
-  for (int s = 1; s < S; s++) {
-    const long long so = seg_out[s];
-    if (so == 0) continue;
-    used[s] = 1;
-    if (s == 1 && seg0_first) {
-      ps[s] = w;                  // DIRECT: appended as is
-      w += so;
-      wp[s] = w;
-      last_used = s;
-      continue;
-    }
-    if (w < (long long)overlap)
-      return c->fail(DSDGPU_ERR_UNSUPPORTED, "stream shorter than the overlap before a seam");
-    const long long pstart = w - (long long)overlap;
-    long long ol = w - pstart;
-    if (ol > so) ol = so;
-    if (ol > (long long)overlap) ol = (long long)overlap;
-    // the previous `overlap` stream decisions must all come from segment
-    // last_used: its copied part starts at base (+ its seam, < overlap)
-    const bool prev_stitched = stitched[last_used] != 0;
-    const long long base_last = last_used == 0 ? 0 : ps[last_used];
-    const long long prev_len = prev_stitched ? seg_out[last_used] : cnt[last_used];
-    if (prev_stitched ? (prev_len < 2 * (long long)overlap) : (prev_len < (long long)overlap))
-      return c->fail(DSDGPU_ERR_UNSUPPORTED, "segment shorter than the overlap");
+  for (const SeamPlan& sp : splan) {
     SeamTask t;
-    t.boundary = s;
-    t.ovl_len = (int)ol;
-    t.prev_seg = last_used;
-    t.prev_off = pstart - base_last;
+    t.boundary = sp.boundary;
+    t.ovl_len = sp.ovl_len;
+    t.prev_seg = sp.prev_seg;
+    t.prev_off = sp.prev_off;
+    t.lat = lat;
     t.prev = nullptr;
     t.next = nullptr;
     tasks.push_back(t);
-    ps[s] = pstart;
-    stitched[s] = 1;
-    w = pstart + so;
-    wp[s] = w;
-    last_used = s;
   }
-  const long long final_count = w;
   if (out_count) *out_count = (size_t)final_count;
   if (out_stride < (size_t)final_count) return c->fail(DSDGPU_ERR_ARG, "output stride too small");
 
@@ -695,41 +623,16 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
                     cudaMemcpyHostToDevice, c->stream);
     int maxL = 0;
     for (auto& t : tasks) maxL = std::max(maxL, t.ovl_len);
-    const size_t smem = ((size_t)(maxL + 15) & ~(size_t)15) + sizeof(int) * (size_t)(maxL + 1) + 64;
-    if (smem > 48 * 1024)
-      cudaFuncSetAttribute(das_seam_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (maxL > 32 * kSeamThreads) return c->fail(DSDGPU_ERR_UNSUPPORTED, "overlap too long for the seam kernel");
-    das_seam_kernel<<<(unsigned)tasks.size(), kSeamThreads, smem, c->stream>>>(
-        c->d_das_tasks, (int)tasks.size(), c->d_das_qfir, lat, c->d_das_bp); c->launches++;
+    if (maxL > kMaxSeamOverlap) return c->fail(DSDGPU_ERR_UNSUPPORTED, "overlap too long for the seam kernel");
+    if (das_seam_prepare(maxL) != 0) return c->cuda_fail(cudaGetLastError(), "seam kernel attributes");
+    rc = launch_das_seams(c->d_das_tasks, (int)tasks.size(), maxL, c->d_das_qfir, c->d_das_bp,
+                          c->stream);
+    if (rc == -2) return c->fail(DSDGPU_ERR_UNSUPPORTED, "overlap too long for the seam kernel");
+    if (rc) return c->cuda_fail(cudaGetLastError(), "seam launch");
+    c->launches++;
   }
 
   // ---- assembly ----
-  std::vector<AssemblePiece> pieces;
-  std::vector<int> order_used;
-  for (int s = 0; s < S; s++)
-    if (used[s]) order_used.push_back(s);
-  for (size_t i = 0; i < order_used.size(); i++) {
-    const int s = order_used[i];
-    AssemblePiece p;
-    p.seg = s;
-    p.base = (s == 0) ? 0 : ps[s];
-    p.stitched = stitched[s];
-    p.end_base = wp[s];
-    p.next_stitched = 0;
-    p.next_seg = 0;
-    p.next_base = 0;
-    if (i + 1 < order_used.size()) {
-      const int n = order_used[i + 1];
-      if (stitched[n]) {
-        p.next_stitched = 1;
-        p.next_seg = n;
-        p.next_base = ps[n];
-      } else {
-        p.end_base = ps[n];   // DIRECT follower starts at our end
-      }
-    }
-    pieces.push_back(p);
-  }
   std::vector<SegBuf> sb((size_t)nch * S);
   for (int ch = 0; ch < nch; ch++)
     for (int s = 0; s < S; s++) sb[(size_t)ch * S + s].ptr = seg_ptr(ch, s);
@@ -742,10 +645,10 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
   cudaMemcpyAsync(c->d_das_segbuf, sb.data(), sizeof(SegBuf) * sb.size(), cudaMemcpyHostToDevice,
                   c->stream);
   if (!pieces.empty()) {
-    const dim3 grid(64, (unsigned)pieces.size());
-    das_assemble_kernel<<<grid, 256, 0, c->stream>>>(c->d_das_pieces, (int)pieces.size(),
-                                                      c->d_das_bp, d_out, out_stride, nch, S,
-                                                      c->d_das_segbuf); c->launches++;
+    if (launch_das_assemble(c->d_das_pieces, (int)pieces.size(), c->d_das_bp, d_out, out_stride, nch,
+                            S, c->d_das_segbuf, c->stream) != 0)
+      return c->cuda_fail(cudaGetLastError(), "assembly launch");
+    c->launches++;
   }
 
   // ---- state carry: persistent <- last temp (src/dsp_plugin.c:2715-2725) ----

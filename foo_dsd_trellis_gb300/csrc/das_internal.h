@@ -1,6 +1,8 @@
 // Device-side plan records of the DAS pipeline.
 #pragma once
+#include <cstddef>
 #include <cstdint>
+#include <cuda_runtime.h>
 
 namespace dsdgpu {
 
@@ -11,11 +13,14 @@ struct SeamTask {
   const uint8_t* prev;
   const uint8_t* next;
   long long prev_off;
-  int boundary;
+  int boundary;           // index into the seam-position array
   int ovl_len;
   int prev_seg;
-  int pad;
+  int lat;                // trellis latency of the stream (density window)
 };
+
+constexpr int kSeamThreads = 512;
+constexpr int kMaxSeamOverlap = 32 * kSeamThreads;   // density values held per thread
 
 // One gather range of the final stream: segment `seg` supplies stream
 // positions [base + (stitched ? bp[seg] : 0), end), where end is the next
@@ -34,5 +39,17 @@ struct AssemblePiece {
 struct SegBuf {
   const uint8_t* ptr;
 };
+
+// Launchers of the DAS kernels (das.cu); 0 on success.
+int launch_das_rms(const double* x, const long long* d_centers, int n, double* d_out,
+                   cudaStream_t stream);
+size_t das_seam_smem(int max_ovl);
+int das_seam_prepare(int max_ovl);   // kernel attributes (call outside stream capture)
+int launch_das_seams(const SeamTask* d_tasks, int ntasks, int max_ovl, const double* d_qfir2,
+                     int* d_bp, cudaStream_t stream);   // -2: overlap above kMaxSeamOverlap
+int launch_das_assemble(const AssemblePiece* d_pieces, int npieces, const int* d_bp, uint8_t* out,
+                        size_t out_stride, int nch, int S, const SegBuf* d_segbuf,
+                        cudaStream_t stream);
+void pop_fir_times_two(double* q2);
 
 }  // namespace dsdgpu

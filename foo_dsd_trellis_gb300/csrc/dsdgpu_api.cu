@@ -2,6 +2,7 @@
 // trellis SDM entry points.  The FIR, DAS and packing entry points live in
 // their own translation units and share the context defined in api_context.h.
 #include "api_context.h"
+#include "das_plan.h"
 
 #include <algorithm>
 #include <cstdio>
@@ -141,29 +142,29 @@ int dsdgpu_context::run_jobs(const std::vector<SdmJob>& jobs) {
 
 // Segment bookkeeping of sdm_process_block / sdm_segment_process: how many
 // leading steps produce no kept decision, and the pending count afterwards.
+int sdm_params_from_abi(const dsdgpu_sdm_params_t* p, dsdgpu::SdmParams* P, const char** err) {
+  if (p->order < 2 || p->order > kMaxOrder) { *err = "order out of range"; return DSDGPU_ERR_ARG; }
+  if (p->depth < 1 || p->depth > 64) { *err = "depth out of range"; return DSDGPU_ERR_ARG; }
+  if (p->cands < 1 || p->cands > kMaxCands) { *err = "cands out of range"; return DSDGPU_ERR_ARG; }
+  if (p->lat < 1 || p->lat > kMaxLat) { *err = "lat out of range"; return DSDGPU_ERR_ARG; }
+  if (p->lat > sdm_max_lat_in_registers()) {
+    *err = "lat above the register-ring limit of this build";
+    return DSDGPU_ERR_UNSUPPORTED;
+  }
+  memset(P, 0, sizeof *P);
+  for (int i = 0; i < p->order; i++) { P->a[i] = p->a[i]; P->g[i] = p->g[i]; }
+  P->state_limit = p->state_limit;
+  P->mask = p->depth >= 64 ? ~0ull : ((1ull << p->depth) - 1ull);
+  P->order = p->order;
+  P->cands = p->cands;
+  P->lat = p->lat;
+  P->depth = p->depth;
+  return DSDGPU_OK;
+}
+
 void dsdgpu_context::plan_steps(int64_t pend, int64_t count, int64_t discard, int64_t* skip,
                                 int64_t* out, int64_t* new_pend) const {
-  const int64_t lat = sdm.lat;
-  if (discard == 0) {
-    int64_t pre = std::min<int64_t>(lat - pend, count);
-    if (pre < 0) pre = 0;
-    *skip = pre;
-    *out = count - pre;
-    *new_pend = pend + pre;
-    return;
-  }
-  const int64_t warm = lat + discard;
-  if (warm > count) {
-    int64_t pre = std::min<int64_t>(lat - pend, count);
-    if (pre < 0) pre = 0;
-    *skip = count;
-    *out = 0;
-    *new_pend = pend + pre;
-  } else {
-    *skip = warm;
-    *out = count - warm;
-    *new_pend = lat;
-  }
+  sdm_plan_steps(sdm.lat, pend, count, discard, skip, out, new_pend);
 }
 
 extern "C" {
@@ -241,23 +242,12 @@ int dsdgpu_synchronize(dsdgpu_context_t* c) {
 
 int dsdgpu_sdm_setup(dsdgpu_context_t* c, const dsdgpu_sdm_params_t* p, int num_contexts) {
   if (!c || !p) return DSDGPU_ERR_ARG;
-  if (p->order < 2 || p->order > kMaxOrder) return c->fail(DSDGPU_ERR_ARG, "order out of range");
-  if (p->depth < 1 || p->depth > 64) return c->fail(DSDGPU_ERR_ARG, "depth out of range");
-  if (p->cands < 1 || p->cands > kMaxCands) return c->fail(DSDGPU_ERR_ARG, "cands out of range");
-  if (p->lat < 1 || p->lat > kMaxLat) return c->fail(DSDGPU_ERR_ARG, "lat out of range");
   if (num_contexts < 1) return c->fail(DSDGPU_ERR_ARG, "num_contexts < 1");
-  if (p->lat > sdm_max_lat_in_registers())
-    return c->fail(DSDGPU_ERR_UNSUPPORTED, "lat above the register-ring limit of this build");
-  cudaSetDevice(c->device);
   SdmParams P;
-  memset(&P, 0, sizeof P);
-  for (int i = 0; i < p->order; i++) { P.a[i] = p->a[i]; P.g[i] = p->g[i]; }
-  P.state_limit = p->state_limit;
-  P.mask = p->depth >= 64 ? ~0ull : ((1ull << p->depth) - 1ull);
-  P.order = p->order;
-  P.cands = p->cands;
-  P.lat = p->lat;
-  P.depth = p->depth;
+  const char* err = nullptr;
+  const int prc = sdm_params_from_abi(p, &P, &err);
+  if (prc) return c->fail(prc, err);
+  cudaSetDevice(c->device);
   if (c->d_ctx) cudaFree(c->d_ctx);
   c->d_ctx = nullptr;
   c->nctx = 0;
@@ -311,7 +301,7 @@ int dsdgpu_sdm_process(dsdgpu_context_t* c, int first, int nch, const double* d_
     j.ctx = idx;
     j.copy_from = -1;
     j.seed_state = nullptr;
-    j.pad = 0;
+    j.flags = 0;
     jobs.push_back(j);
   }
   return c->run_jobs(jobs);
@@ -374,7 +364,7 @@ int dsdgpu_sdm_drain(dsdgpu_context_t* c, int first, int nch, uint8_t* d_out, si
     j.ctx = idx;
     j.copy_from = -1;
     j.seed_state = nullptr;
-    j.pad = 0;
+    j.flags = 0;
     jobs.push_back(j);
   }
   return c->run_jobs(jobs);
@@ -437,7 +427,7 @@ int dsdgpu_sdm_segments(dsdgpu_context_t* c, dsdgpu_segment_t* segs, int nseg) {
     j.ctx = s.channel;
     j.copy_from = (s.seed_from >= 0 && s.seed_from != s.channel) ? s.seed_from : -1;
     j.seed_state = s.d_seed_state;
-    j.pad = 0;
+    j.flags = 0;
     jobs.push_back(j);
   }
   return c->run_jobs(jobs);

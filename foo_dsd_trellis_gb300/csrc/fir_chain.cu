@@ -30,19 +30,20 @@
 
 namespace dsdgpu {
 
-__constant__ FirChainConst c_fir;
-
 // floor division for possibly negative numerators
 __device__ __forceinline__ long long fdiv(long long a, int b) {
   return a >= 0 ? a / b : -((-a + b - 1) / b);
 }
 
+// The chain description is a by-value kernel parameter (constant bank, about
+// 8.5 KB): every launch carries its own chain, so contexts and batch streams
+// with different rate pairs never share mutable device constants.
 __global__ void __launch_bounds__(kFirThreads)
-fir_chain_kernel(const float* __restrict__ pcm, size_t pcm_stride, long long count,
-                 const float* __restrict__ hist, double* __restrict__ out, size_t out_stride,
-                 double g_start, double g_step, int apply_gain, int soft_clip) {
+fir_chain_kernel(const __grid_constant__ FirChainConst F, const float* __restrict__ pcm,
+                 size_t pcm_stride, long long count, const float* __restrict__ hist,
+                 double* __restrict__ out, size_t out_stride, double g_start, double g_step,
+                 int apply_gain, int soft_clip) {
   extern __shared__ float sm[];
-  const FirChainConst& F = c_fir;
   const int ch = blockIdx.y;
   const long long total_out = count * F.ratio;
   const long long o_lo = (long long)blockIdx.x * F.tile;
@@ -256,6 +257,42 @@ size_t chain_smem_bytes(const FirChainConst& F) {
   return (best + 16) * sizeof(float);
 }
 
+int fir_chain_prepare() {
+  // the shared-memory opt-in is a per-device function attribute
+  static bool attr_set[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return -1;
+  if (!attr_set[dev]) {
+    if (cudaFuncSetAttribute(fir_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kFirMaxSmem) != cudaSuccess)
+      return -1;
+    attr_set[dev] = true;
+  }
+  return 0;
+}
+
+int launch_fir_chain(const FirChainConst& F, size_t smem, const float* pcm, size_t pcm_stride,
+                     long long count, const float* hist, double* out, size_t out_stride,
+                     double g_start, double g_step, int apply_gain, int soft_clip, int nch,
+                     cudaStream_t stream) {
+  const long long n_out = count * (long long)F.ratio;
+  if (n_out <= 0) return 0;
+  if (fir_chain_prepare() != 0) return -1;
+  if (smem > (size_t)kFirMaxSmem) return -1;
+  const dim3 grid((unsigned)((n_out + F.tile - 1) / F.tile), (unsigned)nch);
+  fir_chain_kernel<<<grid, kFirThreads, smem, stream>>>(F, pcm, pcm_stride, count, hist, out,
+                                                        out_stride, g_start, g_step, apply_gain,
+                                                        soft_clip);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_fir_history(const float* pcm, size_t pcm_stride, long long count, float* hist, int nch,
+                       cudaStream_t stream) {
+  fir_history_kernel<<<nch, 128, 0, stream>>>(pcm, pcm_stride, count, hist);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 }  // namespace dsdgpu
 
 using namespace dsdgpu;
@@ -278,8 +315,7 @@ int dsdgpu_fir_setup(dsdgpu_context_t* c, const dsdgpu_fir_params_t* p, int num_
   c->fir_params = *p;
   c->fir_channels = num_channels;
   c->fir_smem = chain_smem_bytes(F);
-  if (c->fir_smem > 200 * 1024) return c->fail(DSDGPU_ERR_UNSUPPORTED, "fir tile does not fit shared memory");
-  cudaFuncSetAttribute(fir_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->fir_smem);
+  if (c->fir_smem > (size_t)kFirMaxSmem) return c->fail(DSDGPU_ERR_UNSUPPORTED, "fir tile does not fit shared memory");
   c->fir_ready = true;
   return c->check_status();
 }
@@ -309,17 +345,14 @@ int dsdgpu_fir_process_async(dsdgpu_context_t* c, int first, int nch, const floa
   if (gs == 0.0) gs = ge;
   const int apply = (gs != 1.0 || ge != 1.0) ? 1 : 0;
   const double step = (n_out > 1) ? (ge - gs) / (double)(n_out - 1) : 0.0;
-  cudaError_t e = cudaMemcpyToSymbolAsync(c_fir, &c->fir, sizeof(FirChainConst), 0,
-                                          cudaMemcpyHostToDevice, c->stream);
-  if (e != cudaSuccess) return c->cuda_fail(e, "fir constants");
-  const dim3 grid((unsigned)((n_out + c->fir.tile - 1) / c->fir.tile), (unsigned)nch);
   float* hist = c->d_fir_hist + (size_t)first * kHistory;
-  fir_chain_kernel<<<grid, kFirThreads, c->fir_smem, c->stream>>>(
-      d_in, in_stride, (long long)count, hist, d_out, out_stride, gs, step, apply,
-      c->fir_params.soft_clip); c->launches++;
-  fir_history_kernel<<<nch, 128, 0, c->stream>>>(d_in, in_stride, (long long)count, hist); c->launches++;
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return c->cuda_fail(e, "fir launch");
+  if (launch_fir_chain(c->fir, c->fir_smem, d_in, in_stride, (long long)count, hist, d_out,
+                       out_stride, gs, step, apply, c->fir_params.soft_clip, nch, c->stream) != 0)
+    return c->cuda_fail(cudaGetLastError(), "fir launch");
+  c->launches++;
+  if (launch_fir_history(d_in, in_stride, (long long)count, hist, nch, c->stream) != 0)
+    return c->cuda_fail(cudaGetLastError(), "fir history launch");
+  c->launches++;
   return DSDGPU_OK;
 }
 

@@ -1,5 +1,7 @@
 // Constant-memory description of a fused upsampling FIR chain.
 #pragma once
+#include <cstddef>
+#include <cuda_runtime.h>
 
 namespace dsdgpu {
 
@@ -7,6 +9,7 @@ constexpr int kMaxStages = 9;         // FIR_MAX_STAGES (reference include/fir.h
 constexpr int kMaxChainTaps = 1024;   // non-zero polyphase taps over all stages
 constexpr int kHistory = 256;         // PCM samples kept between blocks per channel
 constexpr int kFirThreads = 256;
+constexpr int kFirMaxSmem = 200 * 1024;   // dynamic shared memory cap of one FIR tile
 
 struct FirChainConst {
   int S;                               // number of stages
@@ -21,5 +24,17 @@ struct FirChainConst {
   float taps[kMaxChainTaps];           // h'[U*j + r] = U * h[U*j + r]
   int lag[kMaxChainTaps];              // j
 };
+
+// Chain construction (fir_chain_init_ex's stage plan and tap design) and the
+// launchers of the fused chain kernel and its history update.
+int build_chain_const(unsigned fs_in, unsigned fs_out, int boxcar, FirChainConst* F);
+size_t chain_smem_bytes(const FirChainConst& F);
+int fir_chain_prepare();   // kernel attributes (call outside stream capture)
+int launch_fir_chain(const FirChainConst& F, size_t smem, const float* pcm, size_t pcm_stride,
+                     long long count, const float* hist, double* out, size_t out_stride,
+                     double g_start, double g_step, int apply_gain, int soft_clip, int nch,
+                     cudaStream_t stream);
+int launch_fir_history(const float* pcm, size_t pcm_stride, long long count, float* hist, int nch,
+                       cudaStream_t stream);
 
 }  // namespace dsdgpu

@@ -52,11 +52,29 @@ __global__ void pack_native_kernel(const uint8_t* __restrict__ bits, size_t stri
   }
 }
 
-static unsigned grid_for(dsdgpu_context* c, size_t items) {
+static unsigned grid_for_sms(int num_sms, size_t items) {
   size_t g = (items + 255) / 256;
-  const size_t cap = (size_t)(c->num_sms > 0 ? c->num_sms : 148) * 16;
+  const size_t cap = (size_t)(num_sms > 0 ? num_sms : 148) * 16;
   if (g > cap) g = cap;
   return (unsigned)(g ? g : 1);
+}
+
+static unsigned grid_for(dsdgpu_context* c, size_t items) { return grid_for_sms(c->num_sms, items); }
+
+int launch_pack_dop(const uint8_t* bits, size_t stride, int nch, size_t frames, int phase,
+                    uint8_t* out, int num_sms, cudaStream_t stream) {
+  if (frames == 0) return 0;
+  pack_dop_kernel<<<grid_for_sms(num_sms, frames * nch), 256, 0, stream>>>(bits, stride, nch,
+                                                                           frames, phase, out);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_pack_native(const uint8_t* bits, size_t stride, int nch, size_t n, uint8_t* out,
+                       size_t out_stride, int num_sms, cudaStream_t stream) {
+  if (n == 0) return 0;
+  pack_native_kernel<<<grid_for_sms(num_sms, ((n + 7) / 8) * nch), 256, 0, stream>>>(
+      bits, stride, nch, n, out, out_stride);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 }  // namespace dsdgpu

@@ -65,10 +65,14 @@ struct SdmJob {
   uint8_t* out;
   long long n_in;
   long long skip_out;
-  int ctx;
+  int ctx;                // < 0: per-CTA scratch bank starting at -ctx - 1
   int copy_from;          // -1: none
   const double* seed_state;  // nullptr: none (kMaxOrder doubles)
-  int pad;
+  int flags;              // kJobNoStore: leave the context unwritten at the end
+};
+
+enum : int {
+  kJobNoStore = 1,        // the run's final state is not needed (whole-stream batch runs)
 };
 
 // Device status word: 0 ok, else an error code from dsdgpu.h.

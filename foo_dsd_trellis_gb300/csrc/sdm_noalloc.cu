@@ -98,7 +98,7 @@ extern "C" int dsdgpu_sdm_process_noalloc(const dsdgpu_sdm_params_t* p, int nch,
     jobs[ch].ctx = ch;
     jobs[ch].copy_from = -1;
     jobs[ch].seed_state = nullptr;
-    jobs[ch].pad = 0;
+    jobs[ch].flags = 0;
   }
   if (count == 0) return DSDGPU_OK;
   if (cudaMemsetAsync(d_status, 0, sizeof(int), s) != cudaSuccess) return DSDGPU_ERR_CUDA;

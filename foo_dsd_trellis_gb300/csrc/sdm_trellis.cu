@@ -155,8 +155,11 @@ template <int N>
 __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restrict__ ctxs,
                         WarpSmem& sm, int* __restrict__ status) {
   const int lane = threadIdx.x & 31;
-  const SdmCtx* src = &ctxs[job.copy_from >= 0 ? job.copy_from : job.ctx];
-  SdmCtx* dst = &ctxs[job.ctx];
+  // ctx < 0: the job's end state goes to a per-CTA scratch context at
+  // index (-ctx - 1) + blockIdx.x (jobs whose end state nobody reads)
+  const int dst_i = job.ctx >= 0 ? job.ctx : (-job.ctx - 1) + (int)blockIdx.x;
+  const SdmCtx* src = &ctxs[job.copy_from >= 0 ? job.copy_from : dst_i];
+  SdmCtx* dst = &ctxs[dst_i];
   const int K = P.cands;
   const int W = (P.lat + 31) >> 5;
   const unsigned long long mask = P.mask;
@@ -569,6 +572,11 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
   }
 
   // ---- store the context (the states were stored at the last sample) ----
+  if (job.flags & kJobNoStore) {
+    err = __reduce_max_sync(kFull, err);
+    if (err && lane == 0) atomicMax(status, err);
+    return;
+  }
   if (lane < n) {
     dst->cost[lane] = cost;
     dst->path[lane] = path;

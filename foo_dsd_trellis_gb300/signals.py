@@ -60,3 +60,48 @@ def sine_tpdf(seconds: float, fs: int = 44100, channels: int = 2, f0: float = 99
         d = tpdf * db_to_amp(dither_db) * np.sqrt(6.0)
         out[c] = (db_to_amp(level_db) * np.sin(2 * np.pi * f0 * t) + d).astype(np.float32)
     return out
+
+
+def bandlimited_noise(n: int, fs: int, rng: np.random.Generator, rms: float,
+                      f_hi: float = 20000.0) -> np.ndarray:
+    """White Gaussian noise low-passed at f_hi (FFT-domain brick wall), scaled
+    to `rms`."""
+    w = rng.standard_normal(n)
+    spec = np.fft.rfft(w)
+    f = np.fft.rfftfreq(n, 1.0 / fs)
+    spec[f > f_hi] = 0.0
+    x = np.fft.irfft(spec, n)
+    return x * (rms / max(1e-30, float(np.sqrt(np.mean(x * x)))))
+
+
+# DSD targets of the 44.1 kHz and 48 kHz families
+_FAMILY = {44100: (5644800, 11289600), 88200: (5644800, 11289600), 176400: (5644800, 11289600),
+           48000: (6144000, 12288000), 96000: (6144000, 12288000), 192000: (6144000, 12288000)}
+
+
+def multistream_layout(nstreams: int = 64, seed: int = 1003, len_lo: float = 0.5,
+                       len_hi: float = 30.0, scale: float = 1.0) -> list[dict]:
+    """The batched workload's stream table: lengths U(len_lo, len_hi) s (times
+    `scale`), input rates drawn from {44.1, 48, 88.2, 96, 176.4, 192} kHz,
+    targets DSD128 or DSD256 of the matching family, stereo."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    rates = sorted(_FAMILY)
+    out = []
+    for i in range(nstreams):
+        fs = int(rates[rng.integers(len(rates))])
+        fo = int(_FAMILY[fs][rng.integers(2)])
+        sec = float(rng.uniform(len_lo, len_hi)) * scale
+        out.append({"fs_in": fs, "fs_out": fo, "channels": 2,
+                    "frames": max(1, int(round(sec * fs))), "seed": seed * 1000 + i})
+    return out
+
+
+def multistream_pcm(entry: dict, level_db: float = -12.0) -> np.ndarray:
+    """One stream of the batched workload: band-limited Gaussian noise at
+    level_db RMS, float32 [channels, frames]."""
+    n, ch = entry["frames"], entry["channels"]
+    out = np.empty((ch, n), np.float32)
+    for c in range(ch):
+        rng = np.random.Generator(np.random.PCG64(entry["seed"] + c))
+        out[c] = bandlimited_noise(n, entry["fs_in"], rng, db_to_amp(level_db)).astype(np.float32)
+    return out

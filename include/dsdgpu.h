@@ -288,6 +288,75 @@ int dsdgpu_probe_fp64(dsdgpu_context_t *ctx, double *gops);
  * num_cands, pending.  best_state may be NULL; info may be NULL (6 values). */
 int dsdgpu_sdm_query(dsdgpu_context_t *ctx, int channel, double *best_state, uint64_t *info);
 
+/* ---- Batched multi-stream plan -------------------------------------------
+ * Many independent PCM streams of uneven length and mixed rates converted in
+ * one pass: per-stream FIR chains, then every DAS segment of every stream in
+ * one persistent SDM launch per trellis parameter set (streams whose NTF, K,
+ * depth and lat agree share a launch; different sets run concurrently),
+ * one seam-search launch over all boundaries, and per-stream assembly and
+ * packing.  The device work of a run is replayed from CUDA graphs captured
+ * at the first run.  This has no single counterpart in the reference, which
+ * converts one stream per plugin instance; each stream's output equals
+ * dsdgpu_pipeline_process on a fresh context with the same parameters
+ * (constant gain, full-parallel DAS seeding, src/dsp_plugin.c:2185-2283).
+ * Each run converts whole streams from fresh state. */
+typedef struct {
+    int32_t fs_in;             /* PCM rate, Hz */
+    int32_t fs_out;            /* DSD rate, Hz: fs_in times a power of two */
+    int32_t channels;          /* 1..8 */
+    int32_t boxcar_taps;       /* 0 = off (engine default 8) */
+    int64_t frames;            /* PCM frames per channel */
+    double gain;               /* FIR output gain, constant over the stream */
+    int32_t soft_clip;         /* tanh soft clip above +-0.95 */
+    int32_t reposition;        /* RMS reposition of quiet DAS boundaries */
+    dsdgpu_sdm_params_t sdm;   /* NTF, K, depth, lat, state limit */
+} dsdgpu_stream_desc_t;
+
+typedef struct {
+    int64_t seg_len;           /* DAS segment length in use */
+    int64_t jobs;              /* SDM segment runs per batch run */
+    int64_t sdm_samples;       /* SDM input samples per run (incl. warm-up) */
+    int64_t out_samples;       /* output DSD samples per run, all channels */
+    int64_t device_bytes;      /* device memory held by the plan */
+    int32_t classes;           /* trellis parameter sets (SDM launches) */
+    int32_t blocks_per_sm;     /* resident SDM warps per SM the launches use */
+    double predicted_ms;       /* autotuner's model of the SDM phase */
+} dsdgpu_plan_info_t;
+
+typedef struct dsdgpu_plan dsdgpu_plan_t;
+
+/* seg_len 0 = pick the DAS segment length (32,768 .. 131,072) and the SDM
+ * launch shape by measurement (the autotuner, cached in the context).
+ * output_format is DSDGPU_OUT_BITS / DOP / NATIVE.  DSDGPU_ERR_TOO_LARGE
+ * when the plan's device buffers would exceed max_device_bytes (0 = no
+ * limit). */
+int dsdgpu_plan_create(dsdgpu_context_t *ctx, const dsdgpu_stream_desc_t *streams,
+                       int nstreams, int64_t seg_len, int output_format,
+                       uint64_t max_device_bytes, dsdgpu_plan_t **plan);
+void dsdgpu_plan_destroy(dsdgpu_plan_t *plan);
+int dsdgpu_plan_info(const dsdgpu_plan_t *plan, dsdgpu_plan_info_t *info);
+/* Device buffers the plan owns for stream i: planar float PCM
+ * [channels][pcm_stride] in, and the packed output (DoP: interleaved
+ * frames; NATIVE: per-channel rows of out_stride bytes; BITS: per-channel
+ * rows of decision bytes, out_stride apart).  out_samples is the stream's
+ * DSD samples per channel; out_bytes the packed size of all channels. */
+int dsdgpu_plan_stream(const dsdgpu_plan_t *plan, int stream, float **d_pcm, size_t *pcm_stride,
+                       uint8_t **d_out, size_t *out_stride, size_t *out_samples,
+                       size_t *out_bytes);
+/* One batch run on the device buffers (waits for completion). */
+int dsdgpu_plan_run(dsdgpu_plan_t *plan);
+/* The same with host buffers: h_pcm[i] planar [channels][frames] floats,
+ * h_out[i] receives out_bytes (contiguous rows for NATIVE / BITS); copies
+ * are inside the call. */
+int dsdgpu_plan_run_host(dsdgpu_plan_t *plan, const float *const *h_pcm, uint8_t *const *h_out);
+/* Milliseconds of the last run: [FIR + RMS, SDM launches, seams + assembly
+ * + packing, whole run]. */
+int dsdgpu_plan_times(const dsdgpu_plan_t *plan, float *ms4);
+/* The one-segment-per-launch form over the first `njobs` segment runs of the
+ * last run (same kernel, one job per launch, launched back to back); returns
+ * the SDM input samples processed and the seconds taken. */
+int dsdgpu_plan_time_plain(dsdgpu_plan_t *plan, int njobs, int64_t *samples, double *seconds);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,155 @@
+"""Batched multi-stream plan vs the oracle, stream by stream.
+
+Each stream of a batch must equal the single-stream path from fresh state:
+the GPU FIR chain (checked against the FP64 oracle elsewhere) feeds the
+oracle's DAS restatement (full-parallel seeding, RMS reposition), whose
+decisions are packed by the oracle's DoP / native packers.  Streams mix input
+rates of both families, DSD128 and DSD256 targets (CLANS-6 and CLANS-8, two
+SDM parameter sets in one plan), uneven lengths, and one stream with a quiet
+stretch over a DAS boundary (the host reposition path between the graphs).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+GAIN = 0.354
+
+
+def _noise(frames, ch, seed, level=0.25):
+    """Band-limited Gaussian noise, float32 [ch, frames] (a seeded moving-average
+    low-pass of white noise, scaled to `level` RMS)."""
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal((ch, frames + 16))
+    k = np.ones(4) / 4.0
+    y = np.stack([np.convolve(w[c], k, mode="same")[8:8 + frames] for c in range(ch)])
+    y *= level / max(1e-12, float(np.sqrt(np.mean(y * y))))
+    return y.astype(np.float32)
+
+
+def _specs(cands=8, depth=16, lat=16):
+    from foo_dsd_trellis_gb300 import ntf
+    from foo_dsd_trellis_gb300.batch import StreamSpec
+    rates = [(44100, 5644800, 2100), (48000, 12288000, 900), (88200, 5644800, 3000),
+             (96000, 12288000, 1700), (176400, 11289600, 3300), (192000, 6144000, 5000)]
+    specs = []
+    for i, (fi, fo, frames) in enumerate(rates):
+        f = ntf.auto_select(fo)
+        specs.append(StreamSpec(fi, fo, 2 if i != 3 else 1, frames, f, cands=cands, depth=depth,
+                                lat=lat, gain=GAIN, boxcar_taps=8 if i % 2 == 0 else 0,
+                                soft_clip=bool(i % 3), reposition=True))
+    return specs
+
+
+def _inputs(specs):
+    xs = []
+    for i, s in enumerate(specs):
+        x = _noise(s.frames, s.channels, 100 + i)
+        if i == 0:
+            # quiet stretch around the DAS boundary at FIR sample 3 * 32768
+            c = 3 * 32768 // (s.fs_out // s.fs_in)
+            x[:, c - 60:c + 60] *= 1e-4
+        xs.append(x)
+    return xs
+
+
+def _oracle_stream(oracle, s, x, seg_len, fmt):
+    """The single-stream path for one stream: GPU FIR from fresh state, then
+    the oracle's DAS and packers."""
+    from foo_dsd_trellis_gb300.batch import OUT_BITS, OUT_DOP
+    from foo_dsd_trellis_gb300.fir import FirChain
+    fc = FirChain(s.fs_in, s.fs_out, boxcar_taps=s.boxcar_taps, soft_clip=s.soft_clip,
+                  num_channels=s.channels)
+    fir = fc.process(torch.from_numpy(x).cuda(), GAIN, GAIN).cpu().numpy()
+    fc.close()
+    bits, seams, starts = oracle.das_run(s.ntf.order, np.array(s.ntf.a), np.array(s.ntf.g),
+                                         s.depth, s.cands, s.lat, 0.0, fir, seg_len=seg_len,
+                                         seed_mode=0, reposition=s.reposition)
+    if fmt == OUT_BITS:
+        return bits, starts
+    if fmt == OUT_DOP:
+        per = [oracle.dop_pack_bits(bits[c], 0)[0].reshape(-1, 3) for c in range(s.channels)]
+        return np.stack(per, axis=1).reshape(-1), starts
+    return np.stack([oracle.bits_pack(bits[c]) for c in range(s.channels)]), starts
+
+
+@pytest.mark.parametrize("fmt", [1, 0, 2], ids=["dop", "bits", "native"])
+def test_batch_equals_single_stream(oracle, fmt):
+    from foo_dsd_trellis_gb300.batch import BatchPlan
+    specs = _specs()
+    xs = _inputs(specs)
+    plan = BatchPlan(specs, seg_len=32768, output_format=fmt)
+    info = plan.info()
+    assert info["classes"] == 2 and info["seg_len"] == 32768
+    plan.load([torch.from_numpy(x).cuda() for x in xs])
+    plan.run()
+    moved = False
+    for i, s in enumerate(specs):
+        want, starts = _oracle_stream(oracle, s, xs[i], 32768, fmt)
+        got = plan.out_view(i).cpu().numpy()
+        if fmt == 2:
+            got = got[:, : want.shape[1]]
+        assert got.shape == want.shape, (i, got.shape, want.shape)
+        bad = np.nonzero(got != want)
+        assert bad[0].size == 0, f"stream {i}: mismatch at {list(zip(*bad))[:5]}"
+        if i == 0:
+            moved = int(starts[3]) != 3 * (s.frames * (s.fs_out // s.fs_in) // len(starts))
+    assert moved, "the quiet stretch did not move a boundary: the reposition path was not covered"
+    plan.close()
+
+
+def test_batch_k32_depth64_lat128(oracle):
+    """The DSD128 trellis of the batched workload (K = 32, depth 64, lat 128)."""
+    from foo_dsd_trellis_gb300 import ntf
+    from foo_dsd_trellis_gb300.batch import OUT_DOP, BatchPlan, StreamSpec
+    specs = [StreamSpec(48000, 6144000, 2, 1700, ntf.auto_select(6144000), gain=GAIN),
+             StreamSpec(44100, 11289600, 1, 900, ntf.auto_select(11289600), gain=GAIN)]
+    xs = [_noise(s.frames, s.channels, 7 + i) for i, s in enumerate(specs)]
+    plan = BatchPlan(specs, seg_len=32768, output_format=OUT_DOP)
+    outs = plan.run_host(xs)
+    for i, s in enumerate(specs):
+        want, _ = _oracle_stream(oracle, s, xs[i], 32768, OUT_DOP)
+        assert np.array_equal(outs[i], want), f"stream {i}"
+    plan.close()
+
+
+def test_batch_autotune_replay_and_host_path():
+    """seg_len 0 picks a tuned length; graph replays are deterministic; the
+    host-buffer run equals the device run; the plain form runs."""
+    from foo_dsd_trellis_gb300.batch import OUT_DOP, BatchPlan
+    specs = _specs()
+    xs = _inputs(specs)
+    plan = BatchPlan(specs, seg_len=0, output_format=OUT_DOP)
+    info = plan.info()
+    assert info["seg_len"] in (32768, 49152, 65536, 98304, 131072)
+    assert info["blocks_per_sm"] in (8, 12, 16) and info["predicted_ms"] > 0
+    plan.load([torch.from_numpy(x).cuda() for x in xs])
+    plan.run()
+    first = [plan.out_view(i).cpu().numpy().copy() for i in range(len(specs))]
+    plan.run()
+    for i in range(len(specs)):
+        assert np.array_equal(plan.out_view(i).cpu().numpy(), first[i])
+    outs = plan.run_host(xs)
+    for i in range(len(specs)):
+        assert np.array_equal(outs[i], first[i])
+    t = plan.times_ms()
+    assert t["sdm"] > 0 and t["total"] >= t["sdm"]
+    smp, sec = plan.time_plain(2)
+    assert smp > 0 and sec > 0
+    plan.close()
+
+
+def test_batch_rejects_bad_streams():
+    from foo_dsd_trellis_gb300 import _lib, ntf
+    from foo_dsd_trellis_gb300.batch import BatchPlan, StreamSpec
+    f = ntf.auto_select(5644800)
+    with pytest.raises(_lib.DsdGpuError) as e:
+        BatchPlan([StreamSpec(44100, 5644801, 2, 1000, f)])
+    assert e.value.code == _lib.ERR_ARG
+    with pytest.raises(_lib.DsdGpuError) as e:
+        BatchPlan([StreamSpec(44100, 5644800, 9, 1000, f)])
+    assert e.value.code == _lib.ERR_ARG
+    with pytest.raises(_lib.DsdGpuError) as e:
+        BatchPlan([StreamSpec(44100, 5644800, 2, 100000, f)], seg_len=32768, max_device_bytes=1 << 20)
+    assert e.value.code == _lib.ERR_TOO_LARGE
