@@ -52,8 +52,12 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--das-seg-len", type=int, default=WL["das_seg_len"],
                     help="nominal DAS segment length (profiling of small cases only)")
-    ap.add_argument("--workload", default="dsd128_das", choices=["dsd128_das", "multistream64"],
-                    help="multistream64: the batched 64-stream form (its own JSON line)")
+    ap.add_argument("--workload", default="dsd128_das",
+                    choices=["dsd128_das", "multistream64", "diff16"],
+                    help="multistream64: the batched 64-stream form; diff16: the adjoint "
+                         "(each prints its own JSON line)")
+    ap.add_argument("--fd-dirs", type=int, default=32,
+                    help="diff16: random unit directions of the finite-difference check")
     ap.add_argument("--ms-scale", type=float, default=1.0,
                     help="multistream64: stream lengths scale (1.0 = 0.5-30 s)")
     ap.add_argument("--ms-seg-len", type=int, default=0,
@@ -449,6 +453,99 @@ def run_multistream(args):
     plan.close()
 
 
+DIFF_METRIC = ("adjoint ms: STE gradient of the in-band loss w.r.t. 127 pre-emphasis taps and "
+               "the order-7 NTF, 16 clips x 2^20 DSD128 samples, checkpoints every 4096")
+
+
+def run_diff(args):
+    """The differentiation workload: 16 mono clips of 8192 frames at 44.1 kHz
+    (31-tone multitone at -26 dBFS per tone plus pink noise at -40 dBFS,
+    seeded) -> 127-tap pre-emphasis (unit impulse + N(0, 1e-3)) -> FP64 chain
+    to DSD128 (2^20 samples per clip) -> exact trellis SDM (CLANS-7, K = 32,
+    depth 64, lat 128) -> in-band loss (255-tap 20 kHz low-pass, decimation
+    64).  One step is one backward pass (the adjoint); the forward, the exact
+    SDM inside it and a surrogate evaluation are reported beside it, with a
+    32-direction FP64 central-difference check (h = 1e-6) of the gradient."""
+    import numpy as np
+    import torch
+    from foo_dsd_trellis_gb300 import ntf, signals
+    from foo_dsd_trellis_gb300.diff import DiffConfig, DiffEngine
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    cfg = DiffConfig()
+    f = ntf.get_filter("clans-7", cfg.fs_out)
+    x = np.empty((cfg.nclips, cfg.frames), np.float32)
+    for c in range(cfg.nclips):
+        rng = np.random.Generator(np.random.PCG64(1004 + 31 * rank + c))
+        x[c] = (signals.multitone(cfg.frames, cfg.fs_in, rng, level_db=-26.0)
+                + signals.pink_noise(cfg.frames, rng, signals.db_to_amp(-40.0))).astype(np.float32)
+    eng = DiffEngine(cfg, f, local)
+    eng.set_input(torch.from_numpy(x).cuda())
+    rng = np.random.default_rng(5)
+    taps = rng.normal(0.0, 1e-3, cfg.preemph_taps)
+    taps[0] += 1.0
+    a, g = np.array(f.a[: f.order]), np.array(f.g[: f.order])
+    loss = eng.forward(taps, a, g)
+    fwd = eng.times_ms()
+    for _ in range(args.warmup):
+        eng.backward()
+    clocks = ClockSampler(local)
+    l0 = eng.launches()
+    clocks.start()
+    adj = []
+    for _ in range(args.steps):
+        gt, ga, gg = eng.backward()
+        adj.append(eng.times_ms()["adjoint"])
+    clk = clocks.stop()
+    launches = (eng.launches() - l0) // max(1, args.steps)
+    sur = eng.surrogate(taps, a, g)
+    sur_ms = eng.times_ms()["surrogate"]
+    # finite differences of the surrogate on random unit directions
+    h = 1e-6
+    worst = worst_rich = 0.0
+    drng = np.random.default_rng(7)
+    for _ in range(args.fd_dirs):
+        # absolute for the taps, relative for the NTF coefficients
+        dt = drng.standard_normal(taps.size)
+        da = a * drng.standard_normal(a.size)
+        dg = g * drng.standard_normal(g.size)
+        ad = gt @ dt + ga @ da + gg @ dg
+        fd = {}
+        for hh in (h, h / 2):
+            lp = eng.surrogate(taps + hh * dt, a + hh * da, g + hh * dg)
+            lm = eng.surrogate(taps - hh * dt, a - hh * da, g - hh * dg)
+            fd[hh] = (lp - lm) / (2 * hh)
+        rich = (4 * fd[h / 2] - fd[h]) / 3
+        worst = max(worst, abs(fd[h] - ad) / max(abs(fd[h]), abs(ad), 1e-300))
+        worst_rich = max(worst_rich, abs(rich - ad) / max(abs(rich), abs(ad), 1e-300))
+    adj_ms = statistics.mean(adj)
+    max_ms = max_over_ranks(adj_ms / 1000.0) * 1000.0
+    n = cfg.frames * (cfg.fs_out // cfg.fs_in)
+    if rank == 0:
+        line = {"metric": DIFF_METRIC, "value": max_ms, "unit": "ms", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": max_ms,
+                "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "diff16_dsd128", "clips": cfg.nclips,
+                           "samples_per_clip": n, "pcm": "44.1 kHz multitone + pink noise",
+                           "preemph_taps": cfg.preemph_taps, "ntf": "clans-7", "cands": cfg.cands,
+                           "depth": cfg.depth, "lat": cfg.lat, "checkpoint": cfg.checkpoint,
+                           "loss": "255-tap 20 kHz low-pass, decimation 64, mean square",
+                           "kappa": cfg.kappa, "l2": "state and adjoint data larger than L2"},
+                "loss": loss, "surrogate_at_forward": sur,
+                "forward_ms": fwd["forward"], "exact_sdm_ms": fwd["exact_sdm"],
+                "surrogate_ms": sur_ms,
+                "fd_check": {"directions": args.fd_dirs, "h": h, "worst_rel_err": worst,
+                             "direction": "taps N(0,1); a_i N(0,1) a_i; g_i N(0,1) g_i",
+                             "worst_rel_err_richardson_h_h2": worst_rich, "tolerance": 1e-4},
+                "grad_norms": {"taps": float(np.linalg.norm(gt)), "a": float(np.linalg.norm(ga)),
+                               "g": float(np.linalg.norm(gg))},
+                "e2e": None, "roofline": None, "cpu_baseline": None, "clocks": clk,
+                "gpu_launches": int(launches)}
+        print(json.dumps(line), flush=True)
+    eng.close()
+
+
 def _probe_fp64(plan) -> float:
     import ctypes as C
     v = C.c_double()
@@ -462,6 +559,8 @@ def main():
         run_reference(args)
     elif args.workload == "multistream64":
         run_multistream(args)
+    elif args.workload == "diff16":
+        run_diff(args)
     else:
         run_ours(args)
 

@@ -71,6 +71,14 @@ class PlanInfo(C.Structure):
                 ("predicted_ms", C.c_double)]
 
 
+class DiffParams(C.Structure):
+    _fields_ = [("fs_in", C.c_int32), ("fs_out", C.c_int32), ("nclips", C.c_int32),
+                ("preemph_taps", C.c_int32), ("frames", C.c_int64), ("decim", C.c_int32),
+                ("lpf_taps", C.c_int32), ("lpf_cutoff_hz", C.c_double), ("kappa", C.c_double),
+                ("gain", C.c_double), ("checkpoint", C.c_int32), ("pad", C.c_int32),
+                ("sdm", SdmParams)]
+
+
 OUT_BITS = 0
 OUT_DOP = 1
 OUT_NATIVE = 2
@@ -85,6 +93,7 @@ DAS_SEG0_FIRST = 1
 _vp = C.c_void_p
 _sz = C.c_size_t
 _szp = C.POINTER(C.c_size_t)
+_dp = C.POINTER(C.c_double)
 
 # name -> (restype, argtypes); the exported surface of include/dsdgpu.h
 SIGNATURES = {
@@ -130,6 +139,14 @@ SIGNATURES = {
     "dsdgpu_plan_times": (C.c_int, [_vp, C.POINTER(C.c_float)]),
     "dsdgpu_plan_time_plain": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int64),
                                          C.POINTER(C.c_double)]),
+    "dsdgpu_diff_create": (C.c_int, [_vp, C.POINTER(DiffParams), C.POINTER(_vp)]),
+    "dsdgpu_diff_destroy": (None, [_vp]),
+    "dsdgpu_diff_set_input": (C.c_int, [_vp, _vp]),
+    "dsdgpu_diff_forward": (C.c_int, [_vp, _dp, _dp, _dp, _dp]),
+    "dsdgpu_diff_backward": (C.c_int, [_vp, _dp, _dp, _dp]),
+    "dsdgpu_diff_surrogate": (C.c_int, [_vp, _dp, _dp, _dp, _dp]),
+    "dsdgpu_diff_times": (C.c_int, [_vp, C.POINTER(C.c_float)]),
+    "dsdgpu_diff_buffers": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(C.c_int64)]),
     "dsdgpu_fir_setup": (C.c_int, [_vp, C.POINTER(FirParams), C.c_int]),
     "dsdgpu_fir_reset": (C.c_int, [_vp]),
     "dsdgpu_fir_process": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp, _sz,

@@ -28,6 +28,8 @@ struct FirChainConst {
 // Chain construction (fir_chain_init_ex's stage plan and tap design) and the
 // launchers of the fused chain kernel and its history update.
 int build_chain_const(unsigned fs_in, unsigned fs_out, int boxcar, FirChainConst* F);
+void design_taps(int ntaps, bool quarter, double* h);      // Kaiser half/quarter-band design
+int plan_chain(unsigned fs_in, unsigned fs_out, int* U, int* L);   // stage factors and lengths
 size_t chain_smem_bytes(const FirChainConst& F);
 int fir_chain_prepare();   // kernel attributes (call outside stream capture)
 int launch_fir_chain(const FirChainConst& F, size_t smem, const float* pcm, size_t pcm_stride,

@@ -357,6 +357,61 @@ int dsdgpu_plan_times(const dsdgpu_plan_t *plan, float *ms4);
  * the SDM input samples processed and the seconds taken. */
 int dsdgpu_plan_time_plain(dsdgpu_plan_t *plan, int njobs, int64_t *samples, double *seconds);
 
+/* ---- Differentiable path: STE adjoint of FIR chain + NTF loop ------------
+ * Training support with no counterpart in the reference's C code (its
+ * training_pipeline/diff_sdm.py runs a soft greedy SDM in PyTorch).  Clips of
+ * PCM go through a pre-emphasis FIR (taps are parameters), the linear FP64
+ * upsampling chain (fir_chain_process_d without boxcar or clip, times a
+ * constant gain), and the exact trellis SDM (one sequential run per clip
+ * plus a drain, so decision t belongs to input sample t).  The loss is the
+ * mean square of a decimating low-pass of (decisions - reference), the
+ * reference being the chain output of the clip without pre-emphasis.
+ * The gradient uses a straight-through surrogate: with the forward decisions
+ * y^ and loop-filter outputs v^ frozen, y = y^ + kappa (v - v^) and the NTF
+ * loop is the linear recurrence driven by y.  The surrogate equals the loss at
+ * the forward's parameters and its exact gradient is what backward returns
+ * (taps, a[], g[]); dsdgpu_diff_surrogate evaluates it anywhere, for finite
+ * differences.  Loop state is checkpointed every `checkpoint` samples and
+ * recomputed in the backward pass. */
+typedef struct {
+    int32_t fs_in;             /* PCM rate, Hz */
+    int32_t fs_out;            /* SDM rate, Hz (fs_in times a power of two) */
+    int32_t nclips;            /* clips per batch */
+    int32_t preemph_taps;      /* pre-emphasis FIR length, 1..255 */
+    int64_t frames;            /* PCM frames per clip */
+    int32_t decim;             /* loss decimation factor */
+    int32_t lpf_taps;          /* loss low-pass length (odd, <= 511) */
+    double lpf_cutoff_hz;      /* loss low-pass cutoff */
+    double kappa;              /* straight-through slope of the quantiser */
+    double gain;               /* chain output gain */
+    int32_t checkpoint;        /* loop-state checkpoint interval (power of two) */
+    int32_t pad;
+    dsdgpu_sdm_params_t sdm;   /* trellis (K, depth, lat) and the NTF order */
+} dsdgpu_diff_params_t;
+
+typedef struct dsdgpu_diff dsdgpu_diff_t;
+
+int dsdgpu_diff_create(dsdgpu_context_t *ctx, const dsdgpu_diff_params_t *p, dsdgpu_diff_t **out);
+void dsdgpu_diff_destroy(dsdgpu_diff_t *d);
+/* Clip PCM, float [nclips][frames] on the device (copied; the reference
+ * signal is computed here). */
+int dsdgpu_diff_set_input(dsdgpu_diff_t *d, const float *d_pcm);
+/* Forward at (taps[preemph_taps], a[order], g[order]) (host arrays): exact
+ * decisions, checkpoints and the loss. */
+int dsdgpu_diff_forward(dsdgpu_diff_t *d, const double *taps, const double *a, const double *g,
+                        double *loss);
+/* Gradient of the surrogate at the last forward (host arrays out). */
+int dsdgpu_diff_backward(dsdgpu_diff_t *d, double *grad_taps, double *grad_a, double *grad_g);
+/* The surrogate loss at other parameters, decisions of the last forward frozen. */
+int dsdgpu_diff_surrogate(dsdgpu_diff_t *d, const double *taps, const double *a, const double *g,
+                          double *loss);
+/* Milliseconds of the last calls: [forward, exact SDM inside it, backward, surrogate]. */
+int dsdgpu_diff_times(const dsdgpu_diff_t *d, float *ms4);
+/* Device buffers of the last forward: SDM input [nclips][n] doubles and the
+ * decisions [nclips][n] (0/1 bytes); n = frames * fs_out / fs_in. */
+int dsdgpu_diff_buffers(const dsdgpu_diff_t *d, const double **d_sdm_in, const uint8_t **d_bits,
+                        int64_t *n);
+
 #ifdef __cplusplus
 }
 #endif
