@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--das-seg-len", type=int, default=WL["das_seg_len"],
                     help="nominal DAS segment length (profiling of small cases only)")
     ap.add_argument("--workload", default="dsd128_das",
-                    choices=["dsd128_das", "multistream64", "diff16"],
+                    choices=["dsd128_das", "multistream64", "diff16", "dsd512conv6"],
                     help="multistream64: the batched 64-stream form; diff16: the adjoint "
                          "(each prints its own JSON line)")
     ap.add_argument("--fd-dirs", type=int, default=32,
@@ -546,6 +546,107 @@ def run_diff(args):
     eng.close()
 
 
+CONV_METRIC = ("trellis SDM DSD Msamples/s & xRT at DSD512 5.1 with UPOLS room convolution "
+               "(P = 4096, 65,536-tap IR), K = 16, depth 48, DAS 262,144, DoP")
+
+
+def room_ir(taps: int, fs: float, seed: int, t60: float = 0.4) -> "np.ndarray":
+    """Synthetic room IR: seeded Gaussian noise under an exponential decay of
+    60 dB per t60 seconds, scaled so the peak of its magnitude response is 1
+    (0 dB), which keeps the SDM input in range."""
+    import numpy as np
+    rng = np.random.Generator(np.random.PCG64(seed))
+    k = np.arange(taps)
+    h = rng.standard_normal(taps) * 10.0 ** (-3.0 * k / (t60 * fs))
+    peak = np.abs(np.fft.rfft(h, 4 * taps)).max()
+    return (h / peak).astype(np.float32)
+
+
+def run_conv(args):
+    """DSD512 5.1: 6 channels of 5 s of 48 kHz pink noise at -18 dBFS (seeded)
+    -> 9-stage FIR chain to 24.576 MHz (127-tap first stage, boxcar 8, engine
+    gain and soft clip) -> UPOLS convolution per channel with its own 65,536-tap
+    room IR (P = 4096, FP32) -> trellis SDM (auto NTF for DSD512, K = 16,
+    depth 48, lat 32) over 262,144-sample DAS segments (full-parallel
+    seeding, the reference's DSD512 mode) -> DoP."""
+    import numpy as np
+    import torch
+    from foo_dsd_trellis_gb300 import ntf, signals
+    from foo_dsd_trellis_gb300.pipeline import OUT_DOP, PCM_FIR_GAIN, Encoder, FULL_PARALLEL
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    fs_in, fs_out, nch, secs = 48000, 24576000, 6, args.seconds if args.seconds != WL["seconds"] else 5.0
+    K, depth, lat, seg = 16, 48, ntf.auto_latency(48000, 24576000), 262144
+    f = ntf.auto_select(fs_out)
+    n = int(round(secs * fs_in))
+    pcm = np.empty((nch, n), np.float32)
+    for c in range(nch):
+        rng = np.random.Generator(np.random.PCG64(1005 + 10 * rank + c))
+        pcm[c] = signals.pink_noise(n, rng, signals.db_to_amp(-18.0)).astype(np.float32)
+    irs = np.stack([room_ir(65536, fs_out, 2005 + 10 * rank + c) for c in range(nch)])
+    enc = Encoder(fs_in, fs_out, nch, f, depth, K, lat, seg_len=seg, seed_mode=FULL_PARALLEL,
+                  reposition=True, boxcar_taps=8, soft_clip=True, output_format=OUT_DOP,
+                  device=local)
+    enc.set_conv(irs, 4096)
+    d_pcm = torch.from_numpy(pcm).cuda()
+    d_out = torch.empty(enc.out_capacity(n) + 64, dtype=torch.uint8, device="cuda")
+    lib_stream = torch.cuda.ExternalStream(enc.stream_ptr)
+    for _ in range(args.warmup):
+        enc.process(d_pcm, d_out)
+    torch.cuda.synchronize()
+    fp64_peak = enc.probe_fp64_gops()
+    clocks = ClockSampler(local)
+    l0 = enc.launches()
+    w0, _ = enc.sdm_work()
+    step_ms, sdm_ms = [], []
+    clocks.start()
+    for _ in range(args.steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(lib_stream)
+        ns, nb = enc.process(d_pcm, d_out)       # 5 s x 6 ch of data far larger than L2
+        e1.record(lib_stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        sdm_ms.append(enc.stage_ms()["sdm"])
+    clk = clocks.stop()
+    launches = (enc.launches() - l0) // max(1, args.steps)
+    sdm_samples = (enc.sdm_work()[0] - w0) / args.steps
+    total_s = max_over_ranks(sum(step_ms) / 1000.0)
+    value = job_throughput(ns * nch, args.steps, world, total_s)
+    h_pcm = torch.from_numpy(pcm).pin_memory().numpy()
+    h_out = torch.empty(enc.out_capacity(n) + 64, dtype=torch.uint8).pin_memory().numpy()
+    t0 = time.perf_counter()
+    ns2, nb2 = enc.process_host(h_pcm, h_out)
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    sdm_s = statistics.mean(sdm_ms) / 1000.0
+    flops = sdm_samples * K * (5 * f.order + 6)
+    if rank == 0:
+        st = enc.stage_ms()
+        line = {"metric": CONV_METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1000 * total_s / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "dsd512_51_upols", "fs_in": fs_in, "fs_out": fs_out,
+                           "channels": nch, "seconds": secs, "signal": "pink noise -18 dBFS",
+                           "ir_taps": 65536, "partition": 4096, "conv_dtype": "f32",
+                           "ntf": f.name, "cands": K, "depth": depth, "lat": lat,
+                           "das_seg_len": seg, "seed_mode": "full_parallel", "output": "dop",
+                           "l2": "working set far larger than L2"},
+                "xrt": ns / fs_out * args.steps / total_s,
+                "e2e": {"value": ns2 * nch / e2e_s / 1e6, "unit": UNIT,
+                        "h2d_bytes_per_step": int(pcm.nbytes), "d2h_bytes_per_step": int(nb2)},
+                "roofline": {"bound": "fp64", "achieved": flops / sdm_s / 1e12,
+                             "peak": fp64_peak / 1000.0, "unit": "TFLOP/s",
+                             "frac": flops / sdm_s / 1e12 / (fp64_peak / 1000.0),
+                             "traffic": SDM_DRAM_BYTES_PER_SAMPLE * sdm_samples,
+                             "kernel": f"sdm_jobs_kernel<{f.order}>"},
+                "cpu_baseline": None, "clocks": clk, "gpu_launches": int(launches),
+                "stages_ms": st}
+        print(json.dumps(line), flush=True)
+    enc.close()
+
+
 def _probe_fp64(plan) -> float:
     import ctypes as C
     v = C.c_double()
@@ -561,6 +662,8 @@ def main():
         run_multistream(args)
     elif args.workload == "diff16":
         run_diff(args)
+    elif args.workload == "dsd512conv6":
+        run_conv(args)
     else:
         run_ours(args)
 

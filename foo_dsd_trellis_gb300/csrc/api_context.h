@@ -27,6 +27,13 @@ int launch_pack_native(const uint8_t* bits, size_t stride, int nch, size_t n, ui
                        size_t out_stride, int num_sms, cudaStream_t stream);
 }  // namespace dsdgpu
 
+struct dsdgpu_conv_state;   // UPOLS convolution (conv.cu)
+struct dsdgpu_context;
+// Convolve a chunk of `nch` channels with the context's IRs (history carried).
+int conv_run(dsdgpu_context* c, int nch, const double* d_in, size_t in_stride, size_t count,
+             double* d_out, size_t out_stride);
+void conv_free(dsdgpu_conv_state* s);
+
 struct dsdgpu_context {
   int device = 0;
   int num_sms = 0;
@@ -86,6 +93,9 @@ struct dsdgpu_context {
   void* d_io = nullptr;           // device staging of the host-buffer entry point
   size_t io_bytes = 0;
 
+  // UPOLS convolution applied after the FIR chain when set up
+  dsdgpu_conv_state* conv = nullptr;
+
   // reusable device scratch for the host-buffer entry points
   void* d_scratch = nullptr;
   size_t scratch_bytes = 0;
@@ -98,6 +108,8 @@ struct dsdgpu_context {
   void plan_steps(int64_t pend, int64_t count, int64_t discard, int64_t* skip, int64_t* out,
                   int64_t* new_pend) const;
   void release_all() {
+    conv_free(conv);
+    conv = nullptr;
     if (d_ctx) cudaFree(d_ctx);
     if (d_jobs) cudaFree(d_jobs);
     if (d_scratch) cudaFree(d_scratch);

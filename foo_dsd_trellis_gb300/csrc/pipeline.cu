@@ -52,6 +52,11 @@ int dsdgpu_pipeline_process(dsdgpu_context_t* c, const float* d_pcm, size_t pcm_
   rc = dsdgpu_fir_process_async(c, 0, nch, d_pcm, pcm_stride, frames, d_fir, fir_stride,
                                 gain_start, gain_end, &fo);
   if (rc) return rc;
+  if (c->conv) {
+    // room-correction convolution at the SDM rate (src/gpu_cuda.c:3432-3492)
+    rc = conv_run(c, nch, d_fir, fir_stride, fo, d_fir, fir_stride);
+    if (rc) return rc;
+  }
   cudaEventRecord(c->ev[1], c->stream);
   size_t n = 0;
   c->timing_das = true;

@@ -77,6 +77,12 @@ class Encoder:
             return ((n + 7) // 8) * self.nch
         return n * self.nch
 
+    def set_conv(self, ir, partition: int = 4096) -> None:
+        """Convolve every channel with its IR (float32 [nch, taps]) between the
+        FIR chain and the SDM (UPOLS, FP32)."""
+        from . import conv
+        conv.setup(self.L, self.h, ir, partition)
+
     def process(self, pcm: torch.Tensor, out: torch.Tensor, gain_start: float = PCM_FIR_GAIN,
                 gain_end: float = PCM_FIR_GAIN):
         """Device buffers: pcm [nch, frames] float32; out a uint8 tensor whose rows

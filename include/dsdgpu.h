@@ -357,6 +357,24 @@ int dsdgpu_plan_times(const dsdgpu_plan_t *plan, float *ms4);
  * the SDM input samples processed and the seconds taken. */
 int dsdgpu_plan_time_plain(dsdgpu_plan_t *plan, int njobs, int64_t *samples, double *seconds);
 
+/* ---- UPOLS convolution at the SDM rate ------------------------------------
+ * Uniformly partitioned overlap-save convolution of every channel with its
+ * own IR (the reference's room-correction convolver: IR partitioning
+ * src/convolution.c:355-405, GPU block processing src/gpu_cuda.c:3432-3492,
+ * partition multiply-accumulate src/kernels/conv_kernels.cu:62-84), FP32,
+ * whole chunks at a time with the input history carried between calls.  Once
+ * set up, dsdgpu_pipeline_process applies it between the FIR chain and the
+ * SDM (the pipeline's channel count must equal nch). */
+/* ir: host floats [nch][ir_len]; partition: power of two (FFT size 2x); at
+ * most 32 partitions. */
+int dsdgpu_conv_setup(dsdgpu_context_t *ctx, const float *ir, size_t ir_len, int nch,
+                      int partition);
+int dsdgpu_conv_reset(dsdgpu_context_t *ctx);   /* zero the input history */
+int dsdgpu_conv_clear(dsdgpu_context_t *ctx);   /* free; the pipeline stops convolving */
+/* d_in / d_out: device doubles [nch][stride]; d_out may equal d_in. */
+int dsdgpu_conv_process(dsdgpu_context_t *ctx, int nch, const double *d_in, size_t in_stride,
+                        size_t count, double *d_out, size_t out_stride);
+
 /* ---- Differentiable path: STE adjoint of FIR chain + NTF loop ------------
  * Training support with no counterpart in the reference's C code (its
  * training_pipeline/diff_sdm.py runs a soft greedy SDM in PyTorch).  Clips of
