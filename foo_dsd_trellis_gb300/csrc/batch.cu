@@ -194,7 +194,7 @@ namespace {
 // ---- autotuner -------------------------------------------------------------
 
 struct TuneCurve {
-  std::vector<int> warps;       // resident warps (all SMs)
+  std::vector<int> warps;       // resident jobs (all SMs)
   std::vector<double> rate;     // SDM input samples per second
   double at(double w) const {
     if (warps.empty()) return 1.0;
@@ -227,7 +227,8 @@ std::string class_key(const SdmParams& P, int device) {
 // short launches of identical synthetic jobs (a two-tone signal at -6 dBFS).
 int measure_curve(dsdgpu_context* c, const SdmParams& P, TuneCurve* out) {
   const int sms = c->num_sms > 0 ? c->num_sms : 1;
-  const int maxw = kTuneWarpLevels[sizeof(kTuneWarpLevels) / sizeof(int) - 1] * sms;
+  const int jpc = sdm_jobs_per_cta(P);
+  const int maxw = kTuneWarpLevels[sizeof(kTuneWarpLevels) / sizeof(int) - 1] * sms * jpc;
   std::vector<double> x(kTuneSamples);
   for (long long i = 0; i < kTuneSamples; i++)
     x[i] = 0.3 * std::sin(0.0021 * (double)i) + 0.2 * std::sin(0.037 * (double)i + 1.0);
@@ -240,7 +241,7 @@ int measure_curve(dsdgpu_context* c, const SdmParams& P, TuneCurve* out) {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (cudaMalloc(&d_x, sizeof(double) * kTuneSamples) != cudaSuccess ||
       cudaMalloc(&d_o, (size_t)maxw * kTuneSamples) != cudaSuccess ||
-      cudaMalloc(&d_c, sizeof(SdmCtx) * (size_t)(1 + maxw)) != cudaSuccess ||
+      cudaMalloc(&d_c, sizeof(SdmCtx) * (size_t)(2 + maxw)) != cudaSuccess ||
       cudaMalloc(&d_j, sizeof(SdmJob) * (size_t)maxw) != cudaSuccess ||
       cudaMalloc(&d_cnt, sizeof(int)) != cudaSuccess ||
       cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
@@ -265,13 +266,13 @@ int measure_curve(dsdgpu_context* c, const SdmParams& P, TuneCurve* out) {
     SdmParams Q = P;
     Q.mode = c->sdm_mode;
     // warm-up
-    if (launch_sdm_jobs(Q, d_j, sms, d_cnt, d_c, c->d_status, sms, c->stream) != 0)
+    if (launch_sdm_jobs(Q, d_j, sms * jpc, d_cnt, d_c, c->d_status, 0, c->stream) != 0)
       rc = c->cuda_fail(cudaGetLastError(), "tuner launch");
     for (int lv : kTuneWarpLevels) {
       if (rc) break;
-      const int w = lv * sms;
+      const int w = lv * sms * jpc;            // resident jobs (lv warps per SM)
       cudaEventRecord(e0, c->stream);
-      if (launch_sdm_jobs(Q, d_j, w, d_cnt, d_c, c->d_status, w, c->stream) != 0) {
+      if (launch_sdm_jobs(Q, d_j, w, d_cnt, d_c, c->d_status, 0, c->stream) != 0) {
         rc = c->cuda_fail(cudaGetLastError(), "tuner launch");
         break;
       }
@@ -315,16 +316,18 @@ double model_seconds(const std::vector<StreamPlan>& st, const std::vector<SdmCla
     }
     J += (long long)s.S * s.d.channels;
   }
-  const double w = (double)std::min<long long>(J, slots);
+  long long cap = slots;
+  for (size_t k = 0; k < nc; k++) cap = std::max<long long>(cap, (long long)slots * sdm_jobs_per_cta(cls[k].P));
+  const double w = (double)std::min<long long>(J, cap);   // resident jobs
   double work = 0.0, tail = 0.0;
   for (size_t k = 0; k < nc; k++) {
     const double R = curves[k]->at(w);
-    const double per_warp = R / w;
+    const double per_job = R / w;
     work += W[k] / R;
-    const double longest = Lmax[k] / per_warp;
-    tail = std::max(tail, J > (long long)slots ? 0.5 * longest : longest);
+    const double longest = Lmax[k] / per_job;
+    tail = std::max(tail, J > cap ? 0.5 * longest : longest);
   }
-  return J > (long long)slots ? work + tail : std::max(work, tail);
+  return J > cap ? work + tail : std::max(work, tail);
 }
 
 // ---- plan construction -----------------------------------------------------
@@ -681,11 +684,12 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
   const int slots = pl->bps * sms;
   int nscratch = 0;
   for (SdmClass& K : pl->cls) {
+    const int jpc = sdm_jobs_per_cta(K.P);
     int gsz = (int)std::llround((double)slots * (double)K.samples / (double)std::max(1LL, pl->sdm_samples));
-    gsz = std::max(1, std::min(gsz, K.njobs));
+    gsz = std::max(1, std::min(gsz, (K.njobs + jpc - 1) / jpc));
     K.grid = gsz;
     K.scratch_first = 1 + nscratch;
-    nscratch += gsz;
+    nscratch += gsz * jpc;       // one scratch context per job slot of the launch
   }
   pl->nscratch = nscratch;
   int ntasks = 0, npieces = 0, nseg = 0, ncen = 0, nbp = 0;

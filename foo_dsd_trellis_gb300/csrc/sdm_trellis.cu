@@ -31,8 +31,8 @@
 
 namespace dsdgpu {
 
-// One warp (one job) per CTA: a few thousand long-running jobs spread evenly
-// over the SMs.  The launch bound (32 threads, 13 CTAs per SM) holds the kernel
+// One warp per CTA (one job, or two half-warp jobs for K <= 16): a few
+// thousand long-running jobs spread evenly over the SMs.  The launch bound (32 threads, 13 CTAs per SM) holds the kernel
 // at 128 registers; a 152-register build measured 50 % slower on the DSD128
 // DAS workload.
 constexpr int kRegRingWords = 8;      // rings held in registers: lat <= 256
@@ -46,9 +46,14 @@ __device__ __forceinline__ double clampd(double v, double lim) {
   return v;
 }
 
-__device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int src) {
-  return (unsigned long long)__shfl_sync(kFull, (long long)v, src);
+template <int LPJ>
+__device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int src, unsigned hm) {
+  return (unsigned long long)__shfl_sync(hm, (long long)v, src, LPJ);
 }
+
+// ballot / match over the job's lanes, as bits of the job's lane numbers
+#define BALLOT(p) (__ballot_sync(hm, (p)) >> sh)
+#define MATCH(v) (__match_any_sync(hm, (v)) >> sh)
 
 // The NTF advance with y = 0 (src/trellis.c:37-151; every order has the
 // same shape): d[0] = (s0 - g0 s1) + x; d[i] = (s[i] + s[i-1]) - g[i] s[i+1];
@@ -119,14 +124,15 @@ __device__ __forceinline__ bool key_less(long long ka, int ia, long long kb, int
   return ka < kb || (ka == kb && ia < ib);
 }
 
-// Bitonic sort of the 64 (key, index) pairs held two per lane (sorted
-// positions 2*lane and 2*lane + 1), ascending.
-template <typename Hook>
-__device__ __forceinline__ void bitonic64(long long& kA, int& iA, long long& kB, int& iB,
-                                          int lane, Hook&& hook) {
+// Bitonic sort of the 2 * LPJ (key, index) pairs of one job, two per lane
+// (sorted positions 2*lane and 2*lane + 1), ascending.  With LPJ = 16 each
+// half-warp sorts its own job (exchange distances stay inside the half).
+template <int LPJ, typename Hook>
+__device__ __forceinline__ void bitonic_sort(long long& kA, int& iA, long long& kB, int& iB,
+                                             int lane, unsigned hm, Hook&& hook) {
   int stage = 0;
 #pragma unroll
-  for (int k = 2; k <= 64; k <<= 1) {
+  for (int k = 2; k <= 2 * LPJ; k <<= 1) {
     const bool asc = ((2 * lane) & k) == 0;
 #pragma unroll
     for (int j = k >> 1; j > 0; j >>= 1) {
@@ -140,24 +146,37 @@ __device__ __forceinline__ void bitonic64(long long& kA, int& iA, long long& kB,
       } else {
         const int lj = j >> 1;
         const bool keep_min = (((lane & lj) == 0) == asc);
-        long long pk = __shfl_xor_sync(kFull, kA, lj);
-        int pi = __shfl_xor_sync(kFull, iA, lj);
+        long long pk = __shfl_xor_sync(hm, kA, lj, LPJ);
+        int pi = __shfl_xor_sync(hm, iA, lj, LPJ);
         if (keep_min == key_less(pk, pi, kA, iA)) { kA = pk; iA = pi; }
-        pk = __shfl_xor_sync(kFull, kB, lj);
-        pi = __shfl_xor_sync(kFull, iB, lj);
+        pk = __shfl_xor_sync(hm, kB, lj, LPJ);
+        pi = __shfl_xor_sync(hm, iB, lj, LPJ);
         if (keep_min == key_less(pk, pi, kB, iB)) { kB = pk; iB = pi; }
       }
     }
   }
 }
 
-template <int N>
+// Stages of the bitonic sort of 2 * LPJ keys (21 for 64, 15 for 32).
+template <int LPJ>
+__host__ __device__ constexpr int sort_stages() { return LPJ == 32 ? 21 : 15; }
+
+// LPJ lanes run one job: 32 (a whole warp) for K > 16, 16 (each half-warp its
+// own job) for K <= 16, so small trellises do not leave half of every FP64
+// warp instruction idle.  `lane` is the lane within the job, `hm` the job's
+// lanes; warp intrinsics use hm and width LPJ, ballots are shifted to the
+// job's bits.
+template <int N, int LPJ>
 __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restrict__ ctxs,
                         WarpSmem& sm, int* __restrict__ status) {
-  const int lane = threadIdx.x & 31;
-  // ctx < 0: the job's end state goes to a per-CTA scratch context at
-  // index (-ctx - 1) + blockIdx.x (jobs whose end state nobody reads)
-  const int dst_i = job.ctx >= 0 ? job.ctx : (-job.ctx - 1) + (int)blockIdx.x;
+  const int wl = threadIdx.x & 31;
+  const int lane = wl & (LPJ - 1);
+  const unsigned sh = (unsigned)(wl - lane);
+  const unsigned hm = LPJ == 32 ? kFull : (0xffffu << sh);
+  // ctx < 0: the job's end state goes to a scratch context, one per job slot
+  // of the launch, at (-ctx - 1) + slot (jobs whose end state nobody reads)
+  const int slot_id = (int)blockIdx.x * (32 / LPJ) + wl / LPJ;
+  const int dst_i = job.ctx >= 0 ? job.ctx : (-job.ctx - 1) + slot_id;
   const SdmCtx* src = &ctxs[job.copy_from >= 0 ? job.copy_from : dst_i];
   SdmCtx* dst = &ctxs[dst_i];
   const int K = P.cands;
@@ -185,7 +204,7 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     for (int w = 0; w < kRegRingWords; w++)
       if (w < W) ring[w] = src->ring[lane][w];
   }
-  for (int i = lane; i < 2 * kSlots; i += 32) {
+  for (int i = lane; i < 2 * kSlots; i += LPJ) {
     const int b = i / kSlots, j = i % kSlots;
     sm.path[b][j] = src->spath[b][j];
     sm.key[b][j] = (long long)src->skey[b][j];
@@ -198,7 +217,7 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     c_drop = src->next_filter_drops;
     c_tot = src->total_children;
   }
-  __syncwarp();
+  __syncwarp(hm);
   if (job.seed_state) {
     // DAS temp seeding: every live candidate gets the estimated state, cost 0.
     if (lane < n) {
@@ -207,7 +226,7 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
       cost = 0.0;
       sm.key[bank][slot] = key_of(0.0);
     }
-    __syncwarp();
+    __syncwarp(hm);
   }
   // the candidate as (s0, s1, shared part of its next advance)
   double cs0 = s[0], cs1 = s[1];
@@ -219,19 +238,19 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
   double x_cur = 0.0, x_nxt = 0.0;
   if (in) {
     if (lane < n_in) x_cur = in[lane];
-    if (32 + lane < n_in) x_nxt = in[32 + lane];
+    if (LPJ + lane < n_in) x_nxt = in[LPJ + lane];
   }
   uint8_t obit = 0;
   int err = 0;
   const bool lim_on = P.state_limit > 0.0;
 
   for (long long t = 0; t < n_in; t++) {
-    const int tl = (int)(t & 31);
+    const int tl = (int)(t & (LPJ - 1));
     if (tl == 0 && t > 0) {
       x_cur = x_nxt;
-      x_nxt = (in && t + 32 + lane < n_in) ? in[t + 32 + lane] : 0.0;
+      x_nxt = (in && t + LPJ + lane < n_in) ? in[t + LPJ + lane] : 0.0;
     }
-    const double x = __shfl_sync(kFull, x_cur, tl);
+    const double x = __shfl_sync(hm, x_cur, tl, LPJ);
     const int nb = bank ^ 1;
     int next_pos = pos + 1;
     if (next_pos == P.lat) next_pos = 0;
@@ -281,7 +300,7 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
       sm.heads[q & (kBuckets - 1)] = -1;
       sm.heads[(q | 1ull) & (kBuckets - 1)] = -1;
     }
-    __syncwarp();
+    __syncwarp(hm);
 
     // the children's shared part, one operation per stage of the sort below
     Pack<N> npk;
@@ -293,33 +312,33 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     // eligible children keep their (cost, index) order (src/trellis.c:628-652).
     long long sk0 = live ? key0 : LLONG_MAX, sk1 = live ? key1 : LLONG_MAX;
     int si0 = 2 * lane, si1 = 2 * lane + 1;
-    bitonic64(sk0, si0, sk1, si1, lane, [&](int st) {
+    bitonic_sort<LPJ>(sk0, si0, sk1, si1, lane, hm, [&](int st) {
       if (st < shared_ops<N>()) shared_op<N>(st, P, S, npk, tg, tu);
     });
 #pragma unroll
-    for (int k = 21; k < shared_ops<N>(); k++) shared_op<N>(k, P, S, npk, tg, tu);
-    const int sn0 = __shfl_sync(kFull, old_next, si0 >> 1);   // traceback bit of each sorted child
-    const int sn1 = __shfl_sync(kFull, old_next, si1 >> 1);
+    for (int k = sort_stages<LPJ>(); k < shared_ops<N>(); k++) shared_op<N>(k, P, S, npk, tg, tu);
+    const int sn0 = __shfl_sync(hm, old_next, si0 >> 1, LPJ);   // traceback bit of each sorted child
+    const int sn1 = __shfl_sync(hm, old_next, si1 >> 1, LPJ);
     const bool sl0 = (si0 >> 1) < n, sl1 = (si1 >> 1) < n;
-    const unsigned nx1 = __ballot_sync(kFull, live && old_next);
+    const unsigned nx1 = BALLOT(live && old_next);
     const int votes1 = 2 * __popc(nx1);
     const int majority = (votes1 > 2 * n - votes1) ? 1 : 0;
-    const long long mk = __shfl_sync(kFull, sk0, 0);
-    int want = __shfl_sync(kFull, sn0, 0);
+    const long long mk = __shfl_sync(hm, sk0, 0, LPJ);
+    int want = __shfl_sync(hm, sn0, 0, LPJ);
     if (want != majority) {
-      const unsigned mA = __ballot_sync(kFull, sl0 && sn0 == majority);
-      const unsigned mB = __ballot_sync(kFull, sl1 && sn1 == majority);
+      const unsigned mA = BALLOT(sl0 && sn0 == majority);
+      const unsigned mB = BALLOT(sl1 && sn1 == majority);
       int pos = 1 << 20;
       if (mA) pos = 2 * (__ffs(mA) - 1);
       if (mB) pos = min(pos, 2 * (__ffs(mB) - 1) + 1);
       if (pos < (1 << 20)) {
-        const long long bA = __shfl_sync(kFull, sk0, pos >> 1);
-        const long long bB = __shfl_sync(kFull, sk1, pos >> 1);
+        const long long bA = __shfl_sync(hm, sk0, pos >> 1, LPJ);
+        const long long bB = __shfl_sync(hm, sk1, pos >> 1, LPJ);
         const double cbm = __longlong_as_double((pos & 1) ? bB : bA);
         if (cbm < __dmul_rn(__longlong_as_double(mk), 1.1)) want = majority;
       }
     }
-    unsigned elig = __ballot_sync(kFull, live && old_next == want);
+    unsigned elig = BALLOT(live && old_next == want);
     c_drop += 2ull * (unsigned)(n - __popc(elig));
     c_tot += 2ull * (unsigned)n;
 
@@ -337,7 +356,7 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     // at K = 32 in bank 1, take the serial path.
     const bool me = live && old_next == want;
     const bool e0 = sl0 && sn0 == want, e1 = sl1 && sn1 == want;
-    const unsigned EA = __ballot_sync(kFull, e0), EB = __ballot_sync(kFull, e1);
+    const unsigned EA = BALLOT(e0), EB = BALLOT(e1);
     const int m2 = __popc(EA) + __popc(EB);
     const bool links_matter = (K == kMaxCands && nb == 1);
     bool fast_ok = (P.mode != kModeExact);
@@ -345,9 +364,9 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     long long f_Lk = LLONG_MAX;
     bool f_h0 = false, f_h1 = false;
     if (fast_ok) {
-      const unsigned mm = __match_any_sync(kFull, q);
-      if (__any_sync(kFull, me && __popc(mm & elig) > 1)) fast_ok = false;
-      if (links_matter && m2 > K && __any_sync(kFull, me && (q & (kBuckets - 1)) == 0))
+      const unsigned mm = MATCH(q);
+      if (__any_sync(hm, me && __popc(mm & elig) > 1)) fast_ok = false;
+      if (links_matter && m2 > K && __any_sync(hm, me && (q & (kBuckets - 1)) == 0))
         fast_ok = false;
     }
     if (fast_ok) {
@@ -362,8 +381,8 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
         const unsigned long long mine = (e0 ? (1ull << si0) : 0ull) | (e1 ? (1ull << si1) : 0ull);
         unsigned long long inc = mine;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const unsigned long long v = (unsigned long long)__shfl_up_sync(kFull, (long long)inc, o);
+        for (int o = 1; o < LPJ; o <<= 1) {
+          const unsigned long long v = (unsigned long long)__shfl_up_sync(hm, (long long)inc, o, LPJ);
           if (lane >= o) inc |= v;
         }
         const unsigned long long before0 = inc & ~mine;
@@ -373,7 +392,7 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
         sm.hashmark2[si0] = (uint8_t)(e0 && p0 < K);
         sm.hashmark2[si1] = (uint8_t)(e1 && p1 < K);
       }
-      __syncwarp();
+      __syncwarp(hm);
       f_cnt = m2 < K ? m2 : K;
       if (lane < f_cnt) {
         f_Ls = sm.act[lane];
@@ -382,13 +401,13 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
       if (links_matter) {
         f_h0 = live && sm.hashmark2[2 * lane] != 0;
         f_h1 = live && sm.hashmark2[2 * lane + 1] != 0;
-        const unsigned H0 = __ballot_sync(kFull, f_h0), H1 = __ballot_sync(kFull, f_h1);
-        const unsigned s0 = __match_any_sync(kFull, (unsigned)(q & (kBuckets - 1))) & H0 & below;
-        const unsigned s1 = __match_any_sync(kFull, (unsigned)((q | 1ull) & (kBuckets - 1))) & H1 & below;
+        const unsigned H0 = BALLOT(f_h0), H1 = BALLOT(f_h1);
+        const unsigned s0 = MATCH((unsigned)(q & (kBuckets - 1))) & H0 & below;
+        const unsigned s1 = MATCH((unsigned)((q | 1ull) & (kBuckets - 1))) & H1 & below;
         f_link0 = s0 ? 2 * (31 - __clz(s0)) : -1;
         f_link1 = s1 ? 2 * (31 - __clz(s1)) + 1 : -1;
       }
-      __syncwarp();
+      __syncwarp(hm);
     }
 
     // ---- 2c. serial selection (exact reference order) ----
@@ -407,7 +426,7 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
       sm.idx_at[2 * lane] = (int8_t)si0;
       sm.idx_at[2 * lane + 1] = (int8_t)si1;
       if (P.mode == kModeVerify && live) { sm.hashmark[2 * lane] = 0; sm.hashmark[2 * lane + 1] = 0; }
-      __syncwarp();
+      __syncwarp(hm);
       const int nch = 2 * n;
       unsigned long long Lm = 0ull;   // the act list, as sorted positions
       unsigned el = elig;
@@ -430,19 +449,19 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
             if (++hops > 4 * kSlots) { err = kStatusChainLimit; t = -1; break; }
           }
           if (t < 0) {
-            __syncwarp();
+            __syncwarp(hm);
             if (lane == 0) {
               sm.link[nb][c] = sm.heads[b];
               sm.heads[b] = (int8_t)c;
               sm.hashmark[c] = 1;
             }
-            __syncwarp();
+            __syncwarp(hm);
             if (cnt == K) {
               const int wp = 63 - __clzll((long long)Lm);
               if (K == kMaxCands && nb == 1) {
                 // the store to act[32] hits path_hash[0] in the reference layout
                 if (lane == 0) sm.heads[0] = sm.idx_at[wp];
-                __syncwarp();
+                __syncwarp(hm);
               }
               Lm = (Lm & ~(1ull << wp)) | (1ull << ps);
             } else {
@@ -467,12 +486,12 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
       const unsigned long long lowA = (1ull << (2 * lane)) - 1ull;
       if ((Lm >> (2 * lane)) & 1ull) sm.act[__popcll(Lm & lowA)] = (int8_t)si0;
       if ((Lm >> (2 * lane + 1)) & 1ull) sm.act[__popcll(Lm & (lowA | (1ull << (2 * lane))))] = (int8_t)si1;
-      __syncwarp();
+      __syncwarp(hm);
       if (lane < cnt) {
         Ls = sm.act[lane];
         Lk = sm.key[nb][Ls];
       }
-      __syncwarp();
+      __syncwarp(hm);
     }
 
     if (fast_ok) {
@@ -484,7 +503,7 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
           if (f_h0 && sm.link[nb][2 * lane] != f_link0) bad = true;
           if (f_h1 && sm.link[nb][2 * lane + 1] != f_link1) bad = true;
         }
-        if (__any_sync(kFull, bad)) err = max(err, (int)kStatusVerifyMismatch);
+        if (__any_sync(hm, bad)) err = max(err, (int)kStatusVerifyMismatch);
       } else {
         cnt = f_cnt;
         Ls = f_Ls;
@@ -493,41 +512,41 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
           if (f_h0) sm.link[nb][2 * lane] = (int8_t)f_link0;
           if (f_h1) sm.link[nb][2 * lane + 1] = (int8_t)f_link1;
         }
-        __syncwarp();
+        __syncwarp(hm);
       }
     }
 
     // ---- 3. commit ----
     const int n_old = n;
     const int n_new = cnt;
-    const double min_cost = __longlong_as_double(__shfl_sync(kFull, Lk, 0));
+    const double min_cost = __longlong_as_double(__shfl_sync(hm, Lk, 0, LPJ));
     const bool surv = lane < n_new;
     const int pp = surv ? (Ls >> 1) : lane;
     const int hh = surv ? (Ls & 1) : 0;
-    const double f00 = __shfl_sync(kFull, s00, pp);
-    const double f01 = __shfl_sync(kFull, s01, pp);
-    const double fS1 = __shfl_sync(kFull, S[1], pp);
+    const double f00 = __shfl_sync(hm, s00, pp, LPJ);
+    const double f01 = __shfl_sync(hm, s01, pp, LPJ);
+    const double fS1 = __shfl_sync(hm, S[1], pp, LPJ);
     Pack<N> fp;
-    fp.G0 = __shfl_sync(kFull, npk.G0, pp);
-    if (N >= 3) fp.G1 = __shfl_sync(kFull, npk.G1, pp);
+    fp.G0 = __shfl_sync(hm, npk.G0, pp, LPJ);
+    if (N >= 3) fp.G1 = __shfl_sync(hm, npk.G1, pp, LPJ);
 #pragma unroll
     for (int i = 2; i < N; i++) {
-      fp.D[i] = __shfl_sync(kFull, npk.D[i], pp);
-      fp.A[i] = __shfl_sync(kFull, npk.A[i], pp);
+      fp.D[i] = __shfl_sync(hm, npk.D[i], pp, LPJ);
+      fp.A[i] = __shfl_sync(hm, npk.A[i], pp, LPJ);
     }
     const bool last = (t == n_in - 1);
     double fs[N];
     if (last) {
       // the full child state is only needed when the context is stored
 #pragma unroll
-      for (int i = 2; i < N; i++) fs[i] = __shfl_sync(kFull, S[i], pp);
+      for (int i = 2; i < N; i++) fs[i] = __shfl_sync(hm, S[i], pp, LPJ);
     }
-    const unsigned long long npath = shfl64(q, pp) | (unsigned long long)hh;
-    const int nnext = __shfl_sync(kFull, new_next, pp);
+    const unsigned long long npath = shfl64<LPJ>(q, pp, hm) | (unsigned long long)hh;
+    const int nnext = __shfl_sync(hm, new_next, pp, LPJ);
     uint32_t nring[kRegRingWords];
 #pragma unroll
     for (int w = 0; w < kRegRingWords; w++)
-      nring[w] = (w < W) ? __shfl_sync(kFull, ring[w], pp) : 0u;
+      nring[w] = (w < W) ? __shfl_sync(hm, ring[w], pp, LPJ) : 0u;
     if (surv) {
       cs0 = hh ? f01 : f00;
       cs1 = fS1;
@@ -554,7 +573,7 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
       }
       sm.key[nb][Ls] = key_of(cost);
     }
-    __syncwarp();
+    __syncwarp(hm);
     if (n_new < n_old) { c_conv++; c_coll++; }
     n = n_new;
     bank = nb;
@@ -563,9 +582,9 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     // ---- output ----
     if (t >= job.skip_out) {
       const long long o = t - job.skip_out;
-      const int ol = (int)(o & 31);
+      const int ol = (int)(o & (LPJ - 1));
       if (lane == ol) obit = (uint8_t)want;
-      if (ol == 31 || t == n_in - 1) {
+      if (ol == LPJ - 1 || t == n_in - 1) {
         if (lane <= ol) job.out[o - ol + lane] = obit;
       }
     }
@@ -573,7 +592,7 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
 
   // ---- store the context (the states were stored at the last sample) ----
   if (job.flags & kJobNoStore) {
-    err = __reduce_max_sync(kFull, err);
+    err = __reduce_max_sync(hm, err);
     if (err && lane == 0) atomicMax(status, err);
     return;
   }
@@ -586,8 +605,8 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     for (int w = 0; w < kRegRingWords; w++)
       if (w < W) dst->ring[lane][w] = ring[w];
   }
-  __syncwarp();
-  for (int i = lane; i < 2 * kSlots; i += 32) {
+  __syncwarp(hm);
+  for (int i = lane; i < 2 * kSlots; i += LPJ) {
     const int b = i / kSlots, j = i % kSlots;
     dst->spath[b][j] = sm.path[b][j];
     dst->skey[b][j] = (unsigned long long)sm.key[b][j];
@@ -602,46 +621,62 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     dst->next_filter_drops = c_drop;
     dst->total_children = c_tot;
   }
-  err = __reduce_max_sync(kFull, err);
+  err = __reduce_max_sync(hm, err);
   if (err && lane == 0) atomicMax(status, err);
 }
 
-template <int N>
+template <int N, int LPJ>
 __global__ void __launch_bounds__(32, 13)
 sdm_jobs_kernel(SdmParams P, const SdmJob* __restrict__ jobs, int njobs,
                 int* __restrict__ job_counter, SdmCtx* __restrict__ ctxs,
                 int* __restrict__ status) {
   extern __shared__ __align__(16) unsigned char sdm_smem_raw[];
-  WarpSmem& sm = reinterpret_cast<WarpSmem*>(sdm_smem_raw)[threadIdx.x >> 5];
-  const int lane = threadIdx.x & 31;
+  const int wl = threadIdx.x & 31;
+  const int lane = wl & (LPJ - 1);
+  const unsigned hm = LPJ == 32 ? kFull : (0xffffu << (wl - lane));
+  WarpSmem& sm = reinterpret_cast<WarpSmem*>(sdm_smem_raw)[(threadIdx.x >> 5) * (32 / LPJ) + wl / LPJ];
   for (;;) {
     int j = 0;
     if (lane == 0) j = atomicAdd(job_counter, 1);
-    j = __shfl_sync(kFull, j, 0);
+    j = __shfl_sync(hm, j, 0, LPJ);
     if (j >= njobs) break;
     const SdmJob job = jobs[j];
-    run_job<N>(P, job, ctxs, sm, status);
-    __syncwarp();
+    run_job<N, LPJ>(P, job, ctxs, sm, status);
+    __syncwarp(hm);
   }
 }
 
-// Host-side launcher: one warp-sized CTA per job.
+int sdm_jobs_per_cta(const SdmParams& P) { return P.cands <= 16 ? 2 : 1; }
+
+// Host-side launcher: one warp-sized CTA runs one job at a time (K > 16) or
+// two, one per half-warp (K <= 16); max_blocks caps the CTAs.
 int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_counter,
                     SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream) {
   if (njobs <= 0) return 0;
-  const int wpb = 1;
-  int blocks = njobs;
+  const int jpc = sdm_jobs_per_cta(P);
+  int blocks = (njobs + jpc - 1) / jpc;
   if (max_blocks > 0 && blocks > max_blocks) blocks = max_blocks;
   cudaMemsetAsync(d_counter, 0, sizeof(int), stream);
-  const dim3 grid(blocks), block(wpb * 32);
-  const size_t smem = sizeof(WarpSmem) * (size_t)wpb;
-  switch (P.order) {
+  const dim3 grid(blocks), block(32);
+  const size_t smem = sizeof(WarpSmem) * (size_t)jpc;
+  if (jpc == 2) {
+    switch (P.order) {
 #define DSD_CASE(NN) \
-  case NN: sdm_jobs_kernel<NN><<<grid, block, smem, stream>>>(P, d_jobs, njobs, d_counter, d_ctxs, d_status); break;
-    DSD_CASE(2) DSD_CASE(3) DSD_CASE(4) DSD_CASE(5) DSD_CASE(6)
-    DSD_CASE(7) DSD_CASE(8) DSD_CASE(9) DSD_CASE(10)
+  case NN: sdm_jobs_kernel<NN, 16><<<grid, block, smem, stream>>>(P, d_jobs, njobs, d_counter, d_ctxs, d_status); break;
+      DSD_CASE(2) DSD_CASE(3) DSD_CASE(4) DSD_CASE(5) DSD_CASE(6)
+      DSD_CASE(7) DSD_CASE(8) DSD_CASE(9) DSD_CASE(10)
 #undef DSD_CASE
-    default: return -1;
+      default: return -1;
+    }
+  } else {
+    switch (P.order) {
+#define DSD_CASE(NN) \
+  case NN: sdm_jobs_kernel<NN, 32><<<grid, block, smem, stream>>>(P, d_jobs, njobs, d_counter, d_ctxs, d_status); break;
+      DSD_CASE(2) DSD_CASE(3) DSD_CASE(4) DSD_CASE(5) DSD_CASE(6)
+      DSD_CASE(7) DSD_CASE(8) DSD_CASE(9) DSD_CASE(10)
+#undef DSD_CASE
+      default: return -1;
+    }
   }
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
