@@ -139,6 +139,13 @@ SIGNATURES = {
     "dsdgpu_plan_times": (C.c_int, [_vp, C.POINTER(C.c_float)]),
     "dsdgpu_plan_time_plain": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int64),
                                          C.POINTER(C.c_double)]),
+    "dsdgpu_dop_unpack": (C.c_int, [_vp, C.c_int, _vp, _sz, _sz, _vp, _sz]),
+    "dsdgpu_boxcar_setup": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "dsdgpu_boxcar_reset": (C.c_int, [_vp]),
+    "dsdgpu_boxcar_process": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp, _sz,
+                                        C.c_double, C.c_double]),
+    "dsdgpu_boxcar_process_async": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp, _sz,
+                                              C.c_double, C.c_double]),
     "dsdgpu_conv_setup": (C.c_int, [_vp, _vp, _sz, C.c_int, C.c_int]),
     "dsdgpu_conv_reset": (C.c_int, [_vp]),
     "dsdgpu_conv_clear": (C.c_int, [_vp]),

@@ -34,6 +34,7 @@ struct dsdgpu_context;
 int conv_run(dsdgpu_context* c, int nch, const double* d_in, size_t in_stride, size_t count,
              double* d_out, size_t out_stride);
 void conv_free(dsdgpu_conv_state* s);
+int samerate_boxcar_taps(unsigned fs);   // engine_init's same-rate boxcar length
 
 struct dsdgpu_context {
   int device = 0;
@@ -94,6 +95,12 @@ struct dsdgpu_context {
   void* d_io = nullptr;           // device staging of the host-buffer entry point
   size_t io_bytes = 0;
 
+  // same-rate DSD input: boxcar ring (last 255 values per channel)
+  int8_t* d_box_hist = nullptr;
+  int box_taps = 0;
+  int box_nch = 0;
+  bool pipe_same_rate = false;    // pipeline input is DoP: unpack + boxcar instead of the FIR
+
   // UPOLS convolution applied after the FIR chain when set up
   dsdgpu_conv_state* conv = nullptr;
 
@@ -111,6 +118,8 @@ struct dsdgpu_context {
   void release_all() {
     conv_free(conv);
     conv = nullptr;
+    if (d_box_hist) cudaFree(d_box_hist);
+    d_box_hist = nullptr;
     if (d_ctx) cudaFree(d_ctx);
     if (d_jobs) cudaFree(d_jobs);
     if (d_scratch) cudaFree(d_scratch);

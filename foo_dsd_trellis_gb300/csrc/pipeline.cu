@@ -16,7 +16,14 @@ int dsdgpu_pipeline_setup(dsdgpu_context_t* c, const dsdgpu_pipeline_params_t* p
     return c->fail(DSDGPU_ERR_ARG, "bad output format");
   int rc = dsdgpu_sdm_setup(c, &p->sdm, nch);
   if (rc) return rc;
-  rc = dsdgpu_fir_setup(c, &p->fir, nch);
+  c->pipe_same_rate = p->fir.fs_in == p->fir.fs_out;
+  if (c->pipe_same_rate) {
+    // DSD in at the output rate: DoP unpack + boxcar (src/engine.c:487-563)
+    const int taps = p->fir.boxcar_taps > 0 ? p->fir.boxcar_taps : samerate_boxcar_taps(p->fir.fs_in);
+    rc = dsdgpu_boxcar_setup(c, taps, nch);
+  } else {
+    rc = dsdgpu_fir_setup(c, &p->fir, nch);
+  }
   if (rc) return rc;
   c->pipe = *p;
   c->pipe_nch = nch;
@@ -37,7 +44,8 @@ int dsdgpu_pipeline_process(dsdgpu_context_t* c, const float* d_pcm, size_t pcm_
   if (frames > 0 && (!d_pcm || !d_out)) return c->fail(DSDGPU_ERR_ARG, "null buffer");
   cudaSetDevice(c->device);
   const int nch = c->pipe_nch;
-  const size_t n_fir = frames * (size_t)c->fir.ratio;
+  // same rate: the input is DoP, 16 decisions per frame
+  const size_t n_fir = frames * (c->pipe_same_rate ? (size_t)16 : (size_t)c->fir.ratio);
   // device work buffers: FIR output (double) and stitched decisions
   const size_t fir_bytes = (n_fir * sizeof(double) + 255) & ~(size_t)255;
   const size_t bit_row = (n_fir + 255) & ~(size_t)255;
@@ -49,8 +57,17 @@ int dsdgpu_pipeline_process(dsdgpu_context_t* c, const float* d_pcm, size_t pcm_
 
   cudaEventRecord(c->ev[0], c->stream);
   size_t fo = 0;
-  rc = dsdgpu_fir_process_async(c, 0, nch, d_pcm, pcm_stride, frames, d_fir, fir_stride,
-                                gain_start, gain_end, &fo);
+  if (c->pipe_same_rate) {
+    // the decision buffer holds the unpacked input until the DAS writes it
+    rc = dsdgpu_dop_unpack(c, nch, d_pcm, pcm_stride, frames, d_bits, bit_row);
+    if (rc) return rc;
+    rc = dsdgpu_boxcar_process_async(c, 0, nch, d_bits, bit_row, n_fir, d_fir, fir_stride,
+                                     gain_start, gain_end);
+    fo = n_fir;
+  } else {
+    rc = dsdgpu_fir_process_async(c, 0, nch, d_pcm, pcm_stride, frames, d_fir, fir_stride,
+                                  gain_start, gain_end, &fo);
+  }
   if (rc) return rc;
   if (c->conv) {
     // room-correction convolution at the SDM rate (src/gpu_cuda.c:3432-3492)
@@ -105,7 +122,7 @@ int dsdgpu_pipeline_process_host(dsdgpu_context_t* c, const float* h_pcm, size_t
   if (frames > 0 && (!h_pcm || !h_out)) return c->fail(DSDGPU_ERR_ARG, "null buffer");
   cudaSetDevice(c->device);
   const int nch = c->pipe_nch;
-  const size_t n_fir = frames * (size_t)c->fir.ratio;
+  const size_t n_fir = frames * (c->pipe_same_rate ? (size_t)16 : (size_t)c->fir.ratio);
   // staging for the input and output on the device, kept across calls
   const size_t in_bytes = (frames * (size_t)nch * sizeof(float) + 255) & ~(size_t)255;
   const size_t out_row = (n_fir + 255) & ~(size_t)255;

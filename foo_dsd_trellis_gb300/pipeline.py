@@ -51,7 +51,8 @@ class Encoder:
         _lib.check(self.h, self.L.dsdgpu_pipeline_setup(self.h, C.byref(p), num_channels))
         self.params = p
         self.nch = num_channels
-        self.ratio = fs_out // fs_in
+        # same rate: the input is DoP (16 DSD samples per frame)
+        self.ratio = 16 if fs_in == fs_out else fs_out // fs_in
         self.output_format = output_format
         self.device = device
         s = C.c_void_p()

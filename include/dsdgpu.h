@@ -357,6 +357,29 @@ int dsdgpu_plan_times(const dsdgpu_plan_t *plan, float *ms4);
  * the SDM input samples processed and the seconds taken. */
 int dsdgpu_plan_time_plain(dsdgpu_plan_t *plan, int njobs, int64_t *samples, double *seconds);
 
+/* ---- Same-rate DSD input (DSD -> DSD re-encode) ----------------------------
+ * dop_unpack (src/dop.c:74-87) and the engine's same-rate boxcar with gain ramp
+ * (engine_process_block, src/engine.c:487-563).  A pipeline set up with
+ * fir.fs_in == fir.fs_out takes DoP floats (planar [nch][frames], 16 DSD
+ * samples per frame) and runs unpack -> boxcar (fir.boxcar_taps, 0 = the
+ * engine's rate default: 32 at DSD64, 64 at DSD128/256, 16 at DSD512) ->
+ * DAS SDM -> packing. */
+/* DoP floats [nch][dop_stride] -> 0/1 decision bytes [nch][bits_stride],
+ * 16 per frame, MSB first. */
+int dsdgpu_dop_unpack(dsdgpu_context_t *ctx, int nch, const float *d_dop, size_t dop_stride,
+                      size_t frames, uint8_t *d_bits, size_t bits_stride);
+int dsdgpu_boxcar_setup(dsdgpu_context_t *ctx, int taps, int nch);   /* taps 1..256 */
+int dsdgpu_boxcar_reset(dsdgpu_context_t *ctx);
+/* Decision bytes -> (window count / taps) * (gain ramp), the window carried
+ * across calls; gain_start 0 means gain_end (the first chunk). */
+int dsdgpu_boxcar_process(dsdgpu_context_t *ctx, int first, int nch, const uint8_t *d_bits,
+                          size_t bits_stride, size_t count, double *d_out, size_t out_stride,
+                          double gain_start, double gain_end);
+int dsdgpu_boxcar_process_async(dsdgpu_context_t *ctx, int first, int nch,
+                                const uint8_t *d_bits, size_t bits_stride, size_t count,
+                                double *d_out, size_t out_stride, double gain_start,
+                                double gain_end);
+
 /* ---- UPOLS convolution at the SDM rate ------------------------------------
  * Uniformly partitioned overlap-save convolution of every channel with its
  * own IR (the reference's room-correction convolver: IR partitioning

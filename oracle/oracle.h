@@ -124,6 +124,14 @@ size_t ora_engine_fir(unsigned fs_in, unsigned fs_out, const float *in, size_t n
                       int boxcar_taps, double g_start, double g_end, int soft_clip,
                       double *out);
 
+/* ---- Same-rate DSD input (src/dop.c:74-87, src/engine.c:527-543) ---- */
+typedef struct ora_boxcar ora_boxcar_t;
+void ora_dop_unpack(const float *pcm24, float *bits, size_t frames);
+ora_boxcar_t *ora_boxcar_new(int taps);
+void ora_boxcar_free(ora_boxcar_t *b);
+void ora_boxcar_gain(ora_boxcar_t *b, const float *in, double *out, size_t count,
+                     double g_start, double g_end);
+
 /* ---- DAS (src/dsp_plugin.c DAS block) ---- */
 typedef struct {
     int    seg_len;        /* nominal segment length in FIR samples (0: from nsegs) */

@@ -159,6 +159,7 @@ def ref_lib(wide: bool = False):
             L.ref_ntf_lookup.argtypes = [C.c_int, C.c_uint]
             L.ref_ntf_auto.argtypes = [C.c_uint]
             L.ref_path_bits.restype = C.c_int
+            L.ref_dop_unpack.argtypes = [_fp, _fp, C.c_size_t]
             _cache[key] = lib
     return _cache[key]
 
@@ -189,6 +190,51 @@ def das_run(order, a, g, depth, cands, lat, state_limit, fir: np.ndarray, seg_le
     return np.stack([o[:n] for o in outs]), list(sp), list(ss)
 
 
+def dop_unpack(pcm: np.ndarray, lib=None) -> np.ndarray:
+    """DoP float samples (one channel) -> +-1.0 float bits, 16 per sample."""
+    pcm = np.ascontiguousarray(pcm, np.float32)
+    out = np.empty(16 * len(pcm), np.float32)
+    L = (lib or oracle_lib()).lib
+    fn = L.ora_dop_unpack if lib is None else L.ref_dop_unpack
+    fn(_ptr(pcm, _fp), _ptr(out, _fp), len(pcm))
+    return out
+
+
+class Boxcar:
+    """The same-rate boxcar of the engine with its ring carried across calls."""
+
+    def __init__(self, taps: int):
+        self.L = oracle_lib().lib
+        self.h = self.L.ora_boxcar_new(taps)
+
+    def process(self, bits: np.ndarray, g_start: float, g_end: float) -> np.ndarray:
+        bits = np.ascontiguousarray(bits, np.float32)
+        out = np.empty(max(len(bits), 1), np.float64)
+        self.L.ora_boxcar_gain(self.h, _ptr(bits, _fp), _ptr(out, _dp), len(bits),
+                               float(g_start), float(g_end))
+        return out[: len(bits)]
+
+    def __del__(self):
+        try:
+            self.L.ora_boxcar_free(self.h)
+        except Exception:
+            pass
+
+
+def dop_float_frames(bits01: np.ndarray, phase: int = 0) -> np.ndarray:
+    """0/1 decision bytes -> DoP float samples (24-bit value / 2^23) with
+    alternating markers, the format a decoder hands the plugin."""
+    bits01 = np.asarray(bits01, np.uint8)
+    frames = len(bits01) // 16
+    w = np.zeros(frames, np.int64)
+    for b in range(16):
+        w = (w << 1) | bits01[b: 16 * frames: 16].astype(np.int64)
+    marker = np.where((np.arange(frames) + phase) % 2 == 0, 0x05, 0xFA)
+    v = (marker << 16) | w
+    v = np.where(v >= 1 << 23, v - (1 << 24), v)
+    return (v.astype(np.float64) / 8388608.0).astype(np.float32)
+
+
 def _bind_oracle_extras(L):
     L.ora_sdm_process_bits.restype = C.c_size_t
     L.ora_sdm_process_bits.argtypes = [C.c_void_p, _dp, _u8p, C.c_size_t]
@@ -205,6 +251,11 @@ def _bind_oracle_extras(L):
     L.ora_engine_fir.argtypes = [C.c_uint, C.c_uint, _fp, C.c_size_t, C.c_int,
                                  C.c_double, C.c_double, C.c_int, _dp]
     L.ora_sdm_run_jobs.restype = C.c_int
+    L.ora_dop_unpack.argtypes = [_fp, _fp, C.c_size_t]
+    L.ora_boxcar_new.restype = C.c_void_p
+    L.ora_boxcar_new.argtypes = [C.c_int]
+    L.ora_boxcar_free.argtypes = [C.c_void_p]
+    L.ora_boxcar_gain.argtypes = [C.c_void_p, _fp, _dp, C.c_size_t, C.c_double, C.c_double]
     L.ora_das_run.restype = C.c_size_t
     L.ora_das_run.argtypes = [C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double,
                               C.POINTER(DasCfg), C.POINTER(_dp), C.c_size_t, C.c_int,

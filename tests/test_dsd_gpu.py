@@ -1,0 +1,97 @@
+"""Same-rate DSD input (DSD -> DSD re-encode): DoP unpack, the engine's
+boxcar with gain ramp, and the whole pipeline, bit-exact against the oracle
+(DoP unpack pinned to the reference's dop.c; boxcar restated from
+src/engine.c:527-543; SDM pinned; DAS restated)."""
+import numpy as np
+import pytest
+
+from signals import multitone
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _dsd_stream(oracle, n, seed, order_name="clans-5", rate=2822400):
+    """A DSD bitstream to re-encode: a quick trellis encode of a multitone."""
+    from foo_dsd_trellis_gb300 import ntf
+    f = ntf.get_filter(order_name, rate)
+    ctx = oracle.sdm(f.order, np.array(f.a), np.array(f.g), 8, 4, 8)
+    x = multitone(n + 8, 7 + seed) * 1.5
+    return oracle.sdm_bits(ctx, x)[:n]
+
+
+def test_dop_unpack(oracle):
+    from foo_dsd_trellis_gb300 import _lib
+    import ctypes as C
+    rng = np.random.default_rng(1)
+    frames, nch = 5003, 3
+    bits = (rng.random((nch, 16 * frames)) > 0.5).astype(np.uint8)
+    dop = np.stack([oracle.dop_float_frames(bits[c], c & 1) for c in range(nch)])
+    L = _lib.load()
+    h = C.c_void_p()
+    assert L.dsdgpu_create(0, C.byref(h)) == 0
+    d_dop = torch.from_numpy(dop).cuda()
+    out = torch.empty((nch, 16 * frames + 64), dtype=torch.uint8, device="cuda")
+    _lib.check(h, L.dsdgpu_dop_unpack(h, nch, C.c_void_p(d_dop.data_ptr()), d_dop.stride(0),
+                                      frames, C.c_void_p(out.data_ptr()), out.stride(0)))
+    got = out[:, : 16 * frames].cpu().numpy()
+    for c in range(nch):
+        want = (oracle.dop_unpack(dop[c]) > 0).astype(np.uint8)
+        assert np.array_equal(got[c], want)
+    L.dsdgpu_destroy(h)
+
+
+@pytest.mark.parametrize("taps", [16, 32, 64])
+def test_boxcar_streamed(oracle, taps):
+    from foo_dsd_trellis_gb300 import _lib
+    import ctypes as C
+    rng = np.random.default_rng(taps)
+    nch, n = 2, 40000
+    bits = (rng.random((nch, n)) > 0.5).astype(np.uint8)
+    L = _lib.load()
+    h = C.c_void_p()
+    assert L.dsdgpu_create(0, C.byref(h)) == 0
+    _lib.check(h, L.dsdgpu_boxcar_setup(h, taps, nch))
+    d_bits = torch.from_numpy(bits).cuda()
+    out = torch.empty((nch, n), dtype=torch.float64, device="cuda")
+    refs = [oracle.Boxcar(taps) for _ in range(nch)]
+    want = [[] for _ in range(nch)]
+    pos = 0
+    for ln, gs, ge in ((7, 0.0, 0.9), (10000, 0.9, 0.7), (29993, 0.7, 0.7)):
+        blk = d_bits[:, pos:pos + ln].contiguous()
+        _lib.check(h, L.dsdgpu_boxcar_process(h, 0, nch, C.c_void_p(blk.data_ptr()), blk.stride(0),
+                                              ln, C.c_void_p(out[:, pos:].data_ptr()), out.stride(0),
+                                              gs, ge))
+        for c in range(nch):
+            want[c].append(refs[c].process(bits[c, pos:pos + ln].astype(np.float32) * 2 - 1, gs, ge))
+        pos += ln
+    got = out.cpu().numpy()
+    for c in range(nch):
+        assert np.array_equal(got[c], np.concatenate(want[c]))   # bit-exact FP64
+    L.dsdgpu_destroy(h)
+
+
+def test_samerate_pipeline(oracle):
+    """DoP in -> unpack -> boxcar (DSD64 default 32 taps) -> DAS trellis SDM
+    (CLANS-5, K = 16, depth 32, lat 32, 32,768-sample segments) -> DoP out,
+    equal byte for byte to the oracle chain."""
+    from foo_dsd_trellis_gb300 import ntf
+    from foo_dsd_trellis_gb300.pipeline import FULL_PARALLEL, OUT_DOP, Encoder
+    rate, K, depth, lat, nch, gain = 2822400, 16, 32, 32, 2, 0.9
+    f = ntf.get_filter("clans-5", rate)
+    n = 16 * 12000
+    src = np.stack([_dsd_stream(oracle, n, c) for c in range(nch)])
+    dop = np.stack([oracle.dop_float_frames(src[c], 0) for c in range(nch)])
+    enc = Encoder(rate, rate, nch, f, depth, K, lat, seg_len=32768, seed_mode=FULL_PARALLEL,
+                  reposition=True, boxcar_taps=0, soft_clip=False, output_format=OUT_DOP)
+    out = torch.empty(enc.out_capacity(dop.shape[1]) + 64, dtype=torch.uint8, device="cuda")
+    ns, nb = enc.process(torch.from_numpy(dop).cuda(), out, gain, gain)
+    box = np.stack([oracle.Boxcar(32).process(oracle.dop_unpack(dop[c]), gain, gain)
+                    for c in range(nch)])
+    bits, _, _ = oracle.das_run(f.order, np.array(f.a), np.array(f.g), depth, K, lat, 0.0, box,
+                                seg_len=32768, seed_mode=0, reposition=True)
+    assert bits.shape[1] == ns
+    per = [oracle.dop_pack_bits(bits[c], 0)[0].reshape(-1, 3) for c in range(nch)]
+    want = np.stack(per, axis=1).reshape(-1)
+    assert nb == want.size
+    assert np.array_equal(out[:nb].cpu().numpy(), want)

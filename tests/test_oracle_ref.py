@@ -183,3 +183,36 @@ def test_packers_equal_reference(ref, oracle):
             wb = np.zeros(max((n + 7) // 8, 1), np.uint8)
             L.ref_bits_pack(fl.ctypes.data_as(oracle._fp), wb.ctypes.data_as(oracle._u8p), n)
             assert np.array_equal(oracle.bits_pack(bits), wb[: (n + 7) // 8])
+
+
+def test_dop_unpack_matches_reference(oracle):
+    """The oracle's DoP unpack equals the reference's own dop_unpack, and the
+    DoP float frames built from decisions unpack back to them."""
+    ref = oracle.ref_lib()
+    if ref is None:
+        pytest.skip("reference sources absent")
+    rng = np.random.default_rng(4)
+    bits = (rng.random(16 * 5000) > 0.5).astype(np.uint8)
+    for phase in (0, 1):
+        pcm = oracle.dop_float_frames(bits, phase)
+        mine = oracle.dop_unpack(pcm)
+        theirs = oracle.dop_unpack(pcm, lib=ref)
+        assert np.array_equal(mine, theirs)
+        assert np.array_equal((mine > 0).astype(np.uint8), bits)
+
+
+def test_samerate_boxcar_restatement(oracle):
+    """Boxcar over +-1 decisions: an exact windowed count times 1/taps times
+    the gain ramp, with the ring carried across blocks."""
+    rng = np.random.default_rng(5)
+    bits = np.where(rng.random(3000) > 0.5, 1.0, -1.0).astype(np.float32)
+    taps = 64
+    bc = oracle.Boxcar(taps)
+    a = bc.process(bits[:1000], 0.0, 0.5)
+    b = bc.process(bits[1000:], 0.5, 0.25)
+    s = np.concatenate([np.zeros(taps - 1), bits.astype(np.float64)])
+    win = np.array([s[i:i + taps].sum() for i in range(len(bits))])
+    ga = 0.5 + 0.0 * np.arange(1000)
+    gb = 0.5 + (0.25 - 0.5) / 1999 * np.arange(2000)
+    np.testing.assert_allclose(a, win[:1000] / taps * ga, rtol=0, atol=1e-15)
+    np.testing.assert_allclose(b, win[1000:] / taps * gb, rtol=0, atol=1e-15)
