@@ -82,6 +82,7 @@ class DiffParams(C.Structure):
 OUT_BITS = 0
 OUT_DOP = 1
 OUT_NATIVE = 2
+OUT_PCM = 3
 
 OPT_SDM_SELECT = 1
 SELECT_FAST, SELECT_EXACT, SELECT_VERIFY = 0, 1, 2
@@ -146,6 +147,12 @@ SIGNATURES = {
                                         C.c_double, C.c_double]),
     "dsdgpu_boxcar_process_async": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp, _sz,
                                               C.c_double, C.c_double]),
+    "dsdgpu_decim_setup": (C.c_int, [_vp, C.c_uint, C.c_uint, C.c_int]),
+    "dsdgpu_decim_reset": (C.c_int, [_vp]),
+    "dsdgpu_decim_process": (C.c_int, [_vp, C.c_int, _vp, _sz, _sz, _vp, _sz, C.c_double,
+                                       C.c_double, _szp]),
+    "dsdgpu_decim_process_async": (C.c_int, [_vp, C.c_int, _vp, _sz, _sz, _vp, _sz, C.c_double,
+                                             C.c_double, _szp]),
     "dsdgpu_conv_setup": (C.c_int, [_vp, _vp, _sz, C.c_int, C.c_int]),
     "dsdgpu_conv_reset": (C.c_int, [_vp]),
     "dsdgpu_conv_clear": (C.c_int, [_vp]),

@@ -29,6 +29,8 @@ int launch_pack_native(const uint8_t* bits, size_t stride, int nch, size_t n, ui
 }  // namespace dsdgpu
 
 struct dsdgpu_conv_state;   // UPOLS convolution (conv.cu)
+struct dsdgpu_decim_state;  // DSD -> PCM decimation (decim.cu)
+void decim_free(dsdgpu_decim_state* s);
 struct dsdgpu_context;
 // Convolve a chunk of `nch` channels with the context's IRs (history carried).
 int conv_run(dsdgpu_context* c, int nch, const double* d_in, size_t in_stride, size_t count,
@@ -101,6 +103,10 @@ struct dsdgpu_context {
   int box_nch = 0;
   bool pipe_same_rate = false;    // pipeline input is DoP: unpack + boxcar instead of the FIR
 
+  // DSD -> PCM decimation chain (pipeline output format DSDGPU_OUT_PCM)
+  dsdgpu_decim_state* decim = nullptr;
+  bool pipe_pcm_out = false;
+
   // UPOLS convolution applied after the FIR chain when set up
   dsdgpu_conv_state* conv = nullptr;
 
@@ -118,6 +124,8 @@ struct dsdgpu_context {
   void release_all() {
     conv_free(conv);
     conv = nullptr;
+    decim_free(decim);
+    decim = nullptr;
     if (d_box_hist) cudaFree(d_box_hist);
     d_box_hist = nullptr;
     if (d_ctx) cudaFree(d_ctx);

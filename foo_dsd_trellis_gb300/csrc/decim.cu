@@ -1,0 +1,202 @@
+// DSD -> PCM decimation on sm_103a: the reference's FIR-only engine branch
+// (src/engine.c:566-577; chain src/fir.c:523-611 with 63-tap half-band /2
+// stages, ipp_downsample_d src/fir.c:467-487; gain ramp src/engine.c:879-889).
+//
+// Every stage is one launch, FP64, y[m] = sum_k h[k] x[2m - k] summed in tap
+// order with separately rounded products (the delay line of the previous call
+// stands in for negative indices), followed by a small launch that keeps the
+// stage's last 62 consumed inputs.  A stage consumes floor(count / 2) * 2
+// inputs, as the reference's numIters = in_count / factor.  The first stage
+// reads 0/1 decision bytes as +-1.  Traffic: about 1 B + 8 B + 8 B per input
+// sample over all stages together, so the chain is HBM-bound.
+#include "api_context.h"
+#include "fir_internal.h"
+
+#include <cstring>
+
+using namespace dsdgpu;
+
+namespace {
+
+constexpr int kDecTaps = 63;
+
+struct DecTaps {
+  double h[kDecTaps];
+};
+
+template <bool kBits>
+__global__ void decim_stage_kernel(const __grid_constant__ DecTaps T, const uint8_t* __restrict__ bits,
+                                   const double* __restrict__ in, size_t in_stride, long long m_out,
+                                   const double* __restrict__ dly, double* __restrict__ out,
+                                   size_t out_stride, int nch) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m_out * nch) return;
+  const long long c = i / m_out, m = i % m_out;
+  const double* dl = dly + (size_t)c * (kDecTaps - 1);
+  double acc = 0.0;
+#pragma unroll 7
+  for (int k = 0; k < kDecTaps; k++) {
+    const long long j = 2 * m - k;
+    double x;
+    if (j >= 0) x = kBits ? (bits[(size_t)c * in_stride + j] ? 1.0 : -1.0) : in[(size_t)c * in_stride + j];
+    else x = dl[kDecTaps - 1 + j];
+    acc = __dadd_rn(acc, __dmul_rn(T.h[k], x));
+  }
+  out[(size_t)c * out_stride + m] = acc;
+}
+
+// delay line <- the last 62 consumed inputs of (delay line ++ stage input)
+template <bool kBits>
+__global__ void decim_dly_kernel(const uint8_t* __restrict__ bits, const double* __restrict__ in,
+                                 size_t in_stride, long long used, double* __restrict__ dly,
+                                 int nch) {
+  const int c = blockIdx.x;
+  if (c >= nch) return;
+  __shared__ double tmp[kDecTaps - 1];
+  double* dl = dly + (size_t)c * (kDecTaps - 1);
+  for (int k = threadIdx.x; k < kDecTaps - 1; k += blockDim.x) {
+    const long long j = used - (kDecTaps - 1) + k;
+    double v;
+    if (j >= 0) v = kBits ? (bits[(size_t)c * in_stride + j] ? 1.0 : -1.0) : in[(size_t)c * in_stride + j];
+    else v = dl[kDecTaps - 1 + j];
+    tmp[k] = v;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < kDecTaps - 1; k += blockDim.x) dl[k] = tmp[k];
+}
+
+__global__ void decim_gain_kernel(const double* __restrict__ y, size_t y_stride, long long n,
+                                  int nch, double g_start, double g_step, int apply,
+                                  float* __restrict__ out, size_t out_stride) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * nch) return;
+  const long long c = i / n, t = i % n;
+  double v = y[(size_t)c * y_stride + t];
+  if (apply) v = __dmul_rn(v, __dadd_rn(g_start, __dmul_rn(g_step, (double)t)));
+  out[(size_t)c * out_stride + t] = (float)v;
+}
+
+unsigned nb(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+struct dsdgpu_decim_state {
+  int stages = 0;
+  int nch = 0;
+  DecTaps taps{};
+  double* d_dly = nullptr;      // [stage][nch][62]
+  double* d_buf = nullptr;      // ping-pong [2][nch][row]
+  size_t row = 0;
+  ~dsdgpu_decim_state() {
+    if (d_dly) cudaFree(d_dly);
+    if (d_buf) cudaFree(d_buf);
+  }
+};
+
+void decim_free(dsdgpu_decim_state* s) { delete s; }
+
+extern "C" {
+
+int dsdgpu_decim_setup(dsdgpu_context_t* c, unsigned fs_in, unsigned fs_out, int nch) {
+  if (!c || nch < 1) return DSDGPU_ERR_ARG;
+  if (fs_out == 0 || fs_in <= fs_out || fs_in % fs_out) return c->fail(DSDGPU_ERR_ARG, "decimation needs fs_in = fs_out * 2^k");
+  unsigned r = fs_in / fs_out;
+  if (r & (r - 1)) return c->fail(DSDGPU_ERR_ARG, "decimation ratio must be a power of two");
+  int S = 0;
+  while (r > 1) { S++; r >>= 1; }
+  if (S > kMaxStages) return c->fail(DSDGPU_ERR_ARG, "too many stages");
+  cudaSetDevice(c->device);
+  dsdgpu_decim_state* s = new (std::nothrow) dsdgpu_decim_state();
+  if (!s) return DSDGPU_ERR_NOMEM;
+  s->stages = S;
+  s->nch = nch;
+  design_taps(kDecTaps, false, s->taps.h);
+  const size_t dbytes = sizeof(double) * (size_t)S * nch * (kDecTaps - 1);
+  if (cudaMalloc(&s->d_dly, dbytes) != cudaSuccess) {
+    delete s;
+    return c->cuda_fail(cudaGetLastError(), "decimation delay lines");
+  }
+  cudaMemsetAsync(s->d_dly, 0, dbytes, c->stream);
+  decim_free(c->decim);
+  c->decim = s;
+  return c->check_status();
+}
+
+int dsdgpu_decim_reset(dsdgpu_context_t* c) {
+  if (!c) return DSDGPU_ERR_ARG;
+  if (!c->decim) return c->fail(DSDGPU_ERR_STATE, "decimation not set up");
+  cudaSetDevice(c->device);
+  dsdgpu_decim_state* s = c->decim;
+  cudaMemsetAsync(s->d_dly, 0, sizeof(double) * (size_t)s->stages * s->nch * (kDecTaps - 1), c->stream);
+  return c->check_status();
+}
+
+int dsdgpu_decim_process_async(dsdgpu_context_t* c, int nch, const uint8_t* d_bits,
+                               size_t bits_stride, size_t count, float* d_pcm, size_t pcm_stride,
+                               double gain_start, double gain_end, size_t* out_count) {
+  if (!c) return DSDGPU_ERR_ARG;
+  dsdgpu_decim_state* s = c->decim;
+  if (!s) return c->fail(DSDGPU_ERR_STATE, "decimation not set up");
+  if (nch != s->nch) return c->fail(DSDGPU_ERR_ARG, "channel count differs from the setup");
+  size_t n = count;
+  for (int k = 0; k < s->stages; k++) n /= 2;
+  if (out_count) *out_count = n;
+  if (count < 2) return DSDGPU_OK;
+  if (!d_bits || !d_pcm) return c->fail(DSDGPU_ERR_ARG, "null buffer");
+  if (pcm_stride < n) return c->fail(DSDGPU_ERR_ARG, "output stride too small");
+  cudaSetDevice(c->device);
+  cudaStream_t st = c->stream;
+  const size_t row = ((count / 2 + 1) + 31) & ~(size_t)31;
+  if (s->row < row) {
+    if (s->d_buf) cudaFree(s->d_buf);
+    s->d_buf = nullptr;
+    s->row = 0;
+    if (cudaMalloc(&s->d_buf, sizeof(double) * 2 * row * (size_t)nch) != cudaSuccess)
+      return c->cuda_fail(cudaGetLastError(), "decimation buffers");
+    s->row = row;
+  }
+  double* buf[2] = {s->d_buf, s->d_buf + s->row * (size_t)nch};
+  size_t cur = count;
+  const double* in = nullptr;
+  for (int k = 0; k < s->stages; k++) {
+    const long long m = (long long)(cur / 2);
+    double* out = buf[k & 1];
+    double* dly = s->d_dly + (size_t)k * nch * (kDecTaps - 1);
+    if (m > 0) {
+      if (k == 0) {
+        decim_stage_kernel<true><<<nb(m * nch, 256), 256, 0, st>>>(s->taps, d_bits, nullptr, bits_stride,
+                                                                  m, dly, out, s->row, nch);
+        decim_dly_kernel<true><<<nch, 64, 0, st>>>(d_bits, nullptr, bits_stride, 2 * m, dly, nch);
+      } else {
+        decim_stage_kernel<false><<<nb(m * nch, 256), 256, 0, st>>>(s->taps, nullptr, in, s->row,
+                                                                   m, dly, out, s->row, nch);
+        decim_dly_kernel<false><<<nch, 64, 0, st>>>(nullptr, in, s->row, 2 * m, dly, nch);
+      }
+      c->launches += 2;
+    }
+    in = out;
+    cur = (size_t)m;
+  }
+  // gain ramp of engine_process_fir_gain (src/engine.c:879-889), then float
+  double gs = gain_start;
+  if (gs == 0.0) gs = gain_end;
+  const int apply = (gs != 1.0 || gain_end != 1.0) ? 1 : 0;
+  const double step = n > 1 ? (gain_end - gs) / (double)(n - 1) : 0.0;
+  if (n > 0) {
+    decim_gain_kernel<<<nb((long long)n * nch, 256), 256, 0, st>>>(in, s->row, (long long)n, nch, gs,
+                                                                 step, apply, d_pcm, pcm_stride);
+    c->launches++;
+  }
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? DSDGPU_OK : c->cuda_fail(e, "decimation launch");
+}
+
+int dsdgpu_decim_process(dsdgpu_context_t* c, int nch, const uint8_t* d_bits, size_t bits_stride,
+                         size_t count, float* d_pcm, size_t pcm_stride, double gain_start,
+                         double gain_end, size_t* out_count) {
+  const int rc = dsdgpu_decim_process_async(c, nch, d_bits, bits_stride, count, d_pcm, pcm_stride,
+                                            gain_start, gain_end, out_count);
+  return rc ? rc : c->check_status();
+}
+
+}  // extern "C"

@@ -12,8 +12,24 @@ extern "C" {
 
 int dsdgpu_pipeline_setup(dsdgpu_context_t* c, const dsdgpu_pipeline_params_t* p, int nch) {
   if (!c || !p || nch < 1) return DSDGPU_ERR_ARG;
-  if (p->output_format < DSDGPU_OUT_BITS || p->output_format > DSDGPU_OUT_NATIVE)
+  if (p->output_format < DSDGPU_OUT_BITS || p->output_format > DSDGPU_OUT_PCM)
     return c->fail(DSDGPU_ERR_ARG, "bad output format");
+  c->pipe_pcm_out = p->output_format == DSDGPU_OUT_PCM;
+  if (c->pipe_pcm_out) {
+    // DSD -> PCM: DoP unpack and the decimation chain, no SDM (src/engine.c:566-577)
+    if (p->fir.fs_out >= p->fir.fs_in) return c->fail(DSDGPU_ERR_ARG, "PCM output needs fs_out < fs_in");
+    const int rc = dsdgpu_decim_setup(c, p->fir.fs_in, p->fir.fs_out, nch);
+    if (rc) return rc;
+    c->pipe = *p;
+    c->pipe_nch = nch;
+    c->pipe_ready = true;
+    c->pipe_same_rate = false;
+    if (!c->ev_ready) {
+      for (int i = 0; i < dsdgpu_context::kEvents; i++) cudaEventCreate(&c->ev[i]);
+      c->ev_ready = true;
+    }
+    return DSDGPU_OK;
+  }
   int rc = dsdgpu_sdm_setup(c, &p->sdm, nch);
   if (rc) return rc;
   c->pipe_same_rate = p->fir.fs_in == p->fir.fs_out;
@@ -44,6 +60,32 @@ int dsdgpu_pipeline_process(dsdgpu_context_t* c, const float* d_pcm, size_t pcm_
   if (frames > 0 && (!d_pcm || !d_out)) return c->fail(DSDGPU_ERR_ARG, "null buffer");
   cudaSetDevice(c->device);
   const int nch = c->pipe_nch;
+  if (c->pipe_pcm_out) {
+    // DSD -> PCM: DoP unpack into decision bytes, decimation to float rows
+    const size_t n_in = 16 * frames;
+    const size_t bit_row = (n_in + 255) & ~(size_t)255;
+    int rc = c->ensure_scratch(bit_row * (size_t)nch + 256);
+    if (rc) return rc;
+    uint8_t* d_bits = (uint8_t*)c->d_scratch;
+    cudaEventRecord(c->ev[0], c->stream);
+    rc = dsdgpu_dop_unpack(c, nch, d_pcm, pcm_stride, frames, d_bits, bit_row);
+    if (rc) return rc;
+    size_t n = 0;
+    rc = dsdgpu_decim_process_async(c, nch, d_bits, bit_row, n_in, (float*)d_out, out_stride,
+                                    gain_start, gain_end, &n);
+    if (rc) return rc;
+    cudaEventRecord(c->ev[5], c->stream);
+    rc = c->check_status();
+    if (rc) return rc;
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, c->ev[0], c->ev[5]);
+    c->stage_ms[0] = ms;
+    c->stage_ms[1] = c->stage_ms[2] = c->stage_ms[3] = 0.0f;
+    c->stage_ms[4] = ms;
+    if (out_samples) *out_samples = n;
+    if (out_bytes) *out_bytes = n * sizeof(float) * (size_t)nch;
+    return DSDGPU_OK;
+  }
   // same rate: the input is DoP, 16 decisions per frame
   const size_t n_fir = frames * (c->pipe_same_rate ? (size_t)16 : (size_t)c->fir.ratio);
   // device work buffers: FIR output (double) and stitched decisions
@@ -122,7 +164,8 @@ int dsdgpu_pipeline_process_host(dsdgpu_context_t* c, const float* h_pcm, size_t
   if (frames > 0 && (!h_pcm || !h_out)) return c->fail(DSDGPU_ERR_ARG, "null buffer");
   cudaSetDevice(c->device);
   const int nch = c->pipe_nch;
-  const size_t n_fir = frames * (c->pipe_same_rate ? (size_t)16 : (size_t)c->fir.ratio);
+  size_t n_fir = frames * (c->pipe_same_rate || c->pipe_pcm_out ? (size_t)16 : (size_t)c->fir.ratio);
+  if (c->pipe_pcm_out) n_fir = n_fir * sizeof(float);   // output rows hold floats (fewer of them)
   // staging for the input and output on the device, kept across calls
   const size_t in_bytes = (frames * (size_t)nch * sizeof(float) + 255) & ~(size_t)255;
   const size_t out_row = (n_fir + 255) & ~(size_t)255;
@@ -141,11 +184,15 @@ int dsdgpu_pipeline_process_host(dsdgpu_context_t* c, const float* h_pcm, size_t
                                   cudaMemcpyHostToDevice, c->stream);
   if (e != cudaSuccess) return c->cuda_fail(e, "pcm upload");
   size_t n = 0, nb = 0;
-  int rc = dsdgpu_pipeline_process(c, d_pcm, frames, frames, gain_start, gain_end, d_out, out_row,
-                                   &n, &nb);
+  int rc = dsdgpu_pipeline_process(c, d_pcm, frames, frames, gain_start, gain_end, d_out,
+                                   c->pipe_pcm_out ? out_row / sizeof(float) : out_row, &n, &nb);
   if (rc) return rc;
   if (nb > out_capacity) return c->fail(DSDGPU_ERR_ARG, "host output buffer too small");
-  if (c->pipe.output_format == DSDGPU_OUT_NATIVE) {
+  if (c->pipe.output_format == DSDGPU_OUT_PCM) {
+    // the rows were written with a stride of out_row bytes / 4 floats
+    e = cudaMemcpy2DAsync(h_out, n * sizeof(float), d_out, out_row, n * sizeof(float), (size_t)nch,
+                          cudaMemcpyDeviceToHost, c->stream);
+  } else if (c->pipe.output_format == DSDGPU_OUT_NATIVE) {
     const size_t rowb = (n + 7) / 8;
     e = cudaMemcpy2DAsync(h_out, rowb, d_out, out_row, rowb, (size_t)nch, cudaMemcpyDeviceToHost,
                           c->stream);

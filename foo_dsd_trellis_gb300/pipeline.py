@@ -51,8 +51,11 @@ class Encoder:
         _lib.check(self.h, self.L.dsdgpu_pipeline_setup(self.h, C.byref(p), num_channels))
         self.params = p
         self.nch = num_channels
-        # same rate: the input is DoP (16 DSD samples per frame)
-        self.ratio = 16 if fs_in == fs_out else fs_out // fs_in
+        # same rate and PCM output: the input is DoP (16 DSD samples per frame)
+        if output_format == _lib.OUT_PCM:
+            self.ratio = 16 / (fs_in // fs_out)
+        else:
+            self.ratio = 16 if fs_in == fs_out else fs_out // fs_in
         self.output_format = output_format
         self.device = device
         s = C.c_void_p()
@@ -71,7 +74,9 @@ class Encoder:
             pass
 
     def out_capacity(self, frames: int) -> int:
-        n = frames * self.ratio
+        n = int(frames * self.ratio)
+        if self.output_format == _lib.OUT_PCM:
+            return 4 * n * self.nch
         if self.output_format == OUT_DOP:
             return (n // 16) * 3 * self.nch
         if self.output_format == OUT_NATIVE:

@@ -102,6 +102,7 @@ typedef struct {
 #define DSDGPU_OUT_BITS    0   /* one byte per decision, [channel][sample] */
 #define DSDGPU_OUT_DOP     1   /* DoP 24-bit frames, [frame][channel][3] */
 #define DSDGPU_OUT_NATIVE  2   /* MSB-first DSD bytes, [channel][byte] */
+#define DSDGPU_OUT_PCM     3   /* DSD -> PCM: float32 rows [channel][sample], stride in floats */
 
 /* Whole-path parameters: the FIR chain with its glue, the trellis SDM, DAS,
  * and the output format. */
@@ -379,6 +380,24 @@ int dsdgpu_boxcar_process_async(dsdgpu_context_t *ctx, int first, int nch,
                                 const uint8_t *d_bits, size_t bits_stride, size_t count,
                                 double *d_out, size_t out_stride, double gain_start,
                                 double gain_end);
+
+/* ---- DSD -> PCM decimation (FIR-only engine branch, src/engine.c:566-577) ---
+ * FP64 chain of 63-tap half-band /2 stages (src/fir.c:467-487,523-611), delay
+ * lines carried across calls, gain ramp, narrowed to float32.  A pipeline with
+ * output_format DSDGPU_OUT_PCM (fir.fs_out < fir.fs_in) takes DoP floats and
+ * returns PCM: unpack -> decimation -> float. */
+int dsdgpu_decim_setup(dsdgpu_context_t *ctx, unsigned fs_in, unsigned fs_out, int nch);
+int dsdgpu_decim_reset(dsdgpu_context_t *ctx);
+/* 0/1 decision bytes [nch][bits_stride] (count per channel) -> float PCM
+ * [nch][pcm_stride]; *out_count = count / (fs_in / fs_out) (each stage keeps
+ * floor(count / 2) outputs). */
+int dsdgpu_decim_process(dsdgpu_context_t *ctx, int nch, const uint8_t *d_bits,
+                         size_t bits_stride, size_t count, float *d_pcm, size_t pcm_stride,
+                         double gain_start, double gain_end, size_t *out_count);
+int dsdgpu_decim_process_async(dsdgpu_context_t *ctx, int nch, const uint8_t *d_bits,
+                               size_t bits_stride, size_t count, float *d_pcm,
+                               size_t pcm_stride, double gain_start, double gain_end,
+                               size_t *out_count);
 
 /* ---- UPOLS convolution at the SDM rate ------------------------------------
  * Uniformly partitioned overlap-save convolution of every channel with its

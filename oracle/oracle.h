@@ -132,6 +132,12 @@ void ora_boxcar_free(ora_boxcar_t *b);
 void ora_boxcar_gain(ora_boxcar_t *b, const float *in, double *out, size_t count,
                      double g_start, double g_end);
 
+/* ---- DSD -> PCM decimation (src/fir.c:467-487,523-611) ---- */
+typedef struct ora_decim ora_decim_t;
+ora_decim_t *ora_decim_new(unsigned fs_in, unsigned fs_out);
+void ora_decim_free(ora_decim_t *d);
+size_t ora_decim_process(ora_decim_t *d, const double *in, size_t n, double *out);
+
 /* ---- DAS (src/dsp_plugin.c DAS block) ---- */
 typedef struct {
     int    seg_len;        /* nominal segment length in FIR samples (0: from nsegs) */

@@ -221,6 +221,28 @@ class Boxcar:
             pass
 
 
+class Decimator:
+    """The reference's DSD -> PCM FP64 decimation chain, streamed."""
+
+    def __init__(self, fs_in: int, fs_out: int):
+        self.L = oracle_lib().lib
+        self.h = self.L.ora_decim_new(fs_in, fs_out)
+        if not self.h:
+            raise ValueError("unsupported rate pair")
+
+    def process(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.float64)
+        out = np.empty(max(len(x), 1), np.float64)
+        n = self.L.ora_decim_process(self.h, _ptr(x, _dp), len(x), _ptr(out, _dp))
+        return out[:n]
+
+    def __del__(self):
+        try:
+            self.L.ora_decim_free(self.h)
+        except Exception:
+            pass
+
+
 def dop_float_frames(bits01: np.ndarray, phase: int = 0) -> np.ndarray:
     """0/1 decision bytes -> DoP float samples (24-bit value / 2^23) with
     alternating markers, the format a decoder hands the plugin."""
@@ -256,6 +278,11 @@ def _bind_oracle_extras(L):
     L.ora_boxcar_new.argtypes = [C.c_int]
     L.ora_boxcar_free.argtypes = [C.c_void_p]
     L.ora_boxcar_gain.argtypes = [C.c_void_p, _fp, _dp, C.c_size_t, C.c_double, C.c_double]
+    L.ora_decim_new.restype = C.c_void_p
+    L.ora_decim_new.argtypes = [C.c_uint, C.c_uint]
+    L.ora_decim_free.argtypes = [C.c_void_p]
+    L.ora_decim_process.restype = C.c_size_t
+    L.ora_decim_process.argtypes = [C.c_void_p, _dp, C.c_size_t, _dp]
     L.ora_das_run.restype = C.c_size_t
     L.ora_das_run.argtypes = [C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double,
                               C.POINTER(DasCfg), C.POINTER(_dp), C.c_size_t, C.c_int,
