@@ -55,7 +55,7 @@ class DasParams(C.Structure):
 
 class PipelineParams(C.Structure):
     _fields_ = [("fir", FirParams), ("sdm", SdmParams), ("das", DasParams),
-                ("output_format", C.c_int)]
+                ("output_format", C.c_int), ("sdm_mode", C.c_int)]
 
 
 class StreamDesc(C.Structure):
@@ -83,6 +83,8 @@ OUT_BITS = 0
 OUT_DOP = 1
 OUT_NATIVE = 2
 OUT_PCM = 3
+SDM_TRELLIS = 0
+SDM_PRECORR = 1
 
 OPT_SDM_SELECT = 1
 SELECT_FAST, SELECT_EXACT, SELECT_VERIFY = 0, 1, 2
@@ -153,6 +155,11 @@ SIGNATURES = {
                                        C.c_double, _szp]),
     "dsdgpu_decim_process_async": (C.c_int, [_vp, C.c_int, _vp, _sz, _sz, _vp, _sz, C.c_double,
                                              C.c_double, _szp]),
+    "dsdgpu_precorr_setup": (C.c_int, [_vp, C.c_int, _vp, _vp, C.c_double, C.c_int]),
+    "dsdgpu_precorr_reset": (C.c_int, [_vp]),
+    "dsdgpu_precorr_table": (C.c_int, [_vp, _vp]),
+    "dsdgpu_precorr_process": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp, _sz]),
+    "dsdgpu_precorr_process_async": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp, _sz]),
     "dsdgpu_conv_setup": (C.c_int, [_vp, _vp, _sz, C.c_int, C.c_int]),
     "dsdgpu_conv_reset": (C.c_int, [_vp]),
     "dsdgpu_conv_clear": (C.c_int, [_vp]),

@@ -31,7 +31,12 @@ int launch_pack_native(const uint8_t* bits, size_t stride, int nch, size_t n, ui
 struct dsdgpu_conv_state;   // UPOLS convolution (conv.cu)
 struct dsdgpu_decim_state;  // DSD -> PCM decimation (decim.cu)
 void decim_free(dsdgpu_decim_state* s);
+struct dsdgpu_precorr_state;  // PreCorr greedy SDM (precorr.cu)
+void precorr_free(dsdgpu_precorr_state* s);
 struct dsdgpu_context;
+// PreCorr decisions for channels [first, first + nch) of the context's state.
+int precorr_run(dsdgpu_context* c, int first, int nch, const double* d_in, size_t in_stride,
+                size_t count, uint8_t* d_bits, size_t bits_stride);
 // Convolve a chunk of `nch` channels with the context's IRs (history carried).
 int conv_run(dsdgpu_context* c, int nch, const double* d_in, size_t in_stride, size_t count,
              double* d_out, size_t out_stride);
@@ -107,6 +112,10 @@ struct dsdgpu_context {
   dsdgpu_decim_state* decim = nullptr;
   bool pipe_pcm_out = false;
 
+  // PreCorr SDM (pipeline sdm_mode DSDGPU_SDM_PRECORR)
+  dsdgpu_precorr_state* precorr = nullptr;
+  bool pipe_precorr = false;
+
   // UPOLS convolution applied after the FIR chain when set up
   dsdgpu_conv_state* conv = nullptr;
 
@@ -126,6 +135,8 @@ struct dsdgpu_context {
     conv = nullptr;
     decim_free(decim);
     decim = nullptr;
+    precorr_free(precorr);
+    precorr = nullptr;
     if (d_box_hist) cudaFree(d_box_hist);
     d_box_hist = nullptr;
     if (d_ctx) cudaFree(d_ctx);

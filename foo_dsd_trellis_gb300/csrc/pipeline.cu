@@ -24,13 +24,19 @@ int dsdgpu_pipeline_setup(dsdgpu_context_t* c, const dsdgpu_pipeline_params_t* p
     c->pipe_nch = nch;
     c->pipe_ready = true;
     c->pipe_same_rate = false;
+    c->pipe_precorr = false;
     if (!c->ev_ready) {
       for (int i = 0; i < dsdgpu_context::kEvents; i++) cudaEventCreate(&c->ev[i]);
       c->ev_ready = true;
     }
     return DSDGPU_OK;
   }
-  int rc = dsdgpu_sdm_setup(c, &p->sdm, nch);
+  if (p->sdm_mode != DSDGPU_SDM_TRELLIS && p->sdm_mode != DSDGPU_SDM_PRECORR)
+    return c->fail(DSDGPU_ERR_ARG, "bad sdm mode");
+  c->pipe_precorr = p->sdm_mode == DSDGPU_SDM_PRECORR;
+  int rc = c->pipe_precorr ? dsdgpu_precorr_setup(c, p->sdm.order, p->sdm.a, p->sdm.g,
+                                                  p->sdm.state_limit, nch)
+                           : dsdgpu_sdm_setup(c, &p->sdm, nch);
   if (rc) return rc;
   c->pipe_same_rate = p->fir.fs_in == p->fir.fs_out;
   if (c->pipe_same_rate) {
@@ -118,10 +124,18 @@ int dsdgpu_pipeline_process(dsdgpu_context_t* c, const float* d_pcm, size_t pcm_
   }
   cudaEventRecord(c->ev[1], c->stream);
   size_t n = 0;
-  c->timing_das = true;
-  rc = dsdgpu_das_process(c, &c->pipe.das, nch, d_fir, fir_stride, fo, d_bits, bit_row, &n,
-                          nullptr, 0);
-  c->timing_das = false;
+  if (c->pipe_precorr) {
+    // PreCorr: sequential per channel, no latency (src/engine.c:557-559, 723-726)
+    cudaEventRecord(c->ev[2], c->stream);
+    rc = precorr_run(c, 0, nch, d_fir, fir_stride, fo, d_bits, bit_row);
+    cudaEventRecord(c->ev[3], c->stream);
+    n = fo;
+  } else {
+    c->timing_das = true;
+    rc = dsdgpu_das_process(c, &c->pipe.das, nch, d_fir, fir_stride, fo, d_bits, bit_row, &n,
+                            nullptr, 0);
+    c->timing_das = false;
+  }
   if (rc) return rc;
   cudaEventRecord(c->ev[4], c->stream);
   size_t nbytes = 0;

@@ -71,6 +71,12 @@ def auto_select(dsd_rate: int) -> NtfFilter:
     return get_filter(name, dsd_rate)
 
 
+def auto_select_precorr(dsd_rate: int) -> NtfFilter:
+    """ntf_auto_select_precorr(rate) (src/ntf.c:857-873): one order above the
+    trellis choice, clans-7 from DSD128 up, clans-6 below."""
+    return get_filter("clans-7" if dsd_rate >= DSD_RATE_128 else "clans-6", dsd_rate)
+
+
 def auto_latency(fs_in: int, fs_out: int) -> int:
     """Auto trellis latency (src/engine.c:1010-1020): 32 at DSD512 and at DSD64,
     128 from DSD128 up to below DSD512."""

@@ -104,6 +104,12 @@ typedef struct {
 #define DSDGPU_OUT_NATIVE  2   /* MSB-first DSD bytes, [channel][byte] */
 #define DSDGPU_OUT_PCM     3   /* DSD -> PCM: float32 rows [channel][sample], stride in floats */
 
+/* SDM of the whole-path pipeline: the reference's sdm_mode_t
+ * (include/dsd_types.h:50-53), numbered so that a zero-filled parameter block
+ * keeps the trellis (the reference numbers PreCorr 0). */
+#define DSDGPU_SDM_TRELLIS 0   /* trellis SDM with DAS */
+#define DSDGPU_SDM_PRECORR 1   /* PreCorr greedy SDM, sequential per channel */
+
 /* Whole-path parameters: the FIR chain with its glue, the trellis SDM, DAS,
  * and the output format. */
 typedef struct {
@@ -111,6 +117,7 @@ typedef struct {
     dsdgpu_sdm_params_t sdm;
     dsdgpu_das_params_t das;
     int                 output_format;   /* DSDGPU_OUT_* */
+    int                 sdm_mode;        /* DSDGPU_SDM_*; 0 = trellis */
 } dsdgpu_pipeline_params_t;
 
 /* ---- lifecycle (replaces gpu_create / gpu_destroy, include/gpu_compute.h:52-55) ---- */
@@ -398,6 +405,32 @@ int dsdgpu_decim_process_async(dsdgpu_context_t *ctx, int nch, const uint8_t *d_
                                size_t bits_stride, size_t count, float *d_pcm,
                                size_t pcm_stride, double gain_start, double gain_end,
                                size_t *out_count);
+
+/* ---- PreCorr greedy SDM (src/precorr.c, include/precorr.h:49-61) ----------
+ * Replaces precorr_context_init / precorr_process_block /
+ * precorr_context_reset (src/precorr.c:198-287) and the reference's GPU entry
+ * points gpu_cuda_precorr_setup / gpu_cuda_precorr (src/gpu_cuda.c:822-850,
+ * 2933-2974; gpu_precorr_process, include/gpu_compute.h:140-144).  Setup
+ * trains the 256 x 8 correction table on the device (65,536 LCG samples at
+ * amplitude 0.1, cells with fewer than 4 hits zero) and resets `nch`
+ * per-channel states; the coefficients are used as float copies, as the
+ * reference's context does.  Decisions equal the reference's CPU build bit for
+ * bit.  A pipeline with sdm_mode DSDGPU_SDM_PRECORR runs this instead of the
+ * trellis (src/engine.c:557-559, 723-726), with its sdm.order/a/g/state_limit. */
+int dsdgpu_precorr_setup(dsdgpu_context_t *ctx, int order, const double *a, const double *g,
+                         double state_limit, int nch);
+/* Zero state, history 0x69, phase 0, previous output 0; the table is kept. */
+int dsdgpu_precorr_reset(dsdgpu_context_t *ctx);
+/* Copy the trained table out: host floats [256][8] (history, phase). */
+int dsdgpu_precorr_table(dsdgpu_context_t *ctx, float *h_table);
+/* FP64 samples [nch][in_stride] (count per channel) for channels
+ * [first, first + nch) -> 0/1 decision bytes [nch][bits_stride]; no latency,
+ * state carried across calls. */
+int dsdgpu_precorr_process(dsdgpu_context_t *ctx, int first, int nch, const double *d_in,
+                           size_t in_stride, size_t count, uint8_t *d_bits, size_t bits_stride);
+int dsdgpu_precorr_process_async(dsdgpu_context_t *ctx, int first, int nch,
+                                 const double *d_in, size_t in_stride, size_t count,
+                                 uint8_t *d_bits, size_t bits_stride);
 
 /* ---- UPOLS convolution at the SDM rate ------------------------------------
  * Uniformly partitioned overlap-save convolution of every channel with its

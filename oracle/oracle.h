@@ -132,6 +132,13 @@ void ora_boxcar_free(ora_boxcar_t *b);
 void ora_boxcar_gain(ora_boxcar_t *b, const float *in, double *out, size_t count,
                      double g_start, double g_end);
 
+/* ---- PreCorr greedy SDM (src/precorr.c) ---- */
+typedef struct ora_precorr ora_precorr_t;
+ora_precorr_t *ora_precorr_new(int order, const double *a, const double *g, double state_limit);
+void ora_precorr_free(ora_precorr_t *p);
+void ora_precorr_table(const ora_precorr_t *p, float *tab);
+size_t ora_precorr_process(ora_precorr_t *p, const double *in, uint8_t *bits, size_t n);
+
 /* ---- DSD -> PCM decimation (src/fir.c:467-487,523-611) ---- */
 typedef struct ora_decim ora_decim_t;
 ora_decim_t *ora_decim_new(unsigned fs_in, unsigned fs_out);

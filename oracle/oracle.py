@@ -221,6 +221,49 @@ class Boxcar:
             pass
 
 
+class PreCorr:
+    """The PreCorr greedy SDM: the oracle's restatement, or (ref=True) the
+    reference's own src/precorr.c compiled into oracle/_ref."""
+
+    def __init__(self, order, a, g, state_limit=0.0, ref=False):
+        aa = np.zeros(10); aa[:order] = a[:order]
+        gg = np.zeros(10); gg[:order] = g[:order]
+        self.ref = ref
+        lib = ref_lib() if ref else oracle_lib()
+        if lib is None:
+            raise RuntimeError("reference build absent")
+        self.L = lib.lib
+        new = self.L.ref_precorr_new if ref else self.L.ora_precorr_new
+        new.restype = C.c_void_p
+        new.argtypes = [C.c_int, _dp, _dp, C.c_double]
+        self.h = new(order, _ptr(aa, _dp), _ptr(gg, _dp), float(state_limit))
+
+    def table(self) -> np.ndarray:
+        t = np.zeros(256 * 8, np.float32)
+        fn = self.L.ref_precorr_table if self.ref else self.L.ora_precorr_table
+        fn.argtypes = [C.c_void_p, _fp]
+        fn(self.h, _ptr(t, _fp))
+        return t.reshape(256, 8)
+
+    def process(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.float64)
+        if self.ref:
+            f = np.zeros(max(len(x), 1), np.float32)
+            self.L.ref_precorr_process.argtypes = [C.c_void_p, _dp, _fp, C.c_size_t]
+            self.L.ref_precorr_process(self.h, _ptr(x, _dp), _ptr(f, _fp), len(x))
+            return (f[: len(x)] > 0).astype(np.uint8)
+        b = np.zeros(max(len(x), 1), np.uint8)
+        self.L.ora_precorr_process.argtypes = [C.c_void_p, _dp, _u8p, C.c_size_t]
+        self.L.ora_precorr_process(self.h, _ptr(x, _dp), _ptr(b, _u8p), len(x))
+        return b[: len(x)]
+
+    def __del__(self):
+        try:
+            (self.L.ref_precorr_free if self.ref else self.L.ora_precorr_free)(C.c_void_p(self.h))
+        except Exception:
+            pass
+
+
 class Decimator:
     """The reference's DSD -> PCM FP64 decimation chain, streamed."""
 

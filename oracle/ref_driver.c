@@ -1,7 +1,8 @@
 /*
  * Test infrastructure only (oracle): a thin driver around the reference's own
- * trellis SDM, NTF table and DoP packers, compiled from the reference sources
- * in place (src/trellis.c, src/ntf.c, src/dop.c) by oracle/Makefile into
+ * trellis SDM, NTF table, DoP packers and PreCorr SDM, compiled from the
+ * reference sources in place (src/trellis.c, src/ntf.c, src/dop.c,
+ * src/precorr.c) by oracle/Makefile into
  * oracle/_ref/.  Nothing here is shipped or measured; the product never links
  * it.  It exists so that the C restatement in oracle/sdm_oracle.c and the CUDA
  * kernels can be checked against the reference's real code.
@@ -22,6 +23,7 @@
 #include "trellis.h"
 #include "ntf.h"
 #include "dop.h"
+#include "precorr.h"
 
 typedef struct {
     ntf_filter_t  filt;     /* the context keeps a pointer to its filter */
@@ -216,3 +218,32 @@ void ref_bits_pack(const float *src, uint8_t *dst, size_t n) { bits_pack(src, ds
 void ref_bits_unpack(const uint8_t *src, float *dst, size_t n) { bits_unpack(src, dst, n); }
 void ref_dop_unpack(const float *pcm, float *bits, size_t frames) { dop_unpack(pcm, bits, frames); }
 void ref_dop_pack(const float *bits, float *pcm, size_t n) { dop_pack(bits, pcm, n); }
+
+/* ---- PreCorr (src/precorr.c) ---- */
+typedef struct {
+    ntf_filter_t filt;
+    precorr_context_t ctx;
+} ref_precorr_t;
+
+void *ref_precorr_new(int order, const double *a, const double *g, double state_limit)
+{
+    ref_precorr_t *p = (ref_precorr_t *)calloc(1, sizeof *p);
+    if (!p) return NULL;
+    p->filt.order = order;
+    for (int i = 0; i < order; i++) { p->filt.a[i] = a[i]; p->filt.g[i] = g[i]; }
+    if (precorr_context_init(&p->ctx, &p->filt) != 0) { free(p); return NULL; }
+    p->ctx.state_limit = (float)state_limit;
+    return p;
+}
+
+void ref_precorr_free(void *h) { free(h); }
+
+size_t ref_precorr_process(void *h, const double *in, float *out, size_t n)
+{
+    return precorr_process_block(&((ref_precorr_t *)h)->ctx, in, out, n);
+}
+
+void ref_precorr_table(void *h, float *tab)
+{
+    memcpy(tab, ((ref_precorr_t *)h)->ctx.pred_table, sizeof(float) * PRECORR_HIST_SIZE * PRECORR_PHASES);
+}

@@ -216,3 +216,20 @@ def test_samerate_boxcar_restatement(oracle):
     gb = 0.5 + (0.25 - 0.5) / 1999 * np.arange(2000)
     np.testing.assert_allclose(a, win[:1000] / taps * ga, rtol=0, atol=1e-15)
     np.testing.assert_allclose(b, win[1000:] / taps * gb, rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("name,rate,limit", [("clans-5", 2822400, 0.0), ("clans-7", 5644800, 0.0),
+                                             ("clans-8", 11289600, 0.0), ("sdm-6", 5644800, 4.0)])
+def test_precorr_matches_reference(oracle, name, rate, limit):
+    """The PreCorr restatement (table training and decisions) equals the
+    reference's src/precorr.c bit for bit, streamed."""
+    if oracle.ref_lib() is None:
+        pytest.skip("reference sources absent")
+    from foo_dsd_trellis_gb300 import ntf
+    f = ntf.get_filter(name, rate)
+    mine = oracle.PreCorr(f.order, np.array(f.a), np.array(f.g), limit)
+    ref = oracle.PreCorr(f.order, np.array(f.a), np.array(f.g), limit, ref=True)
+    assert np.array_equal(mine.table().view(np.uint32), ref.table().view(np.uint32))
+    x = 0.6 * multitone(30000, 3)
+    for lo, hi in ((0, 7), (7, 20000), (20000, 30000)):
+        assert np.array_equal(mine.process(x[lo:hi]), ref.process(x[lo:hi]))
