@@ -84,6 +84,8 @@ OUT_DOP = 1
 OUT_NATIVE = 2
 OUT_PCM = 3
 SDM_TRELLIS = 0
+FILE_DSF = 1
+FILE_DFF = 2
 SDM_PRECORR = 1
 
 OPT_SDM_SELECT = 1
@@ -155,6 +157,10 @@ SIGNATURES = {
                                        C.c_double, _szp]),
     "dsdgpu_decim_process_async": (C.c_int, [_vp, C.c_int, _vp, _sz, _sz, _vp, _sz, C.c_double,
                                              C.c_double, _szp]),
+    "dsdgpu_file_header": (C.c_int, [C.c_int, C.c_int, C.c_uint, C.c_uint64, _vp, _sz, _szp,
+                                     C.POINTER(C.c_uint64)]),
+    "dsdgpu_pack_file": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp,
+                                   C.POINTER(C.c_uint64)]),
     "dsdgpu_precorr_setup": (C.c_int, [_vp, C.c_int, _vp, _vp, C.c_double, C.c_int]),
     "dsdgpu_precorr_reset": (C.c_int, [_vp]),
     "dsdgpu_precorr_table": (C.c_int, [_vp, _vp]),

@@ -406,6 +406,28 @@ int dsdgpu_decim_process_async(dsdgpu_context_t *ctx, int nch, const uint8_t *d_
                                size_t pcm_stride, double gain_start, double gain_end,
                                size_t *out_count);
 
+/* ---- DSF / DSDIFF files (the offline encoder's writers) -------------------
+ * Replace write_dsf / write_dff and their packers pack_dsd_lsb / pack_dsd_msb
+ * (reference tools/dsd_encode.c:80-98, :164-292), which write mono files; the
+ * same layouts extend to 1..6 channels per the formats' specifications.
+ * DSF: 92-byte header (DSD, fmt, data chunk headers), payload
+ * [block][channel][4096 B], decisions LSB first, last block zero-padded.
+ * DFF: FRM8 / FVER 1.5 / PROP (SND, FS, CHNL) / DSD chunk header, payload
+ * bytes interleaved by channel, MSB first (no CMPR chunk, no pad byte after
+ * an odd payload: the reference's bytes).  A file is the header followed by
+ * the payload. */
+#define DSDGPU_FILE_DSF 1
+#define DSDGPU_FILE_DFF 2
+/* Host only (no device work): the header of a file of `samples` decisions per
+ * channel at fs Hz into hdr (capacity cap >= 128); *payload_bytes = the size
+ * of the payload that follows it. */
+int dsdgpu_file_header(int format, int nch, unsigned fs, uint64_t samples, uint8_t *hdr,
+                       size_t cap, size_t *hdr_len, uint64_t *payload_bytes);
+/* 0/1 decision bytes [nch][bits_stride] (n per channel) -> the payload in the
+ * file's layout at d_out (*payload_bytes bytes). */
+int dsdgpu_pack_file(dsdgpu_context_t *ctx, int format, int nch, const uint8_t *d_bits,
+                     size_t bits_stride, size_t n, uint8_t *d_out, uint64_t *payload_bytes);
+
 /* ---- PreCorr greedy SDM (src/precorr.c, include/precorr.h:49-61) ----------
  * Replaces precorr_context_init / precorr_process_block /
  * precorr_context_reset (src/precorr.c:198-287) and the reference's GPU entry

@@ -111,6 +111,8 @@ int  ora_dop_pack_i24(const float *bits, uint8_t *out, size_t n, int phase);
 void ora_bits_pack(const float *src, uint8_t *dst, size_t n);
 int  ora_dop_pack_u8(const uint8_t *bits, uint8_t *out, size_t n, int phase);
 void ora_bits_pack_u8(const uint8_t *bits, uint8_t *dst, size_t n);
+size_t ora_pack_dsf_u8(const uint8_t *bits, size_t stride, int nch, size_t n, uint8_t *out);
+size_t ora_pack_dff_u8(const uint8_t *bits, size_t stride, int nch, size_t n, uint8_t *out);
 
 /* ---- FIR chain + engine glue (src/fir.c, src/engine.c) ---- */
 int  ora_fir_design(int ntaps, int quarter, double *h);

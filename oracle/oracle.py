@@ -400,6 +400,42 @@ def dop_pack_bits(bits: np.ndarray, phase: int = 0):
     return out[: len(bits) // 16 * 3], ph
 
 
+def pack_file_payload(bits: np.ndarray, fmt: str) -> np.ndarray:
+    """DSF ("dsf") or DFF ("dff") payload of 0/1 decisions [nch, n]."""
+    bits = np.ascontiguousarray(np.atleast_2d(bits), np.uint8)
+    nch, n = bits.shape
+    nbytes = (n + 7) // 8
+    total = ((nbytes + 4095) // 4096) * 4096 * nch if fmt == "dsf" else nbytes * nch
+    out = np.zeros(max(total, 1), np.uint8)
+    fn = oracle_lib().lib.ora_pack_dsf_u8 if fmt == "dsf" else oracle_lib().lib.ora_pack_dff_u8
+    fn.restype = C.c_size_t
+    fn.argtypes = [_u8p, C.c_size_t, C.c_int, C.c_size_t, _u8p]
+    got = fn(_ptr(bits, _u8p), n, nch, n, _ptr(out, _u8p))
+    assert got == total
+    return out[:total]
+
+
+def ref_enc_lib():
+    """The reference's offline encoder (tools/dsd_encode.c) compiled with its
+    WAV I/O: file writers and input reader, or None when not built."""
+    if "enc" not in _cache:
+        path = os.path.join(REF_DIR, "libref_enc.so")
+        if not os.path.exists(path):
+            _cache["enc"] = None
+        else:
+            L = C.CDLL(path)
+            for name in ("ref_write_dsf", "ref_write_dff"):
+                getattr(L, name).argtypes = [C.c_char_p, _fp, C.c_size_t, C.c_uint32]
+            L.ref_read_input.restype = C.c_longlong
+            L.ref_read_input.argtypes = [C.c_char_p, _fp, C.c_size_t, C.POINTER(C.c_uint32)]
+            L.ref_wav_read.restype = C.c_longlong
+            L.ref_wav_read.argtypes = [C.c_char_p, _fp, C.c_size_t, C.POINTER(C.c_uint32),
+                                       C.POINTER(C.c_int)]
+            L.ref_wav_write.argtypes = [C.c_char_p, _fp, C.c_uint32, C.c_int, C.c_uint32]
+            _cache["enc"] = L
+    return _cache["enc"]
+
+
 def bits_pack(bits: np.ndarray) -> np.ndarray:
     bits = np.ascontiguousarray(bits, np.uint8)
     out = np.zeros(max((len(bits) + 7) // 8, 1), np.uint8)

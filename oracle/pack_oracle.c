@@ -10,6 +10,8 @@
  */
 #include "oracle.h"
 
+#include <string.h>
+
 #define MARK_A 0x05u
 #define MARK_B 0xFAu
 
@@ -67,4 +69,35 @@ void ora_bits_pack_u8(const uint8_t *bits, uint8_t *dst, size_t n)
         }
         dst[i] = (uint8_t)byte;
     }
+}
+
+/* DSF payload (tools/dsd_encode.c:90-98 pack_dsd_lsb, :238-256 the 4096-byte
+ * block padding; channels interleaved block by block per the DSF format):
+ * [block][channel][4096], decision k of a byte at bit k.  Returns bytes. */
+size_t ora_pack_dsf_u8(const uint8_t *bits, size_t stride, int nch, size_t n, uint8_t *out)
+{
+    size_t bytes = (n + 7) / 8, blocks = (bytes + 4095) / 4096;
+    size_t total = blocks * 4096 * (size_t)nch;
+    memset(out, 0, total);
+    for (int c = 0; c < nch; c++)
+        for (size_t i = 0; i < n; i++)
+            if (bits[(size_t)c * stride + i] & 1u) {
+                size_t byte = i / 8;
+                out[(byte / 4096) * 4096 * (size_t)nch + (size_t)c * 4096 + byte % 4096] |=
+                    (uint8_t)(1u << (i % 8));
+            }
+    return total;
+}
+
+/* DFF payload (tools/dsd_encode.c:80-88 pack_dsd_msb; channels interleaved
+ * byte by byte per DSDIFF): [byte][channel], decision k of a byte at bit 7-k. */
+size_t ora_pack_dff_u8(const uint8_t *bits, size_t stride, int nch, size_t n, uint8_t *out)
+{
+    size_t bytes = (n + 7) / 8, total = bytes * (size_t)nch;
+    memset(out, 0, total);
+    for (int c = 0; c < nch; c++)
+        for (size_t i = 0; i < n; i++)
+            if (bits[(size_t)c * stride + i] & 1u)
+                out[(i / 8) * (size_t)nch + (size_t)c] |= (uint8_t)(0x80u >> (i % 8));
+    return total;
 }
