@@ -53,9 +53,11 @@ def parse():
     ap.add_argument("--das-seg-len", type=int, default=WL["das_seg_len"],
                     help="nominal DAS segment length (profiling of small cases only)")
     ap.add_argument("--workload", default="dsd128_das",
-                    choices=["dsd128_das", "multistream64", "diff16", "dsd512conv6"],
-                    help="multistream64: the batched 64-stream form; diff16: the adjoint "
-                         "(each prints its own JSON line)")
+                    choices=["dsd128_das", "multistream64", "diff16", "dsd512conv6",
+                             "samerate128", "precorr128", "dsd2pcm128"],
+                    help="multistream64: the batched 64-stream form; diff16: the adjoint; "
+                         "samerate128 / precorr128 / dsd2pcm128: the DSD re-encode, PreCorr "
+                         "and DSD -> PCM paths (each prints its own JSON line)")
     ap.add_argument("--fd-dirs", type=int, default=32,
                     help="diff16: random unit directions of the finite-difference check")
     ap.add_argument("--ms-scale", type=float, default=1.0,
@@ -654,10 +656,277 @@ def _probe_fp64(plan) -> float:
     return v.value if rc == 0 else float("nan")
 
 
+NEXT = {
+    "samerate128": dict(
+        metric="same-rate DSD128 re-encode (DoP in -> unpack -> 64-tap boxcar -> DAS trellis "
+               "SDM -> DoP) DSD Msamples/s, bit-exact",
+        workload="samerate_dsd128_stereo_10s", fs=5644800, ntf="clans-7", cands=32, depth=64,
+        lat=128, das_seg_len=65536, boxcar_taps=64, gain="float32(0.708) (path gain)"),
+    "precorr128": dict(
+        metric="PCM 44.1 kHz -> DSD128 with the PreCorr SDM (FIR chain -> PreCorr -> DoP) "
+               "DSD Msamples/s, bit-exact SDM",
+        workload="precorr_dsd128_stereo_10s", fs_in=44100, fs=5644800, ntf="clans-7 (PreCorr auto)",
+        state_limit=12.0, boxcar_taps=8, soft_clip=True),
+    "dsd2pcm128": dict(
+        metric="DSD128 -> 44.1 kHz PCM (DoP in -> unpack -> 7 half-band /2 FP64 stages -> "
+               "float32) DSD input Msamples/s",
+        workload="dsd2pcm_dsd128_stereo_10s", fs=5644800, fs_out=44100, stages=7, taps=63),
+}
+PATH_GAIN = 0.708   # the engine's path gain (a float), include/dsd_types.h path table
+
+
+def _dsd128_source(secs: float, nch: int, seed: int):
+    """A DSD128 decision stream for the DSD-input workloads: the 44.1 kHz
+    multitone + pink noise through this library's PCM path (set-up, untimed)."""
+    import numpy as np
+    import torch
+    from foo_dsd_trellis_gb300 import ntf, signals
+    from foo_dsd_trellis_gb300.pipeline import FULL_PARALLEL, OUT_BITS, PCM_FIR_GAIN, Encoder
+    pcm = signals.dsd128_multitone_pink(secs, 44100, nch, seed)
+    f = ntf.get_filter("clans-7", 5644800)
+    src = Encoder(44100, 5644800, nch, f, 64, 32, 128, seg_len=65536, seed_mode=FULL_PARALLEL,
+                  output_format=OUT_BITS)
+    bits = torch.empty((nch, pcm.shape[1] * 128 + 256), dtype=torch.uint8, device="cuda")
+    ns, _ = src.process(torch.from_numpy(pcm).cuda(), bits, PCM_FIR_GAIN, PCM_FIR_GAIN)
+    src.close()
+    return bits[:, : ns - ns % 16].cpu().numpy()
+
+
+def _next_input(wl: str, secs: float, nch: int, seed: int):
+    import numpy as np
+    from foo_dsd_trellis_gb300 import signals
+    if wl == "precorr128":
+        return signals.dsd128_multitone_pink(secs, 44100, nch, seed), None
+    bits = _dsd128_source(secs, nch, seed)
+    return np.stack([signals.dop_floats(bits[c], 0) for c in range(nch)]), bits
+
+
+def _next_cpu(wl: str, inp, bits, sample_s: float) -> dict:
+    """The CPU leg of a DSD-path workload: the oracle's C port on a leading
+    slice, one thread per channel where the path is serial per channel."""
+    import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle as O
+    from foo_dsd_trellis_gb300 import ntf
+    O.build()
+    cfg = NEXT[wl]
+    nch = inp.shape[0]
+    fs = cfg["fs"]
+    if wl == "samerate128":
+        frames = int(sample_s * fs) // 16
+        x = inp[:, :frames]
+        nthreads = os.cpu_count() or 1
+        f = ntf.get_filter(cfg["ntf"], fs)
+        g = float(np.float32(PATH_GAIN))
+        t0 = time.perf_counter()
+        box = np.stack([O.Boxcar(cfg["boxcar_taps"]).process(O.dop_unpack(x[c]), g, g)
+                        for c in range(nch)])
+        out, _, _ = O.das_run(f.order, np.array(f.a), np.array(f.g), cfg["depth"], cfg["cands"],
+                              cfg["lat"], 0.0, box, seg_len=cfg["das_seg_len"], seed_mode=0,
+                              reposition=True, nthreads=nthreads)
+        for c in range(nch):
+            O.dop_pack_bits(out[c], 0)
+        dt = time.perf_counter() - t0
+        n = out.shape[0] * out.shape[1]
+        what = "DoP unpack + boxcar + trellis SDM port + DAS + DoP"
+    elif wl == "precorr128":
+        frames = int(sample_s * 44100)
+        x = inp[:, :frames]
+        nthreads = nch
+        f = ntf.auto_select_precorr(fs)
+        from foo_dsd_trellis_gb300.pipeline import PCM_FIR_GAIN
+
+        def one(c):
+            y = O.engine_fir(44100, fs, x[c], boxcar_taps=8, g_start=PCM_FIR_GAIN,
+                             g_end=PCM_FIR_GAIN, soft_clip=True)
+            b = O.PreCorr(f.order, np.array(f.a), np.array(f.g), cfg["state_limit"]).process(y)
+            O.dop_pack_bits(b, 0)
+            return len(b)
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(nch) as ex:
+            n = sum(ex.map(one, range(nch)))
+        dt = time.perf_counter() - t0
+        what = "FP64 FIR restatement + PreCorr port (bit-identical to precorr.c) + DoP"
+    else:
+        frames = int(sample_s * fs) // 16
+        x = inp[:, :frames]
+        nthreads = nch
+
+        def one(c):
+            d = O.dop_unpack(x[c])
+            O.Decimator(fs, cfg["fs_out"]).process(d)
+            return len(d)
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(nch) as ex:
+            n = sum(ex.map(one, range(nch)))
+        dt = time.perf_counter() - t0
+        what = "DoP unpack + FP64 decimation restatement"
+    return {"value": n / dt / 1e6, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"first {sample_s:g} s of the workload ({nch} ch): {what}", "seconds": dt}
+
+
+def run_next(args):
+    """The DSD re-encode, PreCorr and DSD -> PCM workloads: 10 s stereo at
+    DSD128 through the whole-path pipeline (device buffers), the host-buffer
+    entry point for e2e, and the oracle's port for the CPU leg."""
+    import numpy as np
+    import torch
+    from foo_dsd_trellis_gb300 import _lib, ntf
+    from foo_dsd_trellis_gb300.pipeline import FULL_PARALLEL, OUT_DOP, PCM_FIR_GAIN, Encoder
+    wl = args.workload
+    cfg = NEXT[wl]
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    nch, fs = 2, cfg["fs"]
+    inp, _ = _next_input(wl, args.seconds, nch, 1101 + 2 * rank)
+    if wl == "samerate128":
+        f = ntf.get_filter(cfg["ntf"], fs)
+        g = float(np.float32(PATH_GAIN))
+        enc = Encoder(fs, fs, nch, f, cfg["depth"], cfg["cands"], cfg["lat"],
+                      seg_len=cfg["das_seg_len"], seed_mode=FULL_PARALLEL, reposition=True,
+                      boxcar_taps=0, soft_clip=False, output_format=OUT_DOP, device=local)
+    elif wl == "precorr128":
+        f = ntf.auto_select_precorr(fs)
+        g = PCM_FIR_GAIN
+        enc = Encoder(cfg["fs_in"], fs, nch, f, 64, 32, 128, state_limit=cfg["state_limit"],
+                      boxcar_taps=8, soft_clip=True, output_format=OUT_DOP,
+                      sdm_mode=_lib.SDM_PRECORR, device=local)
+    else:
+        f = ntf.get_filter("clans-7", fs)
+        g = 1.0
+        enc = Encoder(fs, cfg["fs_out"], nch, f, 64, 32, 128, output_format=_lib.OUT_PCM,
+                      device=local)
+    frames = inp.shape[1]
+    d_in = torch.from_numpy(inp).cuda()
+    if wl == "dsd2pcm128":
+        d_out = torch.empty((nch, frames * 16 // 128 + 64), dtype=torch.float32, device="cuda")
+        n_in_step = frames * 16 * nch
+    else:
+        d_out = torch.empty(enc.out_capacity(frames) + 64, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    lib_stream = torch.cuda.ExternalStream(enc.stream_ptr)
+    for _ in range(args.warmup):
+        enc.process(d_in, d_out, g, g)
+    torch.cuda.synchronize()
+    fp64_peak = enc.probe_fp64_gops()
+    clocks = ClockSampler(local)
+    l0 = enc.launches()
+    w0, _ = enc.sdm_work()
+    step_ms, sdm_ms = [], []
+    clocks.start()
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(lib_stream)
+        ns, nb = enc.process(d_in, d_out, g, g)
+        e1.record(lib_stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        sdm_ms.append(enc.stage_ms()["sdm"])
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = (enc.launches() - l0) // max(1, args.steps)
+    sdm_samples = (enc.sdm_work()[0] - w0) / args.steps
+    total_s = max_over_ranks(sum(step_ms) / 1000.0)
+    units_step = n_in_step if wl == "dsd2pcm128" else ns * nch
+    value = job_throughput(units_step, args.steps, world, total_s)
+    # end to end: host buffers through the C-ABI call, copies inside the clock
+    h_in = torch.from_numpy(inp).pin_memory().numpy()
+    cap = (nch * (frames * 16 // 128 + 64) * 4) if wl == "dsd2pcm128" else enc.out_capacity(frames) + 64
+    h_out = torch.empty(cap, dtype=torch.uint8).pin_memory().numpy()
+    enc.process_host(h_in, h_out, g, g)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ns2, nb2 = enc.process_host(h_in, h_out, g, g)
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_units = (frames * 16 * nch) if wl == "dsd2pcm128" else ns2 * nch
+    e2e = {"value": job_throughput(e2e_units, args.steps, world, e2e_s), "unit": UNIT,
+           "h2d_bytes_per_step": int(inp.nbytes), "d2h_bytes_per_step": int(nb2)}
+    st = enc.stage_ms()
+    if wl == "samerate128":
+        sdm_s = statistics.mean(sdm_ms) / 1000.0
+        flops = sdm_samples * cfg["cands"] * (5 * f.order + 6)
+        roof = {"bound": "fp64", "achieved": flops / sdm_s / 1e12, "peak": fp64_peak / 1000.0,
+                "unit": "TFLOP/s", "frac": flops / sdm_s / 1e12 / (fp64_peak / 1000.0),
+                "traffic": SDM_DRAM_BYTES_PER_SAMPLE * sdm_samples,
+                "kernel": f"sdm_jobs_kernel<{f.order}>",
+                "algorithmic_flops_per_launch": flops, "flops_per_sample": cfg["cands"] * (5 * f.order + 6)}
+    elif wl == "precorr128":
+        pc_s = statistics.mean(sdm_ms) / 1000.0
+        n_pc = ns * nch
+        roof = {"bound": "latency", "achieved": 9.0 * n_pc / pc_s / 1e9, "peak": 6773.2,
+                "unit": "GB/s", "frac": 9.0 * n_pc / pc_s / 1e9 / 6773.2, "traffic": 9.0 * n_pc,
+                "kernel": "precorr_process_kernel<7,true>",
+                "per_channel_msamples_per_s": ns / pc_s / 1e6,
+                "note": "a serial recurrence per channel (one thread each): bound by the latency "
+                        "of the output chain, so HBM (8 B in + 1 B out per sample, of measured "
+                        "MEASURED_PEAKS hbm_gbs) is reported only for scale"}
+    else:
+        step_s = total_s / args.steps
+        flops = sum(63 * 2 * (frames * 16 // 2 ** (k + 1)) for k in range(cfg["stages"])) * nch
+        roof = {"bound": "fp64", "achieved": flops / step_s / 1e12, "peak": fp64_peak / 1000.0,
+                "unit": "TFLOP/s", "frac": flops / step_s / 1e12 / (fp64_peak / 1000.0),
+                "traffic": None, "kernel": "decim_stage_kernel (7 stages, whole step timed)",
+                "algorithmic_flops_per_launch": flops,
+                "flops_per_output": "63 products + 63 sums (FP64, separately rounded)"}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = _next_cpu(wl, inp, None, 1.0 if wl != "samerate128" else 0.5)
+    if rank == 0:
+        line = {"metric": cfg["metric"], "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1000 * total_s / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32" if wl == "precorr128" else "f64", "data": "synthetic",
+                "config": dict({k: v for k, v in cfg.items() if k != "metric"}, channels=nch,
+                               seconds=args.seconds,
+                               l2="512 MiB written between timed steps (outside the events)"),
+                "xrt": (units_step / nch / fs) * args.steps / total_s,
+                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+                "gpu_launches": int(launches), "stages_ms": st, "fp64_peak_gops": fp64_peak}
+        print(json.dumps(line), flush=True)
+    enc.close()
+
+
+def run_next_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+    cfg = NEXT[args.workload]
+    inp, _ = _next_input(args.workload, args.seconds, 2, 1101)
+    sample_s = 1.0 if args.workload != "samerate128" else 0.5
+    for _ in range(args.warmup):
+        _next_cpu(args.workload, inp, None, 0.05)
+    vals, secs = [], []
+    info = None
+    for _ in range(args.steps):
+        info = _next_cpu(args.workload, inp, None, sample_s)
+        vals.append(info["value"])
+        secs.append(info["seconds"])
+    v = float(np.mean(vals))
+    print(json.dumps({"impl": "reference", "metric": cfg["metric"], "value": v, "unit": UNIT,
+                      "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": 1000 * float(np.mean(secs)), "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "data": "synthetic",
+                      "config": dict({k: v for k, v in cfg.items() if k != "metric"},
+                                     cpu_sample_seconds=sample_s),
+                      "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"],
+                                       "kind": "port", "sample": info["sample"]},
+                      "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}), flush=True)
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.impl == "reference" and args.workload in NEXT:
+        run_next_reference(args)
+    elif args.impl == "reference":
         run_reference(args)
+    elif args.workload in NEXT:
+        run_next(args)
     elif args.workload == "multistream64":
         run_multistream(args)
     elif args.workload == "diff16":

@@ -105,3 +105,17 @@ def multistream_pcm(entry: dict, level_db: float = -12.0) -> np.ndarray:
         rng = np.random.Generator(np.random.PCG64(entry["seed"] + c))
         out[c] = bandlimited_noise(n, entry["fs_in"], rng, db_to_amp(level_db)).astype(np.float32)
     return out
+
+
+def dop_floats(bits01: np.ndarray, phase: int = 0) -> np.ndarray:
+    """0/1 decision bytes [n] -> DoP float samples (the 24-bit frame
+    [marker, 16 decisions MSB first] as a signed value / 2^23), markers
+    alternating 0x05 / 0xFA from `phase`: what a decoder hands the plugin."""
+    bits01 = np.asarray(bits01, np.uint8)
+    frames = len(bits01) // 16
+    b = np.packbits(bits01[: 16 * frames].reshape(frames, 16), axis=1).astype(np.int32)
+    w = (b[:, 0] << 8) | b[:, 1]
+    marker = np.where((np.arange(frames) + phase) % 2 == 0, 0x05, 0xFA).astype(np.int32)
+    v = (marker << 16) | w
+    v = np.where(v >= 1 << 23, v - (1 << 24), v)
+    return (v.astype(np.float64) / 8388608.0).astype(np.float32)
