@@ -330,6 +330,8 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(pcm, 2.0)
+        one = cpu_baseline(pcm, 0.1, nthreads=1)
+        cpu["single_core"] = {"value": one["value"], "cores": 1, "sample": one["sample"]}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -537,6 +539,7 @@ def run_diff(args):
                 "loss": loss, "surrogate_at_forward": sur,
                 "forward_ms": fwd["forward"], "exact_sdm_ms": fwd["exact_sdm"],
                 "surrogate_ms": sur_ms,
+                "forward_plus_adjoint_over_adjoint": (fwd["forward"] + max_ms) / max_ms,
                 "fd_check": {"directions": args.fd_dirs, "h": h, "worst_rel_err": worst,
                              "direction": "taps N(0,1); a_i N(0,1) a_i; g_i N(0,1) g_i",
                              "worst_rel_err_richardson_h_h2": worst_rich, "tolerance": 1e-4},

@@ -56,6 +56,7 @@ class _SdmLib:
                                       C.c_double, C.c_int, _dp]),
             ("dop_pack_i24", C.c_int, [_fp, _u8p, C.c_size_t, C.c_int]),
             ("bits_pack", None, [_fp, _u8p, C.c_size_t]),
+            ("sdm_cand", C.c_int, [C.c_void_p, C.c_uint, _dp, _dp, _u64p, C.POINTER(C.c_uint)]),
         ]:
             fn = getattr(L, f"{p}_{name}")
             fn.restype = res
@@ -120,6 +121,25 @@ class Sdm:
         s = np.zeros(10, np.float64)
         self.L.fn("sdm_best_state")(self.h, _ptr(s, _dp))
         return s[: self.order]
+
+    def cand(self, i: int):
+        """Candidate i of the current bank: (state, cost, path, next)."""
+        st = np.zeros(10, np.float64)
+        cost = np.zeros(1, np.float64)
+        path = np.zeros(1, np.uint64)
+        nxt = C.c_uint()
+        rc = self.L.fn("sdm_cand")(self.h, i, _ptr(st, _dp), _ptr(cost, _dp), _ptr(path, _u64p),
+                                   C.byref(nxt))
+        if rc != 0:
+            raise IndexError(i)
+        return st[: self.order], float(cost[0]), int(path[0]), int(nxt.value)
+
+    def trace_row(self) -> bytes:
+        """The current act list in order: cost (binary64), path, next of each
+        candidate, packed little-endian."""
+        import struct
+        n = self.info()["num_cands"]
+        return b"".join(struct.pack("<dQB", *self.cand(i)[1:]) for i in range(n))
 
     def info(self) -> dict:
         v = np.zeros(9, np.uint64)

@@ -4,8 +4,11 @@ The reference's src/trellis.c (built from source by oracle/Makefile into
 oracle/_ref/; the widened build for depth > 32) runs over seeded,
 platform-independent inputs (tests/signals.py).  The fixture stores, per case,
 the parameters, the input recipe, the decision count, the SHA-256 of the
-decision bytes and the first 64 decisions.  Run it where the reference tree is
-present; the JSON is committed.
+decision bytes and the first 64 decisions; and, for the TRACES cases, the
+context after each of the first 512 samples: the act list in order with each
+candidate's cost (binary64 as hex), path and next bit, kept in full for the
+first 4 samples and as a 16-hex-digit SHA-256 prefix per sample after that.
+Run it where the reference tree is present; the JSON is committed.
 """
 import hashlib
 import json
@@ -33,6 +36,29 @@ CASES = [
 ]
 
 
+TRACES = ["dsd64_plain_k16_d32", "dsd128_k32_d64_lat128", "dsd64_k2_d16_lim10"]
+TRACE_SAMPLES = 512
+
+
+def trace(ctx, x, nsamp=TRACE_SAMPLES):
+    """Feed x one sample at a time; per sample the packed act list."""
+    rows = []
+    for t in range(nsamp):
+        ctx.process(x[t:t + 1])
+        rows.append(ctx.trace_row())
+    return rows
+
+
+def trace_record(rows, ctx_order_cands=4):
+    import struct
+    full = []
+    for r in rows[:ctx_order_cands]:
+        cands = [struct.unpack_from("<dQB", r, 17 * i) for i in range(len(r) // 17)]
+        full.append([[float(c).hex(), "%016x" % p, nx] for c, p, nx in cands])
+    return {"samples": len(rows), "full": full,
+            "digests": [hashlib.sha256(r).hexdigest()[:16] for r in rows]}
+
+
 def make_input(kind, n, seed):
     return sdm_input(n, seed, amp=0.45) if kind == "sine" else multitone(n, seed)
 
@@ -55,6 +81,9 @@ def main():
                     "sha256": hashlib.sha256(bits.tobytes()).hexdigest(),
                     "head": "".join(str(b) for b in bits[:64]),
                     "source": "reference src/trellis.c" + (" (64-bit path build)" if depth > 32 else "")})
+        if name in TRACES:
+            tctx = O.Sdm(lib, f.order, np.array(f.a), np.array(f.g), depth, K, lat, lim)
+            out[-1]["trace"] = trace_record(trace(tctx, x))
         print(name, len(bits), out[-1]["sha256"][:16])
     with open(os.path.join(HERE, "sdm_golden.json"), "w") as fh:
         json.dump({"cases": out}, fh, indent=1)

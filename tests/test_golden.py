@@ -41,3 +41,24 @@ def test_sdm_golden_gpu(case):
     bits = g.process_block(torch.from_numpy(_input(case)).cuda())[0].cpu().numpy()
     assert len(bits) == case["count"]
     assert hashlib.sha256(bits.tobytes()).hexdigest() == case["sha256"]
+
+
+@pytest.mark.parametrize("case", [c for c in GOLDEN["cases"] if "trace" in c],
+                         ids=[c["name"] for c in GOLDEN["cases"] if "trace" in c])
+def test_oracle_context_trace(oracle, case):
+    """The oracle's context after each of the first 512 samples equals the
+    reference's (act order, binary64 cost, path, next bit of every candidate)."""
+    import struct
+    from foo_dsd_trellis_gb300 import ntf
+    f = ntf.get_filter(case["ntf"], case["rate"])
+    ctx = oracle.sdm(f.order, np.array(f.a), np.array(f.g), case["depth"], case["cands"],
+                     case["lat"], case["state_limit"])
+    x = _input(case)
+    tr = case["trace"]
+    for t in range(tr["samples"]):
+        ctx.process(x[t:t + 1])
+        row = ctx.trace_row()
+        if t < len(tr["full"]):
+            cands = [struct.unpack_from("<dQB", row, 17 * i) for i in range(len(row) // 17)]
+            assert [[float(c).hex(), "%016x" % p, nx] for c, p, nx in cands] == tr["full"][t], t
+        assert hashlib.sha256(row).hexdigest()[:16] == tr["digests"][t], t
