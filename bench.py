@@ -663,8 +663,11 @@ NEXT = {
     "samerate128": dict(
         metric="same-rate DSD128 re-encode (DoP in -> unpack -> 64-tap boxcar -> DAS trellis "
                "SDM -> DoP) DSD Msamples/s, bit-exact",
-        workload="samerate_dsd128_stereo_10s", fs=5644800, ntf="clans-7", cands=32, depth=64,
-        lat=128, das_seg_len=65536, boxcar_taps=64, gain="float32(0.708) (path gain)"),
+        workload="samerate_dsd128_stereo_10s", fs=5644800,
+        path_table="DSD128 -> DSD128 row of the engine's path table (src/engine.c:61); lat 0 "
+                   "there = auto = 128 at DSD128 (src/engine.c:1008-1021)",
+        ntf="clans-6", cands=2, depth=4, lat=128, das_seg_len=65536, boxcar_taps=64,
+        gain="float32(0.708) (path gain)"),
     "precorr128": dict(
         metric="PCM 44.1 kHz -> DSD128 with the PreCorr SDM (FIR chain -> PreCorr -> DoP) "
                "DSD Msamples/s, bit-exact SDM",

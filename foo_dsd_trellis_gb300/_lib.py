@@ -89,6 +89,7 @@ FILE_DFF = 2
 SDM_PRECORR = 1
 
 OPT_SDM_SELECT = 1
+OPT_SDM_LANES = 2
 SELECT_FAST, SELECT_EXACT, SELECT_VERIFY = 0, 1, 2
 
 DAS_FULL_PARALLEL = 0

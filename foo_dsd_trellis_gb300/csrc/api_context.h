@@ -20,7 +20,8 @@ namespace dsdgpu {
 int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_counter,
                     SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream);
 int init_contexts(SdmCtx* d_ctxs, int first, int count, int keep_counters, cudaStream_t stream);
-int sdm_jobs_per_cta(const SdmParams& P);   // 2 for K <= 16 (one job per half-warp), else 1
+int sdm_jobs_per_cta(const SdmParams& P);   // 32 / lanes_per_job(P)
+int lanes_per_job(const SdmParams& P);      // the fixed width of capped launches
 int sdm_max_lat_in_registers();
 int launch_pack_dop(const uint8_t* bits, size_t stride, int nch, size_t frames, int phase,
                     uint8_t* out, int num_sms, cudaStream_t stream);
@@ -60,6 +61,7 @@ struct dsdgpu_context {
   bool sdm_ready = false;
   dsdgpu::SdmParams sdm{};
   int sdm_mode = 0;               // selection strategy (DSDGPU_OPT_SDM_SELECT)
+  int sdm_lanes = 0;              // lanes per SDM job (DSDGPU_OPT_SDM_LANES), 0 = automatic
   int nctx = 0;
   dsdgpu::SdmCtx* d_ctx = nullptr;
   std::vector<int64_t> pending;   // latency fill per context (host mirror)

@@ -265,6 +265,7 @@ int measure_curve(dsdgpu_context* c, const SdmParams& P, TuneCurve* out) {
     cudaMemcpyAsync(d_j, jobs.data(), sizeof(SdmJob) * jobs.size(), cudaMemcpyHostToDevice, c->stream);
     SdmParams Q = P;
     Q.mode = c->sdm_mode;
+    Q.lanes = lanes_per_job(P);   // the width the plan's capped launches use
     // warm-up
     if (launch_sdm_jobs(Q, d_j, sms * jpc, d_cnt, d_c, c->d_status, 0, c->stream) != 0)
       rc = c->cuda_fail(cudaGetLastError(), "tuner launch");
@@ -383,6 +384,7 @@ int capture_graphs(dsdgpu_plan* pl) {
     SdmClass& K = pl->cls[k];
     SdmParams P = K.P;
     P.mode = c->sdm_mode;
+    P.lanes = c->sdm_lanes;
     if (launch_sdm_jobs(P, pl->d_jobs + K.job_first, K.njobs, pl->d_counters + k, pl->d_ctx,
                         c->d_status, K.grid, forked ? K.side : m) != 0)
       rc = DSDGPU_ERR_CUDA;
@@ -563,6 +565,7 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
     const char* err = nullptr;
     const int prc = sdm_params_from_abi(&d.sdm, &P, &err);
     if (prc) return bail(c->fail(prc, err));
+    P.lanes = c->sdm_lanes;   // part of the class: the plan's job slots depend on it
     s.n_fir = (size_t)d.frames * (size_t)s.F.ratio;
     s.lat = P.lat;
     s.overlap = 64 * (size_t)P.lat;
@@ -983,6 +986,7 @@ int dsdgpu_plan_time_plain(dsdgpu_plan_t* pl, int njobs, int64_t* samples, doubl
   for (int j = 0; j < njobs; j++) {
     SdmParams P = pl->cls[cls_of[j]].P;
     P.mode = c->sdm_mode;
+    P.lanes = c->sdm_lanes;
     if (launch_sdm_jobs(P, pl->d_jobs + j, 1, pl->d_counters, pl->d_ctx, c->d_status, 1, m) != 0)
       return c->cuda_fail(cudaGetLastError(), "plain launch");
     c->launches++;

@@ -917,6 +917,7 @@ int dsdgpu_diff_forward(dsdgpu_diff_t* D, const double* taps, const double* a, c
   int rc = sdm_params_from_abi(&sp, &P, &err);
   if (rc) return c->fail(rc, err);
   P.mode = c->sdm_mode;
+  P.lanes = c->sdm_lanes;
   const int C = D->p.nclips;
   if (init_contexts(D->d_ctx, 0, C, 0, s) != 0) return c->cuda_fail(cudaGetLastError(), "context init");
   c->launches++;

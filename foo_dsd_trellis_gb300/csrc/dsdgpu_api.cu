@@ -134,6 +134,7 @@ int dsdgpu_context::run_jobs(const std::vector<SdmJob>& jobs) {
   if (e != cudaSuccess) return cuda_fail(e, "job table upload");
   SdmParams P = sdm;
   P.mode = sdm_mode;
+  P.lanes = sdm_lanes;
   if (launch_sdm_jobs(P, d_jobs, n, d_counter, d_ctx, d_status, max_blocks, stream) != 0)
     return cuda_fail(cudaGetLastError(), "sdm kernel launch");
   launches++;
@@ -219,6 +220,11 @@ int dsdgpu_set_option(dsdgpu_context_t* c, int option, int value) {
       if (value < DSDGPU_SELECT_FAST || value > DSDGPU_SELECT_VERIFY)
         return c->fail(DSDGPU_ERR_ARG, "bad selection mode");
       c->sdm_mode = value;
+      return DSDGPU_OK;
+    case DSDGPU_OPT_SDM_LANES:
+      if (value != 0 && (value < 2 || value > 32 || (value & (value - 1))))
+        return c->fail(DSDGPU_ERR_ARG, "lanes per job must be 0 or a power of two in 2..32");
+      c->sdm_lanes = value;
       return DSDGPU_OK;
     default:
       return c->fail(DSDGPU_ERR_ARG, "unknown option");

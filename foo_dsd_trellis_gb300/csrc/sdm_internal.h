@@ -23,6 +23,7 @@ struct SdmParams {
   int lat;
   int depth;
   int mode;               // kModeFast, kModeExact or kModeVerify
+  int lanes;              // lanes per job (2..32, a power of two >= K); 0 = automatic
 };
 
 // Survivor selection strategy of the SDM kernel.

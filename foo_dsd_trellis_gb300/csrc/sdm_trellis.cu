@@ -31,8 +31,8 @@
 
 namespace dsdgpu {
 
-// One warp per CTA (one job, or two half-warp jobs for K <= 16): a few
-// thousand long-running jobs spread evenly over the SMs.  The launch bound (32 threads, 13 CTAs per SM) holds the kernel
+// One warp per CTA (one job, or 32 / LPJ jobs side by side for K <= 16): a
+// few thousand long-running jobs spread evenly over the SMs.  The launch bound (32 threads, 13 CTAs per SM) holds the kernel
 // at 128 registers; a 152-register build measured 50 % slower on the DSD128
 // DAS workload.
 constexpr int kRegRingWords = 8;      // rings held in registers: lat <= 256
@@ -107,17 +107,71 @@ __device__ __forceinline__ void shared_all(const SdmParams& P, const double (&S)
   for (int k = 0; k < shared_ops<N>(); k++) shared_op<N>(k, P, S, np, tg, tu);
 }
 
+// Shared memory of one job run by LPJ lanes: the slot memory of both banks
+// for its 2 * LPJ children (K <= LPJ, so children 2K.. are never touched),
+// the 128-bucket path hash and the selection scratch.
+template <int LPJ>
 struct WarpSmem {
-  unsigned long long path[2][kSlots];
-  long long key[2][kSlots];
-  int8_t link[2][kSlots];
+  static constexpr int S = 2 * LPJ;
+  unsigned long long path[2][S];
+  long long key[2][S];
+  int8_t link[2][S];
   int8_t heads[kBuckets];
-  int8_t act[kMaxCands];       // scatter target of the fast selection
-  uint8_t hashmark[kSlots];    // children the serial path hashed (verify mode)
-  uint8_t hashmark2[kSlots];   // children the fast path deems hashed
-  int8_t pos[kSlots];          // sorted position of each child (serial path)
-  int8_t idx_at[kSlots];       // child at each sorted position (serial path)
+  int8_t act[LPJ];             // scatter target of the fast selection
+  uint8_t hashmark[S];         // children the serial path hashed (verify mode)
+  uint8_t hashmark2[S];        // children the fast path deems hashed
+  int8_t pos[S];               // sorted position of each child (serial path)
+  int8_t idx_at[S];            // child at each sorted position (serial path)
 };
+
+// Lanes per job: the smallest power of two >= K (at least 2) is the tightest
+// packing, 32 / LPJ jobs per warp; a requested width (SdmParams::lanes) is
+// raised to it.
+__host__ __device__ constexpr int min_lanes(int K) {
+  return K > 16 ? 32 : K > 8 ? 16 : K > 4 ? 8 : K > 2 ? 4 : 2;
+}
+
+// Fixed rule (the batch plan sizes its job slots with it): a requested width,
+// else a whole warp for K > 16 and a half-warp below.
+int lanes_per_job(const SdmParams& P) {
+  const int lo = min_lanes(P.cands);
+  if (P.lanes > 0) return P.lanes > lo ? P.lanes : lo;
+  return lo > 16 ? 32 : 16;
+}
+
+// Warp slots of the device: 16 one-warp CTAs per SM (128 registers a thread).
+static int resident_warps() {
+  static int cached[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return 152 * 16;
+  if (!cached[dev]) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cached[dev] = (sms > 0 ? sms : 152) * 16;
+  }
+  return cached[dev];
+}
+
+// Lanes for a launch of njobs jobs with no block cap: the widest width whose
+// jobs all fit in one wave of resident warps.  The trellis step of a small-K
+// job is bound by its serial selection chain rather than by FP64 issue, so
+// fewer jobs per warp run faster as long as no job waits for a second wave
+// (10 s stereo same-rate DSD128, 1722 jobs: K = 16 at 32 lanes 289 vs 256 at
+// 16 lanes DSD Msamples/s; K = 2 at 2 lanes 174, at 16 lanes 309).
+static int launch_lanes(const SdmParams& P, int njobs, int max_blocks) {
+  if (P.lanes > 0 || max_blocks > 0) return lanes_per_job(P);
+  const int lo = min_lanes(P.cands);
+  const int slots = resident_warps();
+  int lanes = 32;
+  while (lanes > lo && (long long)njobs * lanes > (long long)slots * 32) lanes >>= 1;
+  return lanes;
+}
+
+template <int LPJ>
+__host__ __device__ constexpr unsigned job_mask(int sh) {
+  return LPJ == 32 ? 0xffffffffu : (((1u << LPJ) - 1u) << sh);
+}
 
 // (key, index) order of the survivor selection: cost bits as int64, then slot.
 __device__ __forceinline__ bool key_less(long long ka, int ia, long long kb, int ib) {
@@ -157,22 +211,26 @@ __device__ __forceinline__ void bitonic_sort(long long& kA, int& iA, long long& 
   }
 }
 
-// Stages of the bitonic sort of 2 * LPJ keys (21 for 64, 15 for 32).
+// Stages of the bitonic sort of 2 * LPJ keys: log2(2 LPJ) (log2(2 LPJ) + 1) / 2
+// (21 for 64 keys, 15 for 32, 10, 6, 3).
 template <int LPJ>
-__host__ __device__ constexpr int sort_stages() { return LPJ == 32 ? 21 : 15; }
+__host__ __device__ constexpr int sort_stages() {
+  return LPJ == 32 ? 21 : LPJ == 16 ? 15 : LPJ == 8 ? 10 : LPJ == 4 ? 6 : 3;
+}
 
-// LPJ lanes run one job: 32 (a whole warp) for K > 16, 16 (each half-warp its
-// own job) for K <= 16, so small trellises do not leave half of every FP64
-// warp instruction idle.  `lane` is the lane within the job, `hm` the job's
-// lanes; warp intrinsics use hm and width LPJ, ballots are shifted to the
-// job's bits.
+// LPJ lanes run one job (lanes_per_job(K)): a whole warp for K > 16, else
+// 32 / LPJ jobs side by side in one warp, so small trellises do not leave
+// most of every FP64 warp instruction idle.  `lane` is the lane within the
+// job, `hm` the job's lanes; warp intrinsics use hm and width LPJ, ballots
+// are shifted to the job's bits.
 template <int N, int LPJ>
 __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restrict__ ctxs,
-                        WarpSmem& sm, int* __restrict__ status) {
+                        WarpSmem<LPJ>& sm, int* __restrict__ status) {
+  constexpr int S = WarpSmem<LPJ>::S;
   const int wl = threadIdx.x & 31;
   const int lane = wl & (LPJ - 1);
   const unsigned sh = (unsigned)(wl - lane);
-  const unsigned hm = LPJ == 32 ? kFull : (0xffffu << sh);
+  const unsigned hm = job_mask<LPJ>((int)sh);
   // ctx < 0: the job's end state goes to a scratch context, one per job slot
   // of the launch, at (-ctx - 1) + slot (jobs whose end state nobody reads)
   const int slot_id = (int)blockIdx.x * (32 / LPJ) + wl / LPJ;
@@ -204,8 +262,8 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     for (int w = 0; w < kRegRingWords; w++)
       if (w < W) ring[w] = src->ring[lane][w];
   }
-  for (int i = lane; i < 2 * kSlots; i += LPJ) {
-    const int b = i / kSlots, j = i % kSlots;
+  for (int i = lane; i < 2 * S; i += LPJ) {
+    const int b = i / S, j = i % S;
     sm.path[b][j] = src->spath[b][j];
     sm.key[b][j] = (long long)src->skey[b][j];
     sm.link[b][j] = src->slink[b][j];
@@ -606,8 +664,8 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
       if (w < W) dst->ring[lane][w] = ring[w];
   }
   __syncwarp(hm);
-  for (int i = lane; i < 2 * kSlots; i += LPJ) {
-    const int b = i / kSlots, j = i % kSlots;
+  for (int i = lane; i < 2 * S; i += LPJ) {
+    const int b = i / S, j = i % S;
     dst->spath[b][j] = sm.path[b][j];
     dst->skey[b][j] = (unsigned long long)sm.key[b][j];
     dst->slink[b][j] = sm.link[b][j];
@@ -633,8 +691,9 @@ sdm_jobs_kernel(SdmParams P, const SdmJob* __restrict__ jobs, int njobs,
   extern __shared__ __align__(16) unsigned char sdm_smem_raw[];
   const int wl = threadIdx.x & 31;
   const int lane = wl & (LPJ - 1);
-  const unsigned hm = LPJ == 32 ? kFull : (0xffffu << (wl - lane));
-  WarpSmem& sm = reinterpret_cast<WarpSmem*>(sdm_smem_raw)[(threadIdx.x >> 5) * (32 / LPJ) + wl / LPJ];
+  const unsigned hm = job_mask<LPJ>(wl - lane);
+  WarpSmem<LPJ>& sm =
+      reinterpret_cast<WarpSmem<LPJ>*>(sdm_smem_raw)[(threadIdx.x >> 5) * (32 / LPJ) + wl / LPJ];
   for (;;) {
     int j = 0;
     if (lane == 0) j = atomicAdd(job_counter, 1);
@@ -646,38 +705,46 @@ sdm_jobs_kernel(SdmParams P, const SdmJob* __restrict__ jobs, int njobs,
   }
 }
 
-int sdm_jobs_per_cta(const SdmParams& P) { return P.cands <= 16 ? 2 : 1; }
+int sdm_jobs_per_cta(const SdmParams& P) { return 32 / lanes_per_job(P); }
 
-// Host-side launcher: one warp-sized CTA runs one job at a time (K > 16) or
-// two, one per half-warp (K <= 16); max_blocks caps the CTAs.
+template <int LPJ>
+static int launch_lpj(const SdmParams& P, dim3 grid, const SdmJob* d_jobs, int njobs,
+                      int* d_counter, SdmCtx* d_ctxs, int* d_status, cudaStream_t stream) {
+  const size_t smem = sizeof(WarpSmem<LPJ>) * (size_t)(32 / LPJ);
+  switch (P.order) {
+#define DSD_CASE(NN)                                                                       \
+  case NN:                                                                                 \
+    sdm_jobs_kernel<NN, LPJ><<<grid, 32, smem, stream>>>(P, d_jobs, njobs, d_counter, d_ctxs, \
+                                                         d_status);                        \
+    break;
+    DSD_CASE(2) DSD_CASE(3) DSD_CASE(4) DSD_CASE(5) DSD_CASE(6)
+    DSD_CASE(7) DSD_CASE(8) DSD_CASE(9) DSD_CASE(10)
+#undef DSD_CASE
+    default: return -1;
+  }
+  return 0;
+}
+
+// Host-side launcher: each warp-sized CTA runs 32 / LPJ jobs side by side
+// (lanes_per_job); max_blocks caps the CTAs.
 int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_counter,
                     SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream) {
   if (njobs <= 0) return 0;
-  const int jpc = sdm_jobs_per_cta(P);
+  const int lanes = launch_lanes(P, njobs, max_blocks);
+  const int jpc = 32 / lanes;
   int blocks = (njobs + jpc - 1) / jpc;
   if (max_blocks > 0 && blocks > max_blocks) blocks = max_blocks;
   cudaMemsetAsync(d_counter, 0, sizeof(int), stream);
-  const dim3 grid(blocks), block(32);
-  const size_t smem = sizeof(WarpSmem) * (size_t)jpc;
-  if (jpc == 2) {
-    switch (P.order) {
-#define DSD_CASE(NN) \
-  case NN: sdm_jobs_kernel<NN, 16><<<grid, block, smem, stream>>>(P, d_jobs, njobs, d_counter, d_ctxs, d_status); break;
-      DSD_CASE(2) DSD_CASE(3) DSD_CASE(4) DSD_CASE(5) DSD_CASE(6)
-      DSD_CASE(7) DSD_CASE(8) DSD_CASE(9) DSD_CASE(10)
-#undef DSD_CASE
-      default: return -1;
-    }
-  } else {
-    switch (P.order) {
-#define DSD_CASE(NN) \
-  case NN: sdm_jobs_kernel<NN, 32><<<grid, block, smem, stream>>>(P, d_jobs, njobs, d_counter, d_ctxs, d_status); break;
-      DSD_CASE(2) DSD_CASE(3) DSD_CASE(4) DSD_CASE(5) DSD_CASE(6)
-      DSD_CASE(7) DSD_CASE(8) DSD_CASE(9) DSD_CASE(10)
-#undef DSD_CASE
-      default: return -1;
-    }
+  const dim3 grid(blocks);
+  int rc = -1;
+  switch (lanes) {
+    case 32: rc = launch_lpj<32>(P, grid, d_jobs, njobs, d_counter, d_ctxs, d_status, stream); break;
+    case 16: rc = launch_lpj<16>(P, grid, d_jobs, njobs, d_counter, d_ctxs, d_status, stream); break;
+    case 8: rc = launch_lpj<8>(P, grid, d_jobs, njobs, d_counter, d_ctxs, d_status, stream); break;
+    case 4: rc = launch_lpj<4>(P, grid, d_jobs, njobs, d_counter, d_ctxs, d_status, stream); break;
+    default: rc = launch_lpj<2>(P, grid, d_jobs, njobs, d_counter, d_ctxs, d_status, stream); break;
   }
+  if (rc) return rc;
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

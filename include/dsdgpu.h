@@ -136,6 +136,10 @@ const char *dsdgpu_last_error(const dsdgpu_context_t *ctx);
 #define DSDGPU_SELECT_VERIFY    2   /*   serial, and the parallel result is checked
                                          against it every sample (a disagreement
                                          returns DSDGPU_ERR_DEVICE) */
+#define DSDGPU_OPT_SDM_LANES    2   /* lanes of a warp per trellis job: 0 = automatic
+                                         (default), or 2, 4, 8, 16, 32 (raised to the
+                                         next power of two >= K); 32 / lanes jobs share
+                                         a warp.  Results do not depend on it. */
 int  dsdgpu_set_option(dsdgpu_context_t *ctx, int option, int value);
 
 /* Number of kernels this context has launched so far. */

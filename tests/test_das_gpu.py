@@ -67,3 +67,36 @@ def test_das_single_segment_is_plain_sdm(oracle):
     plain = oracle.sdm_bits(ref, x[0])
     assert np.array_equal(got[0], plain)
     assert np.array_equal(want[0], plain)
+
+
+@pytest.mark.parametrize("K,depth", [(2, 4), (5, 8), (12, 16)])
+def test_lanes_per_job_do_not_change_results(oracle, K, depth):
+    """Every width of the job packing (2 .. 32 lanes, 16 .. 1 jobs per warp,
+    and the automatic choice) gives the oracle's DAS output: small K with a
+    short path mask takes the serial selection often, in different jobs of
+    the same warp."""
+    from foo_dsd_trellis_gb300 import _lib
+    from foo_dsd_trellis_gb300.das import DasChannels
+    import ctypes as C
+    f = _ntf("clans-6", 5644800)
+    x = np.stack([multitone(150000, 7) * 1.2, multitone(150000, 8) * 0.9, multitone(150000, 9)])
+    want, ws, _ = oracle.das_run(f.order, np.array(f.a), np.array(f.g), depth, K, 16, 0.0, x,
+                                 seg_len=8192, seed_mode=0)
+    for lanes in (0, 2, 4, 8, 16, 32):
+        if lanes and lanes < K:
+            continue
+        d = DasChannels(f.order, f.a, f.g, depth, K, 16, num_channels=3)
+        _lib.check(d.h, d.L.dsdgpu_set_option(d.h, _lib.OPT_SDM_LANES, lanes))
+        got, seams = d.process_chunk(torch.from_numpy(x).cuda(), seg_len=8192, seed_mode=0)
+        assert list(seams) == list(ws), lanes
+        assert np.array_equal(got.cpu().numpy(), want), lanes
+        d.close()
+
+
+def test_lanes_option_rejects_bad_widths():
+    from foo_dsd_trellis_gb300 import _lib
+    from foo_dsd_trellis_gb300.das import DasChannels
+    f = _ntf("clans-6", 5644800)
+    d = DasChannels(f.order, f.a, f.g, 8, 4, 16, num_channels=1)
+    for bad in (1, 3, 12, 64, -2):
+        assert d.L.dsdgpu_set_option(d.h, _lib.OPT_SDM_LANES, bad) == _lib.ERR_ARG
