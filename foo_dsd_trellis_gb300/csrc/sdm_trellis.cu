@@ -725,11 +725,17 @@ static int launch_lpj(const SdmParams& P, dim3 grid, const SdmJob* d_jobs, int n
   return 0;
 }
 
+bool sdm_scalar_eligible(const SdmParams& P, int max_blocks);   // sdm_scalar.cu
+int launch_sdm_scalar(const SdmParams& P, const SdmJob* d_jobs, int njobs, SdmCtx* d_ctxs,
+                      cudaStream_t stream);
+
 // Host-side launcher: each warp-sized CTA runs 32 / LPJ jobs side by side
-// (lanes_per_job); max_blocks caps the CTAs.
+// (lanes_per_job); max_blocks caps the CTAs.  Uncapped launches at K <= 2
+// run one job per thread (sdm_scalar.cu).
 int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_counter,
                     SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream) {
   if (njobs <= 0) return 0;
+  if (sdm_scalar_eligible(P, max_blocks)) return launch_sdm_scalar(P, d_jobs, njobs, d_ctxs, stream);
   const int lanes = launch_lanes(P, njobs, max_blocks);
   const int jpc = 32 / lanes;
   int blocks = (njobs + jpc - 1) / jpc;

@@ -179,3 +179,26 @@ def test_exact_and_fast_modes_agree(oracle):
         g.set_select(mode)
         outs.append(g.process_block(torch.from_numpy(x).cuda())[0].cpu().numpy())
     assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("K,depth,lat,lim", [(2, 4, 128, 0.0), (1, 8, 32, 0.0), (2, 2, 200, 3.0)])
+def test_small_k_streaming_channels_and_drain(oracle, K, depth, lat, lim):
+    """K <= 2 runs one job per thread: streamed blocks over several channels,
+    short path masks (dedup on most samples), the limiter and the drain,
+    against the oracle."""
+    f = _ntf("clans-6", 5644800)
+    nch = 5
+    x = np.stack([multitone(12000, seed=40 + c) * (0.6 + 0.1 * c) for c in range(nch)])
+    refs = [_ora(oracle, f, depth, K, lat, lim) for _ in range(nch)]
+    g = _gpu_sdm(f, depth, K, lat, lim, nctx=nch)
+    for lo, hi in ((0, 1), (1, 77), (77, 5000), (5000, 12000)):
+        got = g.process_block(torch.from_numpy(np.ascontiguousarray(x[:, lo:hi])).cuda())
+        for c in range(nch):
+            np.testing.assert_array_equal(got[c].cpu().numpy(), oracle.sdm_bits(refs[c], x[c, lo:hi]))
+    tail = g.drain(lat + 10, 0, nch)
+    for c in range(nch):
+        np.testing.assert_array_equal(tail[c].cpu().numpy(), (refs[c].drain(lat + 10) > 0).astype(np.uint8))
+        q, info = g.query(c), refs[c].info()
+        assert (q["num_cands"], q["total_children"], q["next_filter_drops"], q["conv_fail"]) == \
+            (info["num_cands"], info["total_children"], info["next_filter_drops"], info["conv_fail"])
+        np.testing.assert_array_equal(q["best_state"], refs[c].best_state())
