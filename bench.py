@@ -675,7 +675,7 @@ NEXT = {
         state_limit=12.0, boxcar_taps=8, soft_clip=True),
     "dsd2pcm128": dict(
         metric="DSD128 -> 44.1 kHz PCM (DoP in -> unpack -> 7 half-band /2 FP64 stages -> "
-               "float32) DSD input Msamples/s",
+               "float32) DSD input Msamples/s, float32 output within 2e-7 of the FP64 restatement",
         workload="dsd2pcm_dsd128_stereo_10s", fs=5644800, fs_out=44100, stages=7, taps=63),
 }
 PATH_GAIN = 0.708   # the engine's path gain (a float), include/dsd_types.h path table
@@ -871,12 +871,16 @@ def run_next(args):
                         "MEASURED_PEAKS hbm_gbs) is reported only for scale"}
     else:
         step_s = total_s / args.steps
-        flops = sum(63 * 2 * (frames * 16 // 2 ** (k + 1)) for k in range(cfg["stages"])) * nch
-        roof = {"bound": "fp64", "achieved": flops / step_s / 1e12, "peak": fp64_peak / 1000.0,
-                "unit": "TFLOP/s", "frac": flops / step_s / 1e12 / (fp64_peak / 1000.0),
-                "traffic": None, "kernel": "decim_stage_kernel (7 stages, whole step timed)",
-                "algorithmic_flops_per_launch": flops,
-                "flops_per_output": "63 products + 63 sums (FP64, separately rounded)"}
+        # FP64 instructions: stage 1 = 4 table sums + the centre tap per output,
+        # stages 2-7 = 33 FMAs per output (the half-band's nonzero taps)
+        outs = [frames * 16 // 2 ** (k + 1) for k in range(cfg["stages"])]
+        instr = (5 * outs[0] + 33 * sum(outs[1:])) * nch
+        roof = {"bound": "fp64", "achieved": instr / step_s / 1e12, "peak": fp64_peak / 1000.0,
+                "unit": "T FP64 instructions/s", "frac": instr / step_s / 1e12 / (fp64_peak / 1000.0),
+                "traffic": None, "kernel": "decim_bits_kernel + decim_stage_kernel (7 stages, whole step timed)",
+                "algorithmic_instructions_per_launch": instr,
+                "per_output": "stage 1: 4 table reads + 5 DADD; stages 2-7: 33 DFMA (an FMA "
+                              "issues as one FP64 instruction; the probe's peak counts DADD/DMUL)"}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = _next_cpu(wl, inp, None, 1.0 if wl != "samerate128" else 0.5)

@@ -2,13 +2,22 @@
 // (src/engine.c:566-577; chain src/fir.c:523-611 with 63-tap half-band /2
 // stages, ipp_downsample_d src/fir.c:467-487; gain ramp src/engine.c:879-889).
 //
-// Every stage is one launch, FP64, y[m] = sum_k h[k] x[2m - k] summed in tap
-// order with separately rounded products (the delay line of the previous call
-// stands in for negative indices), followed by a small launch that keeps the
-// stage's last 62 consumed inputs.  A stage consumes floor(count / 2) * 2
-// inputs, as the reference's numIters = in_count / factor.  The first stage
-// reads 0/1 decision bytes as +-1.  Traffic: about 1 B + 8 B + 8 B per input
-// sample over all stages together, so the chain is HBM-bound.
+// Every stage is one launch, FP64, y[m] = sum_k h[k] x[2m - k] (the delay
+// line of the previous call stands in for negative indices), followed by a
+// small launch that keeps the stage's last 62 consumed inputs.  A stage
+// consumes floor(count / 2) * 2 inputs, as the reference's numIters =
+// in_count / factor.  IPP's summation order and use of FMA are not known, so
+// the stages take the cheapest exact-enough form:
+//   * the 63-tap half-band's taps at odd k other than the centre are the
+//     design's zeros (|h| < 2e-17: they move an output by ~1e-17 of full scale), so
+//     only the 32 even taps and the centre tap are applied;
+//   * FP64 stages: those 33 taps as FMAs in ascending tap order;
+//   * the first stage reads +-1 decisions: the 32 even taps form 4 groups of
+//     8, each group's sum for every pattern of its 8 decisions is a table
+//     entry (4 x 256 FP64 values, sums in tap order), so an output is 4 table
+//     reads, the centre tap's +-h[31] and 4 adds.
+// The result differs from a tap-order sum of separately rounded products by
+// a few FP64 ulps (float32 output within 2e-7 of full scale).
 #include "api_context.h"
 #include "fir_internal.h"
 
@@ -24,23 +33,70 @@ struct DecTaps {
   double h[kDecTaps];
 };
 
-template <bool kBits>
-__global__ void decim_stage_kernel(const __grid_constant__ DecTaps T, const uint8_t* __restrict__ bits,
-                                   const double* __restrict__ in, size_t in_stride, long long m_out,
+// nonzero taps: even k and the centre
+constexpr int kNzTaps = 33;
+struct DecNz {
+  double h[kNzTaps];
+  int k[kNzTaps];
+};
+
+constexpr int kLutGroups = 4;   // 32 even taps in groups of 8
+
+// FP64 stage: the 33 nonzero taps as FMAs in ascending tap order
+__global__ void decim_stage_kernel(const __grid_constant__ DecNz T, const double* __restrict__ in,
+                                   size_t in_stride, long long m_out,
                                    const double* __restrict__ dly, double* __restrict__ out,
                                    size_t out_stride, int nch) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m_out * nch) return;
   const long long c = i / m_out, m = i % m_out;
   const double* dl = dly + (size_t)c * (kDecTaps - 1);
+  const double* xc = in + (size_t)c * in_stride;
   double acc = 0.0;
-#pragma unroll 7
-  for (int k = 0; k < kDecTaps; k++) {
-    const long long j = 2 * m - k;
-    double x;
-    if (j >= 0) x = kBits ? (bits[(size_t)c * in_stride + j] ? 1.0 : -1.0) : in[(size_t)c * in_stride + j];
-    else x = dl[kDecTaps - 1 + j];
-    acc = __dadd_rn(acc, __dmul_rn(T.h[k], x));
+#pragma unroll
+  for (int q = 0; q < kNzTaps; q++) {
+    const long long j = 2 * m - T.k[q];
+    const double x = j >= 0 ? xc[j] : dl[kDecTaps - 1 + j];
+    acc = __fma_rn(T.h[q], x, acc);
+  }
+  out[(size_t)c * out_stride + m] = acc;
+}
+
+// first stage, decision bytes in: 4 group-table reads + the centre tap
+__global__ void __launch_bounds__(256) decim_bits_kernel(const __grid_constant__ DecNz T,
+                                                         const double* __restrict__ lut, double h31,
+                                                         const uint8_t* __restrict__ bits,
+                                                         size_t in_stride, long long m_out,
+                                                         const double* __restrict__ dly,
+                                                         double* __restrict__ out,
+                                                         size_t out_stride, int nch) {
+  __shared__ double tab[kLutGroups * 256];
+  for (int q = threadIdx.x; q < kLutGroups * 256; q += blockDim.x) tab[q] = lut[q];
+  __syncthreads();
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m_out * nch) return;
+  const long long c = i / m_out, m = i % m_out;
+  const double* dl = dly + (size_t)c * (kDecTaps - 1);
+  const uint8_t* bc = bits + (size_t)c * in_stride;
+  double acc = 0.0;
+  if (2 * m < kDecTaps - 1) {
+    // the window reaches the delay line, whose values are zero before the
+    // first call: the 33 taps directly
+#pragma unroll
+    for (int q = 0; q < kNzTaps; q++) {
+      const long long j = 2 * m - T.k[q];
+      const double x = j >= 0 ? (bc[j] & 1u ? 1.0 : -1.0) : dl[kDecTaps - 1 + j];
+      acc = __fma_rn(T.h[q], x, acc);
+    }
+  } else {
+#pragma unroll
+    for (int g = 0; g < kLutGroups; g++) {
+      unsigned p = 0;
+#pragma unroll
+      for (int u = 0; u < 8; u++) p |= (unsigned)(bc[2 * m - 16 * g - 2 * u] & 1u) << u;
+      acc = __dadd_rn(acc, tab[g * 256 + p]);
+    }
+    acc = __dadd_rn(acc, (bc[2 * m - 31] & 1u) ? h31 : -h31);
   }
   out[(size_t)c * out_stride + m] = acc;
 }
@@ -84,10 +140,13 @@ struct dsdgpu_decim_state {
   int stages = 0;
   int nch = 0;
   DecTaps taps{};
+  DecNz nz{};
+  double* d_lut = nullptr;      // [group][pattern] sums of the first stage
   double* d_dly = nullptr;      // [stage][nch][62]
   double* d_buf = nullptr;      // ping-pong [2][nch][row]
   size_t row = 0;
   ~dsdgpu_decim_state() {
+    if (d_lut) cudaFree(d_lut);
     if (d_dly) cudaFree(d_dly);
     if (d_buf) cudaFree(d_buf);
   }
@@ -111,11 +170,25 @@ int dsdgpu_decim_setup(dsdgpu_context_t* c, unsigned fs_in, unsigned fs_out, int
   s->stages = S;
   s->nch = nch;
   design_taps(kDecTaps, false, s->taps.h);
+  for (int q = 0, k = 0; k < kDecTaps; k++)
+    if ((k & 1) == 0 || k == kDecTaps / 2) { s->nz.h[q] = s->taps.h[k]; s->nz.k[q] = k; q++; }
+  // group g, pattern p: sum over u = 0..7 of h[16 g + 2 u] * (bit u of p ? 1 : -1)
+  double lut[kLutGroups * 256];
+  for (int g = 0; g < kLutGroups; g++)
+    for (int p = 0; p < 256; p++) {
+      double acc = 0.0;
+      for (int u = 0; u < 8; u++) {
+        const double h = s->taps.h[16 * g + 2 * u];
+        acc += ((p >> u) & 1) ? h : -h;
+      }
+      lut[g * 256 + p] = acc;
+    }
   const size_t dbytes = sizeof(double) * (size_t)S * nch * (kDecTaps - 1);
-  if (cudaMalloc(&s->d_dly, dbytes) != cudaSuccess) {
+  if (cudaMalloc(&s->d_dly, dbytes) != cudaSuccess || cudaMalloc(&s->d_lut, sizeof lut) != cudaSuccess) {
     delete s;
-    return c->cuda_fail(cudaGetLastError(), "decimation delay lines");
+    return c->cuda_fail(cudaGetLastError(), "decimation buffers");
   }
+  cudaMemcpyAsync(s->d_lut, lut, sizeof lut, cudaMemcpyHostToDevice, c->stream);
   cudaMemsetAsync(s->d_dly, 0, dbytes, c->stream);
   decim_free(c->decim);
   c->decim = s;
@@ -164,12 +237,12 @@ int dsdgpu_decim_process_async(dsdgpu_context_t* c, int nch, const uint8_t* d_bi
     double* dly = s->d_dly + (size_t)k * nch * (kDecTaps - 1);
     if (m > 0) {
       if (k == 0) {
-        decim_stage_kernel<true><<<nb(m * nch, 256), 256, 0, st>>>(s->taps, d_bits, nullptr, bits_stride,
-                                                                  m, dly, out, s->row, nch);
+        decim_bits_kernel<<<nb(m * nch, 256), 256, 0, st>>>(s->nz, s->d_lut, s->taps.h[kDecTaps / 2], d_bits,
+                                                            bits_stride, m, dly, out, s->row, nch);
         decim_dly_kernel<true><<<nch, 64, 0, st>>>(d_bits, nullptr, bits_stride, 2 * m, dly, nch);
       } else {
-        decim_stage_kernel<false><<<nb(m * nch, 256), 256, 0, st>>>(s->taps, nullptr, in, s->row,
-                                                                   m, dly, out, s->row, nch);
+        decim_stage_kernel<<<nb(m * nch, 256), 256, 0, st>>>(s->nz, in, s->row, m, dly, out, s->row,
+                                                             nch);
         decim_dly_kernel<false><<<nch, 64, 0, st>>>(nullptr, in, s->row, 2 * m, dly, nch);
       }
       c->launches += 2;
