@@ -202,3 +202,18 @@ def test_small_k_streaming_channels_and_drain(oracle, K, depth, lat, lim):
         assert (q["num_cands"], q["total_children"], q["next_filter_drops"], q["conv_fail"]) == \
             (info["num_cands"], info["total_children"], info["next_filter_drops"], info["conv_fail"])
         np.testing.assert_array_equal(q["best_state"], refs[c].best_state())
+
+
+def test_small_k_many_jobs_take_the_per_thread_kernel(oracle):
+    """More K <= 2 jobs than the lane-split kernel keeps resident (2,600
+    channels of one launch) run one job per thread; every channel equals the
+    oracle."""
+    f = _ntf("clans-6", 5644800)
+    nch, n = 2600, 300
+    rng = np.random.default_rng(77)
+    x = (rng.standard_normal((nch, n)) * 0.25).astype(np.float64)
+    g = _gpu_sdm(f, 4, 2, 16, 0.0, nctx=nch)
+    got = g.process_block(torch.from_numpy(x).cuda())
+    for c in range(0, nch, 97):
+        ref = _ora(oracle, f, 4, 2, 16)
+        np.testing.assert_array_equal(got[c].cpu().numpy(), oracle.sdm_bits(ref, x[c]))
