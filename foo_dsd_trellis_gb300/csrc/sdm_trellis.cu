@@ -41,8 +41,13 @@ constexpr unsigned kFull = 0xffffffffu;
 __device__ __forceinline__ long long key_of(double c) { return __double_as_longlong(c); }
 
 __device__ __forceinline__ double clampd(double v, double lim) {
-  if (v > lim) return lim;
-  if (v < -lim) return -lim;
+  // the reference's limiter (if v > lim: lim; else if v < -lim: -lim) for a
+  // positive finite lim, on the integer pipe: magnitudes of doubles order like
+  // their bit patterns; NaN (magnitude above +inf's) passes through as in C
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
+  const unsigned long long lb = (unsigned long long)__double_as_longlong(lim);
+  if (mag > lb && mag <= 0x7FF0000000000000ull) return __longlong_as_double((long long)((b & 0x8000000000000000ull) | lb));
   return v;
 }
 
