@@ -392,6 +392,140 @@ adj_full_kernel(LoopCoef C, const double* __restrict__ u, const uint8_t* __restr
   }
 }
 
+// ---- the adjoint scans with one state component per lane ----------------
+//
+// An FP64 instruction costs this part's FP64 unit about the same for one
+// active lane as for 32, so the serial chain of a scan item is its count of
+// FP64 instructions.  These forms give each (clip, block) item a group of G
+// lanes, lane k owning component k of the state and of the adjoint: the
+// per-component operations of loop_d, the adjoint products and loop_mt run
+// once for all k (neighbours by shuffles), with the same operations per
+// component as the one-thread forms above, so the results are the same.
+template <int G>
+struct Lane {
+  int k;
+  unsigned hm;
+};
+
+template <int N, int G>
+__device__ __forceinline__ double loop_d_lane(const LoopCoef& C, const Lane<G>& L, double gk,
+                                              double s, double x) {
+  const double s_prev = __shfl_up_sync(L.hm, s, 1, G);
+  const double s_next = __shfl_down_sync(L.hm, s, 1, G);
+  const double m = __dmul_rn(gk, s_next);
+  const double u = __dadd_rn(s, L.k == 0 ? -m : s_prev);
+  return __dadd_rn(u, L.k == 0 ? x : (L.k < N - 1 ? -m : -0.0));
+}
+
+// mu_j = db_j + db_{j+1} - g_{j-1} db_{j-1} (loop_mt, one component per lane)
+template <int N, int G>
+__device__ __forceinline__ double loop_mt_lane(const Lane<G>& L, double gkm1, double db) {
+  const double dn = __shfl_down_sync(L.hm, db, 1, G);
+  const double dp = __shfl_up_sync(L.hm, db, 1, G);
+  double m = db;
+  if (L.k + 1 < N) m += dn;
+  if (L.k >= 1) m -= gkm1 * dp;
+  return m;
+}
+
+template <int G>
+__device__ __forceinline__ bool lane_setup(Lane<G>& L, long long& item) {
+  const int wl = threadIdx.x & 31;
+  L.k = wl & (G - 1);
+  L.hm = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (wl - L.k));
+  item = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  return true;
+}
+
+template <int N, int G>
+__global__ void adj_local_lane_kernel(LoopCoef C, const double* __restrict__ z,
+                                      const double* __restrict__ h, LossShape S, long long n, int Lb,
+                                      int nb, int nclips, double* __restrict__ loc) {
+  Lane<G> L;
+  long long item;
+  lane_setup<G>(L, item);
+  if (item >= (long long)nclips * nb) return;          // whole groups leave together
+  const int c = (int)(item / nb), b = (int)(item % nb);
+  const double* zc = z + (size_t)c * S.M;
+  const int k = L.k;
+  const double ak = k < N ? C.a[k] : 0.0;
+  const double gkm1 = (k >= 1 && k <= N) ? C.g[k - 1] : 0.0;
+  double mu = 0.0;
+  for (int t = Lb - 1; t >= 0; t--) {
+    const double lam = lam_at(zc, h, S, (long long)b * Lb + t);
+    const double mu0 = __shfl_sync(L.hm, mu, 0, G);
+    const double vb = C.kappa * (lam - mu0);
+    const double db = mu + vb * ak;
+    mu = loop_mt_lane<N, G>(L, gkm1, db);
+  }
+  if (k < N) loc[(size_t)item * N + k] = mu;
+}
+
+template <int N, int G>
+__global__ void __launch_bounds__(kScanThreads)
+adj_full_lane_kernel(LoopCoef C, const double* __restrict__ u, const uint8_t* __restrict__ bits,
+                     const double* __restrict__ z, const double* __restrict__ h, LossShape S,
+                     long long n, int Lb, int nb, int nclips, const double* __restrict__ starts,
+                     const double* __restrict__ cin, double* __restrict__ scr,
+                     double* __restrict__ ubar, double* __restrict__ gpart) {
+  Lane<G> L;
+  long long item;
+  lane_setup<G>(L, item);
+  if (item >= (long long)nclips * nb) return;
+  const int c = (int)(item / nb), b = (int)(item % nb);
+  const size_t base = (size_t)c * n + (size_t)b * Lb;
+  const double* zc = z + (size_t)c * S.M;
+  const int nsub = Lb / kSubLen;
+  const int k = L.k;
+  const bool own = k < N;
+  const double gk = own ? C.g[k] : 0.0;
+  const double ak = own ? C.a[k] : 0.0;
+  const double gkm1 = (k >= 1 && k <= N) ? C.g[k - 1] : 0.0;
+  // the item's scratch: the state entering each sub-block, then the states
+  // entering each sample of the sub-block being reversed (component k at k)
+  double* sub = scr + (size_t)item * (nsub + kSubLen) * N;
+  double* st = sub + (size_t)nsub * N;
+  double s = own ? starts[(size_t)item * N + k] : 0.0;
+  for (int j = 0; j < nsub; j++) {
+    if (own) sub[j * N + k] = s;
+    for (int q = 0; q < kSubLen; q++) {
+      const size_t t = base + (size_t)j * kSubLen + q;
+      s = loop_d_lane<N, G>(C, L, gk, s, u[t]);
+      if (k == 0) s = __dsub_rn(s, bits[t] ? 1.0 : -1.0);
+    }
+  }
+  double mu = own ? cin[(size_t)item * N + k] : 0.0, ga = 0.0, gg = 0.0;
+  for (int j = nsub - 1; j >= 0; j--) {
+    s = own ? sub[j * N + k] : 0.0;
+    for (int q = 0; q < kSubLen; q++) {
+      const size_t t = base + (size_t)j * kSubLen + q;
+      if (own) st[q * N + k] = s;
+      s = loop_d_lane<N, G>(C, L, gk, s, u[t]);
+      if (k == 0) s = __dsub_rn(s, bits[t] ? 1.0 : -1.0);
+    }
+    __syncwarp(L.hm);
+    for (int q = kSubLen - 1; q >= 0; q--) {
+      const size_t t = base + (size_t)j * kSubLen + q;
+      const double sp = own ? st[q * N + k] : 0.0;
+      const double d = loop_d_lane<N, G>(C, L, gk, sp, u[t]);
+      const double lam = lam_at(zc, h, S, (long long)(t - (size_t)c * n));
+      const double mu0 = __shfl_sync(L.hm, mu, 0, G);
+      const double vb = C.kappa * (lam - mu0);
+      const double db = mu + vb * ak;
+      if (k == 0) ubar[t] = db + vb;
+      ga += vb * d;
+      const double sp1 = __shfl_down_sync(L.hm, sp, 1, G);
+      if (k < N - 1) gg -= db * sp1;
+      mu = loop_mt_lane<N, G>(L, gkm1, db);
+    }
+    __syncwarp(L.hm);
+  }
+  if (own) {
+    gpart[(size_t)item * 2 * N + k] = ga;
+    gpart[(size_t)item * 2 * N + N + k] = gg;
+  }
+}
+
 // ---- loss: decimating low-pass of (y - r), block partial sums of z^2 ----
 template <bool kBits>
 __global__ void loss_z_kernel(const uint8_t* __restrict__ bits, const double* __restrict__ yv,
@@ -645,12 +779,15 @@ int launch_scan(const char* which, dsdgpu_diff* D, const LoopCoef& C, const Mat&
     sur_full_kernel<N><<<g, kScanThreads, 0, s>>>(C, u, beta, D->n, Lb, D->nb, D->p.nclips,
                                                   D->d_sstarts, D->d_y);
   } else {
-    adj_local_kernel<N><<<g, kScanThreads, 0, s>>>(C, D->d_z, D->d_h, D->S, D->n, Lb, D->nb,
-                                                   D->p.nclips, D->d_ends);
+    // one state component per lane: G = 8 lanes per item up to order 8
+    constexpr int G = N <= 8 ? 8 : 16;
+    const unsigned gl = grid_of((long long)tot * G, kScanThreads);
+    adj_local_lane_kernel<N, G><<<gl, kScanThreads, 0, s>>>(C, D->d_z, D->d_h, D->S, D->n, Lb,
+                                                           D->nb, D->p.nclips, D->d_ends);
     adj_carry_kernel<N><<<gc, 32, 0, s>>>(carry, D->d_ends, D->nb, D->p.nclips, D->d_cin);
-    adj_full_kernel<N><<<g, kScanThreads, 0, s>>>(C, u, D->d_bits, D->d_z, D->d_h, D->S, D->n, Lb,
-                                                  D->nb, D->p.nclips, D->d_starts, D->d_cin,
-                                                  D->d_scr, D->d_ubar, D->d_gpart);
+    adj_full_lane_kernel<N, G><<<gl, kScanThreads, 0, s>>>(C, u, D->d_bits, D->d_z, D->d_h, D->S,
+                                                          D->n, Lb, D->nb, D->p.nclips, D->d_starts,
+                                                          D->d_cin, D->d_scr, D->d_ubar, D->d_gpart);
   }
   D->c->launches += 3;
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
