@@ -139,85 +139,6 @@ __global__ void fwd_carry_kernel(Mat Q, const double* __restrict__ ends, int nb,
   }
 }
 
-// base trajectory, serial per clip in the reference's operation order: the
-// loop without quantiser feedback is slightly unstable (the delayed
-// resonators have |eigenvalue| > 1), so only the exact operation sequence of
-// the trellis reproduces its bounded states; a reordered evaluation would
-// amplify rounding.  Writes the checkpoints, beta_t = y^_t - kappa v^_t and
-// the largest |state| seen (a sanity bound the host checks).
-//
-// One clip per CTA (its first thread), so every clip has an SM's FP64 unit to
-// itself; inputs and decisions are loaded 16 samples ahead, and the |state|
-// maximum is taken on the integer pipe (magnitudes of doubles order like their
-// bit patterns; a NaN state reads as above every bound).
-constexpr int kBaseAhead = 16;
-
-template <int N>
-__global__ void __launch_bounds__(32) base_serial_kernel(LoopCoef C, const double* __restrict__ u,
-                                                         const uint8_t* __restrict__ bits,
-                                                         long long n, int Lb, int nclips,
-                                                         double* __restrict__ starts,
-                                                         double* __restrict__ beta,
-                                                         double* __restrict__ smax) {
-  const int c = blockIdx.x;
-  if (c >= nclips || threadIdx.x != 0) return;
-  const size_t base = (size_t)c * n;
-  const int nb = (int)(n / Lb);
-  const double* uc = u + base;
-  const uint8_t* bc = bits + base;
-  double s[N], d[N];
-#pragma unroll
-  for (int k = 0; k < N; k++) s[k] = 0.0;
-  unsigned long long mx = 0;
-  double xa[kBaseAhead];
-  uint8_t ya[kBaseAhead];
-#pragma unroll
-  for (int j = 0; j < kBaseAhead; j++) {
-    xa[j] = j < n ? uc[j] : 0.0;
-    ya[j] = j < n ? bc[j] : 0;
-  }
-  for (long long t0 = 0; t0 < n; t0 += kBaseAhead) {
-    double xb[kBaseAhead];
-    uint8_t yb[kBaseAhead];
-#pragma unroll
-    for (int j = 0; j < kBaseAhead; j++) {
-      const long long i = t0 + kBaseAhead + j;
-      xb[j] = i < n ? uc[i] : 0.0;
-      yb[j] = i < n ? bc[i] : 0;
-    }
-#pragma unroll
-    for (int j = 0; j < kBaseAhead; j++) {
-      const long long t = t0 + j;
-      if (t < n) {
-        if ((t & (Lb - 1)) == 0) {
-          const size_t o = ((size_t)c * nb + (size_t)(t / Lb)) * N;
-#pragma unroll
-          for (int k = 0; k < N; k++) starts[o + k] = s[k];
-        }
-        const double x = xa[j];
-        loop_d<N>(C, s, x, d);
-        const double v = loop_v<N>(C, x, d);
-        const double yt = ya[j] ? 1.0 : -1.0;
-        beta[base + t] = yt - C.kappa * v;
-#pragma unroll
-        for (int k = 0; k < N; k++) s[k] = d[k];
-        s[0] = __dsub_rn(s[0], yt);
-#pragma unroll
-        for (int k = 0; k < N; k++) {
-          const unsigned long long m = (unsigned long long)__double_as_longlong(s[k]) & 0x7FFFFFFFFFFFFFFFull;
-          mx = m > mx ? m : mx;
-        }
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < kBaseAhead; j++) {
-      xa[j] = xb[j];
-      ya[j] = yb[j];
-    }
-  }
-  smax[c] = __longlong_as_double((long long)mx);
-}
-
 // surrogate (closed loop), block-local from zero state: end states
 template <int N>
 __global__ void sur_local_kernel(LoopCoef C, const double* __restrict__ u,
@@ -526,6 +447,62 @@ adj_full_lane_kernel(LoopCoef C, const double* __restrict__ u, const uint8_t* __
   }
 }
 
+// base trajectory, serial per clip in the reference's operation order: the
+// loop without quantiser feedback is slightly unstable (the delayed
+// resonators have |eigenvalue| > 1), so only the exact operation sequence of
+// the trellis reproduces its bounded states; a reordered evaluation would
+// amplify rounding.  Writes the checkpoints, beta_t = y^_t - kappa v^_t and
+// the largest |state| seen (a sanity bound the host checks).
+//
+// The |state| maximum is taken on the integer pipe (magnitudes of doubles
+// order like their bit patterns; a NaN state reads as above every bound).
+//
+// One clip per group of G lanes, one state component per lane (the same
+// operations per component as the reference's loop; v's sum stays left to
+// right on the gathered products).
+template <int N, int G>
+__global__ void base_lane_kernel(LoopCoef C, const double* __restrict__ u,
+                                 const uint8_t* __restrict__ bits, long long n, int Lb, int nclips,
+                                 double* __restrict__ starts, double* __restrict__ beta,
+                                 double* __restrict__ smax) {
+  Lane<G> L;
+  long long item;
+  lane_setup<G>(L, item);
+  if (item >= nclips) return;
+  const int c = (int)item, k = L.k;
+  const bool own = k < N;
+  const double gk = own ? C.g[k] : 0.0;
+  const double ak = own ? C.a[k] : 0.0;
+  const size_t base = (size_t)c * n;
+  const int nb = (int)(n / Lb);
+  const double* uc = u + base;
+  const uint8_t* bc = bits + base;
+  double s = 0.0;
+  unsigned long long mx = 0;
+  for (long long t = 0; t < n; t++) {
+    if ((t & (Lb - 1)) == 0 && own) starts[((size_t)c * nb + (size_t)(t / Lb)) * N + k] = s;
+    const double x = __ldg(uc + t);
+    const double d = loop_d_lane<N, G>(C, L, gk, s, x);
+    const double p = __dmul_rn(ak, d);
+    double v = __dadd_rn(x, __shfl_sync(L.hm, p, 0, G));
+#pragma unroll
+    for (int j = 1; j < N; j++) v = __dadd_rn(v, __shfl_sync(L.hm, p, j, G));
+    const double yt = __ldg(bc + t) ? 1.0 : -1.0;
+    if (k == 0) beta[base + t] = yt - C.kappa * v;
+    s = k == 0 ? __dsub_rn(d, yt) : d;
+    if (own) {
+      const unsigned long long m = (unsigned long long)__double_as_longlong(s) & 0x7FFFFFFFFFFFFFFFull;
+      mx = m > mx ? m : mx;
+    }
+  }
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) {
+    const unsigned long long other = __shfl_down_sync(L.hm, mx, o, G);
+    mx = other > mx ? other : mx;
+  }
+  if (k == 0) smax[c] = __longlong_as_double((long long)mx);
+}
+
 // ---- loss: decimating low-pass of (y - r), block partial sums of z^2 ----
 template <bool kBits>
 __global__ void loss_z_kernel(const uint8_t* __restrict__ bits, const double* __restrict__ yv,
@@ -770,8 +747,10 @@ int launch_scan(const char* which, dsdgpu_diff* D, const LoopCoef& C, const Mat&
   cudaStream_t s = D->c->stream;
   const int Lb = D->p.checkpoint;
   if (!strcmp(which, "base")) {
-    base_serial_kernel<N><<<D->p.nclips, 32, 0, s>>>(C, u, D->d_bits, D->n, Lb, D->p.nclips,
-                                                     D->d_starts, D->d_beta, D->d_smax);
+    // one clip per warp, one state component per lane
+    constexpr int GB = N <= 8 ? 8 : 16;
+    base_lane_kernel<N, GB><<<D->p.nclips, GB, 0, s>>>(C, u, D->d_bits, D->n, Lb, D->p.nclips,
+                                                       D->d_starts, D->d_beta, D->d_smax);
     D->c->launches -= 2;
   } else if (!strcmp(which, "sur")) {
     sur_local_kernel<N><<<g, kScanThreads, 0, s>>>(C, u, beta, D->n, Lb, D->nb, D->p.nclips, D->d_ends);
