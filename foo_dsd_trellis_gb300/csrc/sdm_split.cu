@@ -1,4 +1,6 @@
-// Trellis SDM for K <= 2 with each candidate's NTF advance split over lanes.
+// Trellis SDM for K <= 4 with each candidate's NTF advance split over lanes
+// (K <= 2: the engine's path-table default; K = 4: its default for paths the
+// table does not list, include/dsd_types.h:479-481).
 //
 // An FP64 instruction occupies this part's FP64 unit for ~64 cycles per warp,
 // dependent or not and whatever the number of active lanes, so the latency of
@@ -16,14 +18,15 @@
 // adding -0.0 leaves any value unchanged).  Only v = ((x + p_0) + p_1) + ...
 // stays serial (N adds, the products gathered by shuffles).  A step is then
 // about N + 9 FP64 instructions instead of 5N + 6.  Lanes q and q+1 of a
-// candidate form its two children's costs; the selection of at most 4
-// children runs redundantly in every lane of the job (the act list in two
+// candidate form its two children's costs; the selection of at most 8
+// children runs redundantly in every lane of the job (the act list in KC
 // registers, the dedup hash a scan of the children hashed this sample); the
 // survivors pull state components, ring words and bits from their parent's
 // lanes.  Reference: src/trellis.c:868-973 (step), :621-731 (selection).
 //
-// Layout: a job is G = 2H lanes (H = 8 for N <= 8, 16 for N <= 10), 32 / G jobs
-// per warp; candidate c owns lanes [c H, c H + H), lane q < N holds s_q, lane
+// Layout: a job is G = KC H lanes (KC = 2 candidate slots for K <= 2, 4 for
+// K <= 4; H = 8 for N <= 8, 16 above), 32 / G jobs per warp; candidate c owns
+// lanes [c H, c H + H), lane q < N holds s_q, lane
 // q < W ring word q; cost, path and next are held by every lane of the
 // candidate.  The context format is SdmCtx's, as for the other kernels.
 #include "sdm_internal.h"
@@ -32,9 +35,15 @@ namespace dsdgpu {
 
 namespace {
 
-template <typename T>
-__device__ __forceinline__ T pick4s(const T (&a)[4], int i) {
-  return i == 0 ? a[0] : i == 1 ? a[1] : i == 2 ? a[2] : a[3];
+// element i of a register array, without dynamic indexing (which would put
+// the array in local memory)
+template <typename T, int M>
+__device__ __forceinline__ T pickn(const T (&a)[M], int i) {
+  T r = a[0];
+#pragma unroll
+  for (int j = 1; j < M; j++)
+    if (i == j) r = a[j];
+  return r;
 }
 
 __device__ __forceinline__ double clampd_l(double v, double lim) {
@@ -48,10 +57,11 @@ __device__ __forceinline__ double clampd_l(double v, double lim) {
   return v;
 }
 
-template <int N, int H>
+template <int N, int H, int KC>
 __global__ void __launch_bounds__(32) sdm_split_kernel(SdmParams P, const SdmJob* __restrict__ jobs,
                                                       int njobs, SdmCtx* __restrict__ ctxs) {
-  constexpr int G = 2 * H;
+  constexpr int G = KC * H;        // KC candidate slots of H lanes
+  constexpr int NC = 2 * KC;       // children
   const int wl = threadIdx.x & 31;
   const int jl = wl & (G - 1);                 // lane within the job
   const unsigned sh = (unsigned)(wl - jl);
@@ -127,15 +137,15 @@ __global__ void __launch_bounds__(32) sdm_split_kernel(SdmParams P, const SdmJob
     const int newnext = (int)((wn >> (next_pos & 31)) & 1u);
 
     // ---- selection over the children, in every lane of the job ----
-    double ccost[4];
-    long long ckeyv[4];
-    int cnext[4];
-    unsigned long long cpath[4];
-    int nnext[2];
+    double ccost[NC];
+    long long ckeyv[NC];
+    int cnext[NC];
+    unsigned long long cpath[NC];
+    int nnext[KC];
 #pragma unroll
-    for (int ch = 0; ch < 4; ch++) ccost[ch] = __shfl_sync(hm, kc, (ch >> 1) * H + (ch & 1), G);
+    for (int ch = 0; ch < NC; ch++) ccost[ch] = __shfl_sync(hm, kc, (ch >> 1) * H + (ch & 1), G);
 #pragma unroll
-    for (int c = 0; c < 2; c++) {
+    for (int c = 0; c < KC; c++) {
       const int nx = __shfl_sync(hm, next, c * H, G);
       const unsigned long long pth =
           (unsigned long long)__shfl_sync(hm, (long long)path, c * H, G);
@@ -147,34 +157,40 @@ __global__ void __launch_bounds__(32) sdm_split_kernel(SdmParams P, const SdmJob
       }
     }
 #pragma unroll
-    for (int ch = 0; ch < 4; ch++) ckeyv[ch] = __double_as_longlong(ccost[ch]);
+    for (int ch = 0; ch < NC; ch++) ckeyv[ch] = __double_as_longlong(ccost[ch]);
     const int nchild = 2 * n;
     c_tot += (unsigned long long)nchild;
     int mn = 0, votes1 = 0;
 #pragma unroll
-    for (int ch = 0; ch < 4; ch++)
+    for (int ch = 0; ch < NC; ch++)
       if (ch < nchild) {
-        if (ckeyv[ch] < pick4s(ckeyv, mn)) mn = ch;
+        if (ckeyv[ch] < pickn(ckeyv, mn)) mn = ch;
         votes1 += cnext[ch] & 1;
       }
     const int majority = (votes1 > nchild - votes1) ? 1 : 0;
-    if (pick4s(cnext, mn) != majority) {
+    if (pickn(cnext, mn) != majority) {
       int bm = -1;
 #pragma unroll
-      for (int ch = 0; ch < 4; ch++)
-        if (ch < nchild && cnext[ch] == majority && (bm < 0 || ckeyv[ch] < pick4s(ckeyv, bm)))
+      for (int ch = 0; ch < NC; ch++)
+        if (ch < nchild && cnext[ch] == majority && (bm < 0 || ckeyv[ch] < pickn(ckeyv, bm)))
           bm = ch;
-      if (bm >= 0 && pick4s(ccost, bm) < __dmul_rn(pick4s(ccost, mn), 1.1)) mn = bm;
+      if (bm >= 0 && pickn(ccost, bm) < __dmul_rn(pickn(ccost, mn), 1.1)) mn = bm;
     }
-    const int want = pick4s(cnext, mn);
-    int act0 = 0, act1 = 0, na = 0;
+    const int want = pickn(cnext, mn);
+    // the act list: na child indices sorted by cost key, equal keys in
+    // insertion order; inserting after every entry with key <= ks is the
+    // reference's backwards shift, and a full list (K) drops its last entry
+    int act[KC];
+#pragma unroll
+    for (int i = 0; i < KC; i++) act[i] = 0;
+    int na = 0;
     unsigned hashed = 0;
 #pragma unroll
-    for (int ch = 0; ch < 4; ch++) {
+    for (int ch = 0; ch < NC; ch++) {
       if (ch >= nchild) continue;
       if (cnext[ch] != want) { c_drop++; continue; }
       const long long ks = ckeyv[ch];
-      if (na == K && pick4s(ckeyv, na == 2 ? act1 : act0) <= ks) continue;
+      if (na == K && pickn(ckeyv, pickn(act, na - 1)) <= ks) continue;
       int tfound = -1;
 #pragma unroll
       for (int h = 0; h < ch; h++)
@@ -182,27 +198,39 @@ __global__ void __launch_bounds__(32) sdm_split_kernel(SdmParams P, const SdmJob
       if (tfound < 0) {
         hashed |= 1u << ch;
       } else {
-        if (pick4s(ckeyv, tfound) <= ks) continue;
-        if (na >= 1 && act0 == tfound) { act0 = act1; na--; }
-        else if (na == 2 && act1 == tfound) { na--; }
+        if (pickn(ckeyv, tfound) <= ks) continue;
+        // t still in the act list: take it out
+        int tp = KC;
+#pragma unroll
+        for (int i = KC - 1; i >= 0; i--)
+          if (i < na && act[i] == tfound) tp = i;
+        if (tp < KC) {
+#pragma unroll
+          for (int i = 0; i < KC - 1; i++)
+            if (i >= tp) act[i] = act[i + 1];
+          na--;
+        }
       }
-      if (na == 0) {
-        act0 = ch;
-      } else if (na == 1) {
-        if (pick4s(ckeyv, act0) <= ks) { if (K >= 2) act1 = ch; }
-        else { if (K >= 2) act1 = act0; act0 = ch; }
-      } else {
-        if (pick4s(ckeyv, act0) <= ks) act1 = ch;
-        else { act1 = act0; act0 = ch; }
+      int jpos = 0;   // entries with key <= ks (a prefix: the list is sorted)
+#pragma unroll
+      for (int i = 0; i < KC; i++)
+        if (i < na && pickn(ckeyv, act[i]) <= ks) jpos++;
+      if (jpos < K) {
+#pragma unroll
+        for (int i = KC - 1; i >= 1; i--)
+          if (i > jpos) act[i] = act[i - 1];
+#pragma unroll
+        for (int i = 0; i < KC; i++)
+          if (i == jpos) act[i] = ch;
       }
       if (na < K) na++;
     }
     const int n_new = na;
 
     // ---- commit: the lanes of candidate slot `cand` take survivor `cand` ----
-    const double min_cost = pick4s(ccost, act0);
+    const double min_cost = pickn(ccost, act[0]);
     const bool live = cand < n_new;
-    const int ch = cand == 0 ? act0 : act1;
+    const int ch = pickn(act, cand);
     const int par = live ? (ch >> 1) : 0;
     const int b = live ? (ch & 1) : 0;
     const double dpar = __shfl_sync(hm, d, par * H + q, G);
@@ -210,9 +238,9 @@ __global__ void __launch_bounds__(32) sdm_split_kernel(SdmParams P, const SdmJob
     double snew = q == 0 ? __dadd_rn(dpar, b ? -1.0 : 1.0) : dpar;
     if (lim_on) snew = clampd_l(snew, lim);
     sq = q < N ? snew : 0.0;
-    cost = live ? __dsub_rn(pick4s(ccost, ch), min_cost) : 0.0;
-    path = live ? pick4s(cpath, ch) : 0ull;
-    next = par ? nnext[1] : nnext[0];
+    cost = live ? __dsub_rn(pickn(ccost, ch), min_cost) : 0.0;
+    path = live ? pickn(cpath, ch) : 0ull;
+    next = pickn(nnext, par);
     ringw = (q == (pos >> 5)) ? ((rpar & ~(1u << (pos & 31))) | ((uint32_t)b << (pos & 31))) : rpar;
     if (n_new < n) { c_conv++; c_coll++; }
     n = n_new;
@@ -251,14 +279,14 @@ __global__ void __launch_bounds__(32) sdm_split_kernel(SdmParams P, const SdmJob
   }
 }
 
-template <int H>
-int launch_split_h(const SdmParams& P, const SdmJob* d_jobs, int njobs, SdmCtx* d_ctxs,
-                   cudaStream_t stream) {
-  const int jpw = 32 / (2 * H);
+template <int H, int KC>
+int launch_split(const SdmParams& P, const SdmJob* d_jobs, int njobs, SdmCtx* d_ctxs,
+                 cudaStream_t stream) {
+  const int jpw = 32 / (KC * H);
   const dim3 grid((njobs + jpw - 1) / jpw), block(32);
   switch (P.order) {
 #define DSD_CASE(NN) \
-  case NN: sdm_split_kernel<NN, H><<<grid, block, 0, stream>>>(P, d_jobs, njobs, d_ctxs); break;
+  case NN: sdm_split_kernel<NN, H, KC><<<grid, block, 0, stream>>>(P, d_jobs, njobs, d_ctxs); break;
     DSD_CASE(2) DSD_CASE(3) DSD_CASE(4) DSD_CASE(5) DSD_CASE(6) DSD_CASE(7) DSD_CASE(8)
 #undef DSD_CASE
     default: return -1;
@@ -268,22 +296,30 @@ int launch_split_h(const SdmParams& P, const SdmJob* d_jobs, int njobs, SdmCtx* 
 
 }  // namespace
 
-// Jobs per warp of the split kernel for this order: 2 (16 lanes) up to
-// order 8, else 1 (32 lanes).
-int sdm_split_jobs_per_warp(const SdmParams& P) { return P.order <= 8 ? 2 : 1; }
+// The split kernel takes K <= 2 at any order (2 slots of 8 lanes up to order
+// 8, of 16 lanes above) and K = 3, 4 up to order 8 (4 slots of 8 lanes).
+bool sdm_split_supported(const SdmParams& P) {
+  return P.cands <= 2 || (P.cands <= 4 && P.order <= 8);
+}
+
+// Jobs per warp of the split kernel for these parameters.
+int sdm_split_jobs_per_warp(const SdmParams& P) {
+  return (P.cands <= 2 && P.order <= 8) ? 2 : 1;
+}
 
 int launch_sdm_split(const SdmParams& P, const SdmJob* d_jobs, int njobs, SdmCtx* d_ctxs,
                      cudaStream_t stream) {
   if (njobs <= 0) return 0;
-  int rc;
-  if (P.order <= 8) {
-    rc = launch_split_h<8>(P, d_jobs, njobs, d_ctxs, stream);
-  } else {
-    const int jpw = 1;
-    const dim3 grid((njobs + jpw - 1) / jpw), block(32);
+  int rc = -1;
+  if (P.cands <= 2 && P.order <= 8) {
+    rc = launch_split<8, 2>(P, d_jobs, njobs, d_ctxs, stream);
+  } else if (P.cands <= 4 && P.order <= 8) {
+    rc = launch_split<8, 4>(P, d_jobs, njobs, d_ctxs, stream);
+  } else if (P.cands <= 2) {
+    const dim3 grid(njobs), block(32);
     switch (P.order) {
-      case 9: sdm_split_kernel<9, 16><<<grid, block, 0, stream>>>(P, d_jobs, njobs, d_ctxs); rc = 0; break;
-      case 10: sdm_split_kernel<10, 16><<<grid, block, 0, stream>>>(P, d_jobs, njobs, d_ctxs); rc = 0; break;
+      case 9: sdm_split_kernel<9, 16, 2><<<grid, block, 0, stream>>>(P, d_jobs, njobs, d_ctxs); rc = 0; break;
+      case 10: sdm_split_kernel<10, 16, 2><<<grid, block, 0, stream>>>(P, d_jobs, njobs, d_ctxs); rc = 0; break;
       default: rc = -1;
     }
   }

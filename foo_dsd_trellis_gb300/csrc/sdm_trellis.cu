@@ -734,22 +734,25 @@ bool sdm_scalar_eligible(const SdmParams& P, int max_blocks);   // sdm_scalar.cu
 int launch_sdm_scalar(const SdmParams& P, const SdmJob* d_jobs, int njobs, SdmCtx* d_ctxs,
                       cudaStream_t stream);
 int sdm_split_jobs_per_warp(const SdmParams& P);                 // sdm_split.cu
+bool sdm_split_supported(const SdmParams& P);
 int launch_sdm_split(const SdmParams& P, const SdmJob* d_jobs, int njobs, SdmCtx* d_ctxs,
                      cudaStream_t stream);
 
 // Host-side launcher: each warp-sized CTA runs 32 / LPJ jobs side by side
-// (lanes_per_job); max_blocks caps the CTAs.  Uncapped launches at K <= 2
-// take the small-trellis kernels: while the jobs fit in two warps per
+// (lanes_per_job); max_blocks caps the CTAs.  Uncapped launches of small
+// trellises take their own kernels: while the jobs fit in two warps per
 // scheduler, each candidate's NTF advance spread over lanes (sdm_split.cu,
-// the shortest step); beyond that one job per thread (sdm_scalar.cu, the
-// fewest FP64 instructions per job).
+// K <= 2, or K <= 4 up to order 8: the shortest step); beyond that, at
+// K <= 2, one job per thread (sdm_scalar.cu, the fewest FP64 instructions per
+// job).
 int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_counter,
                     SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream) {
   if (njobs <= 0) return 0;
-  if (sdm_scalar_eligible(P, max_blocks)) {
+  if (P.lanes == 0 && max_blocks == 0 && P.lat <= 32 * kRegRingWords) {
     const long long split_cap = (long long)sdm_split_jobs_per_warp(P) * 2 * 4 * (resident_warps() / 16);
-    if (njobs <= split_cap) return launch_sdm_split(P, d_jobs, njobs, d_ctxs, stream);
-    return launch_sdm_scalar(P, d_jobs, njobs, d_ctxs, stream);
+    if (sdm_split_supported(P) && njobs <= split_cap)
+      return launch_sdm_split(P, d_jobs, njobs, d_ctxs, stream);
+    if (sdm_scalar_eligible(P, max_blocks)) return launch_sdm_scalar(P, d_jobs, njobs, d_ctxs, stream);
   }
   const int lanes = launch_lanes(P, njobs, max_blocks);
   const int jpc = 32 / lanes;

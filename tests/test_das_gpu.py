@@ -69,7 +69,7 @@ def test_das_single_segment_is_plain_sdm(oracle):
     assert np.array_equal(want[0], plain)
 
 
-@pytest.mark.parametrize("K,depth", [(2, 4), (5, 8), (12, 16)])
+@pytest.mark.parametrize("K,depth", [(2, 4), (4, 8), (5, 8), (12, 16)])
 def test_lanes_per_job_do_not_change_results(oracle, K, depth):
     """Every width of the job packing (2 .. 32 lanes, 16 .. 1 jobs per warp,
     and the automatic choice) gives the oracle's DAS output: small K with a

@@ -181,11 +181,13 @@ def test_exact_and_fast_modes_agree(oracle):
     assert np.array_equal(outs[0], outs[1])
 
 
-@pytest.mark.parametrize("K,depth,lat,lim", [(2, 4, 128, 0.0), (1, 8, 32, 0.0), (2, 2, 200, 3.0)])
+@pytest.mark.parametrize("K,depth,lat,lim", [(2, 4, 128, 0.0), (1, 8, 32, 0.0), (2, 2, 200, 3.0),
+                                             (4, 8, 32, 0.0), (3, 6, 64, 2.0), (4, 3, 100, 0.0)])
 def test_small_k_streaming_channels_and_drain(oracle, K, depth, lat, lim):
-    """K <= 2 runs one job per thread: streamed blocks over several channels,
-    short path masks (dedup on most samples), the limiter and the drain,
-    against the oracle."""
+    """Small trellises (K <= 4, including the reference's default K = 4,
+    depth 8, lat 32) take the lane-split kernel: streamed blocks over several
+    channels, short path masks (dedup on most samples), the limiter and the
+    drain, against the oracle."""
     f = _ntf("clans-6", 5644800)
     nch = 5
     x = np.stack([multitone(12000, seed=40 + c) * (0.6 + 0.1 * c) for c in range(nch)])
