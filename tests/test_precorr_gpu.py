@@ -96,3 +96,23 @@ def test_pipeline_precorr_mode(oracle):
         y = fir[c]
         want = oracle.PreCorr(f.order, np.array(f.a), np.array(f.g), 12.0).process(y)
         assert np.array_equal(got[c], want), c
+
+
+@pytest.mark.parametrize("order", [2, 3, 4, 9, 10])
+def test_precorr_orders(oracle, order):
+    """PreCorr at orders outside the NTF table (a real NTF truncated to order
+    2, 3 or zero-padded to 9, 10, which keeps the loop bounded): table and
+    decisions equal the restatement."""
+    from foo_dsd_trellis_gb300 import ntf
+    from foo_dsd_trellis_gb300.precorr import PreCorr
+    f = ntf.get_filter("clans-4", 2822400) if order <= 4 else ntf.get_filter("clans-8", 11289600)
+    a, g = np.zeros(order), np.zeros(order)
+    m = min(order, f.order)
+    a[:m], g[:m] = np.array(f.a[:m]), np.array(f.g[:m])
+    gpu = PreCorr(order, a, g, 5.0, num_channels=2)
+    ref = [oracle.PreCorr(order, a, g, 5.0) for _ in range(2)]
+    assert np.array_equal(gpu.table().view(np.uint32), ref[0].table().view(np.uint32))
+    x = np.stack([0.4 * multitone(20000, 50 + order), 0.3 * multitone(20000, 60 + order)])
+    got = gpu.process_block(torch.from_numpy(x).cuda()).cpu().numpy()
+    for c in range(2):
+        assert np.array_equal(got[c], ref[c].process(x[c]))

@@ -219,3 +219,26 @@ def test_small_k_many_jobs_take_the_per_thread_kernel(oracle):
     for c in range(0, nch, 97):
         ref = _ora(oracle, f, 4, 2, 16)
         np.testing.assert_array_equal(got[c].cpu().numpy(), oracle.sdm_bits(ref, x[c]))
+
+
+@pytest.mark.parametrize("order", [2, 3, 9, 10])
+@pytest.mark.parametrize("K", [2, 8])
+def test_orders_outside_the_table(oracle, order, K):
+    """Orders 2, 3, 9 and 10 (accepted by the ABI, absent from the NTF table;
+    a real NTF truncated or zero-padded), through the small-trellis and warp
+    kernels."""
+    src = _ntf("clans-4", 2822400) if order <= 4 else _ntf("clans-8", 11289600)
+    a, g = np.zeros(order), np.zeros(order)
+    m = min(order, src.order)
+    a[:m], g[:m] = np.array(src.a[:m]), np.array(src.g[:m])
+
+    class F:
+        pass
+    f = F()
+    f.order, f.a, f.g = order, list(a), list(g)
+    x = sdm_input(6000, seed=order * 10 + K, amp=0.3)
+    ref = oracle.sdm(order, a, g, 16, K, 24, 0.0)
+    want = oracle.sdm_bits(ref, x)
+    gpu = _gpu_sdm(f, 16, K, 24)
+    got = gpu.process_block(torch.from_numpy(x).cuda())[0].cpu().numpy()
+    np.testing.assert_array_equal(got, want)
