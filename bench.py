@@ -15,6 +15,12 @@ channels (and x realtime).
 oracle's C port on this host's cores; the reference's own trellis.c is built
 from source only where its tree is present, and never on an aarch64 GPU host)
 on a bounded slice of the same workload.
+
+Other workloads (`--workload`, one JSON line each): multistream64 (64 streams
+in one batched plan), diff16 (the adjoint of the differentiable path),
+dsd512conv6 (DSD512 5.1 with UPOLS room convolution), samerate128 (DoP DSD128
+re-encode on the engine's path-table parameters), dsd2pcm128 (DSD128 -> 44.1
+kHz PCM) and precorr128 (PCM -> DSD128 with the PreCorr SDM).
 """
 from __future__ import annotations
 
