@@ -153,3 +153,19 @@ def test_batch_rejects_bad_streams():
     with pytest.raises(_lib.DsdGpuError) as e:
         BatchPlan([StreamSpec(44100, 5644800, 2, 100000, f)], seg_len=32768, max_device_bytes=1 << 20)
     assert e.value.code == _lib.ERR_TOO_LARGE
+
+
+def test_batch_small_k_path_table_parameters(oracle):
+    """The engine's path-table trellis (K = 2, depth 4) through the batched plan:
+    every stream equals the single-stream path."""
+    from foo_dsd_trellis_gb300.batch import OUT_BITS, BatchPlan
+    specs = _specs(cands=2, depth=4, lat=16)[:4]
+    xs = _inputs(specs)
+    plan = BatchPlan(specs, seg_len=32768, output_format=OUT_BITS)
+    plan.load([torch.from_numpy(x).cuda() for x in xs])
+    plan.run()
+    for i, s in enumerate(specs):
+        want, _ = _oracle_stream(oracle, s, xs[i], 32768, OUT_BITS)
+        got = plan.out_view(i).cpu().numpy()
+        assert got.shape == want.shape and np.array_equal(got, want), f"stream {i}"
+    plan.close()
