@@ -13,7 +13,7 @@
 #include "das_internal.h"
 
 // Validated copy of the ABI's trellis parameters (sdm_context_init's limits,
-// src/trellis.c:977-1011, plus this build's register-ring latency bound).
+// src/trellis.c:977-1011, plus the library's register-ring latency bound).
 int sdm_params_from_abi(const dsdgpu_sdm_params_t* p, dsdgpu::SdmParams* P, const char** err);
 
 namespace dsdgpu {

@@ -149,7 +149,7 @@ int sdm_params_from_abi(const dsdgpu_sdm_params_t* p, dsdgpu::SdmParams* P, cons
   if (p->cands < 1 || p->cands > kMaxCands) { *err = "cands out of range"; return DSDGPU_ERR_ARG; }
   if (p->lat < 1 || p->lat > kMaxLat) { *err = "lat out of range"; return DSDGPU_ERR_ARG; }
   if (p->lat > sdm_max_lat_in_registers()) {
-    *err = "lat above the register-ring limit of this build";
+    *err = "lat above the register-ring limit of this library";
     return DSDGPU_ERR_UNSUPPORTED;
   }
   memset(P, 0, sizeof *P);
