@@ -375,11 +375,17 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     // eligible children keep their (cost, index) order (src/trellis.c:628-652).
     long long sk0 = live ? key0 : LLONG_MAX, sk1 = live ? key1 : LLONG_MAX;
     int si0 = 2 * lane, si1 = 2 * lane + 1;
+    // The shared-part operations ride on the sort stages, except the last
+    // kDeferOps, which are issued at the start of the selection so that its
+    // integer work runs while they occupy the FP64 unit.
+    constexpr int kOps = shared_ops<N>();
+    constexpr int kStages = sort_stages<LPJ>();
+    constexpr int kDeferOps = 8;
+    constexpr int kSortOps = (kOps < kStages ? kOps : kStages) > kDeferOps
+                                 ? (kOps < kStages ? kOps : kStages) - kDeferOps : 0;
     bitonic_sort<LPJ>(sk0, si0, sk1, si1, lane, hm, [&](int st) {
-      if (st < shared_ops<N>()) shared_op<N>(st, P, S, npk, tg, tu);
+      if (st < kSortOps) shared_op<N>(st, P, S, npk, tg, tu);
     });
-#pragma unroll
-    for (int k = sort_stages<LPJ>(); k < shared_ops<N>(); k++) shared_op<N>(k, P, S, npk, tg, tu);
     const int sn0 = __shfl_sync(hm, old_next, si0 >> 1, LPJ);   // traceback bit of each sorted child
     const int sn1 = __shfl_sync(hm, old_next, si1 >> 1, LPJ);
     const bool sl0 = (si0 >> 1) < n, sl1 = (si1 >> 1) < n;
@@ -401,6 +407,8 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
         if (cbm < __dmul_rn(__longlong_as_double(mk), 1.1)) want = majority;
       }
     }
+#pragma unroll
+    for (int k = kSortOps; k < kOps; k++) shared_op<N>(k, P, S, npk, tg, tu);
     unsigned elig = BALLOT(live && old_next == want);
     c_drop += 2ull * (unsigned)(n - __popc(elig));
     c_tot += 2ull * (unsigned)n;
