@@ -12,14 +12,18 @@ DFF name is written raw with a warning), then the SDM over the whole signal
 (trellis: sdm_process_block + sdm_drain, so the output has one decision per
 FIR sample; PreCorr: precorr_process_block) and the output file.
 
+The input is processed in chunks (--chunk, 60 s by default) with the FIR
+history and the SDM state carried, so the device holds one chunk's FIR
+output plus the decisions of the whole file.
+
 Differences, all opt-in except the first:
   * the FIR output reaches the SDM as float64 (the tool hands its float32 FIR
     buffer to sdm_process_block's `const double *`, :464 and :517 — a bug);
   * --keep-channels encodes every channel of a WAV instead of a mono mix;
   * --das SEG_LEN runs the trellis segment-parallel with Density-Aligned
-    Stitching (the plugin's DAS, full-parallel seeding), which is what makes
-    long files fast on the GPU; the sequential trellis is one warp per
-    channel.
+    Stitching (the plugin's DAS, full-parallel seeding, chunk by chunk as the
+    plugin does), which is what makes long files fast on the GPU; the
+    sequential trellis is one serial walk per channel.
 """
 from __future__ import annotations
 
@@ -86,54 +90,84 @@ def encode(args) -> int:
     except _lib.DsdGpuError:
         print(f"FIR chain init failed ({pcm_rate} -> {args.dsd_rate})", file=sys.stderr)
         return 1
-    y = fir.process(torch.from_numpy(pcm).to(dev), args.gain, args.gain)
-    fir.close()
-    n = y.shape[1]
-    if not quiet:
-        print(f"FIR: {n_in} -> {n} samples ({ratio}x)", file=sys.stderr)
+    n = n_in * ratio
+    f = None
+    if args.sdm_out:
+        try:
+            f = select_filter(args.ntf, args.sdm, args.dsd_rate)
+        except KeyError:
+            print(f"NTF filter not found: {args.ntf} @ {args.dsd_rate} Hz", file=sys.stderr)
+            return 1
+    fir_fmt = None
+    fir_acc = []
     if args.fir_out:
-        fmt = _detect(args.fir_out)
-        if fmt in ("dsf", "dff"):
+        fir_fmt = _detect(args.fir_out)
+        if fir_fmt in ("dsf", "dff"):
             print("WARNING: FIR reference is multi-bit, DFF/DSF only store 1-bit. Using raw.",
                   file=sys.stderr)
-            fmt = "raw"
-        _write_float(args.fir_out, y.float().cpu().numpy(), args.dsd_rate, fmt)
+            fir_fmt = "raw"
+    # the SDM runs chunk by chunk with its state carried (PreCorr, sequential
+    # trellis: the same decisions as one pass; DAS: per chunk, as the plugin)
+    sdm = None
+    if f is not None:
+        if args.sdm == "precorr":
+            from .precorr import PreCorr
+            sdm = PreCorr(f.order, f.a, f.g, args.state_limit, num_channels=nch, device=args.device)
+        elif args.das > 0:
+            from .das import DasChannels
+            sdm = DasChannels(f.order, f.a, f.g, args.depth, args.cands, args.lat,
+                              state_limit=args.state_limit, num_channels=nch, device=args.device)
+        else:
+            from .sdm import TrellisSdm
+            sdm = TrellisSdm(f.order, f.a, f.g, args.depth, args.cands, args.lat, args.state_limit,
+                             num_contexts=nch, device=args.device)
+    bits = torch.empty((nch, n), dtype=torch.uint8, device=dev) if sdm is not None else None
+    got = 0
+    step = max(1, int(args.chunk * pcm_rate))
+    for lo in range(0, n_in, step):
+        y = fir.process(torch.from_numpy(np.ascontiguousarray(pcm[:, lo:lo + step])).to(dev),
+                        args.gain, args.gain)
+        if fir_fmt:
+            fir_acc.append(y.float().cpu().numpy())
+        if sdm is None:
+            continue
+        if args.sdm == "precorr":
+            b = sdm.process_block(y)
+        elif args.das > 0:
+            b, _ = sdm.process_chunk(y, seg_len=args.das)
+        else:
+            parts = sdm.process_block(y)
+            b = torch.stack(parts) if parts[0].numel() else None
+        if b is not None and b.shape[1]:
+            bits[:, got:got + b.shape[1]] = b
+            got += b.shape[1]
+    fir.close()
+    if not quiet:
+        print(f"FIR: {n_in} -> {n} samples ({ratio}x)", file=sys.stderr)
+    if fir_fmt:
+        _write_float(args.fir_out, np.concatenate(fir_acc, axis=1), args.dsd_rate, fir_fmt)
         if not quiet:
             print(f"FIR ref: {args.fir_out} ({n} samples)", file=sys.stderr)
-    if not args.sdm_out:
+    if sdm is None:
         return 0
-    try:
-        f = select_filter(args.ntf, args.sdm, args.dsd_rate)
-    except KeyError:
-        print(f"NTF filter not found: {args.ntf} @ {args.dsd_rate} Hz", file=sys.stderr)
-        return 1
     if args.sdm == "precorr":
-        from .precorr import PreCorr
-        pc = PreCorr(f.order, f.a, f.g, args.state_limit, num_channels=nch, device=args.device)
-        bits = pc.process_block(y)
-        pc.close()
         if not quiet:
-            print(f"SDM: PreCorr, NTF={args.ntf}, order={f.order}, {n} samples", file=sys.stderr)
+            print(f"SDM: PreCorr, NTF={args.ntf}, order={f.order}, {got} samples", file=sys.stderr)
     elif args.das > 0:
-        from .das import DasChannels
-        d = DasChannels(f.order, f.a, f.g, args.depth, args.cands, args.lat,
-                        state_limit=args.state_limit, num_channels=nch, device=args.device)
-        bits, _ = d.process_chunk(y, seg_len=args.das)
-        d.close()
         if not quiet:
             print(f"SDM: Trellis DAS, NTF={args.ntf}, depth={args.depth}, cands={args.cands}, "
-                  f"lat={args.lat}, {bits.shape[1]} samples", file=sys.stderr)
+                  f"lat={args.lat}, {got} samples", file=sys.stderr)
     else:
-        from .sdm import TrellisSdm
-        s = TrellisSdm(f.order, f.a, f.g, args.depth, args.cands, args.lat, args.state_limit,
-                       num_contexts=nch, device=args.device)
-        head = s.process_block(y)
-        tail = s.drain(n, 0, nch)
-        s.close()
-        bits = torch.stack([torch.cat([head[c], tail[c]])[:n] for c in range(nch)])
+        # drain the latency (sdm_drain, tools/dsd_encode.c:519-524)
+        tail = sdm.drain(n - got, 0, nch)
+        if tail[0].numel():
+            bits[:, got:got + tail[0].numel()] = torch.stack(tail)
+            got += tail[0].numel()
         if not quiet:
             print(f"SDM: Trellis, NTF={args.ntf}, depth={args.depth}, cands={args.cands}, "
-                  f"lat={args.lat}, {bits.shape[1]} samples", file=sys.stderr)
+                  f"lat={args.lat}, {got} samples", file=sys.stderr)
+    sdm.close()
+    bits = bits[:, :got]
     fmt = _detect(args.sdm_out)
     if fmt in ("dsf", "dff"):
         if nch > 6:
@@ -170,6 +204,8 @@ def parser() -> argparse.ArgumentParser:
                    help="encode every WAV channel instead of a mono mix")
     p.add_argument("--das", type=int, default=0, metavar="SEG_LEN",
                    help="segment-parallel trellis with DAS, segments of SEG_LEN samples")
+    p.add_argument("--chunk", type=float, default=60.0, metavar="SECONDS",
+                   help="input processed in chunks of this length (state carried across)")
     p.add_argument("--device", type=int, default=0)
     return p
 

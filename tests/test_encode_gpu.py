@@ -114,3 +114,17 @@ def test_encode_errors(tmp_path):
     assert encode.main(["--input", str(raw), "--pcm-rate", "44100", "--dsd-rate", "2822401",
                         "--sdm-out", str(tmp_path / "o.dsf"), "--quiet"]) == 1
     assert encode.main(["--input", str(raw), "--dsd-rate", "2822400"]) == 1
+
+
+@pytest.mark.parametrize("sdm", ["precorr", "trellis"])
+def test_encode_chunked_equals_one_pass(tmp_path, sdm):
+    """Chunks of 0.01 s (FIR history and SDM state carried) give the same
+    file as one pass over the input."""
+    from foo_dsd_trellis_gb300 import encode
+    wav = tmp_path / "in.wav"
+    _stereo_wav(wav, 2500, 44100, 4)
+    args = ["--input", str(wav), "--dsd-rate", "2822400", "--sdm", sdm, "--cands", "4",
+            "--lat", "32", "--depth", "8", "--keep-channels", "--quiet"]
+    assert encode.main(args + ["--sdm-out", str(tmp_path / "a.dff"), "--chunk", "100"]) == 0
+    assert encode.main(args + ["--sdm-out", str(tmp_path / "b.dff"), "--chunk", "0.01"]) == 0
+    assert (tmp_path / "a.dff").read_bytes() == (tmp_path / "b.dff").read_bytes()
