@@ -19,8 +19,9 @@ on a bounded slice of the same workload.
 Other workloads (`--workload`, one JSON line each): multistream64 (64 streams
 in one batched plan), diff16 (the adjoint of the differentiable path),
 dsd512conv6 (DSD512 5.1 with UPOLS room convolution), samerate128 (DoP DSD128
-re-encode on the engine's path-table parameters), dsd2pcm128 (DSD128 -> 44.1
-kHz PCM) and precorr128 (PCM -> DSD128 with the PreCorr SDM).
+re-encode on the engine's path-table parameters), samerate128lp (the same with
+the engine's 127-tap FIR lowpass instead of the boxcar), dsd2pcm128 (DSD128 ->
+44.1 kHz PCM) and precorr128 (PCM -> DSD128 with the PreCorr SDM).
 """
 from __future__ import annotations
 
@@ -60,10 +61,11 @@ def parse():
                     help="nominal DAS segment length (profiling of small cases only)")
     ap.add_argument("--workload", default="dsd128_das",
                     choices=["dsd128_das", "multistream64", "diff16", "dsd512conv6",
-                             "samerate128", "precorr128", "dsd2pcm128"],
+                             "samerate128", "samerate128lp", "precorr128", "dsd2pcm128"],
                     help="multistream64: the batched 64-stream form; diff16: the adjoint; "
-                         "samerate128 / precorr128 / dsd2pcm128: the DSD re-encode, PreCorr "
-                         "and DSD -> PCM paths (each prints its own JSON line)")
+                         "samerate128 / samerate128lp / precorr128 / dsd2pcm128: the DSD "
+                         "re-encode (boxcar / FIR lowpass), PreCorr and DSD -> PCM paths (each "
+                         "prints its own JSON line)")
     ap.add_argument("--fd-dirs", type=int, default=32,
                     help="diff16: random unit directions of the finite-difference check")
     ap.add_argument("--ms-scale", type=float, default=1.0,
@@ -674,6 +676,14 @@ NEXT = {
                    "there = auto = 128 at DSD128 (src/engine.c:1008-1021)",
         ntf="clans-6", cands=2, depth=4, lat=128, das_seg_len=65536, boxcar_taps=64,
         gain="float32(0.708) (path gain)"),
+    "samerate128lp": dict(
+        metric="same-rate DSD128 re-encode with the FIR lowpass (DoP in -> unpack -> 127-tap "
+               "FP64 lowpass at 50 kHz -> DAS trellis SDM -> DoP) DSD Msamples/s, bit-exact",
+        workload="samerate_lowpass_dsd128_stereo_10s", fs=5644800,
+        path_table="DSD128 -> DSD128 row of the engine's path table (src/engine.c:61) with "
+                   "fir_mode FIR (src/engine.c:168-181)",
+        ntf="clans-6", cands=2, depth=4, lat=128, das_seg_len=65536, lowpass_taps=127,
+        lowpass_cutoff_hz=50000.0, gain="float32(0.708) (path gain)"),
     "precorr128": dict(
         metric="PCM 44.1 kHz -> DSD128 with the PreCorr SDM (FIR chain -> PreCorr -> DoP) "
                "DSD Msamples/s, bit-exact SDM",
@@ -724,15 +734,19 @@ def _next_cpu(wl: str, inp, bits, sample_s: float) -> dict:
     cfg = NEXT[wl]
     nch = inp.shape[0]
     fs = cfg["fs"]
-    if wl == "samerate128":
+    if wl in ("samerate128", "samerate128lp"):
         frames = int(sample_s * fs) // 16
         x = inp[:, :frames]
         nthreads = os.cpu_count() or 1
         f = ntf.get_filter(cfg["ntf"], fs)
         g = float(np.float32(PATH_GAIN))
         t0 = time.perf_counter()
-        box = np.stack([O.Boxcar(cfg["boxcar_taps"]).process(O.dop_unpack(x[c]), g, g)
-                        for c in range(nch)])
+        if wl == "samerate128":
+            box = np.stack([O.Boxcar(cfg["boxcar_taps"]).process(O.dop_unpack(x[c]), g, g)
+                            for c in range(nch)])
+        else:
+            box = np.stack([O.Lowpass(fs, cfg["lowpass_cutoff_hz"], cfg["lowpass_taps"])
+                            .process(O.dop_unpack(x[c]), g, g) for c in range(nch)])
         out, _, _ = O.das_run(f.order, np.array(f.a), np.array(f.g), cfg["depth"], cfg["cands"],
                               cfg["lat"], 0.0, box, seg_len=cfg["das_seg_len"], seed_mode=0,
                               reposition=True, nthreads=nthreads)
@@ -740,7 +754,8 @@ def _next_cpu(wl: str, inp, bits, sample_s: float) -> dict:
             O.dop_pack_bits(out[c], 0)
         dt = time.perf_counter() - t0
         n = out.shape[0] * out.shape[1]
-        what = "DoP unpack + boxcar + trellis SDM port + DAS + DoP"
+        what = ("DoP unpack + " + ("boxcar" if wl == "samerate128" else "FP64 lowpass restatement")
+                + " + trellis SDM port + DAS + DoP")
     elif wl == "precorr128":
         frames = int(sample_s * 44100)
         x = inp[:, :frames]
@@ -791,12 +806,14 @@ def run_next(args):
     torch.cuda.set_device(local)
     nch, fs = 2, cfg["fs"]
     inp, _ = _next_input(wl, args.seconds, nch, 1101 + 2 * rank)
-    if wl == "samerate128":
+    if wl in ("samerate128", "samerate128lp"):
         f = ntf.get_filter(cfg["ntf"], fs)
         g = float(np.float32(PATH_GAIN))
         enc = Encoder(fs, fs, nch, f, cfg["depth"], cfg["cands"], cfg["lat"],
                       seg_len=cfg["das_seg_len"], seed_mode=FULL_PARALLEL, reposition=True,
-                      boxcar_taps=0, soft_clip=False, output_format=OUT_DOP, device=local)
+                      boxcar_taps=0, soft_clip=False, output_format=OUT_DOP,
+                      samerate_filter=_lib.SAMERATE_LOWPASS if wl == "samerate128lp"
+                      else _lib.SAMERATE_BOXCAR, device=local)
     elif wl == "precorr128":
         f = ntf.auto_select_precorr(fs)
         g = PCM_FIR_GAIN
@@ -857,13 +874,14 @@ def run_next(args):
     e2e = {"value": job_throughput(e2e_units, args.steps, world, e2e_s), "unit": UNIT,
            "h2d_bytes_per_step": int(inp.nbytes), "d2h_bytes_per_step": int(nb2)}
     st = enc.stage_ms()
-    if wl == "samerate128":
+    if wl in ("samerate128", "samerate128lp"):
         sdm_s = statistics.mean(sdm_ms) / 1000.0
         flops = sdm_samples * cfg["cands"] * (5 * f.order + 6)
         roof = {"bound": "fp64", "achieved": flops / sdm_s / 1e12, "peak": fp64_peak / 1000.0,
                 "unit": "TFLOP/s", "frac": flops / sdm_s / 1e12 / (fp64_peak / 1000.0),
-                "traffic": SDM_DRAM_BYTES_PER_SAMPLE * sdm_samples,
-                "kernel": f"sdm_jobs_kernel<{f.order}>",
+                "traffic": None,
+                "kernel": f"sdm_split_kernel<{f.order},8,2> (K = 2: one state component per "
+                          "lane, two jobs per warp; latency-bound)",
                 "algorithmic_flops_per_launch": flops, "flops_per_sample": cfg["cands"] * (5 * f.order + 6)}
     elif wl == "precorr128":
         pc_s = statistics.mean(sdm_ms) / 1000.0
@@ -889,7 +907,7 @@ def run_next(args):
                               "issues as one FP64 instruction; the probe's peak counts DADD/DMUL)"}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = _next_cpu(wl, inp, None, 1.0 if wl != "samerate128" else 0.5)
+        cpu = _next_cpu(wl, inp, None, 0.5 if wl.startswith("samerate") else 1.0)
     if rank == 0:
         line = {"metric": cfg["metric"], "value": value, "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup,
@@ -913,7 +931,7 @@ def run_next_reference(args):
     import numpy as np
     cfg = NEXT[args.workload]
     inp, _ = _next_input(args.workload, args.seconds, 2, 1101)
-    sample_s = 1.0 if args.workload != "samerate128" else 0.5
+    sample_s = 0.5 if args.workload.startswith("samerate") else 1.0
     for _ in range(args.warmup):
         _next_cpu(args.workload, inp, None, 0.05)
     vals, secs = [], []

@@ -55,7 +55,7 @@ class DasParams(C.Structure):
 
 class PipelineParams(C.Structure):
     _fields_ = [("fir", FirParams), ("sdm", SdmParams), ("das", DasParams),
-                ("output_format", C.c_int), ("sdm_mode", C.c_int)]
+                ("output_format", C.c_int), ("sdm_mode", C.c_int), ("samerate_filter", C.c_int)]
 
 
 class StreamDesc(C.Structure):
@@ -87,6 +87,8 @@ SDM_TRELLIS = 0
 FILE_DSF = 1
 FILE_DFF = 2
 SDM_PRECORR = 1
+SAMERATE_BOXCAR = 0
+SAMERATE_LOWPASS = 1
 
 OPT_SDM_SELECT = 1
 OPT_SDM_LANES = 2
@@ -152,6 +154,15 @@ SIGNATURES = {
                                         C.c_double, C.c_double]),
     "dsdgpu_boxcar_process_async": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp, _sz,
                                               C.c_double, C.c_double]),
+    "dsdgpu_lowpass_setup": (C.c_int, [_vp, C.c_uint, C.c_double, C.c_int, C.c_int]),
+    "dsdgpu_lowpass_taps": (C.c_int, [_vp, _vp, C.c_int, C.POINTER(C.c_int)]),
+    "dsdgpu_lowpass_design": (C.c_int, [C.c_uint, C.c_double, C.c_int, _vp, C.c_int,
+                                        C.POINTER(C.c_int)]),
+    "dsdgpu_lowpass_reset": (C.c_int, [_vp]),
+    "dsdgpu_lowpass_process": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp, _sz,
+                                         C.c_double, C.c_double]),
+    "dsdgpu_lowpass_process_async": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp, _sz,
+                                               C.c_double, C.c_double]),
     "dsdgpu_decim_setup": (C.c_int, [_vp, C.c_uint, C.c_uint, C.c_int]),
     "dsdgpu_decim_reset": (C.c_int, [_vp]),
     "dsdgpu_decim_process": (C.c_int, [_vp, C.c_int, _vp, _sz, _sz, _vp, _sz, C.c_double,

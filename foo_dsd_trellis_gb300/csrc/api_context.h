@@ -32,6 +32,8 @@ int launch_pack_native(const uint8_t* bits, size_t stride, int nch, size_t n, ui
 struct dsdgpu_conv_state;   // UPOLS convolution (conv.cu)
 struct dsdgpu_decim_state;  // DSD -> PCM decimation (decim.cu)
 void decim_free(dsdgpu_decim_state* s);
+struct dsdgpu_lowpass_state;  // same-rate FIR lowpass (lowpass.cu)
+void lowpass_free(dsdgpu_lowpass_state* s);
 struct dsdgpu_precorr_state;  // PreCorr greedy SDM (precorr.cu)
 void precorr_free(dsdgpu_precorr_state* s);
 struct dsdgpu_context;
@@ -109,6 +111,9 @@ struct dsdgpu_context {
   int box_taps = 0;
   int box_nch = 0;
   bool pipe_same_rate = false;    // pipeline input is DoP: unpack + boxcar instead of the FIR
+  // same-rate FIR lowpass (FIR_MODE_FIR), used instead of the boxcar when set up
+  dsdgpu_lowpass_state* lowpass = nullptr;
+  bool pipe_lowpass = false;
 
   // DSD -> PCM decimation chain (pipeline output format DSDGPU_OUT_PCM)
   dsdgpu_decim_state* decim = nullptr;
@@ -139,6 +144,8 @@ struct dsdgpu_context {
     decim = nullptr;
     precorr_free(precorr);
     precorr = nullptr;
+    lowpass_free(lowpass);
+    lowpass = nullptr;
     if (d_box_hist) cudaFree(d_box_hist);
     d_box_hist = nullptr;
     if (d_ctx) cudaFree(d_ctx);

@@ -25,6 +25,7 @@ int dsdgpu_pipeline_setup(dsdgpu_context_t* c, const dsdgpu_pipeline_params_t* p
     c->pipe_ready = true;
     c->pipe_same_rate = false;
     c->pipe_precorr = false;
+    c->pipe_lowpass = false;
     if (!c->ev_ready) {
       for (int i = 0; i < dsdgpu_context::kEvents; i++) cudaEventCreate(&c->ev[i]);
       c->ev_ready = true;
@@ -39,7 +40,14 @@ int dsdgpu_pipeline_setup(dsdgpu_context_t* c, const dsdgpu_pipeline_params_t* p
                            : dsdgpu_sdm_setup(c, &p->sdm, nch);
   if (rc) return rc;
   c->pipe_same_rate = p->fir.fs_in == p->fir.fs_out;
-  if (c->pipe_same_rate) {
+  if (p->samerate_filter != DSDGPU_SAMERATE_BOXCAR && p->samerate_filter != DSDGPU_SAMERATE_LOWPASS)
+    return c->fail(DSDGPU_ERR_ARG, "bad same-rate filter");
+  c->pipe_lowpass = c->pipe_same_rate && p->samerate_filter == DSDGPU_SAMERATE_LOWPASS;
+  if (c->pipe_lowpass) {
+    // DSD in at the output rate: DoP unpack + FIR lowpass (fir_lowpass_init,
+    // src/engine.c:168-181, 505-523)
+    rc = dsdgpu_lowpass_setup(c, p->fir.fs_in, 50000.0, 127, nch);
+  } else if (c->pipe_same_rate) {
     // DSD in at the output rate: DoP unpack + boxcar (src/engine.c:487-563)
     const int taps = p->fir.boxcar_taps > 0 ? p->fir.boxcar_taps : samerate_boxcar_taps(p->fir.fs_in);
     rc = dsdgpu_boxcar_setup(c, taps, nch);
@@ -109,8 +117,11 @@ int dsdgpu_pipeline_process(dsdgpu_context_t* c, const float* d_pcm, size_t pcm_
     // the decision buffer holds the unpacked input until the DAS writes it
     rc = dsdgpu_dop_unpack(c, nch, d_pcm, pcm_stride, frames, d_bits, bit_row);
     if (rc) return rc;
-    rc = dsdgpu_boxcar_process_async(c, 0, nch, d_bits, bit_row, n_fir, d_fir, fir_stride,
-                                     gain_start, gain_end);
+    rc = c->pipe_lowpass
+             ? dsdgpu_lowpass_process_async(c, 0, nch, d_bits, bit_row, n_fir, d_fir, fir_stride,
+                                            gain_start, gain_end)
+             : dsdgpu_boxcar_process_async(c, 0, nch, d_bits, bit_row, n_fir, d_fir, fir_stride,
+                                           gain_start, gain_end);
     fo = n_fir;
   } else {
     rc = dsdgpu_fir_process_async(c, 0, nch, d_pcm, pcm_stride, frames, d_fir, fir_stride,

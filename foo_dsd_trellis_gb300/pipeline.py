@@ -29,7 +29,7 @@ class Encoder:
                  seg_len: int = 65536, nsegs: int = 0, seed_mode: int = FULL_PARALLEL,
                  reposition: bool = True, boxcar_taps: int = 8, soft_clip: bool = True,
                  output_format: int = OUT_DOP, sdm_mode: int = _lib.SDM_TRELLIS,
-                 device: int = 0):
+                 samerate_filter: int = _lib.SAMERATE_BOXCAR, device: int = 0):
         self.L = _lib.load()
         h = C.c_void_p()
         rc = self.L.dsdgpu_create(device, C.byref(h))
@@ -50,6 +50,7 @@ class Encoder:
         p.das.seed_mode, p.das.reposition = seed_mode, int(reposition)
         p.output_format = output_format
         p.sdm_mode = sdm_mode
+        p.samerate_filter = samerate_filter
         _lib.check(self.h, self.L.dsdgpu_pipeline_setup(self.h, C.byref(p), num_channels))
         self.params = p
         self.nch = num_channels

@@ -112,12 +112,19 @@ typedef struct {
 
 /* Whole-path parameters: the FIR chain with its glue, the trellis SDM, DAS,
  * and the output format. */
+/* Pre-SDM filter of the same-rate DSD path: the reference's fir_mode
+ * (FIR_MODE_BOXCAR 0 / FIR_MODE_FIR 1, include/dsd_types.h:436-438; the
+ * engine's default is the boxcar, src/engine.c:168-181). */
+#define DSDGPU_SAMERATE_BOXCAR  0   /* rate-adaptive running mean (fir.boxcar_taps) */
+#define DSDGPU_SAMERATE_LOWPASS 1   /* 127-tap FP64 lowpass at 50 kHz (fir_lowpass_init) */
+
 typedef struct {
     dsdgpu_fir_params_t fir;
     dsdgpu_sdm_params_t sdm;
     dsdgpu_das_params_t das;
     int                 output_format;   /* DSDGPU_OUT_* */
     int                 sdm_mode;        /* DSDGPU_SDM_*; 0 = trellis */
+    int                 samerate_filter; /* DSDGPU_SAMERATE_*; same-rate input only */
 } dsdgpu_pipeline_params_t;
 
 /* ---- lifecycle (replaces gpu_create / gpu_destroy, include/gpu_compute.h:52-55) ---- */
@@ -374,8 +381,9 @@ int dsdgpu_plan_time_plain(dsdgpu_plan_t *plan, int njobs, int64_t *samples, dou
  * (engine_process_block, src/engine.c:487-563).  A pipeline set up with
  * fir.fs_in == fir.fs_out takes DoP floats (planar [nch][frames], 16 DSD
  * samples per frame) and runs unpack -> boxcar (fir.boxcar_taps, 0 = the
- * engine's rate default: 32 at DSD64, 64 at DSD128/256, 16 at DSD512) ->
- * DAS SDM -> packing. */
+ * engine's rate default: 32 at DSD64, 64 at DSD128/256, 16 at DSD512) or,
+ * with samerate_filter DSDGPU_SAMERATE_LOWPASS, the FIR lowpass below ->
+ * DAS SDM (or PreCorr) -> packing. */
 /* DoP floats [nch][dop_stride] -> 0/1 decision bytes [nch][bits_stride],
  * 16 per frame, MSB first. */
 int dsdgpu_dop_unpack(dsdgpu_context_t *ctx, int nch, const float *d_dop, size_t dop_stride,
@@ -391,6 +399,31 @@ int dsdgpu_boxcar_process_async(dsdgpu_context_t *ctx, int first, int nch,
                                 const uint8_t *d_bits, size_t bits_stride, size_t count,
                                 double *d_out, size_t out_stride, double gain_start,
                                 double gain_end);
+
+/* Same-rate FIR lowpass (fir_lowpass_init_ex / fir_lowpass_process /
+ * fir_lowpass_reset, src/fir.c:795-877; the engine's FIR_MODE_FIR branch,
+ * src/engine.c:505-523, and the plugin's gpu_fir_lowpass_setup /
+ * gpu_fir_lowpass_f64, include/gpu_compute.h:88-103): Kaiser (beta 10)
+ * windowed sinc, ntaps clamped to 3..255 and made odd, cutoff_hz / (fs / 2)
+ * capped at 0.5, normalised to unit sum, FP64; applied to +-1 decisions with
+ * the delay line carried across calls (zero at setup and reset), then the
+ * gain ramp of the boxcar.  fir_lowpass_init is cutoff 50,000 Hz, 127 taps. */
+int dsdgpu_lowpass_setup(dsdgpu_context_t *ctx, unsigned fs, double cutoff_hz, int ntaps,
+                         int nch);
+/* The design alone (host code, no context): taps[0 .. *ntaps). */
+int dsdgpu_lowpass_design(unsigned fs, double cutoff_hz, int ntaps, double *taps, int cap,
+                          int *out_ntaps);
+/* The designed taps (the FP64 coeffs_d of fir_lowpass_t); *ntaps receives the
+ * count, taps may be NULL. */
+int dsdgpu_lowpass_taps(const dsdgpu_context_t *ctx, double *taps, int cap, int *ntaps);
+int dsdgpu_lowpass_reset(dsdgpu_context_t *ctx);
+int dsdgpu_lowpass_process(dsdgpu_context_t *ctx, int first, int nch, const uint8_t *d_bits,
+                           size_t bits_stride, size_t count, double *d_out, size_t out_stride,
+                           double gain_start, double gain_end);
+int dsdgpu_lowpass_process_async(dsdgpu_context_t *ctx, int first, int nch,
+                                 const uint8_t *d_bits, size_t bits_stride, size_t count,
+                                 double *d_out, size_t out_stride, double gain_start,
+                                 double gain_end);
 
 /* ---- DSD -> PCM decimation (FIR-only engine branch, src/engine.c:566-577) ---
  * FP64 chain of 63-tap half-band /2 stages (src/fir.c:467-487,523-611), delay

@@ -137,3 +137,110 @@ size_t ora_decim_process(ora_decim_t *d, const double *in, size_t n, double *out
     free(b);
     return cur;
 }
+
+/*
+ * Same-rate FIR lowpass (the engine's FIR_MODE_FIR alternative to the boxcar,
+ * src/engine.c:168-181 and :505-523):
+ *   - design of fir_lowpass_init_ex (src/fir.c:795-857): ntaps clamped to
+ *     3..255 and made odd, fc = cutoff / (fs / 2) capped at 0.5, Kaiser
+ *     (beta 10) windowed sinc, normalised to unit sum, FP64 throughout, in the
+ *     reference's expression order; fir_lowpass_init uses 50 kHz, 127 taps;
+ *   - filtering (fir_lowpass_process, src/fir.c:863-872, IPP ippsFIRSR_64f):
+ *     y[i] = sum_k h[k] x[i - k] on +-1.0 inputs, delay line zero at init and
+ *     carried across calls, then the gain ramp of src/engine.c:518-523.
+ * IPP's summation order is closed; this restatement fixes one: the taps are
+ * padded with zeros to W = 32 * ceil(ntaps / 32) and summed as W / 8 partial
+ * sums, group j holding taps k = W-1-8j-v for v = 0..7 (oldest sample
+ * first), each partial sum accumulated from 0.0 in v order and the partial
+ * sums added in j order.  Samples before the first input are 0.
+ */
+#include <math.h>
+
+#define ORA_LP_MAX_TAPS 255
+#define ORA_LP_BETA 10.0
+#define ORA_LP_PI 3.14159265358979323846
+
+struct ora_lowpass {
+    int ntaps;
+    int W;
+    double h[ORA_LP_MAX_TAPS + 1];
+    double hist[256];        /* the last 256 inputs, oldest first (0 = not seen) */
+};
+
+static double lp_bessel_i0(double x)
+{
+    double sum = 1.0, term = 1.0;
+    const double q = (x / 2.0) * (x / 2.0);
+    for (int k = 1; k <= 25; k++) {
+        term *= q / ((double)k * (double)k);
+        sum += term;
+        if (term < 1e-20 * sum) break;
+    }
+    return sum;
+}
+
+int ora_lowpass_design(unsigned fs, double cutoff_hz, int ntaps, double *h)
+{
+    if (ntaps < 3) ntaps = 3;
+    if (ntaps > ORA_LP_MAX_TAPS) ntaps = ORA_LP_MAX_TAPS;
+    if (ntaps % 2 == 0) ntaps++;
+    double fc = cutoff_hz / ((double)fs / 2.0);
+    if (fc > 0.5) fc = 0.5;
+    const int M = ntaps - 1;
+    const double i0b = lp_bessel_i0(ORA_LP_BETA);
+    for (int n = 0; n <= M; n++) {
+        const double x = (double)n - (double)M / 2.0;
+        const double s = (fabs(x) < 1e-10) ? 2.0 * fc : sin(2.0 * ORA_LP_PI * fc * x) / (ORA_LP_PI * x);
+        const double t = 2.0 * n / M - 1.0;
+        const double arg = 1.0 - t * t;
+        h[n] = s * (lp_bessel_i0(ORA_LP_BETA * sqrt(fabs(arg))) / i0b);
+    }
+    double sum = 0.0;
+    for (int n = 0; n < ntaps; n++) sum += h[n];
+    if (sum > 0.0)
+        for (int n = 0; n < ntaps; n++) h[n] /= sum;
+    return ntaps;
+}
+
+ora_lowpass_t *ora_lowpass_new(unsigned fs, double cutoff_hz, int ntaps)
+{
+    ora_lowpass_t *lp = (ora_lowpass_t *)calloc(1, sizeof *lp);
+    if (!lp) return NULL;
+    lp->ntaps = ora_lowpass_design(fs, cutoff_hz, ntaps, lp->h);
+    lp->W = 32 * ((lp->ntaps + 31) / 32);
+    return lp;
+}
+
+void ora_lowpass_free(ora_lowpass_t *lp) { free(lp); }
+
+int ora_lowpass_taps(const ora_lowpass_t *lp, double *h)
+{
+    memcpy(h, lp->h, (size_t)lp->ntaps * sizeof(double));
+    return lp->ntaps;
+}
+
+void ora_lowpass_process(ora_lowpass_t *lp, const float *in, double *out, size_t count,
+                         double g_start, double g_end)
+{
+    double *x = (double *)malloc((count + 256) * sizeof(double));
+    if (!x) return;
+    memcpy(x, lp->hist, sizeof lp->hist);
+    for (size_t i = 0; i < count; i++) x[256 + i] = in[i] >= 0.0f ? 1.0 : -1.0;
+    if (g_start == 0.0) g_start = g_end;
+    const double g_step = (count > 1) ? (g_end - g_start) / (double)(count - 1) : 0.0;
+    const int W = lp->W;
+    for (size_t i = 0; i < count; i++) {
+        double acc = 0.0;
+        for (int j = 0; j < W / 8; j++) {
+            double grp = 0.0;
+            for (int v = 0; v < 8; v++) {
+                const int k = W - 1 - 8 * j - v;
+                if (k < lp->ntaps) grp += x[256 + i - k] * lp->h[k];
+            }
+            acc += grp;
+        }
+        out[i] = acc * (g_start + g_step * (double)i);
+    }
+    memcpy(lp->hist, x + count, sizeof lp->hist);
+    free(x);
+}

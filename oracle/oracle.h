@@ -134,6 +134,15 @@ void ora_boxcar_free(ora_boxcar_t *b);
 void ora_boxcar_gain(ora_boxcar_t *b, const float *in, double *out, size_t count,
                      double g_start, double g_end);
 
+/* ---- Same-rate FIR lowpass (src/fir.c:795-872, src/engine.c:505-523) ---- */
+typedef struct ora_lowpass ora_lowpass_t;
+int  ora_lowpass_design(unsigned fs, double cutoff_hz, int ntaps, double *h);
+ora_lowpass_t *ora_lowpass_new(unsigned fs, double cutoff_hz, int ntaps);
+void ora_lowpass_free(ora_lowpass_t *lp);
+int  ora_lowpass_taps(const ora_lowpass_t *lp, double *h);
+void ora_lowpass_process(ora_lowpass_t *lp, const float *in, double *out, size_t count,
+                         double g_start, double g_end);
+
 /* ---- PreCorr greedy SDM (src/precorr.c) ---- */
 typedef struct ora_precorr ora_precorr_t;
 ora_precorr_t *ora_precorr_new(int order, const double *a, const double *g, double state_limit);

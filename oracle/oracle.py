@@ -241,6 +241,40 @@ class Boxcar:
             pass
 
 
+class Lowpass:
+    """The same-rate FIR lowpass (fir_lowpass_init_ex + fir_lowpass_process,
+    src/fir.c:795-872) with its delay line carried across calls and the
+    engine's gain ramp."""
+
+    def __init__(self, fs: int, cutoff_hz: float = 50000.0, ntaps: int = 127):
+        self.L = oracle_lib().lib
+        self.h = self.L.ora_lowpass_new(fs, float(cutoff_hz), ntaps)
+
+    def taps(self) -> np.ndarray:
+        h = np.zeros(256, np.float64)
+        n = self.L.ora_lowpass_taps(self.h, _ptr(h, _dp))
+        return h[:n]
+
+    def process(self, bits: np.ndarray, g_start: float, g_end: float) -> np.ndarray:
+        bits = np.ascontiguousarray(bits, np.float32)
+        out = np.empty(max(len(bits), 1), np.float64)
+        self.L.ora_lowpass_process(self.h, _ptr(bits, _fp), _ptr(out, _dp), len(bits),
+                                   float(g_start), float(g_end))
+        return out[: len(bits)]
+
+    def __del__(self):
+        try:
+            self.L.ora_lowpass_free(self.h)
+        except Exception:
+            pass
+
+
+def lowpass_design(fs: int, cutoff_hz: float = 50000.0, ntaps: int = 127) -> np.ndarray:
+    h = np.zeros(256, np.float64)
+    n = oracle_lib().lib.ora_lowpass_design(fs, float(cutoff_hz), ntaps, _ptr(h, _dp))
+    return h[:n]
+
+
 class PreCorr:
     """The PreCorr greedy SDM: the oracle's restatement, or (ref=True) the
     reference's own src/precorr.c compiled into oracle/_ref."""
@@ -341,6 +375,14 @@ def _bind_oracle_extras(L):
     L.ora_boxcar_new.argtypes = [C.c_int]
     L.ora_boxcar_free.argtypes = [C.c_void_p]
     L.ora_boxcar_gain.argtypes = [C.c_void_p, _fp, _dp, C.c_size_t, C.c_double, C.c_double]
+    L.ora_lowpass_design.restype = C.c_int
+    L.ora_lowpass_design.argtypes = [C.c_uint, C.c_double, C.c_int, _dp]
+    L.ora_lowpass_new.restype = C.c_void_p
+    L.ora_lowpass_new.argtypes = [C.c_uint, C.c_double, C.c_int]
+    L.ora_lowpass_free.argtypes = [C.c_void_p]
+    L.ora_lowpass_taps.restype = C.c_int
+    L.ora_lowpass_taps.argtypes = [C.c_void_p, _dp]
+    L.ora_lowpass_process.argtypes = [C.c_void_p, _fp, _dp, C.c_size_t, C.c_double, C.c_double]
     L.ora_decim_new.restype = C.c_void_p
     L.ora_decim_new.argtypes = [C.c_uint, C.c_uint]
     L.ora_decim_free.argtypes = [C.c_void_p]
