@@ -43,6 +43,11 @@ class Segment(C.Structure):
                 ("d_seed_state", C.c_void_p), ("out_count", C.c_int64)]
 
 
+class EstimateItem(C.Structure):
+    _fields_ = [("d_in", C.c_void_p), ("count", C.c_int64), ("init_state", C.c_double * 10),
+                ("out_state", C.c_double * 10)]
+
+
 class FirParams(C.Structure):
     _fields_ = [("fs_in", C.c_uint), ("fs_out", C.c_uint), ("boxcar_taps", C.c_int),
                 ("soft_clip", C.c_int)]
@@ -119,6 +124,9 @@ SIGNATURES = {
     "dsdgpu_sdm_drain": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _szp]),
     "dsdgpu_sdm_copy_state": (C.c_int, [_vp, C.c_int, C.c_int]),
     "dsdgpu_sdm_segments": (C.c_int, [_vp, C.POINTER(Segment), C.c_int]),
+    "dsdgpu_sdm_state_distance": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
+    "dsdgpu_sdm_estimate_state": (C.c_int, [_vp, C.POINTER(SdmParams), C.c_int,
+                                            C.POINTER(EstimateItem), C.c_int]),
     "dsdgpu_sdm_query": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_double),
                                    C.POINTER(C.c_uint64)]),
     "dsdgpu_das_process": (C.c_int, [_vp, C.POINTER(DasParams), C.c_int, _vp, _sz, _sz, _vp,

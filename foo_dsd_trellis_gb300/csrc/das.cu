@@ -44,9 +44,56 @@ __global__ void das_rms_kernel(const double* __restrict__ x, const long long* __
   out[i] = sqrt(__ddiv_rn(s, (double)win));
 }
 
-// ---- 16-level greedy state estimator (src/trellis.c:1125-1187), serial ----
-// One thread per channel walks the chunk from seg1's start and records the
-// state at every later segment start.
+// ---- greedy multi-level state estimator (src/trellis.c:1125-1187) ----
+// One sample of sdm_estimate_state_multibit: the NTF advance with y = 0, the
+// quantiser (levels <= 2: the sign of v * a0; else v / a0 rounded to the
+// nearest of `levels` values in [-1, 1]), y subtracted from state 0, clamp.
+__device__ __forceinline__ void estimate_step(const SdmParams& P, double* st, double* ns, double xv,
+                                              int levels, double step) {
+  const int N = P.order;
+  ns[0] = __dadd_rn(__dsub_rn(st[0], __dmul_rn(P.g[0], st[1])), xv);
+  double v = __dadd_rn(xv, __dmul_rn(P.a[0], ns[0]));
+  for (int i = 1; i < N - 1; i++) {
+    ns[i] = __dsub_rn(__dadd_rn(st[i], st[i - 1]), __dmul_rn(P.g[i], st[i + 1]));
+    v = __dadd_rn(v, __dmul_rn(P.a[i], ns[i]));
+  }
+  ns[N - 1] = __dadd_rn(st[N - 1], st[N - 2]);
+  v = __dadd_rn(v, __dmul_rn(P.a[N - 1], ns[N - 1]));
+  double y;
+  if (levels <= 2) {
+    y = __dmul_rn(v, P.a[0]) > 0.0 ? 1.0 : -1.0;
+  } else {
+    const double yi = __ddiv_rn(v, P.a[0]);
+    int idx = __double2int_rz(__dadd_rn(__ddiv_rn(__dadd_rn(yi, 1.0), step), 0.5));
+    if (idx < 0) idx = 0;
+    if (idx > levels - 1) idx = levels - 1;
+    y = __dadd_rn(-1.0, __dmul_rn((double)idx, step));
+  }
+  ns[0] = __dsub_rn(ns[0], y);
+  if (P.state_limit > 0.0)
+    for (int i = 0; i < N; i++) {
+      if (ns[i] > P.state_limit) ns[i] = P.state_limit;
+      else if (ns[i] < -P.state_limit) ns[i] = -P.state_limit;
+    }
+  for (int i = 0; i < N; i++) st[i] = ns[i];
+}
+
+// One thread per estimate (sdm_estimate_state(_multibit) on its own input).
+__global__ void estimate_kernel(SdmParams P, const dsdgpu_estimate_t* __restrict__ items, int n,
+                                int levels, double* __restrict__ out /* [n][kMaxOrder] */) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  double st[kMaxOrder], ns[kMaxOrder];
+  for (int k = 0; k < P.order; k++) st[k] = items[j].init_state[k];
+  const double* x = items[j].d_in;
+  const long long count = items[j].count;
+  const double step = __ddiv_rn(2.0, (double)(levels - 1));
+  for (long long t = 0; t < count; t++) estimate_step(P, st, ns, x[t], levels, step);
+  for (int k = 0; k < kMaxOrder; k++) out[(size_t)j * kMaxOrder + k] = k < P.order ? st[k] : 0.0;
+}
+
+// DAS seeding: one thread per channel walks the chunk from seg1's start with
+// the 16-level estimator and records the state at every later segment start.
 __global__ void das_estimate_kernel(SdmParams P, const double* __restrict__ fir, size_t fir_stride,
                                     const SdmCtx* __restrict__ pers, int pers_first,
                                     const long long* __restrict__ starts, int S, long long count,
@@ -64,29 +111,7 @@ __global__ void das_estimate_kernel(SdmParams P, const double* __restrict__ fir,
   for (int s = 1; s < S; s++) {
     const long long bnd = s >= 2 ? starts[s] - est_start : 0;
     if (bnd > pos && bnd <= count - est_start) {
-      for (long long t = pos; t < bnd; t++) {
-        const double xv = x[est_start + t];
-        ns[0] = __dadd_rn(__dsub_rn(st[0], __dmul_rn(P.g[0], st[1])), xv);
-        double v = __dadd_rn(xv, __dmul_rn(P.a[0], ns[0]));
-        for (int i = 1; i < N - 1; i++) {
-          ns[i] = __dsub_rn(__dadd_rn(st[i], st[i - 1]), __dmul_rn(P.g[i], st[i + 1]));
-          v = __dadd_rn(v, __dmul_rn(P.a[i], ns[i]));
-        }
-        ns[N - 1] = __dadd_rn(st[N - 1], st[N - 2]);
-        v = __dadd_rn(v, __dmul_rn(P.a[N - 1], ns[N - 1]));
-        const double yi = __ddiv_rn(v, P.a[0]);
-        int idx = __double2int_rz(__dadd_rn(__ddiv_rn(__dadd_rn(yi, 1.0), step), 0.5));
-        if (idx < 0) idx = 0;
-        if (idx > 15) idx = 15;
-        const double y = __dadd_rn(-1.0, __dmul_rn((double)idx, step));
-        ns[0] = __dsub_rn(ns[0], y);
-        if (P.state_limit > 0.0)
-          for (int i = 0; i < N; i++) {
-            if (ns[i] > P.state_limit) ns[i] = P.state_limit;
-            else if (ns[i] < -P.state_limit) ns[i] = -P.state_limit;
-          }
-        for (int i = 0; i < N; i++) st[i] = ns[i];
-      }
+      for (long long t = pos; t < bnd; t++) estimate_step(P, st, ns, x[est_start + t], 16, step);
       pos = bnd;
     }
     for (int k = 0; k < kMaxOrder; k++) est[((size_t)ch * S + s) * kMaxOrder + k] = k < N ? st[k] : 0.0;
@@ -430,6 +455,44 @@ int ensure_ctx_capacity(dsdgpu_context* c, int need) {
 }  // namespace
 
 extern "C" {
+
+int dsdgpu_sdm_estimate_state(dsdgpu_context_t* c, const dsdgpu_sdm_params_t* p, int num_levels,
+                              dsdgpu_estimate_t* items, int n) {
+  if (!c || !p || n < 0 || (n > 0 && !items)) return DSDGPU_ERR_ARG;
+  if (p->order < 2 || p->order > kMaxOrder) return c->fail(DSDGPU_ERR_ARG, "NTF order out of range (2..10)");
+  if (num_levels < 2) return c->fail(DSDGPU_ERR_ARG, "num_levels below 2");
+  if (n == 0) return DSDGPU_OK;
+  for (int j = 0; j < n; j++)
+    if (items[j].count < 0 || (items[j].count > 0 && !items[j].d_in))
+      return c->fail(DSDGPU_ERR_ARG, "bad estimate input");
+  cudaSetDevice(c->device);
+  SdmParams P{};
+  P.order = p->order;
+  for (int k = 0; k < p->order; k++) {
+    P.a[k] = p->a[k];
+    P.g[k] = p->g[k];
+  }
+  P.state_limit = p->state_limit;
+  const size_t ib = sizeof(dsdgpu_estimate_t) * (size_t)n;
+  const size_t ob = sizeof(double) * kMaxOrder * (size_t)n;
+  int rc = c->ensure_scratch(ib + ob + 256);
+  if (rc) return rc;
+  auto* d_items = (dsdgpu_estimate_t*)c->d_scratch;
+  auto* d_out = (double*)((char*)c->d_scratch + ((ib + 255) & ~(size_t)255));
+  cudaMemcpyAsync(d_items, items, ib, cudaMemcpyHostToDevice, c->stream);
+  estimate_kernel<<<(n + 31) / 32, 32, 0, c->stream>>>(P, d_items, n, num_levels, d_out);
+  c->launches++;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return c->cuda_fail(e, "estimate launch");
+  std::vector<double> out((size_t)n * kMaxOrder);
+  e = cudaMemcpyAsync(out.data(), d_out, ob, cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return c->cuda_fail(e, "estimate read");
+  rc = c->check_status();
+  if (rc) return rc;
+  for (int j = 0; j < n; j++)
+    for (int k = 0; k < kMaxOrder; k++) items[j].out_state[k] = out[(size_t)j * kMaxOrder + k];
+  return DSDGPU_OK;
+}
 
 int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int nch,
                        const double* d_fir, size_t fir_stride, size_t count, uint8_t* d_out,

@@ -464,4 +464,22 @@ int dsdgpu_sdm_query(dsdgpu_context_t* c, int channel, double* best_state, uint6
   return DSDGPU_OK;
 }
 
+int dsdgpu_sdm_state_distance(dsdgpu_context_t* c, int a, int b, double* dist) {
+  // sdm_state_distance (src/trellis.c:1094-1109): the sum over the NTF order
+  // of the squared differences of the two best candidates' states, in order
+  if (!c || !dist) return DSDGPU_ERR_ARG;
+  double sa[dsdgpu::kMaxOrder], sb[dsdgpu::kMaxOrder];
+  int rc = dsdgpu_sdm_query(c, a, sa, nullptr);
+  if (rc) return rc;
+  rc = dsdgpu_sdm_query(c, b, sb, nullptr);
+  if (rc) return rc;
+  double d = 0.0;
+  for (int i = 0; i < c->sdm.order; i++) {
+    const double t = sa[i] - sb[i];
+    d += t * t;
+  }
+  *dist = d;
+  return DSDGPU_OK;
+}
+
 }  // extern "C"

@@ -307,6 +307,25 @@ int dsdgpu_probe_fp64(dsdgpu_context_t *ctx, double *gops);
  * num_cands, pending.  best_state may be NULL; info may be NULL (6 values). */
 int dsdgpu_sdm_query(dsdgpu_context_t *ctx, int channel, double *best_state, uint64_t *info);
 
+/* sdm_state_distance(a, b) (src/trellis.c:1094-1109): sum of the squared
+ * differences of the two contexts' best-candidate states. */
+int dsdgpu_sdm_state_distance(dsdgpu_context_t *ctx, int a, int b, double *dist);
+
+/* sdm_estimate_state / sdm_estimate_state_multibit (src/trellis.c:1118-1187),
+ * many at once (one GPU thread each): the NTF loop of `p` (order, a, g,
+ * state_limit; K, depth and lat are not used) run greedily from init_state
+ * over `count` samples of d_in (device) with a num_levels quantiser (2 = the
+ * 1-bit sign rule, 16 = sdm_estimate_state's default); out_state receives the
+ * state after the last sample.  Waits for completion. */
+typedef struct {
+    const double *d_in;          /* device, `count` doubles */
+    int64_t       count;
+    double        init_state[10];
+    double        out_state[10]; /* written */
+} dsdgpu_estimate_t;
+int dsdgpu_sdm_estimate_state(dsdgpu_context_t *ctx, const dsdgpu_sdm_params_t *p,
+                              int num_levels, dsdgpu_estimate_t *items, int n);
+
 /* ---- Batched multi-stream plan -------------------------------------------
  * Many independent PCM streams of uneven length and mixed rates converted in
  * one pass: per-stream FIR chains, then every DAS segment of every stream in

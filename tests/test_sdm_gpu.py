@@ -242,3 +242,81 @@ def test_orders_outside_the_table(oracle, order, K):
     gpu = _gpu_sdm(f, 16, K, 24)
     got = gpu.process_block(torch.from_numpy(x).cuda())[0].cpu().numpy()
     np.testing.assert_array_equal(got, want)
+
+
+def test_estimate_state_batch(oracle):
+    """dsdgpu_sdm_estimate_state (sdm_estimate_state_multibit, src/trellis.c:1125-1187)
+    over many inputs in one launch equals the oracle (pinned to the reference's
+    compiled estimator), for orders 2..10, 2/3/16 levels, the limiter and
+    counts 0, 1 and 20,000."""
+    import ctypes as C
+    from foo_dsd_trellis_gb300 import _lib, ntf
+    from signals import multitone
+    L = _lib.load()
+    h = C.c_void_p()
+    assert L.dsdgpu_create(0, C.byref(h)) == 0
+    rng = np.random.default_rng(11)
+    names = ["clans-4", "clans-5", "clans-6", "clans-7", "clans-8", "sdm-5", "sdm-8"]
+    for levels in (2, 3, 16):
+        for lim in (0.0, 1.5):
+            for name in names:
+                f = ntf.get_filter(name, 5644800)
+                p = _lib.SdmParams()
+                p.order = f.order
+                for i in range(f.order):
+                    p.a[i], p.g[i] = f.a[i], f.g[i]
+                p.state_limit = lim
+                counts = [0, 1, 20000, 777]
+                xs = [multitone(max(n, 1), int(rng.integers(1000))) * 0.5 for n in counts]
+                d_x = [torch.from_numpy(x).cuda() for x in xs]
+                items = (_lib.EstimateItem * len(counts))()
+                inits = []
+                for j, n in enumerate(counts):
+                    items[j].d_in = d_x[j].data_ptr()
+                    items[j].count = n
+                    init = rng.standard_normal(f.order) * 0.1
+                    inits.append(init)
+                    for k in range(f.order):
+                        items[j].init_state[k] = init[k]
+                _lib.check(h, L.dsdgpu_sdm_estimate_state(h, C.byref(p), levels, items, len(counts)))
+                for j, n in enumerate(counts):
+                    want = oracle.estimate_state(f.order, np.array(f.a), np.array(f.g), inits[j],
+                                                 xs[j][:n], lim, levels)
+                    got = np.array(items[j].out_state[: f.order])
+                    assert np.array_equal(got, want), (name, levels, lim, n)
+    p = _lib.SdmParams()
+    p.order = 1
+    assert L.dsdgpu_sdm_estimate_state(h, C.byref(p), 16, None, 0) == _lib.ERR_ARG
+    p.order = 7
+    assert L.dsdgpu_sdm_estimate_state(h, C.byref(p), 1, None, 0) == _lib.ERR_ARG
+    L.dsdgpu_destroy(h)
+
+
+def test_state_distance(oracle):
+    """dsdgpu_sdm_state_distance (src/trellis.c:1094-1109) of two contexts run on
+    different inputs equals the sum of squared differences of the oracle's best
+    states, added in order."""
+    from foo_dsd_trellis_gb300 import ntf
+    from foo_dsd_trellis_gb300.sdm import TrellisSdm
+    from foo_dsd_trellis_gb300 import _lib
+    import ctypes as C
+    from signals import multitone
+    f = ntf.get_filter("clans-7", 5644800)
+    sdm = TrellisSdm(f.order, f.a, f.g, 16, 8, 32, 0.0, num_contexts=2)
+    xs = [multitone(5000, 3 + c) * 0.6 for c in range(2)]
+    refs = [oracle.sdm(f.order, np.array(f.a), np.array(f.g), 16, 8, 32) for _ in range(2)]
+    sdm.process_block(torch.from_numpy(np.stack(xs)).cuda())
+    for c in range(2):
+        oracle.sdm_bits(refs[c], xs[c])
+    d = C.c_double()
+    _lib.check(sdm.h, sdm.L.dsdgpu_sdm_state_distance(sdm.h, 0, 1, C.byref(d)))
+    sa, sb = refs[0].best_state(), refs[1].best_state()
+    want = 0.0
+    for i in range(f.order):
+        t = sa[i] - sb[i]
+        want += t * t
+    assert d.value == want
+    _lib.check(sdm.h, sdm.L.dsdgpu_sdm_state_distance(sdm.h, 1, 1, C.byref(d)))
+    assert d.value == 0.0
+    assert sdm.L.dsdgpu_sdm_state_distance(sdm.h, 0, 2, C.byref(d)) == _lib.ERR_ARG
+    sdm.close()
