@@ -91,6 +91,7 @@ struct dsdgpu_context {
   dsdgpu::AssemblePiece* d_das_pieces = nullptr;  size_t das_pieces_cap = 0;
   dsdgpu::SegBuf* d_das_segbuf = nullptr;         size_t das_segbuf_cap = 0;
   double* d_das_qfir = nullptr;    size_t das_qfir_cap = 0;
+  unsigned char* d_das_seam_scr = nullptr;  size_t das_seam_scr_cap = 0;   // overlaps > 16,384
   bool das_qfir_ready = false;
 
   // whole-path pipeline
@@ -160,14 +161,15 @@ struct dsdgpu_context {
       for (int i = 0; i < kEvents; i++) cudaEventDestroy(ev[i]);
     ev_ready = false;
     void* das[] = {d_das_bits, d_das_est, d_das_i64, d_das_f64, d_das_bp, d_das_tasks,
-                   d_das_pieces, d_das_segbuf, d_das_qfir};
+                   d_das_pieces, d_das_segbuf, d_das_qfir, d_das_seam_scr};
     for (void* p : das)
       if (p) cudaFree(p);
     d_das_bits = nullptr; d_das_est = nullptr; d_das_i64 = nullptr; d_das_f64 = nullptr;
     d_das_bp = nullptr; d_das_tasks = nullptr; d_das_pieces = nullptr; d_das_segbuf = nullptr;
     d_das_qfir = nullptr;
+    d_das_seam_scr = nullptr;
     das_bits_cap = das_est_cap = das_i64_cap = das_f64_cap = das_bp_cap = 0;
-    das_tasks_cap = das_pieces_cap = das_segbuf_cap = das_qfir_cap = 0;
+    das_tasks_cap = das_pieces_cap = das_segbuf_cap = das_qfir_cap = das_seam_scr_cap = 0;
     das_qfir_ready = false;
     d_ctx = nullptr;
     d_jobs = nullptr;

@@ -152,6 +152,7 @@ struct dsdgpu_plan {
   AssemblePiece* d_pieces = nullptr;
   SegBuf* d_segbuf = nullptr;
   int* d_bp = nullptr;
+  unsigned char* d_seam_scr = nullptr;   // per-boundary seam scratch (overlaps > 16,384)
   int* d_counters = nullptr;
   double* d_seed = nullptr;
   float* d_hist = nullptr;
@@ -409,7 +410,7 @@ int capture_graphs(dsdgpu_plan* pl) {
     return c->cuda_fail(cudaGetLastError(), "graph capture");
   if (!rc && !pl->tasks.empty()) {
     const int r = launch_das_seams(pl->d_tasks, (int)pl->tasks.size(), pl->max_ovl, pl->d_qfir,
-                                   pl->d_bp, m);
+                                   pl->d_bp, pl->d_seam_scr, m);
     if (r) rc = DSDGPU_ERR_CUDA;
   }
   for (StreamPlan& s : pl->st) {
@@ -569,8 +570,6 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
     s.n_fir = (size_t)d.frames * (size_t)s.F.ratio;
     s.lat = P.lat;
     s.overlap = 64 * (size_t)P.lat;
-    if ((int)s.overlap > kMaxSeamOverlap)
-      return bail(c->fail(DSDGPU_ERR_UNSUPPORTED, "overlap too long for the seam kernel"));
     int k = -1;
     for (size_t q = 0; q < pl->cls.size(); q++)
       if (memcmp(&pl->cls[q].P, &P, sizeof P) == 0) { k = (int)q; break; }
@@ -736,6 +735,7 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
       {(void**)&pl->d_qfir, sizeof(double) * 255},
       {(void**)&pl->d_centers, sizeof(long long) * (size_t)std::max(1, ncen)},
       {(void**)&pl->d_rms, sizeof(double) * (size_t)std::max(1, ncen)},
+      {(void**)&pl->d_seam_scr, das_seam_global_bytes(pl->max_ovl) * (size_t)ntasks},
   };
   size_t total = 0;
   for (const Part& p : parts) total += align_up(p.bytes, 256);

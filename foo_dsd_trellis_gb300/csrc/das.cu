@@ -131,17 +131,23 @@ __global__ void das_seed_from_best_kernel(const SdmCtx* __restrict__ ctxs, int f
 }
 
 // ---- seam search, one CTA per boundary (src/dsp_plugin.c:2455-2652) ----
+// kGlobal: overlaps above kMaxSeamOverlap (traceback latencies above 256) keep
+// the match flags, the prefix sums and the density map in a global scratch
+// slice per boundary (das_seam_global_bytes) instead of shared memory.
+template <bool kGlobal>
 __global__ void __launch_bounds__(kSeamThreads)
 das_seam_kernel(const SeamTask* __restrict__ tasks, int ntasks, const double* __restrict__ qfir2,
-                int* __restrict__ bp_out) {
+                int* __restrict__ bp_out, unsigned char* __restrict__ gscr, size_t gstride) {
   const int ti = blockIdx.x;
   if (ti >= ntasks) return;
   const SeamTask T = tasks[ti];
   const int lat = T.lat;
   const int L = T.ovl_len;
   extern __shared__ unsigned char smraw[];
-  int8_t* dif = (int8_t*)smraw;                       // next - prev in {-1, 0, 1} (x2 later)
-  int* dmap = (int*)(smraw + ((L + 15) & ~15));       // density map, L + 1 ints
+  unsigned char* base = kGlobal ? gscr + (size_t)ti * gstride : smraw;
+  int8_t* dif = (int8_t*)base;                        // next - prev in {-1, 0, 1} (x2 later)
+  int* dmap = (int*)(base + ((L + 15) & ~15));        // prefix sums, then the density map
+  int* win = kGlobal ? dmap + ((L + 1 + 3) & ~3) : dmap;   // density map (global form)
   __shared__ int red[32];
   __shared__ int s_peak, s_pp, s_nq, s_best;
   __shared__ int qpos[kMaxQ + 1], qden[kMaxQ + 1];
@@ -194,10 +200,18 @@ das_seam_kernel(const SeamTask* __restrict__ tasks, int ntasks, const double* __
     }
   }
   __syncthreads();
-  // convert the prefix into window counts in place, via registers
+  // convert the prefix into window counts: in place via registers (shared
+  // form, at most 32 per thread), or into their own array (global form)
   int* pref = dmap;
-  int myv[32];
-  {
+  if constexpr (kGlobal) {
+    for (int p = threadIdx.x; p < L; p += blockDim.x) {
+      const int hi = min(L, p + half_w), lo = max(0, p - half_w);
+      win[p] = pref[hi] - pref[lo];
+    }
+    __syncthreads();
+    dmap = win;
+  } else {
+    int myv[32];
     int cnt = 0;
     for (int p = threadIdx.x; p < L && cnt < 32; p += blockDim.x, cnt++) {
       const int hi = min(L, p + half_w), lo = max(0, p - half_w);
@@ -391,19 +405,33 @@ size_t das_seam_smem(int max_ovl) {
   return ((size_t)(max_ovl + 15) & ~(size_t)15) + sizeof(int) * (size_t)(max_ovl + 1) + 64;
 }
 
+size_t das_seam_global_bytes(int max_ovl) {
+  if (max_ovl <= kMaxSeamOverlap) return 0;
+  const size_t L = (size_t)max_ovl;
+  return (((L + 15) & ~(size_t)15) + sizeof(int) * (((L + 1 + 3) & ~(size_t)3) + L) + 255) &
+         ~(size_t)255;
+}
+
 int das_seam_prepare(int max_ovl) {
+  if (max_ovl > kMaxSeamOverlap) return 0;
   const size_t smem = das_seam_smem(max_ovl);
   if (smem <= 48 * 1024) return 0;
-  return cudaFuncSetAttribute(das_seam_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(das_seam_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)smem) == cudaSuccess ? 0 : -1;
 }
 
 int launch_das_seams(const SeamTask* d_tasks, int ntasks, int max_ovl, const double* d_qfir2,
-                     int* d_bp, cudaStream_t stream) {
+                     int* d_bp, unsigned char* d_gscratch, cudaStream_t stream) {
   if (ntasks <= 0) return 0;
-  if (max_ovl > kMaxSeamOverlap) return -2;
-  const size_t smem = das_seam_smem(max_ovl);
-  das_seam_kernel<<<(unsigned)ntasks, kSeamThreads, smem, stream>>>(d_tasks, ntasks, d_qfir2, d_bp);
+  if (max_ovl > kMaxSeamOverlap) {
+    if (!d_gscratch) return -2;
+    das_seam_kernel<true><<<(unsigned)ntasks, kSeamThreads, 0, stream>>>(
+        d_tasks, ntasks, d_qfir2, d_bp, d_gscratch, das_seam_global_bytes(max_ovl));
+  } else {
+    const size_t smem = das_seam_smem(max_ovl);
+    das_seam_kernel<false><<<(unsigned)ntasks, kSeamThreads, smem, stream>>>(d_tasks, ntasks,
+                                                                             d_qfir2, d_bp, nullptr, 0);
+  }
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -686,10 +714,17 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
                     cudaMemcpyHostToDevice, c->stream);
     int maxL = 0;
     for (auto& t : tasks) maxL = std::max(maxL, t.ovl_len);
-    if (maxL > kMaxSeamOverlap) return c->fail(DSDGPU_ERR_UNSUPPORTED, "overlap too long for the seam kernel");
+    unsigned char* gscr = nullptr;
+    const size_t gb = das_seam_global_bytes(maxL);
+    if (gb) {
+      // overlaps above the shared-memory form: per-boundary scratch in HBM
+      rc = ensure_dev(c, &c->d_das_seam_scr, &c->das_seam_scr_cap, gb * tasks.size(), "seam scratch");
+      if (rc) return rc;
+      gscr = c->d_das_seam_scr;
+    }
     if (das_seam_prepare(maxL) != 0) return c->cuda_fail(cudaGetLastError(), "seam kernel attributes");
     rc = launch_das_seams(c->d_das_tasks, (int)tasks.size(), maxL, c->d_das_qfir, c->d_das_bp,
-                          c->stream);
+                          gscr, c->stream);
     if (rc == -2) return c->fail(DSDGPU_ERR_UNSUPPORTED, "overlap too long for the seam kernel");
     if (rc) return c->cuda_fail(cudaGetLastError(), "seam launch");
     c->launches++;

@@ -45,8 +45,11 @@ int launch_das_rms(const double* x, const long long* d_centers, int n, double* d
                    cudaStream_t stream);
 size_t das_seam_smem(int max_ovl);
 int das_seam_prepare(int max_ovl);   // kernel attributes (call outside stream capture)
+// Overlaps above kMaxSeamOverlap need d_gscratch of ntasks x
+// das_seam_global_bytes(max_ovl) bytes (-2 without it).
+size_t das_seam_global_bytes(int max_ovl);
 int launch_das_seams(const SeamTask* d_tasks, int ntasks, int max_ovl, const double* d_qfir2,
-                     int* d_bp, cudaStream_t stream);   // -2: overlap above kMaxSeamOverlap
+                     int* d_bp, unsigned char* d_gscratch, cudaStream_t stream);
 int launch_das_assemble(const AssemblePiece* d_pieces, int npieces, const int* d_bp, uint8_t* out,
                         size_t out_stride, int nch, int S, const SegBuf* d_segbuf,
                         cudaStream_t stream);

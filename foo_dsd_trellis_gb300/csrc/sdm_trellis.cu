@@ -51,6 +51,14 @@ __device__ __forceinline__ double clampd(double v, double lim) {
   return v;
 }
 
+// A ring word kept opaque in a register: without it the word-select loops over
+// a 64-word ring compile to an indexed local-memory array.
+template <int RW>
+__device__ __forceinline__ uint32_t reg_word(uint32_t v) {
+  if constexpr (RW > kRegRingWords) asm volatile("" : "+r"(v));
+  return v;
+}
+
 template <int LPJ>
 __device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int src, unsigned hm) {
   return (unsigned long long)__shfl_sync(hm, (long long)v, src, LPJ);
@@ -139,6 +147,7 @@ __host__ __device__ constexpr int min_lanes(int K) {
 // Fixed rule (the batch plan sizes its job slots with it): a requested width,
 // else a whole warp for K > 16 and a half-warp below.
 int lanes_per_job(const SdmParams& P) {
+  if (P.lat > 32 * kRegRingWords) return 32;   // the wide-ring kernel: one job per warp
   const int lo = min_lanes(P.cands);
   if (P.lanes > 0) return P.lanes > lo ? P.lanes : lo;
   return lo > 16 ? 32 : 16;
@@ -165,7 +174,7 @@ static int resident_warps() {
 // (10 s stereo same-rate DSD128, 1722 jobs: K = 16 at 32 lanes 289 vs 256 at
 // 16 lanes DSD Msamples/s; K = 2 at 2 lanes 174, at 16 lanes 309).
 static int launch_lanes(const SdmParams& P, int njobs, int max_blocks) {
-  if (P.lanes > 0 || max_blocks > 0) return lanes_per_job(P);
+  if (P.lanes > 0 || max_blocks > 0 || P.lat > 32 * kRegRingWords) return lanes_per_job(P);
   const int lo = min_lanes(P.cands);
   const int slots = resident_warps();
   int lanes = 32;
@@ -228,7 +237,7 @@ __host__ __device__ constexpr int sort_stages() {
 // most of every FP64 warp instruction idle.  `lane` is the lane within the
 // job, `hm` the job's lanes; warp intrinsics use hm and width LPJ, ballots
 // are shifted to the job's bits.
-template <int N, int LPJ>
+template <int N, int LPJ, int RW>
 __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restrict__ ctxs,
                         WarpSmem<LPJ>& sm, int* __restrict__ status) {
   constexpr int S = WarpSmem<LPJ>::S;
@@ -250,12 +259,12 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
   double s[N];
   double cost = 0.0;
   unsigned long long path = 0;
-  uint32_t ring[kRegRingWords];
+  uint32_t ring[RW];
   int nxt = 0, slot = 0;
 #pragma unroll
   for (int k = 0; k < N; k++) s[k] = 0.0;
 #pragma unroll
-  for (int w = 0; w < kRegRingWords; w++) ring[w] = 0;
+  for (int w = 0; w < RW; w++) ring[w] = 0;
   if (lane < n) {
 #pragma unroll
     for (int k = 0; k < N; k++) s[k] = src->s[lane][k];
@@ -264,7 +273,7 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     nxt = src->next[lane];
     slot = src->slot[lane];
 #pragma unroll
-    for (int w = 0; w < kRegRingWords; w++)
+    for (int w = 0; w < RW; w++)
       if (w < W) ring[w] = src->ring[lane][w];
   }
   for (int i = lane; i < 2 * S; i += LPJ) {
@@ -353,8 +362,10 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
       q = (path << 1) & mask;
       uint32_t wv = 0;
 #pragma unroll
-      for (int w = 0; w < kRegRingWords; w++)
-        if (w == (next_pos >> 5)) wv = ring[w];
+      for (int w = 0; w < RW; w++) {
+        const uint32_t r = reg_word<RW>(ring[w]);
+        if (w == (next_pos >> 5)) wv = r;
+      }
       new_next = (int)((wv >> (next_pos & 31)) & 1u);
       sm.path[nb][2 * lane] = q;
       sm.path[nb][2 * lane + 1] = q | 1ull;
@@ -614,9 +625,9 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     }
     const unsigned long long npath = shfl64<LPJ>(q, pp, hm) | (unsigned long long)hh;
     const int nnext = __shfl_sync(hm, new_next, pp, LPJ);
-    uint32_t nring[kRegRingWords];
+    uint32_t nring[RW];
 #pragma unroll
-    for (int w = 0; w < kRegRingWords; w++)
+    for (int w = 0; w < RW; w++)
       nring[w] = (w < W) ? __shfl_sync(hm, ring[w], pp, LPJ) : 0u;
     if (surv) {
       cs0 = hh ? f01 : f00;
@@ -637,8 +648,8 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
       nxt = nnext;
       slot = Ls;
 #pragma unroll
-      for (int w = 0; w < kRegRingWords; w++) {
-        uint32_t v = nring[w];
+      for (int w = 0; w < RW; w++) {
+        uint32_t v = reg_word<RW>(nring[w]);
         if (w == (pos >> 5)) v = (v & ~(1u << (pos & 31))) | ((uint32_t)hh << (pos & 31));
         ring[w] = v;
       }
@@ -673,7 +684,7 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
     dst->next[lane] = (uint8_t)nxt;
     dst->slot[lane] = (uint8_t)slot;
 #pragma unroll
-    for (int w = 0; w < kRegRingWords; w++)
+    for (int w = 0; w < RW; w++)
       if (w < W) dst->ring[lane][w] = ring[w];
   }
   __syncwarp(hm);
@@ -713,12 +724,50 @@ sdm_jobs_kernel(SdmParams P, const SdmJob* __restrict__ jobs, int njobs,
     j = __shfl_sync(hm, j, 0, LPJ);
     if (j >= njobs) break;
     const SdmJob job = jobs[j];
-    run_job<N, LPJ>(P, job, ctxs, sm, status);
+    run_job<N, LPJ, kRegRingWords>(P, job, ctxs, sm, status);
     __syncwarp(hm);
   }
 }
 
+// Traceback latencies above 256 (the reference allows up to 2048,
+// include/trellis.h:13): the whole 2048-bit ring in registers, one job per
+// warp; 8 CTAs per SM leave 255 registers a thread.
+template <int N>
+__global__ void __launch_bounds__(32, 8)
+sdm_jobs_wide_kernel(SdmParams P, const SdmJob* __restrict__ jobs, int njobs,
+                     int* __restrict__ job_counter, SdmCtx* __restrict__ ctxs,
+                     int* __restrict__ status) {
+  extern __shared__ __align__(16) unsigned char sdm_smem_raw[];
+  WarpSmem<32>& sm = reinterpret_cast<WarpSmem<32>*>(sdm_smem_raw)[0];
+  for (;;) {
+    int j = 0;
+    if ((threadIdx.x & 31) == 0) j = atomicAdd(job_counter, 1);
+    j = __shfl_sync(kFull, j, 0);
+    if (j >= njobs) break;
+    const SdmJob job = jobs[j];
+    run_job<N, 32, kRingWords>(P, job, ctxs, sm, status);
+    __syncwarp();
+  }
+}
+
 int sdm_jobs_per_cta(const SdmParams& P) { return 32 / lanes_per_job(P); }
+
+static int launch_wide(const SdmParams& P, dim3 grid, const SdmJob* d_jobs, int njobs,
+                       int* d_counter, SdmCtx* d_ctxs, int* d_status, cudaStream_t stream) {
+  const size_t smem = sizeof(WarpSmem<32>);
+  switch (P.order) {
+#define DSD_CASE(NN)                                                                          \
+  case NN:                                                                                    \
+    sdm_jobs_wide_kernel<NN><<<grid, 32, smem, stream>>>(P, d_jobs, njobs, d_counter, d_ctxs, \
+                                                         d_status);                           \
+    break;
+    DSD_CASE(2) DSD_CASE(3) DSD_CASE(4) DSD_CASE(5) DSD_CASE(6)
+    DSD_CASE(7) DSD_CASE(8) DSD_CASE(9) DSD_CASE(10)
+#undef DSD_CASE
+    default: return -1;
+  }
+  return 0;
+}
 
 template <int LPJ>
 static int launch_lpj(const SdmParams& P, dim3 grid, const SdmJob* d_jobs, int njobs,
@@ -769,6 +818,11 @@ int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_
   cudaMemsetAsync(d_counter, 0, sizeof(int), stream);
   const dim3 grid(blocks);
   int rc = -1;
+  if (P.lat > 32 * kRegRingWords) {
+    rc = launch_wide(P, grid, d_jobs, njobs, d_counter, d_ctxs, d_status, stream);
+    if (rc) return rc;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+  }
   switch (lanes) {
     case 32: rc = launch_lpj<32>(P, grid, d_jobs, njobs, d_counter, d_ctxs, d_status, stream); break;
     case 16: rc = launch_lpj<16>(P, grid, d_jobs, njobs, d_counter, d_ctxs, d_status, stream); break;
@@ -780,6 +834,6 @@ int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int sdm_max_lat_in_registers() { return 32 * kRegRingWords; }
+int sdm_max_lat_in_registers() { return 32 * kRingWords; }
 
 }  // namespace dsdgpu

@@ -169,3 +169,24 @@ def test_batch_small_k_path_table_parameters(oracle):
         got = plan.out_view(i).cpu().numpy()
         assert got.shape == want.shape and np.array_equal(got, want), f"stream {i}"
     plan.close()
+
+
+def test_batch_long_latency_with_a_short_one(oracle):
+    """A stream at lat 600 (overlap 38,400: the wide-ring SDM kernel and the
+    seam search in HBM scratch) beside one at lat 16, in one plan."""
+    from foo_dsd_trellis_gb300 import ntf
+    from foo_dsd_trellis_gb300.batch import OUT_BITS, BatchPlan, StreamSpec
+    specs = [StreamSpec(44100, 5644800, 2, 2600, ntf.auto_select(5644800), cands=4, depth=8,
+                        lat=600, gain=GAIN),
+             StreamSpec(48000, 6144000, 1, 1500, ntf.auto_select(6144000), cands=8, depth=16,
+                        lat=16, gain=GAIN)]
+    xs = [_noise(s.frames, s.channels, 31 + i) for i, s in enumerate(specs)]
+    plan = BatchPlan(specs, seg_len=65536, output_format=OUT_BITS)
+    assert plan.info()["classes"] == 2
+    plan.load([torch.from_numpy(x).cuda() for x in xs])
+    plan.run()
+    for i, s in enumerate(specs):
+        want, _ = _oracle_stream(oracle, s, xs[i], 65536, OUT_BITS)
+        got = plan.out_view(i).cpu().numpy()
+        assert got.shape == want.shape and np.array_equal(got, want), f"stream {i}"
+    plan.close()

@@ -48,6 +48,18 @@ def test_das_k32_depth64_lat128(oracle):
     assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("mode", [0, 1], ids=["full_parallel", "seg0_first"])
+def test_das_long_latency(oracle, mode):
+    """lat 300 (overlap 64 * lat = 19,200) on the wide-ring kernel, both
+    seeding modes."""
+    f = _ntf("clans-6", 5644800)
+    x = np.stack([multitone(200000, 21) * 1.8, multitone(200000, 22) * 1.4])
+    want, ws, got, gs = _run(oracle, f, 16, 8, 300, x, seg_len=40000, seed_mode=mode)
+    assert got.shape == want.shape
+    assert list(gs) == list(ws)
+    assert np.array_equal(got, want)
+
+
 def test_das_quiet_boundary_reposition(oracle):
     """A near-silent stretch around a seg>=2 boundary moves it (RMS search)."""
     f = _ntf("clans-5", 2822400)

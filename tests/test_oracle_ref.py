@@ -96,6 +96,18 @@ def test_sdm_restatement_equals_reference_random(ref, wide, oracle):
         _cmp(oracle, wide if depth > 32 else ref, f, depth, K, lat, lim, x, blocks)
 
 
+def test_sdm_long_latencies_equal_reference(ref, wide, oracle):
+    """Traceback latencies above 256 up to SDM_TRELLIS_MAX_LAT = 2048
+    (include/trellis.h:13, the plugin's range 16-2048, src/config.c:509-510)."""
+    t = _table(ref, oracle)
+    rng = np.random.default_rng(77)
+    for lat, K, depth in [(257, 32, 64), (300, 2, 4), (777, 16, 32), (1024, 5, 48), (2048, 32, 32)]:
+        f = t[rng.integers(len(t))]
+        x = sdm_input(lat + 3000, int(rng.integers(1 << 30)), amp=0.5)
+        blocks = [int(rng.integers(1, lat + 500)) for _ in range(8)]
+        _cmp(oracle, wide if depth > 32 else ref, f, depth, K, lat, 0.0, x, blocks)
+
+
 def test_sdm_k32_long_runs(ref, wide, oracle):
     """K = 32 over long inputs, where the act[32] store lands on path_hash[0]."""
     t = {(e[0], e[2]): e for e in _table(ref, oracle)}

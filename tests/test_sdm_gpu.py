@@ -83,6 +83,36 @@ def test_streaming_blocks_and_drain(oracle):
     np.testing.assert_array_equal(got, want)
 
 
+@pytest.mark.parametrize("K,depth,lat,lim", [(32, 64, 257, 0.0), (32, 32, 2048, 0.0),
+                                             (16, 48, 1000, 2.0), (2, 4, 512, 0.0),
+                                             (5, 16, 300, 0.0)])
+def test_long_latency_streaming_and_drain(oracle, K, depth, lat, lim):
+    """Latencies above 256 (up to the reference's 2048) take the wide-ring
+    kernel: ragged streamed blocks over two channels, then drain."""
+    f = _ntf("clans-7", 5644800)
+    nch = 2
+    xs = [sdm_input(lat + 9000, seed=lat + c, amp=0.5) for c in range(nch)]
+    refs = [_ora(oracle, f, depth, K, lat, lim) for _ in range(nch)]
+    g = _gpu_sdm(f, depth, K, lat, lim, nctx=nch)
+    rng = np.random.default_rng(lat)
+    pos = 0
+    n = len(xs[0])
+    while pos < n:
+        b = min(int(rng.integers(1, 2 * lat)), n - pos)
+        blk = np.stack([x[pos:pos + b] for x in xs])
+        pos += b
+        got = g.process_block(torch.from_numpy(blk).cuda())
+        for c in range(nch):
+            np.testing.assert_array_equal(got[c].cpu().numpy(), oracle.sdm_bits(refs[c], blk[c]))
+    got = g.drain(lat + 10, 0, nch)
+    for c in range(nch):
+        want = (refs[c].drain(lat + 10) > 0).astype(np.uint8)
+        assert len(want) == lat
+        np.testing.assert_array_equal(got[c].cpu().numpy(), want)
+    q = g.query(1)
+    np.testing.assert_array_equal(q["best_state"], refs[1].best_state())
+
+
 def test_short_block_then_drain(oracle):
     """Fewer samples than the latency, then drain (test/test_trellis.c:122-140)."""
     f = _ntf("clans-5", 2822400)
