@@ -236,6 +236,41 @@ def test_small_k_streaming_channels_and_drain(oracle, K, depth, lat, lim):
         np.testing.assert_array_equal(q["best_state"], refs[c].best_state())
 
 
+@pytest.mark.parametrize("K,depth", [(2, 4), (4, 8), (1, 6)])
+def test_kernels_share_the_context_format(oracle, K, depth):
+    """One context carried through every SDM kernel in turn: the per-thread
+    kernel (more jobs than the split kernel's cap), the lane-split kernel (few
+    jobs), the warp kernel at 2 and 32 lanes (DSDGPU_OPT_SDM_LANES), then the
+    split kernel again, each call continuing the previous one's state."""
+    from foo_dsd_trellis_gb300 import _lib
+    f = _ntf("clans-6", 5644800)
+    many = 2600          # above the split kernel's 2 x 2 x 4 x 152 jobs (K <= 2)
+    g = _gpu_sdm(f, depth, K, 32, 0.0, nctx=many)
+    refs = [_ora(oracle, f, depth, K, 32) for _ in range(2)]
+    x = np.stack([multitone(15000, seed=90 + c) * 0.7 for c in range(2)])
+    pos = 0
+    for stage, ln in (("all", 3000), ("split", 2500), ("lanes2", 3100), ("lanes32", 2900),
+                      ("split", 3500)):
+        blk = x[:, pos:pos + ln]
+        pos += ln
+        if stage == "all":
+            if K > 2:
+                continue
+            xa = np.zeros((many, ln))
+            xa[:2] = blk
+            got = g.process_block(torch.from_numpy(xa).cuda())[:2]
+        else:
+            g.set_option(_lib.OPT_SDM_LANES, {"split": 0, "lanes2": 2, "lanes32": 32}[stage])
+            got = g.process_block(torch.from_numpy(np.ascontiguousarray(blk)).cuda())
+        for c in range(2):
+            np.testing.assert_array_equal(got[c].cpu().numpy(), oracle.sdm_bits(refs[c], blk[c]),
+                                          err_msg=stage)
+    g.set_option(_lib.OPT_SDM_LANES, 0)
+    got = g.drain(64, 0, 2)
+    for c in range(2):
+        np.testing.assert_array_equal(got[c].cpu().numpy(), (refs[c].drain(64) > 0).astype(np.uint8))
+
+
 def test_small_k_many_jobs_take_the_per_thread_kernel(oracle):
     """More K <= 2 jobs than the lane-split kernel keeps resident (2,600
     channels of one launch) run one job per thread; every channel equals the
