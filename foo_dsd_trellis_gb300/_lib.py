@@ -97,6 +97,7 @@ SAMERATE_LOWPASS = 1
 
 OPT_SDM_SELECT = 1
 OPT_SDM_LANES = 2
+OPT_SDM_BALANCE = 3
 SELECT_FAST, SELECT_EXACT, SELECT_VERIFY = 0, 1, 2
 
 DAS_FULL_PARALLEL = 0

@@ -21,6 +21,14 @@ int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_
                     SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream);
 int init_contexts(SdmCtx* d_ctxs, int first, int count, int keep_counters, cudaStream_t stream);
 int sdm_jobs_per_cta(const SdmParams& P);   // 32 / lanes_per_job(P)
+// Balanced launches (sdm_trellis.cu): warps per SM sub-partition, or 0 for a
+// plain launch; the queue entries the parts need; the launch itself.
+int sdm_balanced_warps(const SdmParams& P, const SdmJob* jobs, int njobs, int sms,
+                       long long part_len);
+long long sdm_parts_total(const SdmJob* jobs, int njobs, long long part_len);
+int launch_sdm_parts(const SdmParams& P, const SdmJob* d_jobs, int njobs, long long part_len,
+                     unsigned long long* d_queue, long long total, int warps_per_pipe, int sms,
+                     SdmCtx* d_ctxs, int* d_status, cudaStream_t stream);
 int lanes_per_job(const SdmParams& P);      // the fixed width of capped launches
 int sdm_max_lat_in_registers();
 int launch_pack_dop(const uint8_t* bits, size_t stride, int nch, size_t frames, int phase,
@@ -64,12 +72,15 @@ struct dsdgpu_context {
   dsdgpu::SdmParams sdm{};
   int sdm_mode = 0;               // selection strategy (DSDGPU_OPT_SDM_SELECT)
   int sdm_lanes = 0;              // lanes per SDM job (DSDGPU_OPT_SDM_LANES), 0 = automatic
+  int sdm_balance = 1;            // balanced launches allowed (DSDGPU_OPT_SDM_BALANCE)
   int nctx = 0;
   dsdgpu::SdmCtx* d_ctx = nullptr;
   std::vector<int64_t> pending;   // latency fill per context (host mirror)
   std::vector<int> draining;
   dsdgpu::SdmJob* d_jobs = nullptr;
   int jobs_cap = 0;
+  unsigned long long* d_parts = nullptr;   // part queue of balanced SDM launches
+  long long parts_cap = 0;
 
   // FIR chain
   bool fir_ready = false;
@@ -151,6 +162,9 @@ struct dsdgpu_context {
     d_box_hist = nullptr;
     if (d_ctx) cudaFree(d_ctx);
     if (d_jobs) cudaFree(d_jobs);
+    if (d_parts) cudaFree(d_parts);
+    d_parts = nullptr;
+    parts_cap = 0;
     if (d_scratch) cudaFree(d_scratch);
     if (d_fir_hist) cudaFree(d_fir_hist);
     d_fir_hist = nullptr;

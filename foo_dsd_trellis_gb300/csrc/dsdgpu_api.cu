@@ -135,6 +135,27 @@ int dsdgpu_context::run_jobs(const std::vector<SdmJob>& jobs) {
   SdmParams P = sdm;
   P.mode = sdm_mode;
   P.lanes = sdm_lanes;
+  // many long jobs a little above a whole number of warps per FP64 pipe: the
+  // balanced launch (parts of 2,048 samples queued over w warps per pipe)
+  constexpr long long kPartLen = 2048;
+  const int wpp = (max_blocks == 0 && sdm_balance)
+                      ? sdm_balanced_warps(P, jobs.data(), n, num_sms, kPartLen) : 0;
+  if (wpp > 0) {
+    const long long total = sdm_parts_total(jobs.data(), n, kPartLen);
+    if (total + 2 > parts_cap) {
+      if (d_parts) cudaFree(d_parts);
+      d_parts = nullptr;
+      parts_cap = 0;
+      e = cudaMalloc(&d_parts, sizeof(unsigned long long) * (size_t)(total + 2));
+      if (e != cudaSuccess) return cuda_fail(e, "part queue allocation");
+      parts_cap = total + 2;
+    }
+    if (launch_sdm_parts(P, d_jobs, n, kPartLen, d_parts, total, wpp, num_sms, d_ctx, d_status,
+                         stream) != 0)
+      return cuda_fail(cudaGetLastError(), "sdm kernel launch");
+    launches += 2;
+    return check_status();
+  }
   if (launch_sdm_jobs(P, d_jobs, n, d_counter, d_ctx, d_status, max_blocks, stream) != 0)
     return cuda_fail(cudaGetLastError(), "sdm kernel launch");
   launches++;
@@ -225,6 +246,10 @@ int dsdgpu_set_option(dsdgpu_context_t* c, int option, int value) {
       if (value != 0 && (value < 2 || value > 32 || (value & (value - 1))))
         return c->fail(DSDGPU_ERR_ARG, "lanes per job must be 0 or a power of two in 2..32");
       c->sdm_lanes = value;
+      return DSDGPU_OK;
+    case DSDGPU_OPT_SDM_BALANCE:
+      if (value != 0 && value != 1) return c->fail(DSDGPU_ERR_ARG, "balance must be 0 or 1");
+      c->sdm_balance = value;
       return DSDGPU_OK;
     default:
       return c->fail(DSDGPU_ERR_ARG, "unknown option");

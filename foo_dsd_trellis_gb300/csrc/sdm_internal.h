@@ -81,6 +81,7 @@ enum : int {
   kStatusOk = 0,
   kStatusChainLimit = 1,   // a path-hash chain walk exceeded its bound
   kStatusVerifyMismatch = 2,  // verify mode: the fast selection disagreed with the serial one
+  kStatusQueueWait = 3,    // a balanced launch's wait for a queued job part gave up
 };
 
 }  // namespace dsdgpu

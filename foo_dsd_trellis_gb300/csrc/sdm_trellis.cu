@@ -750,6 +750,148 @@ sdm_jobs_wide_kernel(SdmParams P, const SdmJob* __restrict__ jobs, int njobs,
   }
 }
 
+// ---- balanced launches: jobs cut into parts, parts queued ----
+// One job per warp pins a job to one SM sub-partition, and every FP64 warp
+// instruction of the warps there shares its FP64 pipe.  1,874 DAS segments
+// over 152 SMs put 4 warps on 50 sub-partitions and 3 on the rest, and the
+// launch lasts as long as the slowest 4-warp pipe (measured: 1,824 jobs, 3 per
+// sub-partition, ran at 0.86 of the FP64 rate, 1,874 at 0.79).  A balanced
+// launch holds exactly w warps per sub-partition, cuts every job into parts
+// of part_len samples, and queues the parts: a warp that finishes part p of
+// job j stores the context (as a streamed block boundary does), publishes
+// part p + 1 at the queue's tail, and takes the next entry at its head, so
+// the jobs move between warps and every pipe stays loaded to the end.
+// Queue layout: [0] head, [1] tail, [2 ..] entries (part << 32 | job; empty
+// ~0).  A wait for an entry that is not yet published is bounded.
+constexpr long long kPartWaitCycles = 8000000000ll;   // ~4 s at 2 GHz
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// The rare wait for an entry not yet published (out of line: inlined, its
+// loop changes the register allocation of the step loop).
+__device__ __noinline__ unsigned long long wait_entry(const unsigned long long* p, int* status) {
+  unsigned long long e = ~0ull;
+  const long long t0 = clock64();
+  do {
+    __nanosleep(1000);
+    e = ld_acquire_u64(p);
+  } while (e == ~0ull && clock64() - t0 < kPartWaitCycles);
+  if (e == ~0ull && (threadIdx.x & 31) == 0) atomicMax(status, kStatusQueueWait);
+  return e;
+}
+
+template <int N>
+__global__ void __launch_bounds__(32, 13)
+sdm_parts_kernel(SdmParams P, const SdmJob* __restrict__ jobs, long long part_len,
+                 unsigned long long* __restrict__ queue, long long total,
+                 SdmCtx* __restrict__ ctxs, int* __restrict__ status) {
+  extern __shared__ __align__(16) unsigned char sdm_smem_raw[];
+  WarpSmem<32>& sm = reinterpret_cast<WarpSmem<32>*>(sdm_smem_raw)[0];
+  const int lane = threadIdx.x & 31;
+  unsigned long long* head = queue;
+  unsigned long long* tail = queue + 1;
+  unsigned long long* ent = queue + 2;
+  for (;;) {
+    unsigned long long idx = 0;
+    if (lane == 0) idx = atomicAdd(head, 1ull);
+    idx = __shfl_sync(kFull, idx, 0);
+    if (idx >= (unsigned long long)total) break;
+    // every lane reads the entry with acquire semantics (one transaction)
+    unsigned long long e = ld_acquire_u64(ent + idx);
+    if (e == ~0ull) e = wait_entry(ent + idx, status);
+    if (e == ~0ull) break;
+    __threadfence();   // the previous part's context is read after the entry
+    const int j = (int)(e & 0xffffffffull);
+    const long long p = (long long)(e >> 32);
+    const SdmJob jb = jobs[j];
+    const long long off = p * part_len;
+    const long long rem = jb.n_in - off;
+    SdmJob pj = jb;
+    pj.n_in = rem < part_len ? rem : part_len;
+    if (jb.in) pj.in = jb.in + off;
+    const long long sk = jb.skip_out - off;
+    pj.skip_out = sk <= 0 ? 0 : (sk < pj.n_in ? sk : pj.n_in);
+    pj.out = jb.out + (off > jb.skip_out ? off - jb.skip_out : 0);
+    if (p > 0) {
+      // later parts continue from the job's own context
+      pj.copy_from = -1;
+      pj.seed_state = nullptr;
+    }
+    const bool more = off + pj.n_in < jb.n_in;
+    run_job<N, 32, kRegRingWords>(P, pj, ctxs, sm, status);
+    __threadfence();   // this part's context and decisions before its successor's entry
+    __syncwarp();
+    if (lane == 0 && more) {
+      const unsigned long long t = atomicAdd(tail, 1ull);
+      atomicExch(ent + t, ((unsigned long long)(p + 1) << 32) | (unsigned long long)(unsigned)j);
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void parts_queue_init_kernel(unsigned long long* queue, long long total, int njobs) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    queue[0] = 0ull;
+    queue[1] = (unsigned long long)njobs;
+  }
+  if (i < total) queue[2 + i] = i < njobs ? (unsigned long long)i : ~0ull;
+}
+
+// Warps per sub-partition of a balanced launch of these jobs on `sms` SMs, or
+// 0 when the plain launch is kept: K > 16 (a whole warp per job), no width
+// or block cap requested, every job on its own context with its state kept,
+// and the jobs only slightly above a whole number of warps per pipe (the
+// parts of the extra jobs are shared out; a plain launch would give those
+// pipes one warp more than the rest for the whole launch).
+int sdm_balanced_warps(const SdmParams& P, const SdmJob* jobs, int njobs, int sms,
+                       long long part_len) {
+  if (P.lanes != 0 || lanes_per_job(P) != 32 || P.lat > 32 * kRegRingWords || sms <= 0) return 0;
+  const long long pipes = 4ll * sms;
+  if (njobs <= pipes) return 0;
+  const long long w = (njobs + pipes - 1) / pipes;   // warps per pipe of the plain launch
+  if (w < 2 || w > 4 || njobs % pipes == 0) return 0;
+  if ((double)njobs > 1.10 * (double)((w - 1) * pipes)) return 0;
+  long long samples = 0;
+  for (int i = 0; i < njobs; i++) {
+    if (jobs[i].ctx < 0 || (jobs[i].flags & kJobNoStore)) return 0;
+    samples += jobs[i].n_in;
+  }
+  if (samples < 8 * part_len * (long long)njobs) return 0;   // parts too coarse to share out
+  return (int)(w - 1);
+}
+
+long long sdm_parts_total(const SdmJob* jobs, int njobs, long long part_len) {
+  long long total = 0;
+  for (int i = 0; i < njobs; i++)
+    total += jobs[i].n_in > 0 ? (jobs[i].n_in + part_len - 1) / part_len : 1;
+  return total;
+}
+
+int launch_sdm_parts(const SdmParams& P, const SdmJob* d_jobs, int njobs, long long part_len,
+                     unsigned long long* d_queue, long long total, int warps_per_pipe, int sms,
+                     SdmCtx* d_ctxs, int* d_status, cudaStream_t stream) {
+  parts_queue_init_kernel<<<(unsigned)((total + 255) / 256), 256, 0, stream>>>(d_queue, total, njobs);
+  const dim3 grid((unsigned)(4 * warps_per_pipe * sms));
+  const size_t smem = sizeof(WarpSmem<32>);
+  switch (P.order) {
+#define DSD_CASE(NN)                                                                        \
+  case NN:                                                                                  \
+    sdm_parts_kernel<NN><<<grid, 32, smem, stream>>>(P, d_jobs, part_len, d_queue, total,   \
+                                                     d_ctxs, d_status);                     \
+    break;
+    DSD_CASE(2) DSD_CASE(3) DSD_CASE(4) DSD_CASE(5) DSD_CASE(6)
+    DSD_CASE(7) DSD_CASE(8) DSD_CASE(9) DSD_CASE(10)
+#undef DSD_CASE
+    default: return -1;
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 int sdm_jobs_per_cta(const SdmParams& P) { return 32 / lanes_per_job(P); }
 
 static int launch_wide(const SdmParams& P, dim3 grid, const SdmJob* d_jobs, int njobs,

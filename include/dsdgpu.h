@@ -147,6 +147,12 @@ const char *dsdgpu_last_error(const dsdgpu_context_t *ctx);
                                          (default), or 2, 4, 8, 16, 32 (raised to the
                                          next power of two >= K); 32 / lanes jobs share
                                          a warp.  Results do not depend on it. */
+#define DSDGPU_OPT_SDM_BALANCE  3   /* 1 (default): an uncapped launch of many long K > 16
+                                         jobs slightly above a whole number of warps per
+                                         FP64 pipe cuts the jobs into 2,048-sample parts
+                                         queued over an even number of warps per pipe;
+                                         0: one job per warp from start to end.  Results
+                                         do not depend on it. */
 int  dsdgpu_set_option(dsdgpu_context_t *ctx, int option, int value);
 
 /* Number of kernels this context has launched so far. */

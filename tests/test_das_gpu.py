@@ -112,3 +112,37 @@ def test_lanes_option_rejects_bad_widths():
     d = DasChannels(f.order, f.a, f.g, 8, 4, 16, num_channels=1)
     for bad in (1, 3, 12, 64, -2):
         assert d.L.dsdgpu_set_option(d.h, _lib.OPT_SDM_LANES, bad) == _lib.ERR_ARG
+
+
+def test_balanced_launch_equals_plain():
+    """Enough DAS segments to land 5 % above one warp per FP64 pipe: the
+    SDM launch cuts the segments into 2,048-sample parts queued over one warp
+    per pipe (DSDGPU_OPT_SDM_BALANCE); the stitched output and seams equal
+    the plain one-segment-per-warp launch, which the other tests pin to the
+    oracle, and the part boundaries are the streamed-block boundaries the
+    oracle tests cover."""
+    import ctypes as C
+    from foo_dsd_trellis_gb300 import _lib
+    from foo_dsd_trellis_gb300.das import DasChannels
+    f = _ntf("clans-7", 6144000)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    pipes = 4 * sms
+    S = (pipes + pipes // 20) // 2 + 1            # segments per channel, 2 channels
+    seg = 20000
+    x = np.stack([multitone(S * seg, 30) * 1.6, multitone(S * seg, 31) * 1.3])
+    fir = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    outs, launches = [], []
+    for balance in (1, 0):
+        d = DasChannels(f.order, f.a, f.g, 16, 32, 32, num_channels=2)
+        _lib.check(d.h, d.L.dsdgpu_set_option(d.h, _lib.OPT_SDM_BALANCE, balance))
+        n0 = C.c_uint64()
+        _lib.check(d.h, d.L.dsdgpu_launch_count(d.h, C.byref(n0)))
+        got, seams = d.process_chunk(fir, nsegs=S, seed_mode=0)
+        n1 = C.c_uint64()
+        _lib.check(d.h, d.L.dsdgpu_launch_count(d.h, C.byref(n1)))
+        outs.append((got.cpu().numpy(), list(seams)))
+        launches.append(n1.value - n0.value)
+        d.close()
+    assert launches[0] == launches[1] + 1        # the queue set-up: the balanced launch ran
+    assert outs[0][1] == outs[1][1]
+    assert np.array_equal(outs[0][0], outs[1][0])
