@@ -46,6 +46,7 @@ WL = dict(workload="dsd128_das_stereo_10s_multitone_pink", fs_in=48000, fs_out=6
           boxcar_taps=8, soft_clip=True, seed=1001)
 FP64_OPS_PER_CAND_SAMPLE = 5 * WL["ntf_order"] + 6   # (2N+1) mul + (3N+5) add
 SDM_DRAM_BYTES_PER_SAMPLE = 9.04                      # measured, see the traffic note below
+SDM_PARTS_DRAM_BYTES_PER_SAMPLE = 9.14                # the balanced launch's (parts kernel), measured
 
 
 def parse():
@@ -308,19 +309,24 @@ def run_ours(args):
     flops = sdm_samples * WL["cands"] * FP64_OPS_PER_CAND_SAMPLE
     achieved = flops / sdm_s / 1e12
     peak = fp64_peak / 1000.0
+    kernel = enc.last_sdm_kernel()
     roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None, "kernel": "sdm_jobs_kernel<7>",
+                "frac": achieved / peak, "traffic": None, "kernel": kernel,
                 "peak_source": "DADD/DMUL issue rate measured in this run (dsdgpu_probe_fp64); "
                                "MEASURED_PEAKS.json has no FP64 entry",
                 "algorithmic_flops_per_launch": flops,
                 "sdm_input_samples_per_launch": sdm_samples,
                 "flops_per_sample": WL["cands"] * FP64_OPS_PER_CAND_SAMPLE}
-    # DRAM bytes per launch: ncu's dram__bytes for the SDM kernel on the 4 s,
-    # 32,768-segment case (profiles/sdm_jobs_kernel_dsd128_das_4s.md) gave
-    # 9.04 B per SDM input sample; the traffic grows with the samples processed.
-    roofline["traffic"] = SDM_DRAM_BYTES_PER_SAMPLE * sdm_samples
-    roofline["traffic_source"] = ("ncu dram__bytes of a 73.7 M-sample launch, "
-                                  "scaled by SDM input samples")
+    # DRAM bytes per launch: ncu's dram__bytes per SDM input sample of the
+    # kernel that ran (one job per warp: the 4 s, 32,768-segment case; parts:
+    # the 3.5 s case, profiles/sdm_parts_kernel_dsd128_das_3p5s.md), scaled by
+    # the samples processed
+    per = SDM_PARTS_DRAM_BYTES_PER_SAMPLE if kernel.startswith("sdm_parts") \
+        else SDM_DRAM_BYTES_PER_SAMPLE
+    roofline["traffic"] = per * sdm_samples if per else None
+    roofline["traffic_source"] = (f"ncu dram__bytes per SDM input sample ({per} B) of a "
+                                  f"{'53.7' if kernel.startswith('sdm_parts') else '73.7'} "
+                                  "M-sample launch of the same kernel, scaled by SDM input samples")
 
     plain = None
     if not args.no_plain and rank == 0:

@@ -125,6 +125,7 @@ SIGNATURES = {
     "dsdgpu_sdm_drain": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _szp]),
     "dsdgpu_sdm_copy_state": (C.c_int, [_vp, C.c_int, C.c_int]),
     "dsdgpu_sdm_segments": (C.c_int, [_vp, C.POINTER(Segment), C.c_int]),
+    "dsdgpu_sdm_last_kernel": (C.c_int, [_vp, C.c_char_p, _sz]),
     "dsdgpu_sdm_state_distance": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
     "dsdgpu_sdm_estimate_state": (C.c_int, [_vp, C.POINTER(SdmParams), C.c_int,
                                             C.POINTER(EstimateItem), C.c_int]),
@@ -227,6 +228,13 @@ def load() -> C.CDLL:
         fn.argtypes = args
     _lib = lib
     return lib
+
+
+def last_sdm_kernel(ctx) -> str:
+    """The kernel (with template arguments) of the context's last trellis SDM launch."""
+    buf = C.create_string_buffer(64)
+    check(ctx, load().dsdgpu_sdm_last_kernel(ctx, buf, 64))
+    return buf.value.decode()
 
 
 def check(ctx, rc: int) -> None:

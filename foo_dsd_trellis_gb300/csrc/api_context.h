@@ -26,6 +26,7 @@ int sdm_jobs_per_cta(const SdmParams& P);   // 32 / lanes_per_job(P)
 int sdm_balanced_warps(const SdmParams& P, const SdmJob* jobs, int njobs, int sms,
                        long long part_len);
 long long sdm_parts_total(const SdmJob* jobs, int njobs, long long part_len);
+const char* sdm_last_kernel();   // kernel of this host thread's last SDM launch
 int launch_sdm_parts(const SdmParams& P, const SdmJob* d_jobs, int njobs, long long part_len,
                      unsigned long long* d_queue, long long total, int warps_per_pipe, int sms,
                      SdmCtx* d_ctxs, int* d_status, cudaStream_t stream);
@@ -63,6 +64,7 @@ struct dsdgpu_context {
   unsigned long long launches = 0;   // kernels this context has launched
   unsigned long long sdm_samples = 0;       // SDM input samples run so far
   unsigned long long sdm_last_samples = 0;  // ... by the last SDM launch
+  std::string sdm_last_kernel;              // ... and its kernel
 
   int* d_counter = nullptr;   // persistent-kernel job counter
   int* d_status = nullptr;    // device status word (bounded walks/waits)

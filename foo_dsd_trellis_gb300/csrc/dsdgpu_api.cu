@@ -153,11 +153,13 @@ int dsdgpu_context::run_jobs(const std::vector<SdmJob>& jobs) {
     if (launch_sdm_parts(P, d_jobs, n, kPartLen, d_parts, total, wpp, num_sms, d_ctx, d_status,
                          stream) != 0)
       return cuda_fail(cudaGetLastError(), "sdm kernel launch");
+    sdm_last_kernel = dsdgpu::sdm_last_kernel();
     launches += 2;
     return check_status();
   }
   if (launch_sdm_jobs(P, d_jobs, n, d_counter, d_ctx, d_status, max_blocks, stream) != 0)
     return cuda_fail(cudaGetLastError(), "sdm kernel launch");
+  sdm_last_kernel = dsdgpu::sdm_last_kernel();
   launches++;
   return check_status();
 }
@@ -486,6 +488,12 @@ int dsdgpu_sdm_query(dsdgpu_context_t* c, int channel, double* best_state, uint6
     info[5] = (uint64_t)c->pending[channel];
   }
   free(h);
+  return DSDGPU_OK;
+}
+
+int dsdgpu_sdm_last_kernel(const dsdgpu_context_t* c, char* name, size_t cap) {
+  if (!c || !name || cap == 0) return DSDGPU_ERR_ARG;
+  snprintf(name, cap, "%s", c->sdm_last_kernel.c_str());
   return DSDGPU_OK;
 }
 

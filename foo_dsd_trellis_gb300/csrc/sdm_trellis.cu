@@ -28,6 +28,7 @@
 #include "sdm_internal.h"
 
 #include <climits>
+#include <cstdio>
 
 namespace dsdgpu {
 
@@ -750,6 +751,18 @@ sdm_jobs_wide_kernel(SdmParams P, const SdmJob* __restrict__ jobs, int njobs,
   }
 }
 
+// The kernel (with its template arguments) of this host thread's last SDM
+// launch, for callers that report what ran.
+static thread_local char g_last_kernel[64] = "";
+
+const char* sdm_last_kernel() { return g_last_kernel; }
+
+static void note_kernel(const char* name, int a, int b = -1, int c = -1) {
+  if (c >= 0) snprintf(g_last_kernel, sizeof g_last_kernel, "%s<%d,%d,%d>", name, a, b, c);
+  else if (b >= 0) snprintf(g_last_kernel, sizeof g_last_kernel, "%s<%d,%d>", name, a, b);
+  else snprintf(g_last_kernel, sizeof g_last_kernel, "%s<%d>", name, a);
+}
+
 // ---- balanced launches: jobs cut into parts, parts queued ----
 // One job per warp pins a job to one SM sub-partition, and every FP64 warp
 // instruction of the warps there shares its FP64 pipe.  1,874 DAS segments
@@ -876,6 +889,7 @@ int launch_sdm_parts(const SdmParams& P, const SdmJob* d_jobs, int njobs, long l
                      unsigned long long* d_queue, long long total, int warps_per_pipe, int sms,
                      SdmCtx* d_ctxs, int* d_status, cudaStream_t stream) {
   parts_queue_init_kernel<<<(unsigned)((total + 255) / 256), 256, 0, stream>>>(d_queue, total, njobs);
+  note_kernel("sdm_parts_kernel", P.order);
   const dim3 grid((unsigned)(4 * warps_per_pipe * sms));
   const size_t smem = sizeof(WarpSmem<32>);
   switch (P.order) {
@@ -949,9 +963,15 @@ int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_
   if (njobs <= 0) return 0;
   if (P.lanes == 0 && max_blocks == 0 && P.lat <= 32 * kRegRingWords) {
     const long long split_cap = (long long)sdm_split_jobs_per_warp(P) * 2 * 4 * (resident_warps() / 16);
-    if (sdm_split_supported(P) && njobs <= split_cap)
+    if (sdm_split_supported(P) && njobs <= split_cap) {
+      if (P.order <= 8) note_kernel("sdm_split_kernel", P.order, 8, P.cands <= 2 ? 2 : 4);
+      else note_kernel("sdm_split_kernel", P.order, 16, 2);
       return launch_sdm_split(P, d_jobs, njobs, d_ctxs, stream);
-    if (sdm_scalar_eligible(P, max_blocks)) return launch_sdm_scalar(P, d_jobs, njobs, d_ctxs, stream);
+    }
+    if (sdm_scalar_eligible(P, max_blocks)) {
+      note_kernel("sdm_scalar_kernel", P.order);
+      return launch_sdm_scalar(P, d_jobs, njobs, d_ctxs, stream);
+    }
   }
   const int lanes = launch_lanes(P, njobs, max_blocks);
   const int jpc = 32 / lanes;
@@ -961,10 +981,12 @@ int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_
   const dim3 grid(blocks);
   int rc = -1;
   if (P.lat > 32 * kRegRingWords) {
+    note_kernel("sdm_jobs_wide_kernel", P.order);
     rc = launch_wide(P, grid, d_jobs, njobs, d_counter, d_ctxs, d_status, stream);
     if (rc) return rc;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
   }
+  note_kernel("sdm_jobs_kernel", P.order, lanes);
   switch (lanes) {
     case 32: rc = launch_lpj<32>(P, grid, d_jobs, njobs, d_counter, d_ctxs, d_status, stream); break;
     case 16: rc = launch_lpj<16>(P, grid, d_jobs, njobs, d_counter, d_ctxs, d_status, stream); break;

@@ -39,6 +39,9 @@ class DasChannels:
     def set_select(self, mode: int) -> None:
         _lib.check(self.h, self.L.dsdgpu_set_option(self.h, _lib.OPT_SDM_SELECT, mode))
 
+    def last_sdm_kernel(self) -> str:
+        return _lib.last_sdm_kernel(self.h)
+
     def close(self):
         if getattr(self, "h", None):
             self.L.dsdgpu_destroy(self.h)

@@ -118,6 +118,9 @@ class Encoder:
         _lib.check(self.h, self.L.dsdgpu_launch_count(self.h, C.byref(v)))
         return v.value
 
+    def last_sdm_kernel(self) -> str:
+        return _lib.last_sdm_kernel(self.h)
+
     def sdm_work(self):
         t, l = C.c_uint64(), C.c_uint64()
         _lib.check(self.h, self.L.dsdgpu_sdm_work(self.h, C.byref(t), C.byref(l)))

@@ -60,6 +60,9 @@ class TrellisSdm:
     def set_option(self, option: int, value: int) -> None:
         _lib.check(self.h, self.L.dsdgpu_set_option(self.h, option, value))
 
+    def last_sdm_kernel(self) -> str:
+        return _lib.last_sdm_kernel(self.h)
+
     def close(self):
         if getattr(self, "h", None):
             self.L.dsdgpu_destroy(self.h)

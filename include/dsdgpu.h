@@ -160,6 +160,10 @@ int  dsdgpu_launch_count(const dsdgpu_context_t *ctx, uint64_t *count);
 /* Input samples the trellis SDM has stepped through: in total, and in the
  * last SDM launch (warm-up and overlap samples of DAS segments included). */
 int  dsdgpu_sdm_work(const dsdgpu_context_t *ctx, uint64_t *total_samples, uint64_t *last_launch);
+/* Name of the kernel the context's last trellis SDM launch ran, with its
+ * template arguments (e.g. "sdm_parts_kernel<7>", "sdm_jobs_kernel<7,32>",
+ * "sdm_split_kernel<6,8,2>"); "" before the first. */
+int  dsdgpu_sdm_last_kernel(const dsdgpu_context_t *ctx, char *name, size_t cap);
 /* Wait for all work queued on the context's stream. */
 int  dsdgpu_synchronize(dsdgpu_context_t *ctx);
 
