@@ -149,7 +149,7 @@ const char *dsdgpu_last_error(const dsdgpu_context_t *ctx);
                                          a warp.  Results do not depend on it. */
 #define DSDGPU_OPT_SDM_BALANCE  3   /* 1 (default): an uncapped launch of many long K > 16
                                          jobs slightly above a whole number of warps per
-                                         FP64 pipe cuts the jobs into 2,048-sample parts
+                                         FP64 pipe cuts the jobs into 1,024-sample parts
                                          queued over an even number of warps per pipe;
                                          0: one job per warp from start to end.  Results
                                          do not depend on it. */

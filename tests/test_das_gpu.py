@@ -116,7 +116,7 @@ def test_lanes_option_rejects_bad_widths():
 
 def test_balanced_launch_equals_plain():
     """Enough DAS segments to land 5 % above one warp per FP64 pipe: the
-    SDM launch cuts the segments into 2,048-sample parts queued over one warp
+    SDM launch cuts the segments into 1,024-sample parts queued over one warp
     per pipe (DSDGPU_OPT_SDM_BALANCE); the stitched output and seams equal
     the plain one-segment-per-warp launch, which the other tests pin to the
     oracle, and the part boundaries are the streamed-block boundaries the
