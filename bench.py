@@ -464,7 +464,7 @@ def run_multistream(args):
                 "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak / 1000.0,
                              "unit": "TFLOP/s", "frac": achieved / (peak / 1000.0),
                              "traffic": SDM_DRAM_BYTES_PER_SAMPLE * info["sdm_samples"],
-                             "kernel": "sdm_jobs_kernel<6>, sdm_jobs_kernel<8> (concurrent)"},
+                             "kernel": "sdm_jobs_kernel<6,32>, sdm_jobs_kernel<8,32> (concurrent)"},
                 "cpu_baseline": None, "clocks": clk, "gpu_launches": int(launches),
                 "plan": info, "stages_ms": plan.times_ms()}
         print(json.dumps(line), flush=True)
@@ -659,7 +659,9 @@ def run_conv(args):
                              "peak": fp64_peak / 1000.0, "unit": "TFLOP/s",
                              "frac": flops / sdm_s / 1e12 / (fp64_peak / 1000.0),
                              "traffic": SDM_DRAM_BYTES_PER_SAMPLE * sdm_samples,
-                             "kernel": f"sdm_jobs_kernel<{f.order}>"},
+                             "traffic_source": "9.04 B per SDM input sample (ncu, sdm_jobs_kernel "
+                                               "at K = 32), scaled by SDM input samples",
+                             "kernel": enc.last_sdm_kernel()},
                 "cpu_baseline": None, "clocks": clk, "gpu_launches": int(launches),
                 "stages_ms": st}
         print(json.dumps(line), flush=True)
@@ -886,8 +888,7 @@ def run_next(args):
         roof = {"bound": "fp64", "achieved": flops / sdm_s / 1e12, "peak": fp64_peak / 1000.0,
                 "unit": "TFLOP/s", "frac": flops / sdm_s / 1e12 / (fp64_peak / 1000.0),
                 "traffic": None,
-                "kernel": f"sdm_split_kernel<{f.order},8,2> (K = 2: one state component per "
-                          "lane, two jobs per warp; latency-bound)",
+                "kernel": enc.last_sdm_kernel() + " (latency-bound small trellis)",
                 "algorithmic_flops_per_launch": flops, "flops_per_sample": cfg["cands"] * (5 * f.order + 6)}
     elif wl == "precorr128":
         pc_s = statistics.mean(sdm_ms) / 1000.0
