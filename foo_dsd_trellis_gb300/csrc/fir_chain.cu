@@ -151,7 +151,7 @@ __global__ void fir_history_kernel(const float* __restrict__ pcm, size_t pcm_str
 }
 
 // FP64 design of the reference's half-band / quarter-band taps (src/fir.c:65-121).
-static double bessel_i0(double x) {
+double bessel_i0(double x) {
   double sum = 1.0, term = 1.0;
   const double q = (x / 2.0) * (x / 2.0);
   for (int k = 1; k <= 25; k++) {

@@ -29,6 +29,7 @@ struct FirChainConst {
 // launchers of the fused chain kernel and its history update.
 int build_chain_const(unsigned fs_in, unsigned fs_out, int boxcar, FirChainConst* F);
 void design_taps(int ntaps, bool quarter, double* h);      // Kaiser half/quarter-band design
+double bessel_i0(double x);   // the reference's 25-term I0 series (src/fir.c:65-77)
 int plan_chain(unsigned fs_in, unsigned fs_out, int* U, int* L);   // stage factors and lengths
 size_t chain_smem_bytes(const FirChainConst& F);
 int fir_chain_prepare();   // kernel attributes (call outside stream capture)

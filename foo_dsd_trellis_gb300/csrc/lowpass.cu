@@ -25,10 +25,13 @@
 //                         reaches before the first sample treat it as 0, the
 //                         reference's zeroed delay line)
 #include "api_context.h"
+#include "fir_internal.h"
 
 #include <cmath>
 #include <cstring>
 #include <vector>
+
+using dsdgpu::bessel_i0;
 
 namespace {
 
@@ -42,17 +45,6 @@ struct LpHist {
   int32_t valid;              // samples seen so far, at most 256
   int32_t pad[3];
 };
-
-double bessel_i0(double x) {
-  double sum = 1.0, term = 1.0;
-  const double q = (x / 2.0) * (x / 2.0);
-  for (int k = 1; k <= 25; k++) {
-    term *= q / ((double)k * (double)k);
-    sum += term;
-    if (term < 1e-20 * sum) break;
-  }
-  return sum;
-}
 
 // fir_lowpass_init_ex's design (src/fir.c:795-825), its expression order kept
 int design_lowpass(unsigned fs, double cutoff_hz, int ntaps, double* h) {

@@ -12,6 +12,19 @@ constexpr int kSlots = 2 * kMaxCands;
 constexpr int kRingWords = kMaxLat / 32;
 constexpr int kBuckets = 128;    // PATH_HASH_SIZE (include/trellis.h:14)
 
+// The reference's state limiter (if v > lim: lim; else if v < -lim: -lim,
+// src/trellis.c:180-186) for a positive finite lim, on the integer pipe:
+// magnitudes of doubles order like their bit patterns; NaN (magnitude above
+// +inf's) passes through as in C.  Shared by every trellis kernel.
+__device__ __forceinline__ double clamp_state(double v, double lim) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
+  const unsigned long long lb = (unsigned long long)__double_as_longlong(lim);
+  if (mag > lb && mag <= 0x7FF0000000000000ull)
+    return __longlong_as_double((long long)((b & 0x8000000000000000ull) | lb));
+  return v;
+}
+
 // Uniform trellis parameters (one NTF and one (K, depth, lat) per launch).
 struct SdmParams {
   double a[kMaxOrder];

@@ -38,17 +38,6 @@ __device__ __forceinline__ T pick4(const T (&a)[4], int i) {
   return i == 0 ? a[0] : i == 1 ? a[1] : i == 2 ? a[2] : a[3];
 }
 
-__device__ __forceinline__ double clampd_s(double v, double lim) {
-  // the reference's limiter (if v > lim: lim; else if v < -lim: -lim) for a
-  // positive finite lim, on the integer pipe: magnitudes of doubles order like
-  // their bit patterns; NaN (magnitude above +inf's) passes through as in C
-  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-  const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
-  const unsigned long long lb = (unsigned long long)__double_as_longlong(lim);
-  if (mag > lb && mag <= 0x7FF0000000000000ull) return __longlong_as_double((long long)((b & 0x8000000000000000ull) | lb));
-  return v;
-}
-
 template <int N>
 struct Cand {
   double s[N];
@@ -142,9 +131,9 @@ __global__ void __launch_bounds__(32) sdm_scalar_kernel(SdmParams P, const SdmJo
         s01[i] = __dsub_rn(d[i][0], 1.0);
         if (lim_on) {
 #pragma unroll
-          for (int q = 1; q < N; q++) d[i][q] = clampd_s(d[i][q], lim);
-          s00[i] = clampd_s(s00[i], lim);
-          s01[i] = clampd_s(s01[i], lim);
+          for (int q = 1; q < N; q++) d[i][q] = clamp_state(d[i][q], lim);
+          s00[i] = clamp_state(s00[i], lim);
+          s01[i] = clamp_state(s01[i], lim);
         }
         const double e0 = __dadd_rn(v, P.a[0]);
         const double e1 = __dsub_rn(v, P.a[0]);

@@ -46,17 +46,6 @@ __device__ __forceinline__ T pickn(const T (&a)[M], int i) {
   return r;
 }
 
-__device__ __forceinline__ double clampd_l(double v, double lim) {
-  // the reference's limiter (if v > lim: lim; else if v < -lim: -lim) for a
-  // positive finite lim, on the integer pipe: magnitudes of doubles order like
-  // their bit patterns; NaN (magnitude above +inf's) passes through as in C
-  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-  const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
-  const unsigned long long lb = (unsigned long long)__double_as_longlong(lim);
-  if (mag > lb && mag <= 0x7FF0000000000000ull) return __longlong_as_double((long long)((b & 0x8000000000000000ull) | lb));
-  return v;
-}
-
 template <int N, int H, int KC>
 __global__ void __launch_bounds__(32) sdm_split_kernel(SdmParams P, const SdmJob* __restrict__ jobs,
                                                       int njobs, SdmCtx* __restrict__ ctxs) {
@@ -236,7 +225,7 @@ __global__ void __launch_bounds__(32) sdm_split_kernel(SdmParams P, const SdmJob
     const double dpar = __shfl_sync(hm, d, par * H + q, G);
     const uint32_t rpar = __shfl_sync(hm, ringw, par * H + q, G);
     double snew = q == 0 ? __dadd_rn(dpar, b ? -1.0 : 1.0) : dpar;
-    if (lim_on) snew = clampd_l(snew, lim);
+    if (lim_on) snew = clamp_state(snew, lim);
     sq = q < N ? snew : 0.0;
     cost = live ? __dsub_rn(pickn(ccost, ch), min_cost) : 0.0;
     path = live ? pickn(cpath, ch) : 0ull;

@@ -41,17 +41,6 @@ constexpr unsigned kFull = 0xffffffffu;
 
 __device__ __forceinline__ long long key_of(double c) { return __double_as_longlong(c); }
 
-__device__ __forceinline__ double clampd(double v, double lim) {
-  // the reference's limiter (if v > lim: lim; else if v < -lim: -lim) for a
-  // positive finite lim, on the integer pipe: magnitudes of doubles order like
-  // their bit patterns; NaN (magnitude above +inf's) passes through as in C
-  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-  const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
-  const unsigned long long lb = (unsigned long long)__double_as_longlong(lim);
-  if (mag > lb && mag <= 0x7FF0000000000000ull) return __longlong_as_double((long long)((b & 0x8000000000000000ull) | lb));
-  return v;
-}
-
 // A ring word kept opaque in a register: without it the word-select loops over
 // a 64-word ring compile to an indexed local-memory array.
 template <int RW>
@@ -352,9 +341,9 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
       for (int i = 2; i < N; i++) S[i] = pk.D[i];
       if (lim_on) {
 #pragma unroll
-        for (int k = 1; k < N; k++) S[k] = clampd(S[k], P.state_limit);
-        s00 = clampd(s00, P.state_limit);
-        s01 = clampd(s01, P.state_limit);
+        for (int k = 1; k < N; k++) S[k] = clamp_state(S[k], P.state_limit);
+        s00 = clamp_state(s00, P.state_limit);
+        s01 = clamp_state(s01, P.state_limit);
       }
       const double e0 = __dadd_rn(v, P.a[0]);
       const double e1 = __dsub_rn(v, P.a[0]);
