@@ -46,7 +46,7 @@ WL = dict(workload="dsd128_das_stereo_10s_multitone_pink", fs_in=48000, fs_out=6
           boxcar_taps=8, soft_clip=True, seed=1001)
 FP64_OPS_PER_CAND_SAMPLE = 5 * WL["ntf_order"] + 6   # (2N+1) mul + (3N+5) add
 SDM_DRAM_BYTES_PER_SAMPLE = 9.04                      # measured, see the traffic note below
-SDM_PARTS_DRAM_BYTES_PER_SAMPLE = 9.14                # the balanced launch's (parts kernel), measured
+SDM_PARTS_DRAM_BYTES_PER_SAMPLE = 9.15                # the balanced launch's (parts kernel), measured
 
 
 def parse():
