@@ -696,7 +696,7 @@ NEXT = {
         metric="PCM 44.1 kHz -> DSD128 with the PreCorr SDM (FIR chain -> PreCorr -> DoP) "
                "DSD Msamples/s, bit-exact SDM",
         workload="precorr_dsd128_stereo_10s", fs_in=44100, fs=5644800, ntf="clans-7 (PreCorr auto)",
-        state_limit=12.0, boxcar_taps=8, soft_clip=True),
+        state_limit=12.0, boxcar_taps=8, soft_clip=False),
     "dsd2pcm128": dict(
         metric="DSD128 -> 44.1 kHz PCM (DoP in -> unpack -> 7 half-band /2 FP64 stages -> "
                "float32) DSD input Msamples/s, float32 output within 2e-7 of the FP64 restatement",
@@ -773,7 +773,7 @@ def _next_cpu(wl: str, inp, bits, sample_s: float) -> dict:
 
         def one(c):
             y = O.engine_fir(44100, fs, x[c], boxcar_taps=8, g_start=PCM_FIR_GAIN,
-                             g_end=PCM_FIR_GAIN, soft_clip=True)
+                             g_end=PCM_FIR_GAIN, soft_clip=False)
             b = O.PreCorr(f.order, np.array(f.a), np.array(f.g), cfg["state_limit"]).process(y)
             O.dop_pack_bits(b, 0)
             return len(b)
@@ -826,7 +826,7 @@ def run_next(args):
         f = ntf.auto_select_precorr(fs)
         g = PCM_FIR_GAIN
         enc = Encoder(cfg["fs_in"], fs, nch, f, 64, 32, 128, state_limit=cfg["state_limit"],
-                      boxcar_taps=8, soft_clip=True, output_format=OUT_DOP,
+                      boxcar_taps=8, soft_clip=False, output_format=OUT_DOP,
                       sdm_mode=_lib.SDM_PRECORR, device=local)
     else:
         f = ntf.get_filter("clans-7", fs)

@@ -158,6 +158,7 @@ SIGNATURES = {
     "dsdgpu_plan_time_plain": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int64),
                                          C.POINTER(C.c_double)]),
     "dsdgpu_dop_unpack": (C.c_int, [_vp, C.c_int, _vp, _sz, _sz, _vp, _sz]),
+    "dsdgpu_dop_unpack_f32": (C.c_int, [_vp, C.c_int, _vp, _sz, _sz, _vp, _sz]),
     "dsdgpu_boxcar_setup": (C.c_int, [_vp, C.c_int, C.c_int]),
     "dsdgpu_boxcar_reset": (C.c_int, [_vp]),
     "dsdgpu_boxcar_process": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _sz, _sz, _vp, _sz,
@@ -175,6 +176,10 @@ SIGNATURES = {
                                                C.c_double, C.c_double]),
     "dsdgpu_decim_setup": (C.c_int, [_vp, C.c_uint, C.c_uint, C.c_int]),
     "dsdgpu_decim_reset": (C.c_int, [_vp]),
+    "dsdgpu_decim_process_f64": (C.c_int, [_vp, C.c_int, _vp, _sz, _sz, _vp, _sz, C.c_double,
+                                           C.c_double, C.c_int, C.POINTER(_sz)]),
+    "dsdgpu_decim_process_f64_async": (C.c_int, [_vp, C.c_int, _vp, _sz, _sz, _vp, _sz,
+                                                 C.c_double, C.c_double, C.c_int, C.POINTER(_sz)]),
     "dsdgpu_decim_process": (C.c_int, [_vp, C.c_int, _vp, _sz, _sz, _vp, _sz, C.c_double,
                                        C.c_double, _szp]),
     "dsdgpu_decim_process_async": (C.c_int, [_vp, C.c_int, _vp, _sz, _sz, _vp, _sz, C.c_double,

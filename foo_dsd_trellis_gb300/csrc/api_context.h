@@ -125,6 +125,11 @@ struct dsdgpu_context {
   int box_taps = 0;
   int box_nch = 0;
   bool pipe_same_rate = false;    // pipeline input is DoP: unpack + boxcar instead of the FIR
+  // DSD -> DSD rate conversion (DoP in at a DSD rate other than the output's):
+  // up through the FIR chain on +-1 floats, down through the FP64 decimation chain
+  bool pipe_dsd_up = false;
+  bool pipe_dsd_down = false;
+  int pipe_down_stages = 0;
   // same-rate FIR lowpass (FIR_MODE_FIR), used instead of the boxcar when set up
   dsdgpu_lowpass_state* lowpass = nullptr;
   bool pipe_lowpass = false;

@@ -132,6 +132,20 @@ __global__ void decim_gain_kernel(const double* __restrict__ y, size_t y_stride,
   out[(size_t)c * out_stride + t] = (float)v;
 }
 
+// FP64 output of the rate-conversion branch (src/engine.c:640-717): gain ramp
+// (when either end differs from 1), then the optional soft clip
+__global__ void decim_gain_f64_kernel(const double* __restrict__ y, size_t y_stride, long long n,
+                                      int nch, double g_start, double g_step, int apply,
+                                      int soft_clip, double* __restrict__ out, size_t out_stride) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * nch) return;
+  const long long c = i / n, t = i % n;
+  double v = y[(size_t)c * y_stride + t];
+  if (apply) v = __dmul_rn(v, __dadd_rn(g_start, __dmul_rn(g_step, (double)t)));
+  if (soft_clip) v = soft_clip_095(v);
+  out[(size_t)c * out_stride + t] = v;
+}
+
 unsigned nb(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
 }  // namespace
@@ -262,6 +276,71 @@ int dsdgpu_decim_process_async(dsdgpu_context_t* c, int nch, const uint8_t* d_bi
   }
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? DSDGPU_OK : c->cuda_fail(e, "decimation launch");
+}
+
+int dsdgpu_decim_process_f64_async(dsdgpu_context_t* c, int nch, const double* d_in,
+                                   size_t in_stride, size_t count, double* d_out,
+                                   size_t out_stride, double gain_start, double gain_end,
+                                   int soft_clip, size_t* out_count) {
+  if (!c) return DSDGPU_ERR_ARG;
+  dsdgpu_decim_state* s = c->decim;
+  if (!s) return c->fail(DSDGPU_ERR_STATE, "decimation not set up");
+  if (nch != s->nch) return c->fail(DSDGPU_ERR_ARG, "channel count differs from the setup");
+  size_t n = count;
+  for (int k = 0; k < s->stages; k++) n /= 2;
+  if (out_count) *out_count = n;
+  if (count < 2) return DSDGPU_OK;
+  if (!d_in || !d_out) return c->fail(DSDGPU_ERR_ARG, "null buffer");
+  if (nch > 1 && (in_stride < count || out_stride < n))
+    return c->fail(DSDGPU_ERR_ARG, "row stride shorter than the count");
+  cudaSetDevice(c->device);
+  cudaStream_t st = c->stream;
+  const size_t row = ((count / 2 + 1) + 31) & ~(size_t)31;
+  if (s->row < row) {
+    if (s->d_buf) cudaFree(s->d_buf);
+    s->d_buf = nullptr;
+    s->row = 0;
+    if (cudaMalloc(&s->d_buf, sizeof(double) * 2 * row * (size_t)nch) != cudaSuccess)
+      return c->cuda_fail(cudaGetLastError(), "decimation buffers");
+    s->row = row;
+  }
+  double* buf[2] = {s->d_buf, s->d_buf + s->row * (size_t)nch};
+  size_t cur = count;
+  const double* in = d_in;
+  size_t istride = in_stride;
+  for (int k = 0; k < s->stages; k++) {
+    const long long m = (long long)(cur / 2);
+    double* out = buf[k & 1];
+    double* dly = s->d_dly + (size_t)k * nch * (kDecTaps - 1);
+    if (m > 0) {
+      decim_stage_kernel<<<nb(m * nch, 256), 256, 0, st>>>(s->nz, in, istride, m, dly, out, s->row, nch);
+      decim_dly_kernel<false><<<nch, 64, 0, st>>>(nullptr, in, istride, 2 * m, dly, nch);
+      c->launches += 2;
+    }
+    in = out;
+    istride = s->row;
+    cur = (size_t)m;
+  }
+  // gain ramp of the rate-conversion branch (src/engine.c:646-651), soft clip (:704-717)
+  double gs = gain_start;
+  if (gs == 0.0) gs = gain_end;
+  const int apply = (gs != 1.0 || gain_end != 1.0) ? 1 : 0;
+  const double step = n > 1 ? (gain_end - gs) / (double)(n - 1) : 0.0;
+  if (n > 0) {
+    decim_gain_f64_kernel<<<nb((long long)n * nch, 256), 256, 0, st>>>(
+        in, istride, (long long)n, nch, gs, step, apply, soft_clip ? 1 : 0, d_out, out_stride);
+    c->launches++;
+  }
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? DSDGPU_OK : c->cuda_fail(e, "decimation launch");
+}
+
+int dsdgpu_decim_process_f64(dsdgpu_context_t* c, int nch, const double* d_in, size_t in_stride,
+                             size_t count, double* d_out, size_t out_stride, double gain_start,
+                             double gain_end, int soft_clip, size_t* out_count) {
+  const int rc = dsdgpu_decim_process_f64_async(c, nch, d_in, in_stride, count, d_out, out_stride,
+                                                gain_start, gain_end, soft_clip, out_count);
+  return rc ? rc : c->check_status();
 }
 
 int dsdgpu_decim_process(dsdgpu_context_t* c, int nch, const uint8_t* d_bits, size_t bits_stride,

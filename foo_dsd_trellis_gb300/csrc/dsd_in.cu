@@ -36,6 +36,21 @@ __global__ void dop_unpack_kernel(const float* __restrict__ dop, size_t dop_stri
   for (int b = 0; b < 16; b++) o[b] = (uint8_t)((w >> (15 - b)) & 1u);
 }
 
+// the reference's own output form of dop_unpack: +-1.0f per decision
+__global__ void dop_unpack_f32_kernel(const float* __restrict__ dop, size_t dop_stride,
+                                      long long frames, int nch, float* __restrict__ out,
+                                      size_t out_stride) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= frames * nch) return;
+  const long long c = i / frames, f = i % frames;
+  const double d = (double)dop[(size_t)c * dop_stride + f] * 8388608.0;
+  const int v = d >= 0.0 ? (int)(d + 0.5) : (int)(d - 0.5);
+  const unsigned w = (unsigned)v & 0xFFFFu;
+  float* o = out + (size_t)c * out_stride + 16 * (size_t)f;
+#pragma unroll
+  for (int b = 0; b < 16; b++) o[b] = ((w >> (15 - b)) & 1u) ? 1.0f : -1.0f;
+}
+
 __global__ void boxcar_kernel(const uint8_t* __restrict__ bits, size_t bits_stride, long long count,
                               const int8_t* __restrict__ hist, int taps, int nch,
                               double g_start, double g_step, double* __restrict__ out,
@@ -93,6 +108,19 @@ int dsdgpu_dop_unpack(dsdgpu_context_t* c, int nch, const float* d_dop, size_t d
   cudaSetDevice(c->device);
   dop_unpack_kernel<<<nblk((long long)frames * nch, 256), 256, 0, c->stream>>>(
       d_dop, dop_stride, (long long)frames, nch, d_bits, bits_stride);
+  c->launches++;
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? DSDGPU_OK : c->cuda_fail(e, "dop unpack launch");
+}
+
+int dsdgpu_dop_unpack_f32(dsdgpu_context_t* c, int nch, const float* d_dop, size_t dop_stride,
+                          size_t frames, float* d_out, size_t out_stride) {
+  if (!c || nch < 1 || (frames > 0 && (!d_dop || !d_out))) return DSDGPU_ERR_ARG;
+  if (out_stride < 16 * frames) return c->fail(DSDGPU_ERR_ARG, "output row shorter than 16 x frames");
+  if (frames == 0) return DSDGPU_OK;
+  cudaSetDevice(c->device);
+  dop_unpack_f32_kernel<<<nblk((long long)frames * nch, 256), 256, 0, c->stream>>>(
+      d_dop, dop_stride, (long long)frames, nch, d_out, out_stride);
   c->launches++;
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? DSDGPU_OK : c->cuda_fail(e, "dop unpack launch");

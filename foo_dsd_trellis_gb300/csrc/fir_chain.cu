@@ -122,10 +122,7 @@ fir_chain_kernel(const __grid_constant__ FirChainConst F, const float* __restric
         } else {
           double y = (double)acc0 + (double)acc1;
           if (apply_gain) y = __dmul_rn(y, __dadd_rn(g_start, __dmul_rn(g_step, (double)m)));
-          if (soft_clip) {
-            if (y > 0.95) y = 0.95 + 0.05 * tanh((y - 0.95) * 20.0);
-            else if (y < -0.95) y = -0.95 - 0.05 * tanh((-y - 0.95) * 20.0);
-          }
+          if (soft_clip) y = soft_clip_095(y);
           out[(size_t)ch * out_stride + m] = y;
         }
       }

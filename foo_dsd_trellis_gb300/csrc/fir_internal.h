@@ -11,6 +11,19 @@ constexpr int kHistory = 256;         // PCM samples kept between blocks per cha
 constexpr int kFirThreads = 256;
 constexpr int kFirMaxSmem = 200 * 1024;   // dynamic shared memory cap of one FIR tile
 
+// The engine's tanh soft clip above +-0.95 (src/engine.c:704-717), its
+// constants formed as the reference forms them (1 - 0.95 and 1 / (1 - 0.95)
+// in FP64, not the decimal literals 0.05 and 20).
+__device__ __forceinline__ double soft_clip_095(double x) {
+  const double thresh = 0.95;
+  const double knee = 1.0 - thresh;
+  const double inv_knee = 1.0 / knee;
+  if (x > thresh) return __dadd_rn(thresh, __dmul_rn(knee, tanh(__dmul_rn(__dsub_rn(x, thresh), inv_knee))));
+  if (x < -thresh)
+    return __dsub_rn(-thresh, __dmul_rn(knee, tanh(__dmul_rn(__dsub_rn(-x, thresh), inv_knee))));
+  return x;
+}
+
 struct FirChainConst {
   int S;                               // number of stages
   int ratio;                           // total upsampling factor

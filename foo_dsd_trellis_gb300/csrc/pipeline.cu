@@ -8,6 +8,10 @@
 
 #include <cstring>
 
+namespace {
+constexpr unsigned kDsd64Rate = 2822400u;   // DSD_RATE_64: inputs at or above it are DSD
+}  // namespace
+
 extern "C" {
 
 int dsdgpu_pipeline_setup(dsdgpu_context_t* c, const dsdgpu_pipeline_params_t* p, int nch) {
@@ -26,6 +30,8 @@ int dsdgpu_pipeline_setup(dsdgpu_context_t* c, const dsdgpu_pipeline_params_t* p
     c->pipe_same_rate = false;
     c->pipe_precorr = false;
     c->pipe_lowpass = false;
+    c->pipe_dsd_up = false;
+    c->pipe_dsd_down = false;
     if (!c->ev_ready) {
       for (int i = 0; i < dsdgpu_context::kEvents; i++) cudaEventCreate(&c->ev[i]);
       c->ev_ready = true;
@@ -43,7 +49,22 @@ int dsdgpu_pipeline_setup(dsdgpu_context_t* c, const dsdgpu_pipeline_params_t* p
   if (p->samerate_filter != DSDGPU_SAMERATE_BOXCAR && p->samerate_filter != DSDGPU_SAMERATE_LOWPASS)
     return c->fail(DSDGPU_ERR_ARG, "bad same-rate filter");
   c->pipe_lowpass = c->pipe_same_rate && p->samerate_filter == DSDGPU_SAMERATE_LOWPASS;
-  if (c->pipe_lowpass) {
+  // DSD input at another DSD rate (the engine's rate-conversion branch with DSD
+  // in, src/engine.c:600-729: boxcar at the input rate, FIR up or down, gain,
+  // soft clip unless PreCorr)
+  const bool dsd_in = p->fir.fs_in >= kDsd64Rate;
+  c->pipe_dsd_up = dsd_in && p->fir.fs_out > p->fir.fs_in;
+  c->pipe_dsd_down = dsd_in && p->fir.fs_out < p->fir.fs_in;
+  c->pipe_down_stages = 0;
+  dsdgpu_fir_params_t fp = p->fir;
+  if (c->pipe_precorr) fp.soft_clip = 0;   // the engine does not clip ahead of PreCorr
+  if (c->pipe_dsd_down) {
+    const int taps = p->fir.boxcar_taps > 0 ? p->fir.boxcar_taps : 8;
+    rc = dsdgpu_boxcar_setup(c, taps, nch);
+    if (!rc) rc = dsdgpu_decim_setup(c, p->fir.fs_in, p->fir.fs_out, nch);
+    if (!rc)
+      for (unsigned r = p->fir.fs_in / p->fir.fs_out; r > 1; r >>= 1) c->pipe_down_stages++;
+  } else if (c->pipe_lowpass) {
     // DSD in at the output rate: DoP unpack + FIR lowpass (fir_lowpass_init,
     // src/engine.c:168-181, 505-523)
     rc = dsdgpu_lowpass_setup(c, p->fir.fs_in, 50000.0, 127, nch);
@@ -52,10 +73,11 @@ int dsdgpu_pipeline_setup(dsdgpu_context_t* c, const dsdgpu_pipeline_params_t* p
     const int taps = p->fir.boxcar_taps > 0 ? p->fir.boxcar_taps : samerate_boxcar_taps(p->fir.fs_in);
     rc = dsdgpu_boxcar_setup(c, taps, nch);
   } else {
-    rc = dsdgpu_fir_setup(c, &p->fir, nch);
+    rc = dsdgpu_fir_setup(c, &fp, nch);
   }
   if (rc) return rc;
   c->pipe = *p;
+  c->pipe.fir = fp;
   c->pipe_nch = nch;
   c->pipe_ready = true;
   c->dop_phase = 0;
@@ -100,15 +122,27 @@ int dsdgpu_pipeline_process(dsdgpu_context_t* c, const float* d_pcm, size_t pcm_
     if (out_bytes) *out_bytes = n * sizeof(float) * (size_t)nch;
     return DSDGPU_OK;
   }
-  // same rate: the input is DoP, 16 decisions per frame
-  const size_t n_fir = frames * (c->pipe_same_rate ? (size_t)16 : (size_t)c->fir.ratio);
-  // device work buffers: FIR output (double) and stitched decisions
+  // DoP input (same rate, DSD up or down): 16 decisions per frame
+  const bool dop_in = c->pipe_same_rate || c->pipe_dsd_up || c->pipe_dsd_down;
+  const size_t n_in = dop_in ? 16 * frames : frames;
+  size_t n_fir = c->pipe_same_rate ? n_in : n_in * (size_t)c->fir.ratio;
+  if (c->pipe_dsd_down) {
+    n_fir = n_in;
+    for (int k = 0; k < c->pipe_down_stages; k++) n_fir /= 2;
+  }
+  // device work buffers: FIR output (double), stitched decisions, and for DSD
+  // rate conversion the unpacked input (+-1 floats up; decisions and their
+  // boxcar mean down)
   const size_t fir_bytes = (n_fir * sizeof(double) + 255) & ~(size_t)255;
   const size_t bit_row = (n_fir + 255) & ~(size_t)255;
-  int rc = c->ensure_scratch(fir_bytes * (size_t)nch + bit_row * (size_t)nch + 256);
+  const size_t in_f32 = c->pipe_dsd_up ? ((n_in * sizeof(float) + 255) & ~(size_t)255) : 0;
+  const size_t in_bits = c->pipe_dsd_down ? ((n_in + 255) & ~(size_t)255) : 0;
+  const size_t in_f64 = c->pipe_dsd_down ? ((n_in * sizeof(double) + 255) & ~(size_t)255) : 0;
+  int rc = c->ensure_scratch((fir_bytes + bit_row + in_f32 + in_bits + in_f64) * (size_t)nch + 256);
   if (rc) return rc;
   double* d_fir = (double*)c->d_scratch;
   uint8_t* d_bits = (uint8_t*)c->d_scratch + fir_bytes * (size_t)nch;
+  uint8_t* d_extra = d_bits + bit_row * (size_t)nch;
   const size_t fir_stride = fir_bytes / sizeof(double);
 
   cudaEventRecord(c->ev[0], c->stream);
@@ -123,6 +157,26 @@ int dsdgpu_pipeline_process(dsdgpu_context_t* c, const float* d_pcm, size_t pcm_
              : dsdgpu_boxcar_process_async(c, 0, nch, d_bits, bit_row, n_fir, d_fir, fir_stride,
                                            gain_start, gain_end);
     fo = n_fir;
+  } else if (c->pipe_dsd_up) {
+    // +-1.0 floats at the input DSD rate, then the FIR chain with its boxcar
+    float* d_f = (float*)d_extra;
+    const size_t f_stride = in_f32 / sizeof(float);
+    rc = dsdgpu_dop_unpack_f32(c, nch, d_pcm, pcm_stride, frames, d_f, f_stride);
+    if (rc) return rc;
+    rc = dsdgpu_fir_process_async(c, 0, nch, d_f, f_stride, n_in, d_fir, fir_stride, gain_start,
+                                  gain_end, &fo);
+  } else if (c->pipe_dsd_down) {
+    // decisions, their boxcar mean (gain 1: the sum times 1/taps exactly as
+    // the engine forms it), then the FP64 decimation chain, gain and clip
+    uint8_t* d_in_bits = d_extra;
+    double* d_box = (double*)(d_extra + in_bits * (size_t)nch);
+    const size_t box_stride = in_f64 / sizeof(double);
+    rc = dsdgpu_dop_unpack(c, nch, d_pcm, pcm_stride, frames, d_in_bits, in_bits);
+    if (rc) return rc;
+    rc = dsdgpu_boxcar_process_async(c, 0, nch, d_in_bits, in_bits, n_in, d_box, box_stride, 1.0, 1.0);
+    if (rc) return rc;
+    rc = dsdgpu_decim_process_f64_async(c, nch, d_box, box_stride, n_in, d_fir, fir_stride,
+                                        gain_start, gain_end, c->pipe.fir.soft_clip, &fo);
   } else {
     rc = dsdgpu_fir_process_async(c, 0, nch, d_pcm, pcm_stride, frames, d_fir, fir_stride,
                                   gain_start, gain_end, &fo);
@@ -190,6 +244,11 @@ int dsdgpu_pipeline_process_host(dsdgpu_context_t* c, const float* h_pcm, size_t
   cudaSetDevice(c->device);
   const int nch = c->pipe_nch;
   size_t n_fir = frames * (c->pipe_same_rate || c->pipe_pcm_out ? (size_t)16 : (size_t)c->fir.ratio);
+  if (c->pipe_dsd_up) n_fir = 16 * frames * (size_t)c->fir.ratio;
+  if (c->pipe_dsd_down) {
+    n_fir = 16 * frames;
+    for (int k = 0; k < c->pipe_down_stages; k++) n_fir /= 2;
+  }
   if (c->pipe_pcm_out) n_fir = n_fir * sizeof(float);   // output rows hold floats (fewer of them)
   // staging for the input and output on the device, kept across calls
   const size_t in_bytes = (frames * (size_t)nch * sizeof(float) + 255) & ~(size_t)255;

@@ -54,11 +54,14 @@ class Encoder:
         _lib.check(self.h, self.L.dsdgpu_pipeline_setup(self.h, C.byref(p), num_channels))
         self.params = p
         self.nch = num_channels
-        # same rate and PCM output: the input is DoP (16 DSD samples per frame)
+        # DSD input (fs_in at or above DSD64) is DoP, 16 DSD samples per frame
+        dsd_in = fs_in >= 2822400
         if output_format == _lib.OUT_PCM:
             self.ratio = 16 / (fs_in // fs_out)
+        elif dsd_in:
+            self.ratio = 16 * fs_out / fs_in
         else:
-            self.ratio = 16 if fs_in == fs_out else fs_out // fs_in
+            self.ratio = fs_out // fs_in
         self.output_format = output_format
         self.device = device
         s = C.c_void_p()

@@ -111,7 +111,18 @@ typedef struct {
 #define DSDGPU_SDM_PRECORR 1   /* PreCorr greedy SDM, sequential per channel */
 
 /* Whole-path parameters: the FIR chain with its glue, the trellis SDM, DAS,
- * and the output format. */
+ * and the output format.  The input is PCM below DSD64's 2,822,400 Hz and DoP
+ * at or above it, as the engine decides (src/engine.c:156-164):
+ *   PCM in                   boxcar, FIR upsampling chain, gain, soft clip
+ *   DSD in, same rate        DoP unpack, boxcar or lowpass (samerate_filter)
+ *   DSD in, higher DSD rate  DoP unpack to +-1, boxcar, FIR upsampling chain,
+ *                            gain, soft clip (the engine's rate-conversion
+ *                            branch; fir.boxcar_taps 8 as the engine sets it)
+ *   DSD in, lower DSD rate   DoP unpack, boxcar, FP64 decimation chain, gain,
+ *                            soft clip (the same branch, downsampling)
+ *   DSD in, PCM out          DoP unpack, decimation chain, float32
+ * then the SDM and packing.  The soft clip is never applied ahead of PreCorr
+ * (src/engine.c:704-717). */
 /* Pre-SDM filter of the same-rate DSD path: the reference's fir_mode
  * (FIR_MODE_BOXCAR 0 / FIR_MODE_FIR 1, include/dsd_types.h:436-438; the
  * engine's default is the boxcar, src/engine.c:168-181). */
@@ -417,6 +428,10 @@ int dsdgpu_plan_time_plain(dsdgpu_plan_t *plan, int njobs, int64_t *samples, dou
  * 16 per frame, MSB first. */
 int dsdgpu_dop_unpack(dsdgpu_context_t *ctx, int nch, const float *d_dop, size_t dop_stride,
                       size_t frames, uint8_t *d_bits, size_t bits_stride);
+/* The same unpack in dop_unpack's own output form: +-1.0f floats
+ * [nch][out_stride], 16 per frame. */
+int dsdgpu_dop_unpack_f32(dsdgpu_context_t *ctx, int nch, const float *d_dop, size_t dop_stride,
+                          size_t frames, float *d_out, size_t out_stride);
 int dsdgpu_boxcar_setup(dsdgpu_context_t *ctx, int taps, int nch);   /* taps 1..256 */
 int dsdgpu_boxcar_reset(dsdgpu_context_t *ctx);
 /* Decision bytes -> (window count / taps) * (gain ramp), the window carried
@@ -460,6 +475,18 @@ int dsdgpu_lowpass_process_async(dsdgpu_context_t *ctx, int first, int nch,
  * output_format DSDGPU_OUT_PCM (fir.fs_out < fir.fs_in) takes DoP floats and
  * returns PCM: unpack -> decimation -> float. */
 int dsdgpu_decim_setup(dsdgpu_context_t *ctx, unsigned fs_in, unsigned fs_out, int nch);
+/* The same chain on FP64 input with FP64 output: the downsampling half of the
+ * engine's rate-conversion branch (fir_chain_process_d, then the gain ramp
+ * when either end differs from 1 and, when soft_clip, the tanh clip above
+ * +-0.95; src/engine.c:600-717). */
+int dsdgpu_decim_process_f64(dsdgpu_context_t *ctx, int nch, const double *d_in,
+                             size_t in_stride, size_t count, double *d_out, size_t out_stride,
+                             double gain_start, double gain_end, int soft_clip,
+                             size_t *out_count);
+int dsdgpu_decim_process_f64_async(dsdgpu_context_t *ctx, int nch, const double *d_in,
+                                   size_t in_stride, size_t count, double *d_out,
+                                   size_t out_stride, double gain_start, double gain_end,
+                                   int soft_clip, size_t *out_count);
 int dsdgpu_decim_reset(dsdgpu_context_t *ctx);
 /* 0/1 decision bytes [nch][bits_stride] (count per channel) -> float PCM
  * [nch][pcm_stride]; *out_count = count / (fs_in / fs_out) (each stage keeps

@@ -139,6 +139,28 @@ size_t ora_decim_process(ora_decim_t *d, const double *in, size_t n, double *out
 }
 
 /*
+ * The rate-conversion branch of engine_process_block for DSD input at a higher
+ * rate than the output (src/engine.c:600-717 with fir_chain_init_ex's
+ * downsampling chain): the +-1 input widened, the boxcar's running FP64 mean
+ * (ring carried in bc), the FP64 decimation chain (delay lines carried in d),
+ * the gain ramp when either end differs from 1 (a g_start of 0 means g_end),
+ * and the tanh soft clip when asked (the engine skips it ahead of PreCorr).
+ */
+size_t ora_engine_down(ora_boxcar_t *bc, ora_decim_t *d, const float *in, size_t n,
+                       double g_start, double g_end, int soft_clip, double *out)
+{
+    double *w = (double *)malloc((n + 1) * sizeof(double));
+    if (!w) return 0;
+    ora_boxcar_gain(bc, in, w, n, 1.0, 1.0);
+    const size_t m = ora_decim_process(d, w, n, out);
+    free(w);
+    if (g_start == 0.0) g_start = g_end;
+    ora_gain_ramp(out, m, g_start, g_end);
+    if (soft_clip) ora_soft_clip(out, m);
+    return m;
+}
+
+/*
  * Same-rate FIR lowpass (the engine's FIR_MODE_FIR alternative to the boxcar,
  * src/engine.c:168-181 and :505-523):
  *   - design of fir_lowpass_init_ex (src/fir.c:795-857): ntaps clamped to

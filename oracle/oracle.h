@@ -155,6 +155,9 @@ typedef struct ora_decim ora_decim_t;
 ora_decim_t *ora_decim_new(unsigned fs_in, unsigned fs_out);
 void ora_decim_free(ora_decim_t *d);
 size_t ora_decim_process(ora_decim_t *d, const double *in, size_t n, double *out);
+/* DSD -> DSD downsampling branch (src/engine.c:600-717, downsampling chain) */
+size_t ora_engine_down(ora_boxcar_t *bc, ora_decim_t *d, const float *in, size_t n,
+                       double g_start, double g_end, int soft_clip, double *out);
 
 /* ---- DAS (src/dsp_plugin.c DAS block) ---- */
 typedef struct {

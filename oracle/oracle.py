@@ -340,6 +340,17 @@ class Decimator:
             pass
 
 
+def engine_down(bc: "Boxcar", dec: Decimator, x: np.ndarray, g_start: float, g_end: float,
+                soft_clip: bool) -> np.ndarray:
+    """DSD -> DSD downsampling branch of the engine: boxcar mean, FP64
+    decimation, gain ramp, optional soft clip (state carried in bc and dec)."""
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.empty(max(len(x), 1), np.float64)
+    n = oracle_lib().lib.ora_engine_down(bc.h, dec.h, _ptr(x, _fp), len(x), float(g_start),
+                                         float(g_end), int(soft_clip), _ptr(out, _dp))
+    return out[:n]
+
+
 def dop_float_frames(bits01: np.ndarray, phase: int = 0) -> np.ndarray:
     """0/1 decision bytes -> DoP float samples (24-bit value / 2^23) with
     alternating markers, the format a decoder hands the plugin."""
@@ -383,6 +394,9 @@ def _bind_oracle_extras(L):
     L.ora_lowpass_taps.restype = C.c_int
     L.ora_lowpass_taps.argtypes = [C.c_void_p, _dp]
     L.ora_lowpass_process.argtypes = [C.c_void_p, _fp, _dp, C.c_size_t, C.c_double, C.c_double]
+    L.ora_engine_down.restype = C.c_size_t
+    L.ora_engine_down.argtypes = [C.c_void_p, C.c_void_p, _fp, C.c_size_t, C.c_double,
+                                  C.c_double, C.c_int, _dp]
     L.ora_decim_new.restype = C.c_void_p
     L.ora_decim_new.argtypes = [C.c_uint, C.c_uint]
     L.ora_decim_free.argtypes = [C.c_void_p]

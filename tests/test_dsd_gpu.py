@@ -95,3 +95,93 @@ def test_samerate_pipeline(oracle):
     want = np.stack(per, axis=1).reshape(-1)
     assert nb == want.size
     assert np.array_equal(out[:nb].cpu().numpy(), want)
+
+
+def _gpu_fir_for_dsd(dop, fs_in, fs_out, soft_clip, gs, ge):
+    """The FIR stage of the DSD rate-conversion pipeline from the library's
+    separate entry points: unpack, then the FIR upsampling chain (boxcar 8) or
+    the boxcar + FP64 decimation chain, with gain and clip."""
+    import ctypes as C
+    from foo_dsd_trellis_gb300 import _lib
+    from foo_dsd_trellis_gb300.fir import FirChain
+    nch, frames = dop.shape
+    n_in = 16 * frames
+    d_dop = torch.from_numpy(np.ascontiguousarray(dop)).cuda()
+    L = _lib.load()
+    h = C.c_void_p()
+    assert L.dsdgpu_create(0, C.byref(h)) == 0
+    try:
+        if fs_out > fs_in:
+            x = torch.empty((nch, n_in), dtype=torch.float32, device="cuda")
+            _lib.check(h, L.dsdgpu_dop_unpack_f32(h, nch, C.c_void_p(d_dop.data_ptr()), frames,
+                                                  frames, C.c_void_p(x.data_ptr()), n_in))
+            torch.cuda.synchronize()
+            fc = FirChain(fs_in, fs_out, boxcar_taps=8, soft_clip=soft_clip, num_channels=nch)
+            y = fc.process(x, gs, ge).cpu().numpy()
+            fc.close()
+            return y, x.cpu().numpy()
+        bits = torch.empty((nch, n_in), dtype=torch.uint8, device="cuda")
+        box = torch.empty((nch, n_in), dtype=torch.float64, device="cuda")
+        _lib.check(h, L.dsdgpu_dop_unpack(h, nch, C.c_void_p(d_dop.data_ptr()), frames, frames,
+                                          C.c_void_p(bits.data_ptr()), n_in))
+        _lib.check(h, L.dsdgpu_boxcar_setup(h, 8, nch))
+        _lib.check(h, L.dsdgpu_boxcar_process(h, 0, nch, C.c_void_p(bits.data_ptr()), n_in, n_in,
+                                              C.c_void_p(box.data_ptr()), n_in, 1.0, 1.0))
+        _lib.check(h, L.dsdgpu_decim_setup(h, fs_in, fs_out, nch))
+        out = torch.empty((nch, n_in), dtype=torch.float64, device="cuda")
+        n = C.c_size_t()
+        _lib.check(h, L.dsdgpu_decim_process_f64(h, nch, C.c_void_p(box.data_ptr()), n_in, n_in,
+                                                 C.c_void_p(out.data_ptr()), n_in, gs, ge,
+                                                 int(soft_clip), C.byref(n)))
+        return out[:, : n.value].cpu().numpy(), bits.cpu().numpy().astype(np.float32) * 2 - 1
+    finally:
+        L.dsdgpu_destroy(h)
+
+
+@pytest.mark.parametrize("fs_in,fs_out,mode", [(2822400, 5644800, "precorr"),
+                                               (2822400, 11289600, "trellis"),
+                                               (5644800, 2822400, "trellis"),
+                                               (11289600, 5644800, "precorr")])
+def test_dsd_rate_conversion_pipeline(oracle, fs_in, fs_out, mode):
+    """DSD -> DSD at another rate, the engine's rate-conversion branch with DSD
+    input (src/engine.c:600-729): DoP unpack, boxcar 8, FIR up (FP32 polyphase,
+    FP64 epilogue) or FP64 decimation down, gain ramp, soft clip unless
+    PreCorr, then the DAS trellis or PreCorr and packing.  The FIR stage is
+    checked against the oracle's FP64 restatement (1e-6 of full scale up, as
+    the PCM chain; 1e-12 down, FP64 throughout) and the pipeline's decisions
+    equal the oracle's SDM on that stage's output byte for byte."""
+    from foo_dsd_trellis_gb300 import _lib, ntf
+    from foo_dsd_trellis_gb300.pipeline import FULL_PARALLEL, OUT_BITS, Encoder
+    nch, K, depth, lat, ge = 2, 2, 4, 32, float(np.float32(0.708))
+    frames = 6000 if fs_out > fs_in else 12000
+    src = np.stack([_dsd_stream(oracle, 16 * frames, 5 + c, "clans-5", fs_in) for c in range(nch)])
+    dop = np.stack([oracle.dop_float_frames(src[c], 0) for c in range(nch)])
+    precorr = mode == "precorr"
+    f = ntf.auto_select_precorr(fs_out) if precorr else ntf.get_filter("clans-6", fs_out)
+    clip = not precorr
+    fir, x = _gpu_fir_for_dsd(dop, fs_in, fs_out, clip, 0.0, ge)
+    if fs_out > fs_in:
+        want_fir = np.stack([oracle.engine_fir(fs_in, fs_out, x[c], 8, ge, ge, clip) for c in range(nch)])
+        tol = 1e-6
+    else:
+        want_fir = np.stack([oracle.engine_down(oracle.Boxcar(8), oracle.Decimator(fs_in, fs_out),
+                                                x[c], 0.0, ge, clip) for c in range(nch)])
+        tol = 1e-12
+    assert fir.shape == want_fir.shape
+    assert np.max(np.abs(fir - want_fir)) <= tol * np.max(np.abs(want_fir))
+    enc = Encoder(fs_in, fs_out, nch, f, depth, K, lat, seg_len=32768, seed_mode=FULL_PARALLEL,
+                  reposition=True, boxcar_taps=8, soft_clip=True, output_format=OUT_BITS,
+                  sdm_mode=_lib.SDM_PRECORR if precorr else _lib.SDM_TRELLIS)
+    n_fir = fir.shape[1]
+    out = torch.empty((nch, n_fir + 256), dtype=torch.uint8, device="cuda")
+    ns, _ = enc.process(torch.from_numpy(dop).cuda(), out, 0.0, ge)
+    got = out[:, :ns].cpu().numpy()
+    if precorr:
+        want = np.stack([oracle.PreCorr(f.order, np.array(f.a), np.array(f.g), 0.0).process(fir[c])
+                         for c in range(nch)])
+    else:
+        want, _, _ = oracle.das_run(f.order, np.array(f.a), np.array(f.g), depth, K, lat, 0.0, fir,
+                                    seg_len=32768, seed_mode=0, reposition=True)
+    assert got.shape == want.shape
+    assert np.array_equal(got, want)
+    enc.close()

@@ -84,3 +84,20 @@ def test_das_oracle_structural_properties(oracle):
     b6, seams, starts = oracle.das_run(f.order, a, g, 16, 8, 16, 0.0, x, nsegs=6, seed_mode=0)
     # full-parallel: seg0 is cut back to its nominal length before the first overlap
     assert b6.shape[1] == len(x) - 64 * 16
+
+
+def test_oracle_dsd_down_branch_streams(oracle):
+    """The oracle's DSD -> DSD downsampling branch (boxcar, FP64 decimation,
+    gain, clip) carries its state: two chunks equal one pass, and with unit
+    gain and no clip it is the decimation of the boxcar mean."""
+    import numpy as np
+    rng = np.random.default_rng(4)
+    x = np.where(rng.random(40000) > 0.5, 1.0, -1.0).astype(np.float32)
+    one = oracle.engine_down(oracle.Boxcar(8), oracle.Decimator(5644800, 2822400), x, 0.7, 0.7, True)
+    bc, dec = oracle.Boxcar(8), oracle.Decimator(5644800, 2822400)
+    two = np.concatenate([oracle.engine_down(bc, dec, x[:12346], 0.7, 0.7, True),
+                          oracle.engine_down(bc, dec, x[12346:], 0.7, 0.7, True)])
+    assert np.array_equal(one, two)
+    plain = oracle.engine_down(oracle.Boxcar(8), oracle.Decimator(11289600, 2822400), x, 1.0, 1.0, False)
+    mean = oracle.Boxcar(8).process(x, 1.0, 1.0)
+    assert np.array_equal(plain, oracle.Decimator(11289600, 2822400).process(mean))

@@ -90,7 +90,9 @@ def test_pipeline_precorr_mode(oracle):
     ns, _ = enc.process(torch.from_numpy(pcm).cuda(), out, gain, gain)
     assert ns == n_fir
     got = out[:, :ns].cpu().numpy()
-    fc = FirChain(fs_in, fs_out, boxcar_taps=8, soft_clip=True, num_channels=nch)
+    # the engine does not soft-clip ahead of PreCorr (src/engine.c:704-717):
+    # the pipeline drops the clip it was given
+    fc = FirChain(fs_in, fs_out, boxcar_taps=8, soft_clip=False, num_channels=nch)
     fir = fc.process(torch.from_numpy(pcm).cuda(), gain, gain).cpu().numpy()
     for c in range(nch):
         y = fir[c]
