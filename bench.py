@@ -21,7 +21,8 @@ in one batched plan), diff16 (the adjoint of the differentiable path),
 dsd512conv6 (DSD512 5.1 with UPOLS room convolution), samerate128 (DoP DSD128
 re-encode on the engine's path-table parameters), samerate128lp (the same with
 the engine's 127-tap FIR lowpass instead of the boxcar), dsd2pcm128 (DSD128 ->
-44.1 kHz PCM) and precorr128 (PCM -> DSD128 with the PreCorr SDM).
+44.1 kHz PCM), precorr128 (PCM -> DSD128 with the PreCorr SDM) and dsd256to128
+(DoP DSD256 -> DSD128 through the FP64 decimation chain and the DAS trellis).
 """
 from __future__ import annotations
 
@@ -62,7 +63,8 @@ def parse():
                     help="nominal DAS segment length (profiling of small cases only)")
     ap.add_argument("--workload", default="dsd128_das",
                     choices=["dsd128_das", "multistream64", "diff16", "dsd512conv6",
-                             "samerate128", "samerate128lp", "precorr128", "dsd2pcm128"],
+                             "samerate128", "samerate128lp", "precorr128", "dsd2pcm128",
+                             "dsd256to128"],
                     help="multistream64: the batched 64-stream form; diff16: the adjoint; "
                          "samerate128 / samerate128lp / precorr128 / dsd2pcm128: the DSD "
                          "re-encode (boxcar / FIR lowpass), PreCorr and DSD -> PCM paths (each "
@@ -692,6 +694,15 @@ NEXT = {
                    "fir_mode FIR (src/engine.c:168-181)",
         ntf="clans-6", cands=2, depth=4, lat=128, das_seg_len=65536, lowpass_taps=127,
         lowpass_cutoff_hz=50000.0, gain="float32(0.708) (path gain)"),
+    "dsd256to128": dict(
+        metric="DSD256 -> DSD128 re-encode (DoP in -> unpack -> boxcar 8 -> FP64 half-band /2 -> "
+               "gain -> soft clip -> DAS trellis SDM -> DoP) DSD Msamples/s, bit-exact given the "
+               "FIR stage",
+        workload="dsd256_to_dsd128_stereo_10s", fs_in=11289600, fs=5644800,
+        path_table="DSD256 -> DSD128 row of the engine's path table (src/engine.c:78): SDM-6, "
+                   "K = 2, depth 8; lat 0 there = auto = 128 at DSD128",
+        ntf="sdm-6", cands=2, depth=8, lat=128, das_seg_len=65536, boxcar_taps=8,
+        gain="float32(0.708) (path gain)"),
     "precorr128": dict(
         metric="PCM 44.1 kHz -> DSD128 with the PreCorr SDM (FIR chain -> PreCorr -> DoP) "
                "DSD Msamples/s, bit-exact SDM",
@@ -705,18 +716,20 @@ NEXT = {
 PATH_GAIN = 0.708   # the engine's path gain (a float), include/dsd_types.h path table
 
 
-def _dsd128_source(secs: float, nch: int, seed: int):
-    """A DSD128 decision stream for the DSD-input workloads: the 44.1 kHz
-    multitone + pink noise through this library's PCM path (set-up, untimed)."""
+def _dsd128_source(secs: float, nch: int, seed: int, rate: int = 5644800):
+    """A DSD decision stream (DSD128 unless `rate` says otherwise) for the
+    DSD-input workloads: the 44.1 kHz multitone + pink noise through this
+    library's PCM path (set-up, untimed)."""
     import numpy as np
     import torch
     from foo_dsd_trellis_gb300 import ntf, signals
     from foo_dsd_trellis_gb300.pipeline import FULL_PARALLEL, OUT_BITS, PCM_FIR_GAIN, Encoder
     pcm = signals.dsd128_multitone_pink(secs, 44100, nch, seed)
-    f = ntf.get_filter("clans-7", 5644800)
-    src = Encoder(44100, 5644800, nch, f, 64, 32, 128, seg_len=65536, seed_mode=FULL_PARALLEL,
+    f = ntf.get_filter("clans-7", rate)
+    src = Encoder(44100, rate, nch, f, 64, 32, 128, seg_len=65536, seed_mode=FULL_PARALLEL,
                   output_format=OUT_BITS)
-    bits = torch.empty((nch, pcm.shape[1] * 128 + 256), dtype=torch.uint8, device="cuda")
+    bits = torch.empty((nch, pcm.shape[1] * (rate // 44100) + 256), dtype=torch.uint8,
+                       device="cuda")
     ns, _ = src.process(torch.from_numpy(pcm).cuda(), bits, PCM_FIR_GAIN, PCM_FIR_GAIN)
     src.close()
     return bits[:, : ns - ns % 16].cpu().numpy()
@@ -727,7 +740,7 @@ def _next_input(wl: str, secs: float, nch: int, seed: int):
     from foo_dsd_trellis_gb300 import signals
     if wl == "precorr128":
         return signals.dsd128_multitone_pink(secs, 44100, nch, seed), None
-    bits = _dsd128_source(secs, nch, seed)
+    bits = _dsd128_source(secs, nch, seed, NEXT[wl].get("fs_in", 5644800))
     return np.stack([signals.dop_floats(bits[c], 0) for c in range(nch)]), bits
 
 
@@ -764,6 +777,24 @@ def _next_cpu(wl: str, inp, bits, sample_s: float) -> dict:
         n = out.shape[0] * out.shape[1]
         what = ("DoP unpack + " + ("boxcar" if wl == "samerate128" else "FP64 lowpass restatement")
                 + " + trellis SDM port + DAS + DoP")
+    elif wl == "dsd256to128":
+        fs_in = cfg["fs_in"]
+        frames = int(sample_s * fs_in) // 16
+        x = inp[:, :frames]
+        nthreads = os.cpu_count() or 1
+        f = ntf.get_filter(cfg["ntf"], fs)
+        g = float(np.float32(PATH_GAIN))
+        t0 = time.perf_counter()
+        fir = np.stack([O.engine_down(O.Boxcar(cfg["boxcar_taps"]), O.Decimator(fs_in, fs),
+                                      O.dop_unpack(x[c]), g, g, True) for c in range(nch)])
+        out, _, _ = O.das_run(f.order, np.array(f.a), np.array(f.g), cfg["depth"], cfg["cands"],
+                              cfg["lat"], 0.0, fir, seg_len=cfg["das_seg_len"], seed_mode=0,
+                              reposition=True, nthreads=nthreads)
+        for c in range(nch):
+            O.dop_pack_bits(out[c], 0)
+        dt = time.perf_counter() - t0
+        n = out.shape[0] * out.shape[1]
+        what = "DoP unpack + boxcar + FP64 decimation restatement + trellis SDM port + DAS + DoP"
     elif wl == "precorr128":
         frames = int(sample_s * 44100)
         x = inp[:, :frames]
@@ -822,6 +853,13 @@ def run_next(args):
                       boxcar_taps=0, soft_clip=False, output_format=OUT_DOP,
                       samerate_filter=_lib.SAMERATE_LOWPASS if wl == "samerate128lp"
                       else _lib.SAMERATE_BOXCAR, device=local)
+    elif wl == "dsd256to128":
+        f = ntf.get_filter(cfg["ntf"], fs)
+        g = float(np.float32(PATH_GAIN))
+        enc = Encoder(cfg["fs_in"], fs, nch, f, cfg["depth"], cfg["cands"], cfg["lat"],
+                      seg_len=cfg["das_seg_len"], seed_mode=FULL_PARALLEL, reposition=True,
+                      boxcar_taps=cfg["boxcar_taps"], soft_clip=True, output_format=OUT_DOP,
+                      device=local)
     elif wl == "precorr128":
         f = ntf.auto_select_precorr(fs)
         g = PCM_FIR_GAIN
@@ -882,7 +920,7 @@ def run_next(args):
     e2e = {"value": job_throughput(e2e_units, args.steps, world, e2e_s), "unit": UNIT,
            "h2d_bytes_per_step": int(inp.nbytes), "d2h_bytes_per_step": int(nb2)}
     st = enc.stage_ms()
-    if wl in ("samerate128", "samerate128lp"):
+    if wl in ("samerate128", "samerate128lp", "dsd256to128"):
         sdm_s = statistics.mean(sdm_ms) / 1000.0
         flops = sdm_samples * cfg["cands"] * (5 * f.order + 6)
         roof = {"bound": "fp64", "achieved": flops / sdm_s / 1e12, "peak": fp64_peak / 1000.0,
