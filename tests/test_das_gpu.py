@@ -141,3 +141,21 @@ def test_balanced_launch_equals_plain():
     assert kernels == ["sdm_parts_kernel<7>", "sdm_jobs_kernel<7,32>"]
     assert outs[0][1] == outs[1][1]
     assert np.array_equal(outs[0][0], outs[1][0])
+
+
+def test_das_output_counts_over_chunks(oracle):
+    """The plugin's DAS output check (src/dsp_plugin.c:2729-2745): in seg0-first
+    mode a channel's first chunk comes out trellis_lat samples short of its
+    FIR count (the latency fill) and every later chunk exactly at it, so
+    chunks of a multiple of 16 keep the DoP frame alignment."""
+    from foo_dsd_trellis_gb300.das import DasChannels
+    f = _ntf("clans-6", 5644800)
+    lat = 64
+    d = DasChannels(f.order, f.a, f.g, 16, 8, lat, num_channels=2)
+    for k, n in enumerate((160000, 96000, 131072)):
+        x = np.stack([multitone(n, 40 + k) * 1.4, multitone(n, 50 + k) * 1.2])
+        got, _ = d.process_chunk(torch.from_numpy(x).cuda(), seg_len=32768, seed_mode=1)
+        want = n - lat if k == 0 else n
+        assert got.shape == (2, want)
+        assert want % 16 == 0
+    d.close()
