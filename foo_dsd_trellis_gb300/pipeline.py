@@ -1,10 +1,17 @@
-"""Host-side mirror of the reference's PCM -> DSD conversion with DAS.
+"""Host-side mirror of the reference's PCM/DSD -> DSD conversion with DAS.
 
 `Encoder` drives libdsdgpu's whole-path entry points: FIR chain with the
 engine glue (boxcar, gain ramp, soft clip), segment-parallel trellis SDM with
-Density-Aligned Stitching, and DoP / native packing — the GPU counterpart of
-plugin_process_pcm with the DAS phases of plugin_process
-(reference src/dsp_plugin.c:2990-3216, 1283-2945).
+Density-Aligned Stitching (or PreCorr), and DoP / native packing — the GPU
+counterpart of plugin_process_pcm with the DAS phases of plugin_process
+(reference src/dsp_plugin.c:2990-3216, 1283-2945) and of engine_process_block's
+DSD branches (src/engine.c:479-729).
+
+The input follows the rates, as the engine decides: below 2,822,400 Hz it is
+planar float32 PCM; at or above it, planar DoP floats (16 DSD samples a frame),
+re-encoded at the same rate (boxcar or, with samerate_filter, the FIR
+lowpass), converted to a higher DSD rate (FIR upsampling on the +-1 input) or
+a lower one (FP64 decimation), or decimated to PCM with output_format OUT_PCM.
 """
 from __future__ import annotations
 
