@@ -33,9 +33,12 @@
 namespace dsdgpu {
 
 // One warp per CTA (one job, or 32 / LPJ jobs side by side for K <= 16): a
-// few thousand long-running jobs spread evenly over the SMs.  The launch bound (32 threads, 13 CTAs per SM) holds the kernel
-// at 128 registers; a 152-register build measured 50 % slower on the DSD128
-// DAS workload.
+// few thousand long-running jobs spread evenly over the SMs.  At 32 lanes the
+// launch bound (32 threads, 13 CTAs per SM) holds the kernel at 128 registers
+// (a 152-register build measured 50 % slower on the DSD128 DAS workload, with
+// fewer warps per FP64 pipe); narrower widths take 10 CTAs per SM, which left
+// the 16-lane order-8 kernel at 168 registers with 60 bytes of spills instead
+// of 344 and ran the DSD512 workload 6.7 % faster (442.1 -> 471.5).
 constexpr int kRegRingWords = 8;      // rings held in registers: lat <= 256
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -166,9 +169,12 @@ static int resident_warps() {
 static int launch_lanes(const SdmParams& P, int njobs, int max_blocks) {
   if (P.lanes > 0 || max_blocks > 0 || P.lat > 32 * kRegRingWords) return lanes_per_job(P);
   const int lo = min_lanes(P.cands);
-  const int slots = resident_warps();
   int lanes = 32;
-  while (lanes > lo && (long long)njobs * lanes > (long long)slots * 32) lanes >>= 1;
+  // warp slots of a width: 16 one-warp CTAs per SM at 32 lanes (128 registers),
+  // 10 below (their launch bound leaves up to 204 registers)
+  while (lanes > lo &&
+         (long long)njobs * lanes > (long long)resident_warps() / 16 * (lanes == 32 ? 16 : 10) * 32)
+    lanes >>= 1;
   return lanes;
 }
 
@@ -698,7 +704,7 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
 }
 
 template <int N, int LPJ>
-__global__ void __launch_bounds__(32, 13)
+__global__ void __launch_bounds__(32, LPJ == 32 ? 13 : 10)
 sdm_jobs_kernel(SdmParams P, const SdmJob* __restrict__ jobs, int njobs,
                 int* __restrict__ job_counter, SdmCtx* __restrict__ ctxs,
                 int* __restrict__ status) {
