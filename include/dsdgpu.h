@@ -219,7 +219,7 @@ int dsdgpu_sdm_copy_state(dsdgpu_context_t *ctx, int dst, int src);
 int dsdgpu_sdm_segments(dsdgpu_context_t *ctx, dsdgpu_segment_t *segs, int nseg);
 
 /* ---- FIR chain (replaces fir_chain_init_ex / fir_chain_process_d /
- *      fir_chain_reset, include/fir.h:178-203, and gpu_cuda_fir_chain_f64,
+ *      fir_chain_reset, include/fir.h:55-83, and gpu_cuda_fir_chain_f64,
  *      include/gpu_compute.h) ---- */
 
 /* Plan the chain and allocate per-channel history for `num_channels`. */
