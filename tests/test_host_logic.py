@@ -101,3 +101,14 @@ def test_oracle_dsd_down_branch_streams(oracle):
     plain = oracle.engine_down(oracle.Boxcar(8), oracle.Decimator(11289600, 2822400), x, 1.0, 1.0, False)
     mean = oracle.Boxcar(8).process(x, 1.0, 1.0)
     assert np.array_equal(plain, oracle.Decimator(11289600, 2822400).process(mean))
+
+
+def test_reference_citations_resolve():
+    """Every reference file:line cited in the repository's tracked files
+    exists in the reference tree (checked where the oracle is built)."""
+    import pytest
+    from oracle import check_citations
+    if not check_citations.reference_present():
+        pytest.skip("reference tree not present")
+    bad = check_citations.bad_citations()
+    assert not bad, bad[:10]
