@@ -1,7 +1,7 @@
 """NTF coefficient sets and their lookup rules.
 
 The coefficients are the reference's (src/ntf.c:16-790), carried bit-exactly
-in ntf_table.json (hex floats, regenerated by gen_ntf_table.py).  The lookup
+in ntf_table.json (hex floats, regenerated by oracle/gen_ntf_table.py).  The lookup
 functions follow the reference's: ntf_get_filter picks the first table entry
 whose name matches and whose design rate is <= the DSD rate
 (src/ntf.c:814-832), so 48 kHz-family rates use the 44.1 kHz table below them;

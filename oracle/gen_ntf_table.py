@@ -1,10 +1,12 @@
-"""Regenerate ntf_table.json from the reference's own NTF table (src/ntf.c).
+"""Regenerate foo_dsd_trellis_gb300/ntf_table.json from the reference's own
+NTF table (src/ntf.c).
 
-The coefficients must be bit-identical to the reference's, so they are not
-retyped: this script compiles the reference's src/ntf.c (via oracle/Makefile,
-target `ref`, which reads the reference sources where they lie) and dumps every
-entry with exact hex-float encodings.  Run it only where the reference tree is
-present; the JSON it writes is committed.
+Test and build infrastructure, not product code: the package only reads the
+JSON this writes.  The coefficients must be bit-identical to the reference's,
+so they are not retyped: this script compiles the reference's src/ntf.c (via
+oracle/Makefile, target `ref`, which reads the reference sources where they
+lie) and dumps every entry with exact hex-float encodings.  Run it only where
+the reference tree is present; the JSON it writes is committed.
 """
 from __future__ import annotations
 
@@ -17,6 +19,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
+TABLE = os.path.join(ROOT, "foo_dsd_trellis_gb300", "ntf_table.json")
 sys.path.insert(0, ROOT)
 
 
@@ -49,7 +52,7 @@ def main() -> None:
                   "whose name matches and whose freq <= the DSD rate, src/ntf.c:814-832)",
         "filters": entries,
     }
-    with open(os.path.join(HERE, "ntf_table.json"), "w") as f:
+    with open(TABLE, "w") as f:
         json.dump(doc, f, indent=1)
     print(f"wrote {len(entries)} filters")
 
