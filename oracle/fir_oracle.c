@@ -86,19 +86,22 @@ int ora_fir_plan(unsigned fs_in, unsigned fs_out, int *factors, int *ntaps)
     return stages;
 }
 
-/* One upsampling stage, fresh delay line. */
+/* One upsampling stage, fresh delay line.  Output m = U*i + r sums
+ * h[k] * z[m - k] over k = r, r + U, ... (ascending), and z[m - k] is the
+ * input sample in[i - j] for k = r + U*j; terms before the stream start
+ * (j > i) are the zero delay line and are skipped. */
 static void upsample_stage(const double *in, size_t n, int U, const double *h, int ntaps,
                            double *out)
 {
-    for (size_t m = 0; m < n * (size_t)U; m++) {
-        double acc = 0.0;
-        const int r = (int)(m % (size_t)U);
-        for (int k = r; k < ntaps; k += U) {
-            long long src = (long long)m - k;       /* index into the stuffed stream */
-            if (src < 0) break;
-            acc += h[k] * in[src / U];
+    for (size_t i = 0; i < n; i++) {
+        const size_t jmax = i;
+        for (int r = 0; r < U; r++) {
+            double acc = 0.0;
+            size_t j = 0;
+            for (int k = r; k < ntaps && j <= jmax; k += U, j++)
+                acc += h[k] * in[i - j];
+            out[i * (size_t)U + (size_t)r] = acc;
         }
-        out[m] = acc;
     }
 }
 
