@@ -44,7 +44,11 @@ UNIT = "DSD Msamples/s"
 WL = dict(workload="dsd128_das_stereo_10s_multitone_pink", fs_in=48000, fs_out=6144000,
           channels=2, seconds=10.0, ntf="clans-7", ntf_order=7, cands=32, depth=64, lat=128,
           das_seg_len=65536, das_overlap=64 * 128, seed_mode="full_parallel", output="dop",
-          boxcar_taps=8, soft_clip=True, seed=1001)
+          boxcar_taps=8, soft_clip=True, seed=1001,
+          # engine_channel_init's PCM gain: float32(0.708) * 0.5 (src/engine.c:206-210)
+          fir_gain=0.3540000021457672,
+          l2="GPU arm: 512 MiB written between timed steps, outside the events; the CPU arm "
+             "has no device cache to flush")
 FP64_OPS_PER_CAND_SAMPLE = 5 * WL["ntf_order"] + 6   # (2N+1) mul + (3N+5) add
 SDM_DRAM_BYTES_PER_SAMPLE = 9.04                      # measured, see the traffic note below
 SDM_PARTS_DRAM_BYTES_PER_SAMPLE = 9.15                # the balanced launch's (parts kernel), measured
@@ -154,59 +158,143 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(pcm, seconds_sample: float, nthreads: int | None = None) -> dict:
-    """The oracle's C port of the same path (FP64 FIR restatement, trellis SDM
-    port bit-identical to the reference's trellis.c, DAS restatement, DoP) on a
-    leading slice of the workload, on this host's cores."""
+def _cpu_fir(O, pcm):
+    """FP64 FIR restatement per channel, one thread per channel as the
+    reference's DAS phase 1 runs it (src/dsp_plugin.c:1381-1460)."""
     import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+    from foo_dsd_trellis_gb300.pipeline import PCM_FIR_GAIN
+
+    def one(c):
+        return O.engine_fir(WL["fs_in"], WL["fs_out"], pcm[c], boxcar_taps=WL["boxcar_taps"],
+                            g_start=PCM_FIR_GAIN, g_end=PCM_FIR_GAIN, soft_clip=True)
+    with ThreadPoolExecutor(max_workers=pcm.shape[0]) as ex:
+        return np.stack(list(ex.map(one, range(pcm.shape[0]))))
+
+
+def _cpu_das_dop(O, f, fir, nthreads):
+    """Trellis SDM port + DAS + DoP over one chunk; returns (decisions, DoP
+    bytes interleaved [n/16][nch][3] as the plugin writes frames)."""
+    import numpy as np
+    bits, _, _ = O.das_run(f.order, np.array(f.a), np.array(f.g), WL["depth"], WL["cands"],
+                           WL["lat"], 0.0, fir, seg_len=WL["das_seg_len"], seed_mode=0,
+                           reposition=True, nthreads=nthreads)
+    frames = [O.dop_pack_bits(bits[c], 0)[0].reshape(-1, 3) for c in range(bits.shape[0])]
+    return bits, np.stack(frames, axis=1).reshape(-1)
+
+
+def cpu_baseline(pcm, seconds_sample: float, nthreads: int | None = None,
+                 first_frame: int = 0) -> dict:
+    """The oracle's C port of the same path (FP64 FIR restatement, trellis SDM
+    port bit-identical to the reference's trellis.c, DAS restatement, DoP) on
+    one slice of the workload converted as its own chunk, on this host's cores."""
     from oracle import oracle as O
     from foo_dsd_trellis_gb300 import ntf
     O.build()
     f = ntf.get_filter(WL["ntf"], WL["fs_out"])
-    frames = int(seconds_sample * WL["fs_in"])
-    x = pcm[:, :frames]
-    from foo_dsd_trellis_gb300.pipeline import PCM_FIR_GAIN
+    frames = int(round(seconds_sample * WL["fs_in"]))
+    x = pcm[:, first_frame:first_frame + frames]
     nthreads = nthreads or os.cpu_count() or 1
     t0 = time.perf_counter()
-    fir = np.stack([O.engine_fir(WL["fs_in"], WL["fs_out"], x[c], boxcar_taps=WL["boxcar_taps"],
-                                 g_start=PCM_FIR_GAIN, g_end=PCM_FIR_GAIN, soft_clip=True)
-                    for c in range(x.shape[0])])
-    bits, _, _ = O.das_run(f.order, np.array(f.a), np.array(f.g), WL["depth"], WL["cands"],
-                           WL["lat"], 0.0, fir, seg_len=WL["das_seg_len"], seed_mode=0,
-                           reposition=True, nthreads=nthreads)
-    for c in range(bits.shape[0]):
-        O.dop_pack_bits(bits[c], 0)
+    fir = _cpu_fir(O, x)
+    bits, _ = _cpu_das_dop(O, f, fir, nthreads)
     dt = time.perf_counter() - t0
     n_out = bits.shape[0] * bits.shape[1]
     return {"value": n_out / dt / 1e6, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"first {seconds_sample:g} s of the workload ({x.shape[0]} ch, "
-                      f"{n_out} DSD samples): FP64 FIR restatement + trellis SDM port + DAS + DoP",
+            "sample": f"{seconds_sample:g} s of the workload from frame {first_frame} "
+                      f"({x.shape[0]} ch, {n_out} DSD samples) as one chunk: FP64 FIR "
+                      "restatement + trellis SDM port + DAS + DoP",
             "seconds": dt}
 
 
+def parity_and_cpu_baseline(pcm, gpu_dop, device: int) -> tuple[dict, dict]:
+    """Outside the timed region: the oracle over the whole workload.
+
+    The GPU FIR output (same kernel and parameters, a separate context) goes
+    through the oracle's DAS (trellis SDM pinned to the reference's trellis.c)
+    and DoP packer on every host core; its bytes are compared with the timed
+    run's DoP output.  The same oracle run, plus the FP64 FIR restatement over
+    the whole input, is the CPU baseline on the full workload."""
+    import hashlib
+
+    import numpy as np
+    import torch
+    from oracle import oracle as O
+    from foo_dsd_trellis_gb300 import ntf
+    from foo_dsd_trellis_gb300.fir import FirChain
+    from foo_dsd_trellis_gb300.pipeline import PCM_FIR_GAIN
+    O.build()
+    f = ntf.get_filter(WL["ntf"], WL["fs_out"])
+    nthreads = os.cpu_count() or 1
+    fc = FirChain(WL["fs_in"], WL["fs_out"], boxcar_taps=WL["boxcar_taps"], soft_clip=True,
+                  num_channels=pcm.shape[0], device=device)
+    gfir = fc.process(torch.from_numpy(pcm).cuda(), PCM_FIR_GAIN, PCM_FIR_GAIN).cpu().numpy()
+    fc.close()
+    t0 = time.perf_counter()
+    bits, want = _cpu_das_dop(O, f, gfir, nthreads)
+    t_das = time.perf_counter() - t0
+    del gfir
+    t0 = time.perf_counter()
+    _cpu_fir(O, pcm)
+    t_fir = time.perf_counter() - t0
+    got = np.asarray(gpu_dop, np.uint8)
+    same_len = len(got) == len(want)
+    diff = np.nonzero(got[:len(want)] != want[:len(got)])[0]
+    parity = {"bit_exact": bool(same_len and diff.size == 0), "dop_bytes": int(len(want)),
+              "gpu_dop_bytes": int(len(got)), "differing_bytes": int(diff.size),
+              "sha256": hashlib.sha256(want.tobytes()).hexdigest(),
+              "sha256_gpu": hashlib.sha256(got.tobytes()).hexdigest(),
+              "oracle": "oracle DAS (trellis SDM port pinned to the reference's trellis.c) + "
+                        "DoP packer over the GPU FIR output of the whole workload, compared "
+                        "with the last timed step's DoP bytes"}
+    n_out = bits.shape[0] * bits.shape[1]
+    cpu = {"value": n_out / (t_fir + t_das) / 1e6, "unit": UNIT, "cores": nthreads,
+           "kind": "port", "seconds": t_fir + t_das, "fir_seconds": t_fir, "das_seconds": t_das,
+           "sample": f"the whole workload ({pcm.shape[0]} ch, {n_out} DSD samples): FP64 FIR "
+                     "restatement (one thread per channel) + trellis SDM port + DAS + DoP on "
+                     f"{nthreads} threads; the DAS leg runs on the GPU's FIR output, so its "
+                     "decisions are the parity check"}
+    return parity, cpu
+
+
+REF_SLICES = 20
+
+
 def run_reference(args):
+    """The CPU arm: every step converts one of REF_SLICES equal slices of the
+    workload's input as its own DAS chunk (65,536-sample segments, the same
+    trellis and seeding), in rotation, so REF_SLICES timed steps convert the
+    whole input once."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     import numpy as np
     from foo_dsd_trellis_gb300 import signals
     pcm = signals.dsd128_multitone_pink(args.seconds, WL["fs_in"], WL["channels"], WL["seed"])
-    sample_s = 0.5
-    for _ in range(args.warmup):
-        cpu_baseline(pcm, 0.05)
-    vals, secs = [], []
+    frames = pcm.shape[1]
+    per = frames // REF_SLICES
+    sample_s = per / WL["fs_in"]
+    for i in range(args.warmup):
+        cpu_baseline(pcm, sample_s, first_frame=(i % REF_SLICES) * per)
+    vals, secs, outs = [], [], 0
     info = None
-    for _ in range(args.steps):
-        info = cpu_baseline(pcm, sample_s)
-        vals.append(info["value"])
+    for i in range(args.steps):
+        info = cpu_baseline(pcm, sample_s, first_frame=(i % REF_SLICES) * per)
         secs.append(info["seconds"])
-    v = float(np.mean(vals))
+        outs += info["value"] * info["seconds"]
+    v = float(outs / sum(secs))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * float(np.mean(secs)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": dict(WL, seconds=args.seconds, cpu_sample_seconds=sample_s),
+            "data": "synthetic", "config": dict(WL, seconds=args.seconds),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": "port",
-                             "sample": info["sample"]},
+                             "sample": f"each step converts one {sample_s:g} s slice "
+                                       f"({REF_SLICES} slices of the {args.seconds:g} s input, "
+                                       "taken in rotation, so every "
+                                       f"{REF_SLICES} steps convert the whole input) as one "
+                                       "DAS chunk of the workload's segment length: FP64 FIR "
+                                       "restatement (one thread per channel) + trellis SDM "
+                                       "port + DAS + DoP"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -260,7 +348,11 @@ def run_ours(args):
             import torch.distributed as dist
             dist.barrier()
 
+    # every step converts the 10 s input as a new stream (plugin_flush between
+    # steps, outside the timed region), so every step's output is the same and
+    # the last one can be checked against the oracle
     for _ in range(args.warmup):
+        enc.flush()
         enc.process(d_pcm, d_out)
     torch.cuda.synchronize()
 
@@ -274,6 +366,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     clocks.start()
     for _ in range(args.steps):
+        enc.flush()
         flush.fill_(1)                      # evict L2 between steps (outside the events)
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -299,26 +392,47 @@ def run_ours(args):
     # end to end through the host-buffer C-ABI call (pinned host memory)
     h_pcm = torch.from_numpy(pcm).pin_memory().numpy()
     h_out = torch.empty(enc.out_capacity(frames) + 64, dtype=torch.uint8).pin_memory().numpy()
+    enc.flush()
     enc.process_host(h_pcm, h_out)
     t0 = time.perf_counter()
     for _ in range(args.steps):
+        enc.flush()
         ns, nb = enc.process_host(h_pcm, h_out)
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e_value = job_throughput(ns * nch, args.steps, world, e2e_s)
 
-    # roofline of the dominant kernel: the persistent trellis SDM launch
+    # roofline of the dominant kernel: the persistent trellis SDM launch.  The
+    # algorithmic work is the reference's K (5N + 6) FP64 operations per
+    # candidate and OUTPUT sample (both channels); the DAS warm-up and overlap
+    # extension of every segment are the algorithm's own redundancy and are
+    # reported beside it, not counted as work.
     sdm_s = statistics.mean(sdm_ms) / 1000.0
-    flops = sdm_samples * WL["cands"] * FP64_OPS_PER_CAND_SAMPLE
+    flops_per_sample = WL["cands"] * FP64_OPS_PER_CAND_SAMPLE
+    flops = out_samples_step * flops_per_sample
     achieved = flops / sdm_s / 1e12
+    issued = sdm_samples * flops_per_sample / sdm_s / 1e12
     peak = fp64_peak / 1000.0
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    sm_mhz = clk.get("sm_mhz") or 0.0
+    # 2 FP64 add/mul per clock per SM (a 64-cycle warp instruction per sub-partition)
+    peak_nominal = 2.0 * sms * sm_mhz * 1e6 / 1e12 if sm_mhz else None
     kernel = enc.last_sdm_kernel()
     roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak, "traffic": None, "kernel": kernel,
                 "peak_source": "DADD/DMUL issue rate measured in this run (dsdgpu_probe_fp64); "
                                "MEASURED_PEAKS.json has no FP64 entry",
                 "algorithmic_flops_per_launch": flops,
+                "output_samples_per_launch": out_samples_step,
+                "flops_per_sample": flops_per_sample,
+                "flops_definition": "output DSD samples (both channels) x K x (5N + 6)",
+                "peak_nominal": peak_nominal,
+                "frac_nominal": achieved / peak_nominal if peak_nominal else None,
+                "peak_nominal_source": "2 FP64 add/mul per clock per SM x SMs x median SM clock "
+                                       "sampled during the timed steps",
                 "sdm_input_samples_per_launch": sdm_samples,
-                "flops_per_sample": WL["cands"] * FP64_OPS_PER_CAND_SAMPLE}
+                "das_redundancy": sdm_samples / out_samples_step - 1.0,
+                "issued_tflops": issued,
+                "issue_frac": issued / peak}
     # DRAM bytes per launch: ncu's dram__bytes per SDM input sample of the
     # kernel that ran (one job per warp: the 4 s, 32,768-segment case; parts:
     # the 3.5 s case, profiles/sdm_parts_kernel_dsd128_das_3p5s.md), scaled by
@@ -343,9 +457,10 @@ def run_ours(args):
                  "batched_over_plain": batched_sps / plain_sps,
                  "note": "SDM input samples/s; plain = one 81,920-sample DAS segment per launch"}
 
-    cpu = None
+    cpu = parity = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(pcm, 2.0)
+        gpu_dop = d_out[:nbytes].cpu().numpy()
+        parity, cpu = parity_and_cpu_baseline(pcm, gpu_dop, local)
         one = cpu_baseline(pcm, 0.1, nthreads=1)
         cpu["single_core"] = {"value": one["value"], "cores": 1, "sample": one["sample"]}
 
@@ -354,12 +469,12 @@ def run_ours(args):
                 "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": 1000 * total_s / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": dict(WL, seconds=args.seconds, l2="512 MiB written between timed steps (outside the events)",
-                               fir_gain=PCM_FIR_GAIN),
+                "config": dict(WL, seconds=args.seconds),
                 "xrt": xrt,
                 "e2e": {"value": e2e_value, "unit": UNIT,
                         "h2d_bytes_per_step": int(pcm.nbytes), "d2h_bytes_per_step": int(nb)},
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+                "parity": parity,
                 "gpu_launches": int(launches), "stages_ms": stages, "plain": plain,
                 "fp64_peak_gops": fp64_peak}
         print(json.dumps(line), flush=True)

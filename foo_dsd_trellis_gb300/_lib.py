@@ -137,14 +137,15 @@ SIGNATURES = {
                                   C.POINTER(C.c_int)]),
     "dsdgpu_pack_native": (C.c_int, [_vp, C.c_int, _vp, _sz, _sz, _vp, _sz]),
     "dsdgpu_pipeline_setup": (C.c_int, [_vp, C.POINTER(PipelineParams), C.c_int]),
+    "dsdgpu_pipeline_flush": (C.c_int, [_vp]),
     "dsdgpu_pipeline_process": (C.c_int, [_vp, _vp, _sz, _sz, C.c_double, C.c_double, _vp, _sz,
                                           _szp, _szp]),
     "dsdgpu_pipeline_process_host": (C.c_int, [_vp, _vp, _sz, C.c_double, C.c_double, _vp, _sz,
                                                _szp, _szp]),
     "dsdgpu_stage_times": (C.c_int, [_vp, C.POINTER(C.c_float)]),
     "dsdgpu_get_stream": (C.c_int, [_vp, C.POINTER(_vp)]),
-    "dsdgpu_sdm_process_noalloc": (C.c_int, [C.POINTER(SdmParams), C.c_int, _vp, _sz, _sz,
-                                             _vp, _sz, _szp, _vp]),
+    "dsdgpu_sdm_process_noalloc": (C.c_int, [C.POINTER(SdmParams), C.c_int, C.c_int, _vp, _sz,
+                                             _sz, _vp, _sz, _szp, _vp]),
     "dsdgpu_probe_fp64": (C.c_int, [_vp, C.POINTER(C.c_double)]),
     "dsdgpu_plan_create": (C.c_int, [_vp, C.POINTER(StreamDesc), C.c_int, C.c_int64, C.c_int,
                                      C.c_uint64, C.POINTER(_vp)]),

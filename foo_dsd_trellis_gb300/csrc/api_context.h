@@ -31,7 +31,6 @@ int launch_sdm_parts(const SdmParams& P, const SdmJob* d_jobs, int njobs, long l
                      unsigned long long* d_queue, long long total, int warps_per_pipe, int sms,
                      SdmCtx* d_ctxs, int* d_status, cudaStream_t stream);
 int lanes_per_job(const SdmParams& P);      // the fixed width of capped launches
-int sdm_max_lat_in_registers();
 int launch_pack_dop(const uint8_t* bits, size_t stride, int nch, size_t frames, int phase,
                     uint8_t* out, int num_sms, cudaStream_t stream);
 int launch_pack_native(const uint8_t* bits, size_t stride, int nch, size_t n, uint8_t* out,

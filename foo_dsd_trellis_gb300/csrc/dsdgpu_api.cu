@@ -13,7 +13,6 @@ namespace dsdgpu {
 
 int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_counter,
                     SdmCtx* d_ctxs, int* d_status, int max_blocks, cudaStream_t stream);
-int sdm_max_lat_in_registers();
 
 // (Re)initialise contexts [first, first + count) to the state sdm_context_init
 // leaves (src/trellis.c:977-1011): one live candidate in slot 0 of bank 0,
@@ -173,10 +172,6 @@ int sdm_params_from_abi(const dsdgpu_sdm_params_t* p, dsdgpu::SdmParams* P, cons
   if (p->depth < 1 || p->depth > 64) { *err = "depth out of range"; return DSDGPU_ERR_ARG; }
   if (p->cands < 1 || p->cands > kMaxCands) { *err = "cands out of range"; return DSDGPU_ERR_ARG; }
   if (p->lat < 1 || p->lat > kMaxLat) { *err = "lat out of range"; return DSDGPU_ERR_ARG; }
-  if (p->lat > sdm_max_lat_in_registers()) {
-    *err = "lat above the register-ring limit of this library";
-    return DSDGPU_ERR_UNSUPPORTED;
-  }
   memset(P, 0, sizeof *P);
   for (int i = 0; i < p->order; i++) { P->a[i] = p->a[i]; P->g[i] = p->g[i]; }
   P->state_limit = p->state_limit;
@@ -319,6 +314,17 @@ int dsdgpu_sdm_process(dsdgpu_context_t* c, int first, int nch, const double* d_
   if (!c->sdm_ready) return c->fail(DSDGPU_ERR_STATE, "sdm not set up");
   if (first < 0 || nch < 1 || first + nch > c->nctx) return c->fail(DSDGPU_ERR_ARG, "bad channel range");
   if (count > 0 && (!d_in || !d_out)) return c->fail(DSDGPU_ERR_ARG, "null buffer");
+  if (nch > 1 && count > 0) {
+    // rows of different channels must not overlap
+    int64_t max_out = 0;
+    for (int ch = 0; ch < nch; ch++) {
+      int64_t skip, out, np;
+      c->plan_steps(c->pending[first + ch], (int64_t)count, 0, &skip, &out, &np);
+      max_out = std::max(max_out, out);
+    }
+    if (in_stride < count || out_stride < (size_t)max_out)
+      return c->fail(DSDGPU_ERR_ARG, "row stride shorter than a channel's rows");
+  }
   cudaSetDevice(c->device);
   std::vector<SdmJob> jobs;
   for (int ch = 0; ch < nch; ch++) {

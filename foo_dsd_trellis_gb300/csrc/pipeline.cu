@@ -88,6 +88,35 @@ int dsdgpu_pipeline_setup(dsdgpu_context_t* c, const dsdgpu_pipeline_params_t* p
   return DSDGPU_OK;
 }
 
+// plugin_flush (src/dsp_plugin.c:3622-3653): every channel's SDM (or PreCorr)
+// state, the filters' histories and the DoP marker phase start over, so the
+// next chunk converts as the first chunk of a new stream.
+int dsdgpu_pipeline_flush(dsdgpu_context_t* c) {
+  if (!c) return DSDGPU_ERR_ARG;
+  if (!c->pipe_ready) return c->fail(DSDGPU_ERR_STATE, "pipeline not set up");
+  int rc = DSDGPU_OK;
+  if (c->pipe_pcm_out) {
+    rc = dsdgpu_decim_reset(c);
+  } else {
+    rc = c->pipe_precorr ? dsdgpu_precorr_reset(c) : dsdgpu_sdm_reset(c, -1);
+    if (!rc) {
+      if (c->pipe_dsd_down) {
+        rc = dsdgpu_boxcar_reset(c);
+        if (!rc) rc = dsdgpu_decim_reset(c);
+      } else if (c->pipe_lowpass) {
+        rc = dsdgpu_lowpass_reset(c);
+      } else if (c->pipe_same_rate) {
+        rc = dsdgpu_boxcar_reset(c);
+      } else {
+        rc = dsdgpu_fir_reset(c);
+      }
+    }
+    if (!rc && c->conv) rc = dsdgpu_conv_reset(c);
+  }
+  c->dop_phase = 0;
+  return rc;
+}
+
 int dsdgpu_pipeline_process(dsdgpu_context_t* c, const float* d_pcm, size_t pcm_stride,
                             size_t frames, double gain_start, double gain_end, uint8_t* d_out,
                             size_t out_stride, size_t* out_samples, size_t* out_bytes) {

@@ -993,6 +993,5 @@ int launch_sdm_jobs(const SdmParams& P, const SdmJob* d_jobs, int njobs, int* d_
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int sdm_max_lat_in_registers() { return 32 * kRingWords; }
 
 }  // namespace dsdgpu

@@ -102,6 +102,11 @@ class Encoder:
         from . import conv
         conv.setup(self.L, self.h, ir, partition)
 
+    def flush(self) -> None:
+        """Start a new stream (plugin_flush, src/dsp_plugin.c:3622-3653): SDM
+        state, filter histories and the DoP marker phase are reset."""
+        _lib.check(self.h, self.L.dsdgpu_pipeline_flush(self.h))
+
     def process(self, pcm: torch.Tensor, out: torch.Tensor, gain_start: float = PCM_FIR_GAIN,
                 gain_end: float = PCM_FIR_GAIN):
         """Device buffers: pcm [nch, frames] float32; out a uint8 tensor whose rows

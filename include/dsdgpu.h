@@ -193,7 +193,9 @@ int dsdgpu_sdm_reset(dsdgpu_context_t *ctx, int channel);
 /* sdm_process_block on contexts [first, first + nch): channel c reads
  * d_in[c * in_stride ...] (count doubles) and writes its decisions to
  * d_out[c * out_stride ...].  out_counts[c] receives the decisions of channel
- * c (count minus what is still filling the latency); may be NULL. */
+ * c (count minus what is still filling the latency); may be NULL.  With more
+ * than one channel, in_stride must be at least count and out_stride at least
+ * the decisions a channel writes (DSDGPU_ERR_ARG otherwise). */
 int dsdgpu_sdm_process(dsdgpu_context_t *ctx, int first, int nch,
                        const double *d_in, size_t in_stride, size_t count,
                        uint8_t *d_out, size_t out_stride, size_t *out_counts);
@@ -294,6 +296,11 @@ int dsdgpu_pipeline_process(dsdgpu_context_t *ctx, const float *d_pcm, size_t pc
 int dsdgpu_pipeline_process_host(dsdgpu_context_t *ctx, const float *h_pcm, size_t frames,
                                  double gain_start, double gain_end, uint8_t *h_out,
                                  size_t out_capacity, size_t *out_samples, size_t *out_bytes);
+/* plugin_flush (src/dsp_plugin.c:3622-3653): reset every channel's SDM or
+ * PreCorr state, the FIR / boxcar / lowpass / decimation / convolution
+ * histories and the DoP marker phase, so that the next
+ * dsdgpu_pipeline_process call starts a new stream (seek, track change). */
+int dsdgpu_pipeline_flush(dsdgpu_context_t *ctx);
 /* Milliseconds of the last pipeline call, measured with CUDA events on the
  * context's stream: [FIR, segment SDM launch, DAS total, pack, whole call]. */
 int dsdgpu_stage_times(const dsdgpu_context_t *ctx, float *ms5);
@@ -303,20 +310,33 @@ int dsdgpu_get_stream(const dsdgpu_context_t *ctx, void **stream);
 /* Allocation-free trellis SDM (no counterpart in the reference; added for
  * callers that cannot allocate device memory, such as a player's real-time
  * audio callback, where an allocation can block and cause a dropout, or a host
- * that grants a fixed device-memory budget).  It runs sdm_context_init and
- * then sdm_process_block on up to 8 channels from fresh contexts, with all of
- * its scratch (context bank, job table, counter, status word) in a fixed
+ * that grants a fixed device-memory budget).  With keep_state 0 it runs
+ * sdm_context_init and then sdm_process_block on up to 8 channels; with
+ * keep_state 1 it continues from the contexts the previous call on this
+ * device left behind (same parameters and channel count, else
+ * DSDGPU_ERR_STATE), so successive callback blocks form one stream per
+ * channel, the latency fill applying to the first block only.  All of its
+ * scratch (context bank, job table, counter, status word) is in a fixed
  * device array of about 110 KB that every GPU which loads the library keeps
  * until exit; it calls no cudaMalloc, cudaFree or allocating library routine.
- * More than 8 channels is rejected with DSDGPU_ERR_TOO_LARGE; lat must be
- * <= 256.  The first call on a device looks up the array's device address
- * (make it before any stream capture).  Calls share the array: two calls whose
- * work overlaps on the GPU race and must not be issued.  Work is queued on
- * `stream` (a cudaStream_t, NULL for the default stream) and the call waits
- * for it.  Inputs, outputs and out_counts are as for dsdgpu_sdm_process. */
-int dsdgpu_sdm_process_noalloc(const dsdgpu_sdm_params_t *p, int nch, const double *d_in,
-                               size_t in_stride, size_t count, uint8_t *d_out,
-                               size_t out_stride, size_t *out_counts, void *stream);
+ * More than 8 channels is rejected with DSDGPU_ERR_TOO_LARGE; parameters are
+ * checked as for dsdgpu_sdm_setup (lat up to 2048).  With more than one
+ * channel, in_stride must be at least count and out_stride at least the
+ * decisions a channel writes (DSDGPU_ERR_ARG otherwise).
+ * The first call on a device looks up the array's device address (make it
+ * before any stream capture); the address is not valid across
+ * cudaDeviceReset.  CUDA loads kernels lazily, so make one warm-up call with
+ * the same parameters and channel count outside the real-time path (or set
+ * CUDA_MODULE_LOADING=EAGER): the first use of a kernel variant can allocate
+ * inside the driver.  Calls share the array: two calls whose work overlaps on
+ * the GPU race and must not be issued.  Work is queued on `stream` (a
+ * cudaStream_t, NULL for the default stream) and the call waits for it to
+ * finish before returning.  Inputs, outputs and out_counts are as for
+ * dsdgpu_sdm_process. */
+int dsdgpu_sdm_process_noalloc(const dsdgpu_sdm_params_t *p, int nch, int keep_state,
+                               const double *d_in, size_t in_stride, size_t count,
+                               uint8_t *d_out, size_t out_stride, size_t *out_counts,
+                               void *stream);
 
 /* Measured FP64 add/multiply issue rate of the device in Gop/s (separate
  * DADD and DMUL, the operations the trellis SDM is made of). */

@@ -35,10 +35,17 @@
  *  assembly  the same positions on every channel; in full-parallel mode seg0's
  *            output is cut back to its nominal length before the first
  *            overlap, exactly as the reference does        (:2420-2430, 2683-2714)
+ *  carry     across the chunks of a stream, the persistent context continues
+ *            in seg0 and is replaced by the last segment's final context
+ *                                                          (:2714-2721)
  *
- * Parity: the SDM underneath is pinned to the reference; the seam search and
- * assembly are unpinned (the reference has no golden vectors for them and
- * src/dsp_plugin.c does not build outside Windows).
+ * Parity: pinned to the reference's own plugin_process (src/dsp_plugin.c
+ * compiled here with its engine, FIR chain and trellis by oracle/ref_plugin.c,
+ * IPP and Win32 replaced by stand-ins): the DoP output of both seed modes,
+ * explicit and automatic segment counts, same-rate and rate-converting paths
+ * and chunk streams agree byte for byte (tests/test_oracle_ref.py).  The
+ * reference's segment count comes from its thread pool (at most 8 per channel
+ * per chunk); larger counts use the same per-segment and per-boundary rules.
  */
 #include "oracle.h"
 #include <math.h>
@@ -206,6 +213,16 @@ size_t ora_das_run(int order, const double *a, const double *g, int depth,
                    int nch, uint8_t *const *out_bits, int *stitch_pos,
                    size_t *seg_starts, int nthreads)
 {
+    return ora_das_run_carry(order, a, g, depth, cands, lat, state_limit, cfg, fir, count, nch,
+                             out_bits, stitch_pos, seg_starts, nthreads, NULL);
+}
+
+size_t ora_das_run_carry(int order, const double *a, const double *g, int depth,
+                         int cands, int lat, double state_limit,
+                         const ora_das_cfg_t *cfg, const double *const *fir, size_t count,
+                         int nch, uint8_t *const *out_bits, int *stitch_pos,
+                         size_t *seg_starts, int nthreads, ora_sdm_t *const *carry)
+{
     const size_t overlap = 64 * (size_t)lat;
     int S = cfg->seg_len > 0 ? (int)(count / (size_t)cfg->seg_len) : cfg->nsegs;
     if (S < 1) S = 1;
@@ -264,8 +281,12 @@ size_t ora_das_run(int order, const double *a, const double *g, int depth,
     uint8_t **buf = (uint8_t **)calloc((size_t)nch * (size_t)S, sizeof(void *));
     size_t *cnt = (size_t *)calloc((size_t)nch * (size_t)S, sizeof(size_t));
     double (*est)[ORA_MAX_ORDER] = calloc((size_t)nch * (size_t)S, sizeof *est);
+    /* the last segment's final context per channel: the next chunk's
+     * persistent context (src/dsp_plugin.c:2714-2721) */
+    ora_sdm_t **last = (ora_sdm_t **)calloc((size_t)nch, sizeof(void *));
     for (int ch = 0; ch < nch; ch++) {
-        pers[ch] = ora_sdm_new(order, a, g, depth, cands, lat, state_limit);
+        pers[ch] = carry ? carry[ch] : ora_sdm_new(order, a, g, depth, cands, lat, state_limit);
+        if (carry && S > 1) last[ch] = ora_sdm_new(order, a, g, depth, cands, lat, state_limit);
         for (int s = 0; s < S; s++)
             buf[ch * S + s] = (uint8_t *)malloc(size[s] + 2 * overlap + 16);
     }
@@ -281,6 +302,7 @@ size_t ora_das_run(int order, const double *a, const double *g, int depth,
                 size_t in_cnt = size[1];
                 if (S > 2 && start[1] + size[1] + overlap <= count) in_cnt += overlap;
                 cnt[ch * S + 1] = ora_sdm_process_bits(t, fir[ch] + start[1], buf[ch * S + 1], in_cnt);
+                if (last[ch] && S == 2) ora_sdm_copy(last[ch], t);
                 ora_sdm_free(t);
             }
             if (S > 2) {
@@ -338,6 +360,9 @@ size_t ora_das_run(int order, const double *a, const double *g, int depth,
                 j->seed_state = est[ch * S + s];
             }
             j->bits = buf[ch * S + s];
+            /* one segment: the chunk is a plain continuation of the
+             * persistent context (the plugin's non-DAS path) */
+            j->final_ctx = (s == S - 1) ? (S > 1 ? last[ch] : (carry ? pers[ch] : NULL)) : NULL;
         }
     }
     ora_sdm_run_jobs(order, a, g, depth, cands, lat, state_limit, jobs, nj, nthreads);
@@ -382,10 +407,14 @@ size_t ora_das_run(int order, const double *a, const double *g, int depth,
 
     for (int ch = 0; ch < nch; ch++) {
         if (!seg0_first) ora_sdm_free(snap[ch]);
-        ora_sdm_free(pers[ch]);
+        if (last[ch]) {
+            ora_sdm_copy(pers[ch], last[ch]);
+            ora_sdm_free(last[ch]);
+        }
+        if (!carry) ora_sdm_free(pers[ch]);
         for (int s = 0; s < S; s++) free(buf[ch * S + s]);
     }
-    free(bp); free(jobs); free(snap); free(est); free(cnt); free(buf); free(pers);
+    free(bp); free(jobs); free(snap); free(est); free(cnt); free(buf); free(pers); free(last);
     free(start); free(size);
     return final_count;
 }

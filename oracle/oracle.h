@@ -101,6 +101,7 @@ typedef struct {
     size_t        out_count;   /* written */
     const ora_sdm_t *seed;     /* context to copy before running (NULL: fresh) */
     const double *seed_state;  /* if non-NULL: seed active candidates */
+    ora_sdm_t    *final_ctx;   /* if non-NULL: receives the context after the job */
 } ora_seg_job_t;
 int ora_sdm_run_jobs(int order, const double *a, const double *g, int depth,
                      int cands, int lat, double state_limit,
@@ -171,6 +172,15 @@ size_t ora_das_run(int order, const double *a, const double *g, int depth,
                    const ora_das_cfg_t *cfg, const double *const *fir, size_t count,
                    int nch, uint8_t *const *out_bits, int *stitch_pos,
                    size_t *seg_starts, int nthreads);
+/* The same for one chunk of a stream: carry[ch] is the channel's persistent
+ * context (fresh for the first chunk), continued by seg0 and replaced by the
+ * last segment's final context when the chunk has more than one segment
+ * (src/dsp_plugin.c:2714-2721). */
+size_t ora_das_run_carry(int order, const double *a, const double *g, int depth,
+                         int cands, int lat, double state_limit,
+                         const ora_das_cfg_t *cfg, const double *const *fir, size_t count,
+                         int nch, uint8_t *const *out_bits, int *stitch_pos,
+                         size_t *seg_starts, int nthreads, ora_sdm_t *const *carry);
 
 #ifdef __cplusplus
 }

@@ -190,9 +190,11 @@ class DasCfg(C.Structure):
 
 
 def das_run(order, a, g, depth, cands, lat, state_limit, fir: np.ndarray, seg_len=0, nsegs=0,
-            seed_mode=0, reposition=True, nthreads=None):
+            seed_mode=0, reposition=True, nthreads=None, carry=None):
     """DAS over one chunk; fir is [nch, count] float64.  Returns (bits [nch, n],
-    stitch positions per segment, segment starts)."""
+    stitch positions per segment, segment starts).  carry: one Sdm per channel
+    (the persistent contexts of a stream, fresh for its first chunk), updated
+    in place for the next chunk."""
     L = oracle_lib().lib
     fir = np.ascontiguousarray(np.atleast_2d(fir), np.float64)
     nch, count = fir.shape
@@ -205,8 +207,14 @@ def das_run(order, a, g, depth, cands, lat, state_limit, fir: np.ndarray, seg_le
     smax = max(1, (count // seg_len) if seg_len > 0 else nsegs)
     sp = (C.c_int * smax)()
     ss = (C.c_size_t * smax)()
-    n = L.ora_das_run(order, _ptr(aa, _dp), _ptr(gg, _dp), depth, cands, lat, float(state_limit),
-                      C.byref(cfg), fps, count, nch, ops, sp, ss, nthreads or os.cpu_count() or 1)
+    cp = None
+    if carry is not None:
+        if len(carry) != nch:
+            raise ValueError("one carried context per channel")
+        cp = (C.c_void_p * nch)(*[c.h for c in carry])
+    n = L.ora_das_run_carry(order, _ptr(aa, _dp), _ptr(gg, _dp), depth, cands, lat,
+                            float(state_limit), C.byref(cfg), fps, count, nch, ops, sp, ss,
+                            nthreads or os.cpu_count() or 1, cp)
     return np.stack([o[:n] for o in outs]), list(sp), list(ss)
 
 
@@ -402,6 +410,11 @@ def _bind_oracle_extras(L):
     L.ora_decim_free.argtypes = [C.c_void_p]
     L.ora_decim_process.restype = C.c_size_t
     L.ora_decim_process.argtypes = [C.c_void_p, _dp, C.c_size_t, _dp]
+    L.ora_das_run_carry.restype = C.c_size_t
+    L.ora_das_run_carry.argtypes = [C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double,
+                                    C.POINTER(DasCfg), C.POINTER(_dp), C.c_size_t, C.c_int,
+                                    C.POINTER(_u8p), C.POINTER(C.c_int),
+                                    C.POINTER(C.c_size_t), C.c_int, C.POINTER(C.c_void_p)]
     L.ora_das_run.restype = C.c_size_t
     L.ora_das_run.argtypes = [C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double,
                               C.POINTER(DasCfg), C.POINTER(_dp), C.c_size_t, C.c_int,
@@ -510,6 +523,90 @@ def ref_enc_lib():
             L.ref_wav_write.argtypes = [C.c_char_p, _fp, C.c_uint32, C.c_int, C.c_uint32]
             _cache["enc"] = L
     return _cache["enc"]
+
+
+class RefPluginCfg(C.Structure):
+    """ref_plugin_cfg_t of oracle/ref_plugin.c."""
+    _fields_ = [("fs_out", C.c_uint), ("cands", C.c_int), ("depth", C.c_int), ("lat", C.c_int),
+                ("ntf_filter", C.c_int), ("par_mode", C.c_int), ("threads", C.c_int),
+                ("fir_prec", C.c_int), ("fir_mode", C.c_int), ("state_limit", C.c_float)]
+
+
+def ref_plugin_lib():
+    """The reference's DSP plugin core (src/dsp_plugin.c with its engine, FIR
+    chain and trellis) compiled by oracle/ref_plugin.c, or None when not built."""
+    if "plugin" not in _cache:
+        path = os.path.join(REF_DIR, "libref_plugin.so")
+        if not os.path.exists(path):
+            _cache["plugin"] = None
+        else:
+            L = C.CDLL(path)
+            L.ref_plugin_new.restype = C.c_void_p
+            L.ref_plugin_new.argtypes = [C.POINTER(RefPluginCfg), C.c_int, C.c_uint]
+            L.ref_plugin_process.restype = C.c_size_t
+            L.ref_plugin_process.argtypes = [C.c_void_p, _fp, _u8p, C.c_size_t, C.c_int, C.c_uint]
+            L.ref_plugin_fir.restype = C.c_size_t
+            L.ref_plugin_fir.argtypes = [C.c_void_p, C.c_int, _dp, C.c_size_t]
+            L.ref_plugin_segments.argtypes = [C.c_void_p]
+            L.ref_plugin_engine_state.argtypes = [C.c_void_p, C.c_int] + [C.c_void_p] * 8
+            L.ref_plugin_free.argtypes = [C.c_void_p]
+            _cache["plugin"] = L
+    return _cache["plugin"]
+
+
+class RefPlugin:
+    """One instance of the reference plugin on DoP input (plugin_process,
+    src/dsp_plugin.c:1146-2990), trellis mode, GPU and ML absent."""
+
+    def __init__(self, fs_in, fs_out, nch, cands, depth, lat, par_mode=-1, threads=16,
+                 ntf_filter=-1, fir_prec=-1, fir_mode=-1, state_limit=-1.0):
+        self.L = ref_plugin_lib()
+        self.fs_in, self.fs_out, self.nch = fs_in, fs_out, nch
+        cfg = RefPluginCfg(fs_out, cands, depth, lat, ntf_filter, par_mode, threads, fir_prec,
+                           fir_mode, state_limit)
+        self.h = self.L.ref_plugin_new(C.byref(cfg), nch, fs_in)
+        if not self.h:
+            raise ValueError("plugin engine init failed")
+
+    def process(self, dop: np.ndarray) -> np.ndarray:
+        """dop: interleaved DoP floats [frames, nch] -> interleaved DoP bytes."""
+        dop = np.ascontiguousarray(dop, np.float32)
+        frames = dop.shape[0]
+        ratio = max(1, self.fs_out // self.fs_in)
+        out = np.zeros(frames * ratio * 3 * self.nch + 4096, np.uint8)
+        nf = self.L.ref_plugin_process(self.h, _ptr(dop, _fp), _ptr(out, _u8p), frames,
+                                       self.nch, self.fs_in // 16)
+        return out[: nf * 3 * self.nch]
+
+    def fir(self) -> np.ndarray:
+        """The last chunk's FIR output per channel (the DAS phase's input)."""
+        rows = []
+        for c in range(self.nch):
+            n = self.L.ref_plugin_fir(self.h, c, None, 0)
+            buf = np.zeros(max(n, 1))
+            self.L.ref_plugin_fir(self.h, c, _ptr(buf, _dp), n)
+            rows.append(buf[:n])
+        return np.stack(rows)
+
+    def segments(self) -> int:
+        return self.L.ref_plugin_segments(self.h)
+
+    def engine(self, ch=0) -> dict:
+        """The trellis parameters the engine resolved for a channel."""
+        k, d, lat, order = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        a, g = np.zeros(10), np.zeros(10)
+        sl, fg = C.c_double(), C.c_float()
+        mode = self.L.ref_plugin_engine_state(self.h, ch, C.byref(k), C.byref(d), C.byref(lat),
+                                              C.byref(order), a.ctypes.data, g.ctypes.data,
+                                              C.byref(sl), C.byref(fg))
+        return dict(sdm_mode=mode, cands=k.value, depth=d.value, lat=lat.value,
+                    order=order.value, a=a, g=g, state_limit=sl.value, fir_gain=fg.value)
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            self.L.ref_plugin_free(h)
+            self.h = None
 
 
 def bits_pack(bits: np.ndarray) -> np.ndarray:

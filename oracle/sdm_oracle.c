@@ -482,6 +482,7 @@ static void *pool_worker(void *arg)
         else memcpy(c, p->proto, sizeof *c);
         if (jb->seed_state) ora_sdm_seed(c, jb->seed_state);
         jb->out_count = ora_sdm_segment_bits(c, jb->in, jb->bits, jb->count, jb->discard);
+        if (jb->final_ctx) ora_sdm_copy(jb->final_ctx, c);
     }
     free(c);
     return NULL;

@@ -159,3 +159,30 @@ def test_das_output_counts_over_chunks(oracle):
         assert got.shape == (2, want)
         assert want % 16 == 0
     d.close()
+
+
+def test_pipeline_flush_restarts_the_stream():
+    """dsdgpu_pipeline_flush (plugin_flush, src/dsp_plugin.c:3622-3653): a chunk
+    after a flush equals the same chunk on a fresh pipeline, and differs from
+    the chunk that continues the stream."""
+    from foo_dsd_trellis_gb300 import ntf, signals
+    from foo_dsd_trellis_gb300.pipeline import FULL_PARALLEL, OUT_DOP, Encoder
+    f = ntf.get_filter("clans-7", 6144000)
+    pcm = torch.from_numpy(signals.dsd128_multitone_pink(0.3, 48000, 2, 7)).cuda()
+
+    def enc():
+        return Encoder(48000, 6144000, 2, f, 32, 16, 64, seg_len=65536, seed_mode=FULL_PARALLEL,
+                       output_format=OUT_DOP)
+    a, b = enc(), enc()
+    cap = a.out_capacity(pcm.shape[1]) + 64
+    outs = []
+    for e, flush in ((a, False), (b, True)):
+        o1 = torch.zeros(cap, dtype=torch.uint8, device="cuda")
+        o2 = torch.zeros(cap, dtype=torch.uint8, device="cuda")
+        _, n1 = e.process(pcm, o1)
+        if flush:
+            e.flush()
+        _, n2 = e.process(pcm, o2)
+        outs.append((o1[:n1].cpu().numpy(), o2[:n2].cpu().numpy()))
+    assert np.array_equal(outs[1][1], outs[0][0])          # flushed == fresh
+    assert not np.array_equal(outs[0][1], outs[0][0])      # continued != fresh
