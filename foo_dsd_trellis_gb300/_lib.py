@@ -98,6 +98,8 @@ SAMERATE_LOWPASS = 1
 OPT_SDM_SELECT = 1
 OPT_SDM_LANES = 2
 OPT_SDM_BALANCE = 3
+OPT_FAILURE_TEST = 4
+FAIL_PART_WAIT, FAIL_CHAIN_WALK = 1, 2
 SELECT_FAST, SELECT_EXACT, SELECT_VERIFY = 0, 1, 2
 
 DAS_FULL_PARALLEL = 0

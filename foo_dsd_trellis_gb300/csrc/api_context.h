@@ -74,6 +74,7 @@ struct dsdgpu_context {
   int sdm_mode = 0;               // selection strategy (DSDGPU_OPT_SDM_SELECT)
   int sdm_lanes = 0;              // lanes per SDM job (DSDGPU_OPT_SDM_LANES), 0 = automatic
   int sdm_balance = 1;            // balanced launches allowed (DSDGPU_OPT_SDM_BALANCE)
+  int failure_test = 0;           // DSDGPU_OPT_FAILURE_TEST bits
   int nctx = 0;
   dsdgpu::SdmCtx* d_ctx = nullptr;
   std::vector<int64_t> pending;   // latency fill per context (host mirror)

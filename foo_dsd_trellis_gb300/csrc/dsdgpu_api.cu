@@ -134,6 +134,9 @@ int dsdgpu_context::run_jobs(const std::vector<SdmJob>& jobs) {
   SdmParams P = sdm;
   P.mode = sdm_mode;
   P.lanes = sdm_lanes;
+  // failure-path tests: waits and walks that give up early (see the option)
+  P.hop_limit = (failure_test & DSDGPU_FAIL_CHAIN_WALK) ? 1 : 0;
+  P.part_wait_cycles = (failure_test & DSDGPU_FAIL_PART_WAIT) ? 2000000ll : 0;
   // many long jobs a little above a whole number of warps per FP64 pipe: the
   // balanced launch (parts of 1,024 samples queued over w warps per pipe; on
   // the DSD128 headline 1,024 / 2,048 / 4,096 ran 270.1 / 268.8 / 265.4 DSD
@@ -142,7 +145,10 @@ int dsdgpu_context::run_jobs(const std::vector<SdmJob>& jobs) {
   const int wpp = (max_blocks == 0 && sdm_balance)
                       ? sdm_balanced_warps(P, jobs.data(), n, num_sms, kPartLen) : 0;
   if (wpp > 0) {
-    const long long total = sdm_parts_total(jobs.data(), n, kPartLen);
+    // with DSDGPU_FAIL_PART_WAIT the queue holds one entry that no part
+    // publishes: the warp that takes it waits (bounded) and gives up
+    const long long total = sdm_parts_total(jobs.data(), n, kPartLen) +
+                            ((failure_test & DSDGPU_FAIL_PART_WAIT) ? 1 : 0);
     if (total + 2 > parts_cap) {
       if (d_parts) cudaFree(d_parts);
       d_parts = nullptr;
@@ -249,6 +255,11 @@ int dsdgpu_set_option(dsdgpu_context_t* c, int option, int value) {
     case DSDGPU_OPT_SDM_BALANCE:
       if (value != 0 && value != 1) return c->fail(DSDGPU_ERR_ARG, "balance must be 0 or 1");
       c->sdm_balance = value;
+      return DSDGPU_OK;
+    case DSDGPU_OPT_FAILURE_TEST:
+      if (value & ~(DSDGPU_FAIL_PART_WAIT | DSDGPU_FAIL_CHAIN_WALK))
+        return c->fail(DSDGPU_ERR_ARG, "unknown failure-test bits");
+      c->failure_test = value;
       return DSDGPU_OK;
     default:
       return c->fail(DSDGPU_ERR_ARG, "unknown option");

@@ -37,6 +37,10 @@ struct SdmParams {
   int depth;
   int mode;               // kModeFast, kModeExact or kModeVerify
   int lanes;              // lanes per job (2..32, a power of two >= K); 0 = automatic
+  // bounds of the kernels' waits and walks; 0 = the built-in bound (shortened
+  // only by the failure-path tests, DSDGPU_OPT_FAILURE_TEST)
+  int hop_limit;                // path-hash chain walk, hops
+  long long part_wait_cycles;   // balanced launch: wait for an unpublished part
 };
 
 // Survivor selection strategy of the SDM kernel.

@@ -521,10 +521,11 @@ __device__ void run_job(const SdmParams& P, const SdmJob& job, SdmCtx* __restric
           const int b = (int)(sp & (kBuckets - 1));
           int t = sm.heads[b];
           int hops = 0;
+          const int hop_limit = P.hop_limit > 0 ? P.hop_limit : 4 * kSlots;
           while (t >= 0) {
             if (sm.path[nb][t] == sp) break;
             t = sm.link[nb][t];
-            if (++hops > 4 * kSlots) { err = kStatusChainLimit; t = -1; break; }
+            if (++hops > hop_limit) { err = kStatusChainLimit; t = -1; break; }
           }
           if (t < 0) {
             __syncwarp(hm);
@@ -781,13 +782,15 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
 
 // The rare wait for an entry not yet published (out of line: inlined, its
 // loop changes the register allocation of the step loop).
-__device__ __noinline__ unsigned long long wait_entry(const unsigned long long* p, int* status) {
+__device__ __noinline__ unsigned long long wait_entry(const unsigned long long* p, int* status,
+                                                     long long limit) {
   unsigned long long e = ~0ull;
   const long long t0 = clock64();
+  if (limit <= 0) limit = kPartWaitCycles;
   do {
     __nanosleep(1000);
     e = ld_acquire_u64(p);
-  } while (e == ~0ull && clock64() - t0 < kPartWaitCycles);
+  } while (e == ~0ull && clock64() - t0 < limit);
   if (e == ~0ull && (threadIdx.x & 31) == 0) atomicMax(status, kStatusQueueWait);
   return e;
 }
@@ -810,7 +813,7 @@ sdm_parts_kernel(SdmParams P, const SdmJob* __restrict__ jobs, long long part_le
     if (idx >= (unsigned long long)total) break;
     // every lane reads the entry with acquire semantics (one transaction)
     unsigned long long e = ld_acquire_u64(ent + idx);
-    if (e == ~0ull) e = wait_entry(ent + idx, status);
+    if (e == ~0ull) e = wait_entry(ent + idx, status, P.part_wait_cycles);
     if (e == ~0ull) break;
     __threadfence();   // the previous part's context is read after the entry
     const int j = (int)(e & 0xffffffffull);

@@ -164,6 +164,17 @@ const char *dsdgpu_last_error(const dsdgpu_context_t *ctx);
                                          queued over an even number of warps per pipe;
                                          0: one job per warp from start to end.  Results
                                          do not depend on it. */
+#define DSDGPU_OPT_FAILURE_TEST 4   /* failure-path tests only (default 0): bits that
+                                         make the kernels' bounded waits and walks give
+                                         up early, so a test can check that the call
+                                         returns DSDGPU_ERR_DEVICE and the context stays
+                                         usable.  No fault is raised; no wait is
+                                         unbounded. */
+#define DSDGPU_FAIL_PART_WAIT   1   /*   a balanced launch's part queue gets one entry
+                                         that no part publishes, and the wait for it
+                                         gives up after ~1 ms instead of ~4 s */
+#define DSDGPU_FAIL_CHAIN_WALK  2   /*   the serial selection's path-hash chain walk
+                                         gives up after one hop */
 int  dsdgpu_set_option(dsdgpu_context_t *ctx, int option, int value);
 
 /* Number of kernels this context has launched so far. */
