@@ -126,3 +126,82 @@ def test_das_quiet_boundary_reposition(plug):
     n = info[0]["fir_count"]
     nominal = [s * (n // 6) + min(s, n % 6) for s in range(6)]
     assert list(info[0]["starts"]) != nominal
+
+
+@pytest.mark.parametrize("fs_in,fs_out,chunks", [
+    (2822400, 11289600, 2),     # 2 half-band stages up
+    (2822400, DSD512, 1),       # 4x quarter-band + 2x stages
+    (3072000, 24576000, 1),     # 48k family, 127-tap first stage of a 3-stage chain
+    (11289600, 5644800, 2),     # FP64 decimation
+    (22579200, 2822400, 1),     # three /2 stages
+], ids=["up4", "up8_512", "up8_512_48k", "down2", "down8"])
+def test_fir_phase_equals_reference_engine(plug, fs_in, fs_out, chunks):
+    """The FIR phase of the plugin's DAS path, engine_process_fir_gain
+    (src/engine.c:789-900) with the reference's own fir.c (stage plan, tap
+    design, FP64 chain with delay lines carried over chunks), against the
+    oracle's FP64 restatement of the same chain on the +-1 input with the
+    path gain and no boxcar or clip: bit for bit.  IPP's arithmetic is the
+    published FIRMR semantics on both sides, so this pins the plan, the taps
+    and the glue."""
+    O = plug
+    nch = 1
+    dop = _dsd_input(fs_in, 0.02 if fs_out > fs_in else 0.03, nch)
+    plug_ = O.RefPlugin(fs_in, fs_out, nch, 4, 8, 16, par_mode=4)
+    e = plug_.engine()
+    gain = float(np.float32(e["fir_gain"]))
+    per = dop.shape[0] // chunks
+    if fs_out > fs_in:
+        hist = np.zeros(0, np.float32)
+    else:
+        dec = O.Decimator(fs_in, fs_out)
+        bc = O.Boxcar(1)
+    for k in range(chunks):
+        plug_.process(dop[k * per:(k + 1) * per])
+        got = plug_.fir()[0]
+        x = O.dop_unpack(dop[k * per:(k + 1) * per, 0])
+        if fs_out > fs_in:
+            # the chain is LTI with zero initial delay lines: restate it on the
+            # whole input so far and take this chunk's outputs
+            hist = np.concatenate([hist, x])
+            full = O.engine_fir(fs_in, fs_out, hist, boxcar_taps=0, g_start=gain, g_end=gain,
+                                soft_clip=False)
+            want = full[-len(x) * (fs_out // fs_in):]
+        else:
+            want = O.engine_down(bc, dec, x, gain, gain, False)
+        assert len(got) == len(want), (k, len(got), len(want))
+        assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), (
+            k, np.max(np.abs(got - want)))
+
+
+def test_sequential_path_equals_reference_engine(plug):
+    """With one segment per channel (TRELLIS_PAR_SEQUENTIAL) the plugin runs
+    engine_process_block per channel (src/engine.c:600-729: boxcar 8, FIR
+    chain, gain ramp, tanh soft clip, sdm_process_block): its DoP output over
+    two chunks equals the oracle's FIR glue (boxcar, chain, gain, clip) and
+    its trellis, pinned to trellis.c, continued across the chunks."""
+    O = plug
+    fs_in, fs_out, nch, K, depth, lat = 2822400, 11289600, 2, 8, 16, 32
+    dop = _dsd_input(fs_in, 0.04, nch)
+    p = O.RefPlugin(fs_in, fs_out, nch, K, depth, lat, par_mode=0)
+    e = p.engine()
+    gain = float(np.float32(e["fir_gain"]))
+    ctx = [O.sdm(e["order"], e["a"], e["g"], depth, K, lat, e["state_limit"]) for _ in range(nch)]
+    per = dop.shape[0] // 2
+    hist = [np.zeros(0, np.float32) for _ in range(nch)]
+    phase = 0
+    for k in range(2):
+        got = p.process(dop[k * per:(k + 1) * per])
+        assert p.segments() == 1
+        bits = []
+        for c in range(nch):
+            x = O.dop_unpack(dop[k * per:(k + 1) * per, c])
+            hist[c] = np.concatenate([hist[c], x])
+            full = O.engine_fir(fs_in, fs_out, hist[c], boxcar_taps=8, g_start=gain, g_end=gain,
+                                soft_clip=True)
+            bits.append(O.sdm_bits(ctx[c], full[-len(x) * (fs_out // fs_in):]))
+        n = min(len(b) for b in bits) // 16 * 16
+        packs = [O.dop_pack_bits(b[:n], phase) for b in bits]
+        phase = packs[0][1]
+        want = np.stack([q[0].reshape(-1, 3) for q in packs], axis=1).reshape(-1)
+        assert len(got) == len(want)
+        assert np.array_equal(got, want), k
