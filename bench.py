@@ -22,7 +22,9 @@ dsd512conv6 (DSD512 5.1 with UPOLS room convolution), samerate128 (DoP DSD128
 re-encode on the engine's path-table parameters), samerate128lp (the same with
 the engine's 127-tap FIR lowpass instead of the boxcar), dsd2pcm128 (DSD128 ->
 44.1 kHz PCM), precorr128 (PCM -> DSD128 with the PreCorr SDM) and dsd256to128
-(DoP DSD256 -> DSD128 through the FP64 decimation chain and the DAS trellis).
+(DoP DSD256 -> DSD128 through the FP64 decimation chain and the DAS trellis) and
+dsd128_seg0first (the headline's signal and trellis with the reference's own
+seeding rule below DSD512, seg0-first, on 1 s chunks of one stream).
 """
 from __future__ import annotations
 
@@ -68,7 +70,7 @@ def parse():
     ap.add_argument("--workload", default="dsd128_das",
                     choices=["dsd128_das", "multistream64", "diff16", "dsd512conv6",
                              "samerate128", "samerate128lp", "precorr128", "dsd2pcm128",
-                             "dsd256to128"],
+                             "dsd256to128", "dsd128_seg0first"],
                     help="multistream64: the batched 64-stream form; diff16: the adjoint; "
                          "samerate128 / samerate128lp / precorr128 / dsd2pcm128: the DSD "
                          "re-encode (boxcar / FIR lowpass), PreCorr and DSD -> PCM paths (each "
@@ -785,6 +787,112 @@ def run_conv(args):
     enc.close()
 
 
+SEG0_METRIC = ("DSD128 trellis SDM + DAS with the reference's own seeding rule below DSD512 "
+               "(seg0-first), 1 s chunks of one stream, DSD Msamples/s")
+
+
+def run_seg0first(args):
+    """The headline's signal and trellis (DSD128 stereo, 48 kHz multitone + pink,
+    CLANS-7, K = 32, depth 64, lat 128, 65,536-sample segments) under the
+    reference's DSD128 seeding rule, seg0-first (src/dsp_plugin.c:2185-2283):
+    seg0 serial on the channel's context, seg1 DIRECT from its end state, the
+    16-level estimator walked serially over the rest of the chunk, then seg2+
+    in parallel.  The input is one stream converted in 1 s chunks (the state
+    carried from chunk to chunk as the plugin carries it), so each chunk has
+    two serial trellis runs and one serial estimator pass on its critical
+    path.  The CPU leg is the oracle's port of the same chunks on every host
+    core; decisions are checked against it."""
+    import numpy as np
+    import torch
+    from oracle import oracle as O
+    from foo_dsd_trellis_gb300 import ntf, signals
+    from foo_dsd_trellis_gb300.fir import FirChain
+    from foo_dsd_trellis_gb300.pipeline import OUT_BITS, PCM_FIR_GAIN, SEG0_FIRST, Encoder
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    secs = args.seconds if args.seconds != WL["seconds"] else 2.0
+    chunk = WL["fs_in"]                               # 1 s of input per chunk
+    f = ntf.get_filter(WL["ntf"], WL["fs_out"])
+    pcm = signals.dsd128_multitone_pink(secs, WL["fs_in"], WL["channels"], WL["seed"])
+    nch, frames = pcm.shape
+    nchunks = frames // chunk
+    enc = Encoder(WL["fs_in"], WL["fs_out"], nch, f, WL["depth"], WL["cands"], WL["lat"],
+                  seg_len=WL["das_seg_len"], seed_mode=SEG0_FIRST, reposition=True,
+                  boxcar_taps=WL["boxcar_taps"], soft_clip=True, output_format=OUT_BITS,
+                  device=local)
+    d_pcm = [torch.from_numpy(np.ascontiguousarray(pcm[:, k * chunk:(k + 1) * chunk])).cuda()
+             for k in range(nchunks)]
+    ratio = WL["fs_out"] // WL["fs_in"]
+    outs = [torch.empty((nch, chunk * ratio + 256), dtype=torch.uint8, device="cuda")
+            for _ in range(nchunks)]
+    lib_stream = torch.cuda.ExternalStream(enc.stream_ptr)
+
+    def one_pass():
+        enc.flush()
+        counts = []
+        for k in range(nchunks):
+            n, _ = enc.process(d_pcm[k], outs[k])
+            counts.append(n)
+        return counts
+
+    for _ in range(args.warmup):
+        one_pass()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    step_ms = []
+    counts = []
+    for _ in range(args.steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(lib_stream)
+        counts = one_pass()
+        e1.record(lib_stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+    clk = clocks.stop()
+    total_s = sum(step_ms) / 1000.0
+    n_out = sum(counts) * nch
+    value = n_out * args.steps / total_s / 1e6
+    got = [outs[k][:, :counts[k]].cpu().numpy() for k in range(nchunks)]
+
+    # the oracle on the GPU's FIR output of the same chunks (carry across chunks)
+    fc = FirChain(WL["fs_in"], WL["fs_out"], boxcar_taps=WL["boxcar_taps"], soft_clip=True,
+                  num_channels=nch, device=local)
+    carry = [O.sdm(f.order, np.array(f.a), np.array(f.g), WL["depth"], WL["cands"], WL["lat"])
+             for _ in range(nch)]
+    nthreads = os.cpu_count() or 1
+    t_cpu = 0.0
+    same = True
+    for k in range(nchunks):
+        fir = fc.process(d_pcm[k], PCM_FIR_GAIN, PCM_FIR_GAIN).cpu().numpy()
+        t0 = time.perf_counter()
+        want, _, _ = O.das_run(f.order, np.array(f.a), np.array(f.g), WL["depth"], WL["cands"],
+                               WL["lat"], 0.0, fir, seg_len=WL["das_seg_len"], seed_mode=1,
+                               reposition=True, nthreads=nthreads, carry=carry)
+        t_cpu += time.perf_counter() - t0
+        same = same and want.shape == got[k].shape and bool(np.array_equal(want, got[k]))
+    fc.close()
+    cpu_value = n_out / t_cpu / 1e6
+    stages = enc.stage_ms()
+    line = {"metric": SEG0_METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * total_s / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": dict(WL, workload="dsd128_seg0first_stereo_1s_chunks", seconds=secs,
+                           seed_mode="seg0_first", chunk_frames=chunk,
+                           l2="inputs stream through chunk by chunk; no flush"),
+            "xrt": (sum(counts) / WL["fs_out"]) * args.steps / total_s,
+            "parity": {"bit_exact": same, "oracle": "oracle DAS with the chunk carry on the "
+                       "GPU's FIR output of every chunk"},
+            "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": f"the same {nchunks} chunks: trellis SDM port + DAS "
+                                       "(seg0-first, carry) on the GPU's FIR output"},
+            "last_chunk_stages_ms": stages, "clocks": clk}
+    print(json.dumps(line), flush=True)
+    enc.close()
+
+
 def _probe_fp64(plan) -> float:
     import ctypes as C
     v = C.c_double()
@@ -810,14 +918,14 @@ NEXT = {
         ntf="clans-6", cands=2, depth=4, lat=128, das_seg_len=65536, lowpass_taps=127,
         lowpass_cutoff_hz=50000.0, gain="float32(0.708) (path gain)"),
     "dsd256to128": dict(
-        metric="DSD256 -> DSD128 re-encode (DoP in -> unpack -> boxcar 8 -> FP64 half-band /2 -> "
-               "gain -> soft clip -> DAS trellis SDM -> DoP) DSD Msamples/s, bit-exact given the "
-               "FIR stage",
+        metric="DSD256 -> DSD128 re-encode through the plugin's DAS path (DoP in -> unpack -> "
+               "FP64 half-band /2 -> gain, engine_process_fir_gain -> DAS trellis SDM -> DoP) "
+               "DSD Msamples/s, bit-exact given the FIR stage",
         workload="dsd256_to_dsd128_stereo_10s", fs_in=11289600, fs=5644800,
         path_table="DSD256 -> DSD128 row of the engine's path table (src/engine.c:78): SDM-6, "
                    "K = 2, depth 8; lat 0 there = auto = 128 at DSD128",
-        ntf="sdm-6", cands=2, depth=8, lat=128, das_seg_len=65536, boxcar_taps=8,
-        gain="float32(0.708) (path gain)"),
+        ntf="sdm-6", cands=2, depth=8, lat=128, das_seg_len=65536, boxcar_taps=0,
+        soft_clip=False, gain="float32(0.708) (path gain)"),
     "precorr128": dict(
         metric="PCM 44.1 kHz -> DSD128 with the PreCorr SDM (FIR chain -> PreCorr -> DoP) "
                "DSD Msamples/s, bit-exact SDM",
@@ -900,8 +1008,9 @@ def _next_cpu(wl: str, inp, bits, sample_s: float) -> dict:
         f = ntf.get_filter(cfg["ntf"], fs)
         g = float(np.float32(PATH_GAIN))
         t0 = time.perf_counter()
-        fir = np.stack([O.engine_down(O.Boxcar(cfg["boxcar_taps"]), O.Decimator(fs_in, fs),
-                                      O.dop_unpack(x[c]), g, g, True) for c in range(nch)])
+        fir = np.stack([O.engine_down(O.Boxcar(max(1, cfg["boxcar_taps"])),
+                                      O.Decimator(fs_in, fs), O.dop_unpack(x[c]), g, g,
+                                      cfg["soft_clip"]) for c in range(nch)])
         out, _, _ = O.das_run(f.order, np.array(f.a), np.array(f.g), cfg["depth"], cfg["cands"],
                               cfg["lat"], 0.0, fir, seg_len=cfg["das_seg_len"], seed_mode=0,
                               reposition=True, nthreads=nthreads)
@@ -973,8 +1082,8 @@ def run_next(args):
         g = float(np.float32(PATH_GAIN))
         enc = Encoder(cfg["fs_in"], fs, nch, f, cfg["depth"], cfg["cands"], cfg["lat"],
                       seg_len=cfg["das_seg_len"], seed_mode=FULL_PARALLEL, reposition=True,
-                      boxcar_taps=cfg["boxcar_taps"], soft_clip=True, output_format=OUT_DOP,
-                      device=local)
+                      boxcar_taps=cfg["boxcar_taps"], soft_clip=cfg["soft_clip"],
+                      output_format=OUT_DOP, device=local)
     elif wl == "precorr128":
         f = ntf.auto_select_precorr(fs)
         g = PCM_FIR_GAIN
@@ -1127,6 +1236,8 @@ def main():
         run_diff(args)
     elif args.workload == "dsd512conv6":
         run_conv(args)
+    elif args.workload == "dsd128_seg0first":
+        run_seg0first(args)
     else:
         run_ours(args)
 

@@ -48,11 +48,48 @@ __global__ void das_rms_kernel(const double* __restrict__ x, const long long* __
 // One sample of sdm_estimate_state_multibit: the NTF advance with y = 0, the
 // quantiser (levels <= 2: the sign of v * a0; else v / a0 rounded to the
 // nearest of `levels` values in [-1, 1]), y subtracted from state 0, clamp.
-__device__ __forceinline__ void estimate_step(const SdmParams& P, double* st, double* ns, double xv,
-                                              int levels, double step) {
-  const int N = P.order;
+// The estimate is one serial chain per channel, so its cost is the latency of
+// that chain.  The state is held in registers (the step is instantiated per
+// NTF order), and the quantiser's index
+//     idx = trunc((v / a0 + 1) / step + 0.5), clamped to [0, levels - 1]
+// is first taken with the two divisions replaced by products with their
+// rounded reciprocals (within ~1e-14 of the exact value for |w| < 2^20): the
+// integer is the same wherever that value is more than 1e-9 from an integer
+// in [1, levels - 1], and the correctly rounded divisions decide the rest
+// (and NaN or huge values).  y = -1 + idx * step comes from a table of the
+// same products.
+struct EstConst {
+  double ra0;       // 1 / a0, rounded
+  double rstep;     // 1 / step, rounded
+  double step;
+  double ylev[64];  // -1 + k * step for k < min(levels, 64)
+  int levels;
+};
+
+__device__ __forceinline__ int quant_index(double v, double a0, const EstConst& E) {
+  const double w = __dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(v, E.ra0), 1.0), E.rstep), 0.5);
+  const int L = E.levels;
+  if (w < 1.0 - 1e-9) return 0;                        // trunc < 1 or negative: clamped to 0
+  if (w >= (double)(L - 1) + 1e-9 && w < 1048576.0) return L - 1;
+  if (w < 1048576.0 && L <= 1024) {
+    const double r = rint(w);
+    if (fabs(w - r) > 1e-9) return (int)w;             // w > 0: trunc == floor
+  }
+  // near a level boundary (or not finite): the reference's expression
+  const double yi = __ddiv_rn(v, a0);
+  int idx = __double2int_rz(__dadd_rn(__ddiv_rn(__dadd_rn(yi, 1.0), E.step), 0.5));
+  if (idx < 0) idx = 0;
+  if (idx > L - 1) idx = L - 1;
+  return idx;
+}
+
+template <int N>
+__device__ __forceinline__ void estimate_step_n(const SdmParams& P, const EstConst& E, double* st,
+                                                double xv) {
+  double ns[N];
   ns[0] = __dadd_rn(__dsub_rn(st[0], __dmul_rn(P.g[0], st[1])), xv);
   double v = __dadd_rn(xv, __dmul_rn(P.a[0], ns[0]));
+#pragma unroll
   for (int i = 1; i < N - 1; i++) {
     ns[i] = __dsub_rn(__dadd_rn(st[i], st[i - 1]), __dmul_rn(P.g[i], st[i + 1]));
     v = __dadd_rn(v, __dmul_rn(P.a[i], ns[i]));
@@ -60,62 +97,112 @@ __device__ __forceinline__ void estimate_step(const SdmParams& P, double* st, do
   ns[N - 1] = __dadd_rn(st[N - 1], st[N - 2]);
   v = __dadd_rn(v, __dmul_rn(P.a[N - 1], ns[N - 1]));
   double y;
-  if (levels <= 2) {
-    y = __dmul_rn(v, P.a[0]) > 0.0 ? 1.0 : -1.0;
-  } else {
-    const double yi = __ddiv_rn(v, P.a[0]);
-    int idx = __double2int_rz(__dadd_rn(__ddiv_rn(__dadd_rn(yi, 1.0), step), 0.5));
-    if (idx < 0) idx = 0;
-    if (idx > levels - 1) idx = levels - 1;
-    y = __dadd_rn(-1.0, __dmul_rn((double)idx, step));
+  if (E.levels <= 2) y = __dmul_rn(v, P.a[0]) > 0.0 ? 1.0 : -1.0;
+  else {
+    const int idx = quant_index(v, P.a[0], E);
+    y = idx < 64 ? E.ylev[idx] : __dadd_rn(-1.0, __dmul_rn((double)idx, E.step));
   }
   ns[0] = __dsub_rn(ns[0], y);
-  if (P.state_limit > 0.0)
+  if (P.state_limit > 0.0) {
+#pragma unroll
     for (int i = 0; i < N; i++) {
       if (ns[i] > P.state_limit) ns[i] = P.state_limit;
       else if (ns[i] < -P.state_limit) ns[i] = -P.state_limit;
     }
+  }
+#pragma unroll
   for (int i = 0; i < N; i++) st[i] = ns[i];
 }
 
+EstConst make_est_const(double a0, int levels) {
+  EstConst E;
+  memset(&E, 0, sizeof E);
+  E.levels = levels;
+  E.step = 2.0 / (double)(levels - 1);
+  E.ra0 = 1.0 / a0;
+  E.rstep = 1.0 / E.step;
+  for (int k = 0; k < levels && k < 64; k++) E.ylev[k] = -1.0 + (double)k * E.step;
+  return E;
+}
+
 // One thread per estimate (sdm_estimate_state(_multibit) on its own input).
-__global__ void estimate_kernel(SdmParams P, const dsdgpu_estimate_t* __restrict__ items, int n,
-                                int levels, double* __restrict__ out /* [n][kMaxOrder] */) {
+template <int N>
+__global__ void estimate_kernel(SdmParams P, EstConst E, const dsdgpu_estimate_t* __restrict__ items,
+                                int n, double* __restrict__ out /* [n][kMaxOrder] */) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
-  double st[kMaxOrder], ns[kMaxOrder];
-  for (int k = 0; k < P.order; k++) st[k] = items[j].init_state[k];
+  double st[N];
+#pragma unroll
+  for (int k = 0; k < N; k++) st[k] = items[j].init_state[k];
   const double* x = items[j].d_in;
   const long long count = items[j].count;
-  const double step = __ddiv_rn(2.0, (double)(levels - 1));
-  for (long long t = 0; t < count; t++) estimate_step(P, st, ns, x[t], levels, step);
-  for (int k = 0; k < kMaxOrder; k++) out[(size_t)j * kMaxOrder + k] = k < P.order ? st[k] : 0.0;
+  for (long long t = 0; t < count; t++) estimate_step_n<N>(P, E, st, x[t]);
+  for (int k = 0; k < kMaxOrder; k++) out[(size_t)j * kMaxOrder + k] = 0.0;
+#pragma unroll
+  for (int k = 0; k < N; k++) out[(size_t)j * kMaxOrder + k] = st[k];
 }
 
 // DAS seeding: one thread per channel walks the chunk from seg1's start with
 // the 16-level estimator and records the state at every later segment start.
-__global__ void das_estimate_kernel(SdmParams P, const double* __restrict__ fir, size_t fir_stride,
-                                    const SdmCtx* __restrict__ pers, int pers_first,
-                                    const long long* __restrict__ starts, int S, long long count,
-                                    double* __restrict__ est /* [nch][S][kMaxOrder] */, int nch) {
+template <int N>
+__global__ void das_estimate_kernel(SdmParams P, EstConst E, const double* __restrict__ fir,
+                                    size_t fir_stride, const SdmCtx* __restrict__ pers,
+                                    int pers_first, const long long* __restrict__ starts, int S,
+                                    long long count, double* __restrict__ est /* [nch][S][kMaxOrder] */,
+                                    int nch) {
   const int ch = blockIdx.x * blockDim.x + threadIdx.x;
   if (ch >= nch) return;
-  const int N = P.order;
-  double st[kMaxOrder], ns[kMaxOrder];
+  double st[N];
   const SdmCtx* c = &pers[pers_first + ch];
+#pragma unroll
   for (int k = 0; k < N; k++) st[k] = c->s[0][k];
   const double* x = fir + (size_t)ch * fir_stride;
   const long long est_start = starts[1];
-  const double step = 2.0 / 15.0;
   long long pos = 0;
   for (int s = 1; s < S; s++) {
     const long long bnd = s >= 2 ? starts[s] - est_start : 0;
     if (bnd > pos && bnd <= count - est_start) {
-      for (long long t = pos; t < bnd; t++) estimate_step(P, st, ns, x[est_start + t], 16, step);
+      for (long long t = pos; t < bnd; t++) estimate_step_n<N>(P, E, st, x[est_start + t]);
       pos = bnd;
     }
-    for (int k = 0; k < kMaxOrder; k++) est[((size_t)ch * S + s) * kMaxOrder + k] = k < N ? st[k] : 0.0;
+    double* o = est + ((size_t)ch * S + s) * kMaxOrder;
+    for (int k = 0; k < kMaxOrder; k++) o[k] = 0.0;
+#pragma unroll
+    for (int k = 0; k < N; k++) o[k] = st[k];
   }
+}
+
+int launch_estimate(const SdmParams& P, int levels, const dsdgpu_estimate_t* d_items, int n,
+                    double* d_out, cudaStream_t stream) {
+  const EstConst E = make_est_const(P.a[0], levels);
+  switch (P.order) {
+#define DSD_CASE(NN) \
+  case NN: estimate_kernel<NN><<<(n + 31) / 32, 32, 0, stream>>>(P, E, d_items, n, d_out); break;
+    DSD_CASE(2) DSD_CASE(3) DSD_CASE(4) DSD_CASE(5) DSD_CASE(6)
+    DSD_CASE(7) DSD_CASE(8) DSD_CASE(9) DSD_CASE(10)
+#undef DSD_CASE
+    default: return -1;
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_das_estimate(const SdmParams& P, const double* fir, size_t fir_stride, const SdmCtx* pers,
+                        int pers_first, const long long* starts, int S, long long count, double* est,
+                        int nch, cudaStream_t stream) {
+  const EstConst E = make_est_const(P.a[0], 16);
+  switch (P.order) {
+#define DSD_CASE(NN)                                                                          \
+  case NN:                                                                                    \
+    das_estimate_kernel<NN><<<(nch + 31) / 32, 32, 0, stream>>>(P, E, fir, fir_stride, pers,  \
+                                                               pers_first, starts, S, count, \
+                                                               est, nch);                    \
+    break;
+    DSD_CASE(2) DSD_CASE(3) DSD_CASE(4) DSD_CASE(5) DSD_CASE(6)
+    DSD_CASE(7) DSD_CASE(8) DSD_CASE(9) DSD_CASE(10)
+#undef DSD_CASE
+    default: return -1;
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 // Best-candidate state of the persistent contexts, replicated per segment
@@ -508,7 +595,8 @@ int dsdgpu_sdm_estimate_state(dsdgpu_context_t* c, const dsdgpu_sdm_params_t* p,
   auto* d_items = (dsdgpu_estimate_t*)c->d_scratch;
   auto* d_out = (double*)((char*)c->d_scratch + ((ib + 255) & ~(size_t)255));
   cudaMemcpyAsync(d_items, items, ib, cudaMemcpyHostToDevice, c->stream);
-  estimate_kernel<<<(n + 31) / 32, 32, 0, c->stream>>>(P, d_items, n, num_levels, d_out);
+  if (launch_estimate(P, num_levels, d_items, n, d_out, c->stream) != 0)
+    return c->cuda_fail(cudaGetLastError(), "estimate launch");
   c->launches++;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return c->cuda_fail(e, "estimate launch");
@@ -631,9 +719,10 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
       rc = ensure_dev(c, &c->d_das_i64, &c->das_i64_cap, (size_t)S, "starts");
       if (rc) return rc;
       cudaMemcpyAsync(c->d_das_i64, st.data(), sizeof(long long) * S, cudaMemcpyHostToDevice, c->stream);
-      das_estimate_kernel<<<(nch + 31) / 32, 32, 0, c->stream>>>(
-          c->sdm, d_fir, fir_stride, c->d_ctx, 0, c->d_das_i64, S, (long long)count,
-          c->d_das_est, nch); c->launches++;
+      if (launch_das_estimate(c->sdm, d_fir, fir_stride, c->d_ctx, 0, c->d_das_i64, S,
+                              (long long)count, c->d_das_est, nch, c->stream) != 0)
+        return c->cuda_fail(cudaGetLastError(), "estimate launch");
+      c->launches++;
     }
     // seg2+ copy the persistent context after seg0: snapshot it so the
     // parallel launch reads a context nothing writes

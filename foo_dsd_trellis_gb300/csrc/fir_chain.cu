@@ -4,15 +4,16 @@
 //   PCM float  -> boxcar running mean over `taps` samples (optional)
 //              -> S upsampling stages (2x half-band 63/127 taps, or a 4x
 //                 quarter-band 127-tap stage), FP32 FMA polyphase
-//              -> FP64 gain ramp g_start + step * i
-//              -> FP64 tanh soft clip above +-0.95 (optional)
+//              -> gain ramp g_start + step * i and the soft clip's threshold
+//                 test in FP32, the tanh knee above +-0.95 in FP64 (optional)
 //              -> double output for the trellis SDM
 //
 // One CTA produces a tile of final output samples for one channel.  It walks
 // the chain backwards to find the input range each stage needs, stages the
 // PCM window (with its history halo) and every intermediate signal in shared
-// memory, and writes only the final double tile to HBM: the chain's HBM
-// traffic is one read of the PCM input and one write of the output.
+// memory, and writes only the final double tile to HBM, two outputs per
+// 16-byte store: the chain's HBM traffic is one read of the PCM input and one
+// write of the output.
 //
 // Stream continuity: a call may be one block of a longer stream.  The last
 // kHistory PCM samples of the previous block are kept per channel and stand in
@@ -35,14 +36,112 @@ __device__ __forceinline__ long long fdiv(long long a, int b) {
   return a >= 0 ? a / b : -((-a + b - 1) / b);
 }
 
+// One 63-tap half-band 2x stage (the chain's common stage): outputs m in
+// [mlo, mhi) of the signal whose input window in shared memory is [ilo, ihi).
+// out[2i] = sum_t h'[2t] x[i - t] (32 taps), out[2i + 1] = h'[31] x[i - 15].
+// A thread computes kHbR consecutive input indices from a register window of
+// kHbR + 31 inputs (each input read once from shared memory for up to 32
+// products); kHbR is odd, so the warp's window loads, kHbR floats apart per
+// lane, fall in distinct banks.
+constexpr int kHbR = 9;
+constexpr int kHbTaps = 32;
+
+__device__ __forceinline__ void halfband_stage(const FirChainConst& F, const float* in,
+                                               long long ilo, long long ihi, float* out,
+                                               long long mlo, long long mhi) {
+  // indices relative to the stage's windows in shared memory (32-bit)
+  const long long i0 = fdiv(mlo, 2);
+  const int n_in = (int)(ihi - ilo);
+  const int n_out = (int)(mhi - mlo);
+  const int i0r = (int)(i0 - ilo);           // >= 31: the stage's halo
+  const int moff = (int)(2 * ilo - mlo);     // out index of input index r: 2 r + moff
+  const int nb = (int)((fdiv(mhi - 1, 2) + 1 - i0 + kHbR - 1) / kHbR);
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    const int ib = i0r + b * kHbR;
+    float w[kHbR + kHbTaps - 1];
+    if (ib + kHbR - 1 < n_in) {
+#pragma unroll
+      for (int j = 0; j < kHbR + kHbTaps - 1; j++) w[j] = in[ib - (kHbTaps - 1) + j];
+    } else {
+#pragma unroll
+      for (int j = 0; j < kHbR + kHbTaps - 1; j++) {
+        const int idx = ib - (kHbTaps - 1) + j;
+        w[j] = idx < n_in ? in[idx] : 0.0f;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kHbR; q++) {
+      float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll
+      for (int t = 0; t < kHbTaps; t += 2) {
+        a0 = fmaf(F.hb[t], w[q + kHbTaps - 1 - t], a0);
+        a1 = fmaf(F.hb[t + 1], w[q + kHbTaps - 2 - t], a1);
+      }
+      const int m = 2 * (ib + q) + moff;
+      if ((unsigned)m < (unsigned)n_out) out[m] = a0 + a1;
+      if ((unsigned)(m + 1) < (unsigned)n_out) out[m + 1] = F.hb_center * w[q + kHbTaps - 16];
+    }
+  }
+}
+
+// Any other stage (the 127-tap first stage into DSD512, the 4x quarter-band
+// stage): one thread per input index i, outputs U*i + r.
+__device__ __forceinline__ void generic_stage(const FirChainConst& F, int k, const float* in,
+                                              long long ilo, float* out, long long mlo,
+                                              long long mhi) {
+  const int U = F.U[k];
+  const long long i0 = fdiv(mlo, U), i1 = fdiv(mhi - 1, U) + 1;
+  for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    for (int r = 0; r < U; r++) {
+      const long long m = (long long)U * i + r;
+      if (m < mlo || m >= mhi) continue;
+      const int nt = F.nphase[k][r];
+      const int toff = F.phase_off[k][r];
+      float acc0 = 0.0f, acc1 = 0.0f;
+      int t = 0;
+      for (; t + 1 < nt; t += 2) {
+        acc0 = fmaf(F.taps[toff + t], in[i - F.lag[toff + t] - ilo], acc0);
+        acc1 = fmaf(F.taps[toff + t + 1], in[i - F.lag[toff + t + 1] - ilo], acc1);
+      }
+      if (t < nt) acc0 = fmaf(F.taps[toff + t], in[i - F.lag[toff + t] - ilo], acc0);
+      out[m - mlo] = acc0 + acc1;
+    }
+  }
+}
+
+// The engine's epilogue of one output (src/engine.c:646-651, 704-717): gain
+// ramp and the soft clip's threshold test in FP32 (within the chain's 1e-6
+// contract), the tanh knee in FP64 on the rare samples above the threshold,
+// one widening per output.
+// float -> double without the FP64 pipe: a normal binary32 value is the
+// binary64 value with the exponent rebiased (127 -> 1023) and the significand
+// shifted up by 29 bits, exactly; zeros, subnormals, infinities and NaNs take
+// the hardware conversion.
+__device__ __forceinline__ double widen_exact(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)f;
+  const unsigned long long bits = ((unsigned long long)(u >> 31) << 63) |
+                                  ((unsigned long long)(e + 896u) << 52) |
+                                  ((unsigned long long)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+__device__ __forceinline__ double fir_epilogue(float v, long long m, float gs, float gstep,
+                                               int apply_gain, int soft_clip) {
+  const float y = apply_gain ? v * fmaf(gstep, (float)m, gs) : v;
+  if (soft_clip && fabsf(y) > 0.95f) return soft_clip_095((double)y);
+  return widen_exact(y);
+}
+
 // The chain description is a by-value kernel parameter (constant bank, about
-// 8.5 KB): every launch carries its own chain, so contexts and batch streams
+// 8.7 KB): every launch carries its own chain, so contexts and batch streams
 // with different rate pairs never share mutable device constants.
 __global__ void __launch_bounds__(kFirThreads)
 fir_chain_kernel(const __grid_constant__ FirChainConst F, const float* __restrict__ pcm,
                  size_t pcm_stride, long long count, const float* __restrict__ hist,
-                 double* __restrict__ out, size_t out_stride, double g_start, double g_step,
-                 int apply_gain, int soft_clip) {
+                 double* __restrict__ out, size_t out_stride, float g_start, float g_step,
+                 int apply_gain, int soft_clip, int vec2) {
   extern __shared__ float sm[];
   const int ch = blockIdx.y;
   const long long total_out = count * F.ratio;
@@ -61,7 +160,7 @@ fir_chain_kernel(const __grid_constant__ FirChainConst F, const float* __restric
   const int bt = F.boxcar;
   const long long p_lo = lo[0] - (bt > 0 ? bt - 1 : 0);
 
-  // shared layout: [pcm window][sig 0][sig 1]...[sig S-1]
+  // shared layout: [pcm window][sig 0][sig 1]...[sig S-1][final tile]
   float* buf[kMaxStages + 1];
   float* pw = sm;
   int off = (int)(hi[0] - p_lo);
@@ -69,6 +168,7 @@ fir_chain_kernel(const __grid_constant__ FirChainConst F, const float* __restric
     buf[k] = sm + off;
     off += (int)(hi[k] - lo[k]);
   }
+  buf[F.S] = sm + ((off + 3) & ~3);
 
   const float* x = pcm + (size_t)ch * pcm_stride;
   const float* hx = hist + (size_t)ch * kHistory;
@@ -97,37 +197,32 @@ fir_chain_kernel(const __grid_constant__ FirChainConst F, const float* __restric
   __syncthreads();
 
   for (int k = 0; k < F.S; k++) {
-    const int U = F.U[k];
-    const float* in = buf[k];
-    const long long ilo = lo[k];
-    const long long mlo = lo[k + 1], mhi = hi[k + 1];
-    const bool last = (k == F.S - 1);
-    // one thread per input index i: outputs U*i + r, r = 0..U-1
-    const long long i0 = fdiv(mlo, U), i1 = fdiv(mhi - 1, U) + 1;
-    for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-      for (int r = 0; r < U; r++) {
-        const long long m = (long long)U * i + r;
-        if (m < mlo || m >= mhi) continue;
-        const int nt = F.nphase[k][r];
-        const int toff = F.phase_off[k][r];
-        float acc0 = 0.0f, acc1 = 0.0f;
-        int t = 0;
-        for (; t + 1 < nt; t += 2) {
-          acc0 = fmaf(F.taps[toff + t], in[i - F.lag[toff + t] - ilo], acc0);
-          acc1 = fmaf(F.taps[toff + t + 1], in[i - F.lag[toff + t + 1] - ilo], acc1);
-        }
-        if (t < nt) acc0 = fmaf(F.taps[toff + t], in[i - F.lag[toff + t] - ilo], acc0);
-        if (!last) {
-          buf[k + 1][m - mlo] = acc0 + acc1;
-        } else {
-          double y = (double)acc0 + (double)acc1;
-          if (apply_gain) y = __dmul_rn(y, __dadd_rn(g_start, __dmul_rn(g_step, (double)m)));
-          if (soft_clip) y = soft_clip_095(y);
-          out[(size_t)ch * out_stride + m] = y;
-        }
+    if (F.hb_stage[k])
+      halfband_stage(F, buf[k], lo[k], hi[k], buf[k + 1], lo[k + 1], hi[k + 1]);
+    else
+      generic_stage(F, k, buf[k], lo[k], buf[k + 1], lo[k + 1], hi[k + 1]);
+    __syncthreads();
+  }
+
+  // the final tile to HBM: consecutive threads write consecutive outputs,
+  // two per 16-byte store where the row allows it
+  const float* fin = buf[F.S];
+  const long long n = o_hi - o_lo;
+  double* dst = out + (size_t)ch * out_stride + o_lo;
+  if (vec2) {
+    for (long long p = 2 * (long long)threadIdx.x; p < n; p += 2 * (long long)blockDim.x) {
+      const double y0 = fir_epilogue(fin[p], o_lo + p, g_start, g_step, apply_gain, soft_clip);
+      if (p + 1 < n) {
+        const double y1 =
+            fir_epilogue(fin[p + 1], o_lo + p + 1, g_start, g_step, apply_gain, soft_clip);
+        *reinterpret_cast<double2*>(dst + p) = make_double2(y0, y1);
+      } else {
+        dst[p] = y0;
       }
     }
-    __syncthreads();
+  } else {
+    for (long long p = threadIdx.x; p < n; p += blockDim.x)
+      dst[p] = fir_epilogue(fin[p], o_lo + p, g_start, g_step, apply_gain, soft_clip);
   }
 }
 
@@ -228,6 +323,11 @@ int build_chain_const(unsigned fs_in, unsigned fs_out, int boxcar, FirChainConst
       F->nphase[k][r] = n;
       toff += n;
     }
+    if (U[k] == 2 && L[k] == 63 && F->nphase[k][0] == 32 && F->nphase[k][1] == 1) {
+      F->hb_stage[k] = 1;
+      for (int t = 0; t < 32; t++) F->hb[t] = F->taps[F->phase_off[k][0] + t];
+      F->hb_center = F->taps[F->phase_off[k][1]];
+    }
     rows *= U[k];
   }
   // output tile: a few thousand final samples per CTA
@@ -249,6 +349,7 @@ size_t chain_smem_bytes(const FirChainConst& F) {
     }
     size_t tot = (size_t)(hi[0] - lo[0] + (F.boxcar > 0 ? F.boxcar - 1 : 0));
     for (int k = 0; k < F.S; k++) tot += (size_t)(hi[k] - lo[k]);
+    tot = ((tot + 3) & ~(size_t)3) + (size_t)F.tile;   // the final tile
     if (tot > best) best = tot;
   }
   return (best + 16) * sizeof(float);
@@ -262,7 +363,9 @@ int fir_chain_prepare() {
   if (dev < 0 || dev >= 64) return -1;
   if (!attr_set[dev]) {
     if (cudaFuncSetAttribute(fir_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kFirMaxSmem) != cudaSuccess)
+                             kFirMaxSmem) != cudaSuccess ||
+        cudaFuncSetAttribute(fir_chain_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             100) != cudaSuccess)
       return -1;
     attr_set[dev] = true;
   }
@@ -278,9 +381,13 @@ int launch_fir_chain(const FirChainConst& F, size_t smem, const float* pcm, size
   if (fir_chain_prepare() != 0) return -1;
   if (smem > (size_t)kFirMaxSmem) return -1;
   const dim3 grid((unsigned)((n_out + F.tile - 1) / F.tile), (unsigned)nch);
+  // 16-byte stores of output pairs: tiles start at even outputs, so the rows
+  // and the base have to be 16-byte aligned
+  const int vec2 = ((reinterpret_cast<uintptr_t>(out) & 15) == 0 && (out_stride & 1) == 0 &&
+                    (F.tile & 1) == 0) ? 1 : 0;
   fir_chain_kernel<<<grid, kFirThreads, smem, stream>>>(F, pcm, pcm_stride, count, hist, out,
-                                                        out_stride, g_start, g_step, apply_gain,
-                                                        soft_clip);
+                                                        out_stride, (float)g_start, (float)g_step,
+                                                        apply_gain, soft_clip, vec2);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -36,6 +36,12 @@ struct FirChainConst {
   int phase_off[kMaxStages][4];        // offset into taps[] / lag[]
   float taps[kMaxChainTaps];           // h'[U*j + r] = U * h[U*j + r]
   int lag[kMaxChainTaps];              // j
+  // the 63-tap half-band 2x stage (every stage but a 127-tap first stage and
+  // the 4x quarter-band one): its 32 even-phase taps and the centre tap, at
+  // fixed offsets so that the unrolled kernel reads them as constant operands
+  int hb_stage[kMaxStages];            // 1: stage k is a 63-tap half-band 2x stage
+  float hb[32];                        // h'[2t], lag t
+  float hb_center;                     // h'[31], lag 15
 };
 
 // Chain construction (fir_chain_init_ex's stage plan and tap design) and the

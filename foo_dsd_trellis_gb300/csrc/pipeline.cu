@@ -59,7 +59,10 @@ int dsdgpu_pipeline_setup(dsdgpu_context_t* c, const dsdgpu_pipeline_params_t* p
   dsdgpu_fir_params_t fp = p->fir;
   if (c->pipe_precorr) fp.soft_clip = 0;   // the engine does not clip ahead of PreCorr
   if (c->pipe_dsd_down) {
-    const int taps = p->fir.boxcar_taps > 0 ? p->fir.boxcar_taps : 8;
+    // boxcar_taps 0: no pre-smooth, as the plugin's DAS FIR phase
+    // (engine_process_fir_gain, src/engine.c:789-900); a one-tap mean is the
+    // identity on the +-1 input
+    const int taps = p->fir.boxcar_taps > 0 ? p->fir.boxcar_taps : 1;
     rc = dsdgpu_boxcar_setup(c, taps, nch);
     if (!rc) rc = dsdgpu_decim_setup(c, p->fir.fs_in, p->fir.fs_out, nch);
     if (!rc)

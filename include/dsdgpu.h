@@ -78,8 +78,11 @@ typedef struct {
     unsigned fs_in;       /* input rate (PCM or DSD), Hz */
     unsigned fs_out;      /* output DSD rate, fs_in * 2^k, k = 1..9 */
     int      boxcar_taps; /* running-mean pre-smooth at the input rate: 8 on the
-                             rate-conversion path, 0 = off (DAS FIR phase) */
-    int      soft_clip;   /* 1: tanh knee above +-0.95 before the SDM */
+                             engine's rate-conversion path (engine_process_block),
+                             0 = off (the plugin's DAS FIR phase,
+                             engine_process_fir_gain, src/engine.c:789-900) */
+    int      soft_clip;   /* 1: tanh knee above +-0.95 before the SDM
+                             (engine_process_block); 0 in the DAS FIR phase */
 } dsdgpu_fir_params_t;
 
 /* DAS seeding modes (reference src/dsp_plugin.c:2185-2283). */

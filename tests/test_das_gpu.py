@@ -186,3 +186,26 @@ def test_pipeline_flush_restarts_the_stream():
         outs.append((o1[:n1].cpu().numpy(), o2[:n2].cpu().numpy()))
     assert np.array_equal(outs[1][1], outs[0][0])          # flushed == fresh
     assert not np.array_equal(outs[0][1], outs[0][0])      # continued != fresh
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["full_parallel", "seg0_first"])
+def test_das_stream_of_chunks_equals_oracle(oracle, mode):
+    """Three chunks of one stream: the GPU's persistent contexts carry from
+    chunk to chunk (seg0 continues them; the last segment's final state
+    replaces them, src/dsp_plugin.c:2714-2721) exactly as the oracle's, which
+    is pinned to the reference's plugin_process over chunk streams."""
+    from foo_dsd_trellis_gb300.das import DasChannels
+    f = _ntf("clans-6", 5644800)
+    K, depth, lat = 8, 16, 32
+    n = 3 * 90000
+    x = np.stack([multitone(n, 51) * 1.7, multitone(n, 52) * 1.2])
+    carry = [oracle.sdm(f.order, np.array(f.a), np.array(f.g), depth, K, lat) for _ in range(2)]
+    d = DasChannels(f.order, f.a, f.g, depth, K, lat, num_channels=2)
+    for k in range(3):
+        chunk = np.ascontiguousarray(x[:, k * 90000:(k + 1) * 90000])
+        want, ws, _ = oracle.das_run(f.order, np.array(f.a), np.array(f.g), depth, K, lat, 0.0,
+                                     chunk, nsegs=5, seed_mode=mode, carry=carry)
+        got, gs = d.process_chunk(torch.from_numpy(chunk).cuda(), nsegs=5, seed_mode=mode)
+        assert list(gs) == list(ws), k
+        assert np.array_equal(got.cpu().numpy(), want), k
+    d.close()

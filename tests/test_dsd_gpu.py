@@ -97,10 +97,11 @@ def test_samerate_pipeline(oracle):
     assert np.array_equal(out[:nb].cpu().numpy(), want)
 
 
-def _gpu_fir_for_dsd(dop, fs_in, fs_out, soft_clip, gs, ge):
+def _gpu_fir_for_dsd(dop, fs_in, fs_out, soft_clip, gs, ge, boxcar=8):
     """The FIR stage of the DSD rate-conversion pipeline from the library's
-    separate entry points: unpack, then the FIR upsampling chain (boxcar 8) or
-    the boxcar + FP64 decimation chain, with gain and clip."""
+    separate entry points: unpack, then the FIR upsampling chain (boxcar 8, or
+    none) or the boxcar + FP64 decimation chain (a one-tap mean for none),
+    with gain and clip."""
     import ctypes as C
     from foo_dsd_trellis_gb300 import _lib
     from foo_dsd_trellis_gb300.fir import FirChain
@@ -116,7 +117,7 @@ def _gpu_fir_for_dsd(dop, fs_in, fs_out, soft_clip, gs, ge):
             _lib.check(h, L.dsdgpu_dop_unpack_f32(h, nch, C.c_void_p(d_dop.data_ptr()), frames,
                                                   frames, C.c_void_p(x.data_ptr()), n_in))
             torch.cuda.synchronize()
-            fc = FirChain(fs_in, fs_out, boxcar_taps=8, soft_clip=soft_clip, num_channels=nch)
+            fc = FirChain(fs_in, fs_out, boxcar_taps=boxcar, soft_clip=soft_clip, num_channels=nch)
             y = fc.process(x, gs, ge).cpu().numpy()
             fc.close()
             return y, x.cpu().numpy()
@@ -124,7 +125,7 @@ def _gpu_fir_for_dsd(dop, fs_in, fs_out, soft_clip, gs, ge):
         box = torch.empty((nch, n_in), dtype=torch.float64, device="cuda")
         _lib.check(h, L.dsdgpu_dop_unpack(h, nch, C.c_void_p(d_dop.data_ptr()), frames, frames,
                                           C.c_void_p(bits.data_ptr()), n_in))
-        _lib.check(h, L.dsdgpu_boxcar_setup(h, 8, nch))
+        _lib.check(h, L.dsdgpu_boxcar_setup(h, max(1, boxcar), nch))
         _lib.check(h, L.dsdgpu_boxcar_process(h, 0, nch, C.c_void_p(bits.data_ptr()), n_in, n_in,
                                               C.c_void_p(box.data_ptr()), n_in, 1.0, 1.0))
         _lib.check(h, L.dsdgpu_decim_setup(h, fs_in, fs_out, nch))
@@ -184,4 +185,41 @@ def test_dsd_rate_conversion_pipeline(oracle, fs_in, fs_out, mode):
                                     seg_len=32768, seed_mode=0, reposition=True)
     assert got.shape == want.shape
     assert np.array_equal(got, want)
+    enc.close()
+
+
+
+@pytest.mark.parametrize("fs_in,fs_out", [(2822400, 11289600), (11289600, 5644800)],
+                         ids=["up4", "down2"])
+def test_dsd_rate_conversion_das_glue(oracle, fs_in, fs_out):
+    """The plugin's DAS path for DSD input at another rate runs the engine's FIR
+    phase without the boxcar and the soft clip (engine_process_fir_gain,
+    src/engine.c:789-900; pinned to the reference's engine.c on the CPU): the
+    pipeline with boxcar_taps 0 and soft_clip 0 equals that FIR stage (1e-6 of
+    full scale up, 1e-12 down against the oracle's restatement) followed by the
+    oracle's DAS, byte for byte."""
+    from foo_dsd_trellis_gb300 import ntf
+    from foo_dsd_trellis_gb300.pipeline import FULL_PARALLEL, OUT_BITS, Encoder
+    nch, K, depth, lat, ge = 2, 2, 4, 32, float(np.float32(0.708))
+    frames = 6000 if fs_out > fs_in else 12000
+    src = np.stack([_dsd_stream(oracle, 16 * frames, 9 + c, "clans-5", fs_in) for c in range(nch)])
+    dop = np.stack([oracle.dop_float_frames(src[c], 0) for c in range(nch)])
+    f = ntf.get_filter("clans-6", fs_out)
+    fir, x = _gpu_fir_for_dsd(dop, fs_in, fs_out, False, ge, ge, boxcar=0)
+    if fs_out > fs_in:
+        want_fir = np.stack([oracle.engine_fir(fs_in, fs_out, x[c], 0, ge, ge, False) for c in range(nch)])
+        tol = 1e-6
+    else:
+        want_fir = np.stack([oracle.engine_down(oracle.Boxcar(1), oracle.Decimator(fs_in, fs_out),
+                                                x[c], ge, ge, False) for c in range(nch)])
+        tol = 1e-12
+    assert fir.shape == want_fir.shape
+    assert np.max(np.abs(fir - want_fir)) <= tol * np.max(np.abs(want_fir))
+    enc = Encoder(fs_in, fs_out, nch, f, depth, K, lat, seg_len=32768, seed_mode=FULL_PARALLEL,
+                  reposition=True, boxcar_taps=0, soft_clip=False, output_format=OUT_BITS)
+    out = torch.empty((nch, fir.shape[1] + 256), dtype=torch.uint8, device="cuda")
+    ns, _ = enc.process(torch.from_numpy(dop).cuda(), out, ge, ge)
+    want, _, _ = oracle.das_run(f.order, np.array(f.a), np.array(f.g), depth, K, lat, 0.0, fir,
+                                seg_len=32768, seed_mode=0, reposition=True)
+    assert np.array_equal(out[:, :ns].cpu().numpy(), want)
     enc.close()

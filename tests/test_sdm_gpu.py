@@ -312,7 +312,8 @@ def test_orders_outside_the_table(oracle, order, K):
 def test_estimate_state_batch(oracle):
     """dsdgpu_sdm_estimate_state (sdm_estimate_state_multibit, src/trellis.c:1125-1187)
     over many inputs in one launch equals the oracle (pinned to the reference's
-    compiled estimator), for orders 2..10, 2/3/16 levels, the limiter and
+    compiled estimator), for orders 2..10, 2/3/16/97/2000 levels (the quantiser
+    index from reciprocal products, its table, and the exact divisions), the limiter and
     counts 0, 1 and 20,000."""
     import ctypes as C
     from foo_dsd_trellis_gb300 import _lib, ntf
@@ -322,7 +323,7 @@ def test_estimate_state_batch(oracle):
     assert L.dsdgpu_create(0, C.byref(h)) == 0
     rng = np.random.default_rng(11)
     names = ["clans-4", "clans-5", "clans-6", "clans-7", "clans-8", "sdm-5", "sdm-8"]
-    for levels in (2, 3, 16):
+    for levels in (2, 3, 16, 97, 2000):
         for lim in (0.0, 1.5):
             for name in names:
                 f = ntf.get_filter(name, 5644800)
