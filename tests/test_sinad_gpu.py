@@ -1,13 +1,25 @@
 """End-to-end in-band quality: the GPU path (FP32 FIR chain, trellis SDM,
 DAS) against the reference pipeline restated in the oracle (FP64 FIR, the
-reference's trellis and DAS).  The two bitstreams are different noise
-realisations once the FIR outputs differ in the last bits, so the check is on
-what the reference's users measure: SINAD after a decimating low-pass at the
-test tone, within 0.05 dB of the reference's, and above the reference's own
-60 dB floor (test/test_trellis.c:277-301).  The SINAD of one stereo second
-varies by about 0.05 dB (standard deviation) between noise realisations of
-the reference itself, so the power average runs over 8 channels with
-independent dither (16 channel-seconds at DSD64, 8 at DSD128)."""
+reference's trellis and DAS, both pinned).  The two bitstreams are different
+noise realisations once the FIR outputs differ in the last bits (the trellis
+decisions diverge), so the check is on what the reference's users measure,
+in-band error or SINAD after a decimating low-pass, and its tolerance comes
+from the spread of the reference's own realisations: each metric below was
+measured on 8 realisations of the oracle pipeline whose FP64 FIR output was
+scaled by 1 + k * 2^-40 (k = 0..7), and two realisations of a metric with
+standard deviation s differ by more than 3 * sqrt(2) * s with probability
+below 0.3 %.
+
+  DSD64 one segment, 997 Hz sine, 8 channels x 2 s     s = 0.015 dB
+  DSD128 DAS, 997 Hz sine, 8 channels x 1 s: interior  s = 0.34 dB
+                                               whole   s = 0.26 dB
+  DSD128 DAS, the headline's 10 s multitone + pink,
+  whole-stream in-band error                           s = 0.054 dB
+
+The first and the last are tight enough to check the 0.05 dB / 0.25 dB
+bounds used below; the DAS sine case varies by tenths of a dB between
+realisations of the reference itself (its seams and the pure tone's idle
+patterns), so it is checked against its measured spread."""
 import concurrent.futures as cf
 import os
 
@@ -108,11 +120,10 @@ def test_sinad_dsd128_das(oracle):
                                 ref_fir, seg_len=65536, seed_mode=0, reposition=True)
     assert want.shape[1] == ns
     # With 94 seams a second the seams' residual discontinuities dominate the
-    # whole-stream in-band error of both (about 56 dB; the reference's 60 dB
-    # floor is for the plain trellis), and those few hundred events vary by
-    # tenths of a dB between noise realisations.  The FIR's precision shows in
-    # the steady-state noise: the SINAD is taken over the segment interiors,
-    # 2 x overlap clear of every boundary.
+    # whole-stream error of both (about 56 dB; the reference's 60 dB floor is
+    # for the plain trellis); the interior SINAD, 2 x overlap clear of every
+    # boundary, is the steady-state noise.  Both are asserted, each against
+    # the reference's measured realisation spread.
     S = n_fir // 65536
     base = n_fir // S
     ov = 64 * lat
@@ -123,5 +134,79 @@ def test_sinad_dsd128_das(oracle):
     s_want = _mean_power_db([sinad_db(b, fs_out, 997.0, keep=keep) for b in want])
     whole = (_mean_power_db([sinad_db(b, fs_out, 997.0) for b in got]),
              _mean_power_db([sinad_db(b, fs_out, 997.0) for b in want]))
+    print(f"DSD128 DAS sine SINAD: interior GPU {s_got:.3f} / reference {s_want:.3f} dB, "
+          f"whole stream GPU {whole[0]:.3f} / reference {whole[1]:.3f} dB")
     assert s_want > 60.0 and s_got > 60.0, (s_got, s_want, whole)
-    assert abs(s_got - s_want) <= 0.05, (s_got, s_want, whole)
+    assert abs(s_got - s_want) <= 3 * np.sqrt(2) * 0.34, (s_got, s_want, whole)
+    assert abs(whole[0] - whole[1]) <= 3 * np.sqrt(2) * 0.26, (s_got, s_want, whole)
+
+
+def _inband_snr_db(bits: np.ndarray, ideal: np.ndarray, fs: float, jump_at: int, shift: int,
+                   band: float = 20000.0) -> float:
+    """In-band signal-to-error ratio of a 0/1 decision stream against the
+    modulator's input `ideal`, both through the same brick-wall low-pass to
+    `band` (FFT on the device), over the whole stream, seams included.  In the
+    full-parallel layout the stream's decision m is input sample m before the
+    first seam and input m + shift after it (seg0 is cut to its nominal length
+    while seg1 starts one overlap early, src/dsp_plugin.c:2417-2424 and
+    2650-2660), so the input is laid out the same way before filtering."""
+    n = len(bits)
+    x = np.concatenate([ideal[:jump_at], ideal[jump_at + shift: n + shift]])
+    assert len(x) == n
+    y = torch.from_numpy(bits).cuda().to(torch.float64) * 2.0 - 1.0
+    xd = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    keep = torch.from_numpy(np.fft.rfftfreq(n, 1.0 / fs) <= band).cuda()
+    ly = torch.fft.irfft(torch.fft.rfft(y) * keep, n)
+    lx = torch.fft.irfft(torch.fft.rfft(xd) * keep, n)
+    e = ly - lx
+    return float(10.0 * torch.log10(torch.sum(lx * lx) / torch.sum(e * e)))
+
+
+def test_inband_error_headline_whole_stream(oracle):
+    """The headline workload end to end, as the quality contract states it:
+    10 s of the 48 kHz multitone + pink signal (seed 1001) -> DSD128 through the
+    GPU path (FP32 FIR chain, trellis SDM K = 32 / depth 64 / lat 128, DAS over
+    65,536-sample segments, full-parallel) and through the reference pipeline
+    restated in the oracle (FP64 FIR, the reference's trellis and DAS, both
+    pinned).  In-band (0-20 kHz) error after the low-pass over the whole
+    stream, every seam included, against the FP64 FIR output: the GPU's is
+    within 0.25 dB of the reference's (3 sqrt(2) x the 0.054 dB standard
+    deviation of the reference's own realisations)."""
+    from foo_dsd_trellis_gb300 import ntf, signals
+    from foo_dsd_trellis_gb300.das import DasChannels
+    from foo_dsd_trellis_gb300.fir import FirChain
+    from foo_dsd_trellis_gb300.pipeline import FULL_PARALLEL, PCM_FIR_GAIN
+    fs_in, fs_out, K, depth, lat, nch, seg = 48000, 6144000, 32, 64, 128, 2, 65536
+    f = ntf.get_filter("clans-7", fs_out)
+    pcm = signals.dsd128_multitone_pink(10.0, fs_in, nch, 1001)
+    gain = float(PCM_FIR_GAIN)
+    # the pipeline's own kernels stage by stage (bit for bit the whole-path call)
+    fc = FirChain(fs_in, fs_out, boxcar_taps=8, soft_clip=True, num_channels=nch)
+    fir32 = fc.process(torch.from_numpy(pcm).cuda(), gain, gain)
+    d = DasChannels(f.order, f.a, f.g, depth, K, lat, num_channels=nch)
+    got, got_seams = d.process_chunk(fir32, seg_len=seg, seed_mode=FULL_PARALLEL)
+    got = got.cpu().numpy()
+    d.close()
+    fc.close()
+
+    def fir64(c):
+        return oracle.engine_fir(fs_in, fs_out, pcm[c], boxcar_taps=8, g_start=gain,
+                                 g_end=gain, soft_clip=True)
+    with cf.ThreadPoolExecutor(max_workers=nch) as ex:
+        ref_fir = np.stack(list(ex.map(fir64, range(nch))))
+    want, want_seams, starts = oracle.das_run(f.order, np.array(f.a), np.array(f.g), depth, K,
+                                              lat, 0.0, ref_fir, seg_len=seg, seed_mode=0,
+                                              reposition=True, nthreads=os.cpu_count())
+    n = ref_fir.shape[1]
+    overlap = 64 * lat
+    assert want.shape == got.shape == (nch, n - overlap)
+    size0 = starts[1]
+
+    def snr(bits, seams):
+        at = size0 - overlap + int(seams[1])          # where the first seam lands
+        return _mean_power_db([_inband_snr_db(bits[c], ref_fir[c], fs_out, at, overlap - lat)
+                               for c in range(nch)])
+    s_got, s_want = snr(got, got_seams), snr(want, want_seams)
+    print(f"in-band SNR, whole stream: GPU {s_got:.3f} dB, reference {s_want:.3f} dB")
+    assert s_want > 40.0
+    assert abs(s_got - s_want) <= 0.25, (s_got, s_want)
