@@ -24,7 +24,10 @@ the engine's 127-tap FIR lowpass instead of the boxcar), dsd2pcm128 (DSD128 ->
 44.1 kHz PCM), precorr128 (PCM -> DSD128 with the PreCorr SDM) and dsd256to128
 (DoP DSD256 -> DSD128 through the FP64 decimation chain and the DAS trellis) and
 dsd128_seg0first (the headline's signal and trellis with the reference's own
-seeding rule below DSD512, seg0-first, on 1 s chunks of one stream).
+seeding rule below DSD512, seg0-first, on 1 s chunks of one stream).  The
+default run (N = 1) also runs the quick ones after the headline's timed steps,
+each in its own process, and summarises them under "also" (`--also none` skips
+them).
 """
 from __future__ import annotations
 
@@ -56,6 +59,49 @@ SDM_DRAM_BYTES_PER_SAMPLE = 9.04                      # measured, see the traffi
 SDM_PARTS_DRAM_BYTES_PER_SAMPLE = 9.15                # the balanced launch's (parts kernel), measured
 
 
+# The rows beside the headline, measured by the default run as well: the
+# same-rate re-encode (boxcar and FIR lowpass), DSD256 -> DSD128, DSD -> PCM,
+# PreCorr, the DSD512 5.1 UPOLS configuration and the adjoint.  The 64-stream
+# batched form (about a minute per step) runs only on request.
+ALSO_DEFAULT = ["samerate128", "samerate128lp", "dsd256to128", "dsd2pcm128", "precorr128",
+                "dsd512conv6", "diff16"]
+
+
+def run_also(names: list[str]) -> dict:
+    """Each workload in its own process after the headline's timed steps; the
+    headline's numbers are final by then.  Returns name -> summary."""
+    out = {}
+    for w in names:
+        cmd = [sys.executable, os.path.abspath(__file__), "--workload", w, "--steps", "3",
+               "--warmup", "3"]
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+            lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+            if r.returncode != 0 or not lines:
+                out[w] = {"error": f"exit {r.returncode}: {r.stderr.strip()[-300:]}"}
+                continue
+            d = json.loads(lines[-1])
+        except Exception as e:   # a failed side run never voids the headline line
+            out[w] = {"error": repr(e)[:300]}
+            continue
+        rf = d.get("roofline") or {}
+        cb = d.get("cpu_baseline") or {}
+        out[w] = {"metric": d.get("metric"), "value": d.get("value"), "unit": d.get("unit"),
+                  "higher_is_better": d.get("higher_is_better"),
+                  "ms_per_step": d.get("ms_per_step"), "steps": d.get("steps"),
+                  "warmup": d.get("warmup"),
+                  "e2e": (d.get("e2e") or {}).get("value"),
+                  "roofline_frac": rf.get("frac"), "roofline_kernel": rf.get("kernel"),
+                  "cpu_baseline": {k: cb.get(k) for k in ("value", "cores", "kind", "sample")}
+                  if cb else None,
+                  "workload": (d.get("config") or {}).get("workload"),
+                  "clocks": d.get("clocks"), "gpu_launches": d.get("gpu_launches")}
+        for k in ("forward_ms", "exact_sdm_ms", "fd_check", "stages_ms", "parity"):
+            if k in d:
+                out[w][k] = d[k]
+    return out
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -75,6 +121,10 @@ def parse():
                          "samerate128 / samerate128lp / precorr128 / dsd2pcm128: the DSD "
                          "re-encode (boxcar / FIR lowpass), PreCorr and DSD -> PCM paths (each "
                          "prints its own JSON line)")
+    ap.add_argument("--also", default=",".join(ALSO_DEFAULT),
+                    help="dsd128_das at N=1: other workloads run after the headline, one "
+                         "subprocess each (3 warm-up + 3 timed steps), summarised under "
+                         "'also' in the headline's JSON line; 'none' skips them")
     ap.add_argument("--fd-dirs", type=int, default=32,
                     help="diff16: random unit directions of the finite-difference check")
     ap.add_argument("--ms-scale", type=float, default=1.0,
@@ -479,8 +529,16 @@ def run_ours(args):
                 "parity": parity,
                 "gpu_launches": int(launches), "stages_ms": stages, "plain": plain,
                 "fp64_peak_gops": fp64_peak}
+        names = [w for w in args.also.split(",") if w and w != "none"]
+        if world == 1 and names:
+            enc.close()
+            enc = None
+            del d_pcm, d_out, flush
+            torch.cuda.empty_cache()
+            line["also"] = run_also(names)
         print(json.dumps(line), flush=True)
-    enc.close()
+    if enc is not None:
+        enc.close()
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

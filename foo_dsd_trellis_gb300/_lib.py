@@ -149,6 +149,7 @@ SIGNATURES = {
     "dsdgpu_sdm_process_noalloc": (C.c_int, [C.POINTER(SdmParams), C.c_int, C.c_int, _vp, _sz,
                                              _sz, _vp, _sz, _szp, _vp]),
     "dsdgpu_probe_fp64": (C.c_int, [_vp, C.POINTER(C.c_double)]),
+    "dsdgpu_selftest_convert": (C.c_int, [_vp, C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64)]),
     "dsdgpu_plan_create": (C.c_int, [_vp, C.POINTER(StreamDesc), C.c_int, C.c_int64, C.c_int,
                                      C.c_uint64, C.POINTER(_vp)]),
     "dsdgpu_plan_destroy": (None, [_vp]),

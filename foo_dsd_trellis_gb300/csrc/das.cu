@@ -5,10 +5,12 @@
 // the segments run as one persistent SDM launch; then
 //
 //   das_seam_kernel     one CTA per boundary: match density by block prefix
-//                       sum, the reference's candidate scan, the run nearest
-//                       the density peak, and the 255-tap FP64 pop metric for
-//                       every candidate (threads over (candidate, offset);
-//                       each dot product keeps the reference's tap order);
+//                       sum, the reference's candidate scan and the run
+//                       nearest the density peak (from match bitmasks, in
+//                       parallel), and the 255-tap pop metric of every
+//                       candidate (an FP32 pass over all offsets, then the
+//                       reference's FP64 sum, in its tap order, for the
+//                       offsets that can hold the maximum);
 //   das_assemble_kernel gathers the final stream for every channel.
 //
 // The stitch search of a boundary only reads the last `overlap` decisions of
@@ -19,6 +21,8 @@
 #include "api_context.h"
 #include "das_internal.h"
 #include "das_plan.h"
+
+#include <cuda_fp16.h>
 
 #include <algorithm>
 #include <cmath>
@@ -219,10 +223,184 @@ __global__ void das_seed_from_best_kernel(const SdmCtx* __restrict__ ctxs, int f
 
 // ---- seam search, one CTA per boundary (src/dsp_plugin.c:2455-2652) ----
 // kGlobal: overlaps above kMaxSeamOverlap (traceback latencies above 256) keep
-// the match flags, the prefix sums and the density map in a global scratch
-// slice per boundary (das_seam_global_bytes) instead of shared memory.
+// the match flags, the prefix sums, the density map and the search scratch in
+// a global slice per boundary (das_seam_global_bytes) instead of shared memory.
+//
+// The reference's scans are restated in parallel, with the same results:
+//  - candidate runs: a run start is the first position of a maximal run of
+//    matches whose density reaches the floor (the serial scan stops there and
+//    jumps to the run's end); the starts with runs of at least 4 are listed
+//    in order from match / floor bitmasks, and the spacing rule is applied
+//    greedily over that list;
+//  - the run near the density peak: the first hit in the scan order
+//    (r = 0, 1, ..., pp - r before pp + r) of a run of 8, else of 4, else the
+//    LAST single match in that order (the serial loop keeps overwriting its
+//    pick below 4), else the peak itself;
+//  - pop metric: max over 639 offsets of |sum of +-q2[k]| in tap order.  Every
+//    offset is first summed in FP32 together with a rigorous bound E on
+//    |v32 - v64|: the running error of recursive summation (Higham, Accuracy
+//    and Stability of Numerical Algorithms, 2nd ed., section 4.2:
+//    |s^ - s| <= u/(1-u) sum_i |s^_i| over the computed partial sums, taken
+//    twice here), plus u * sum|q2| for the taps rounded to FP32, plus 2^-40
+//    for the FP64 sum's own rounding.  LB = max_j (|v32_j| - E_j) bounds the
+//    FP64 maximum from below, so an offset with |v32_j| + E_j < LB cannot hold
+//    it; the rest (about one per candidate) are summed in FP64 in the
+//    reference's order.  Bounds are formed with directed rounding.  If more
+//    than kPopList offsets qualify, every offset is summed in FP64.
+constexpr int kPopJlo = -127, kPopJhi = 512, kPopJ = kPopJhi - kPopJlo;
+constexpr int kPopR = 4;                                     // offsets per screening thread
+constexpr int kPopBlocks = (kPopJ + kPopR - 1) / kPopR;
+constexpr int kPopList = 512;
+constexpr int kPopTaps = 256;                                // 255 taps and a zero
+
+__host__ __device__ inline size_t seam_scratch_bytes(int L) {
+  const size_t W = ((size_t)L + 31) / 32;
+  const size_t runs = 4 * ((size_t)L / 5 + 8);
+  const size_t pop = 4 * (size_t)(kMaxQ + 1) * kPopBlocks + 4 * (size_t)kPopList;
+  return 8 * W + (runs > pop ? runs : pop);
+}
+
+// block-wide exclusive scans (blockDim a multiple of 32, at most 1024)
+__device__ __forceinline__ int block_excl_sum(int v, int* red, int* total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int n = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += n;
+  }
+  __syncthreads();
+  if (lane == 31) red[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int y = lane < nw ? red[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int n = __shfl_up_sync(0xffffffffu, y, o);
+      if (lane >= o) y += n;
+    }
+    red[lane] = y;
+  }
+  __syncthreads();
+  const int r = x - v + (w > 0 ? red[w - 1] : 0);
+  if (total) *total = red[nw - 1];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ int block_excl_max(int v, int* red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int n = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x = max(x, n);
+  }
+  int ex = __shfl_up_sync(0xffffffffu, x, 1);
+  if (lane == 0) ex = -1;
+  __syncthreads();
+  if (lane == 31) red[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int y = lane < nw ? red[lane] : -1;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int n = __shfl_up_sync(0xffffffffu, y, o);
+      if (lane >= o) y = max(y, n);
+    }
+    red[lane] = y;
+  }
+  __syncthreads();
+  const int r = max(ex, w > 0 ? red[w - 1] : -1);
+  __syncthreads();
+  return r;
+}
+
+// Run starts of one thread's words [w0, w1) in order: fn(p) for every p that
+// opens the serial scan's run (see above) with p < L - 3 and a run of >= 4.
+// czf / cnz: last match-at-floor / last mismatch position before word w0.
+template <class Fn>
+__device__ __forceinline__ void seam_runs(const unsigned* zb, const unsigned* fb, int W, int L,
+                                          int w0, int w1, int czf, int cnz, Fn fn) {
+  for (int w = w0; w < w1; w++) {
+    const unsigned z = zb[w], zfw = z & fb[w], nz = ~z;   // bits at >= L: mismatches
+    unsigned zf = zfw;
+    while (zf) {
+      const int b = __ffs(zf) - 1;
+      zf &= zf - 1u;
+      const int p = (w << 5) + b;
+      if (p >= L - 3) return;
+      const unsigned below = (1u << b) - 1u;
+      const unsigned zfb = zfw & below, nzb = nz & below;
+      const int pzf = zfb ? (w << 5) + 31 - __clz(zfb) : czf;
+      const int pnz = nzb ? (w << 5) + 31 - __clz(nzb) : cnz;
+      if (pzf >= 0 && pnz < pzf) continue;          // same run as an earlier start
+      const unsigned above = nz & ~below;           // bit b is a match
+      int e;
+      if (above) {
+        e = (w << 5) + __ffs(above) - 1;
+      } else {
+        int w2 = w + 1;
+        while (w2 < W && zb[w2] == 0xffffffffu) w2++;
+        e = w2 < W ? (w2 << 5) + __ffs(~zb[w2]) - 1 : L;
+      }
+      if (e > L) e = L;
+      if (e - p >= 4) fn(p);
+    }
+    if (zfw) czf = (w << 5) + 31 - __clz(zfw);
+    if (nz) cnz = (w << 5) + 31 - __clz(nz);
+  }
+}
+
+// mr consecutive matches from tp (tp + mr <= L)
+__device__ __forceinline__ bool seam_zrun(const unsigned* zb, int W, int L, int tp, int mr) {
+  if (tp < 0 || tp + mr > L) return false;
+  const int w = tp >> 5, b = tp & 31;
+  unsigned long long v = zb[w];
+  if (w + 1 < W) v |= (unsigned long long)zb[w + 1] << 32;
+  const unsigned long long m = ((1ull << mr) - 1ull) << b;
+  return (v & m) == m;
+}
+
+// FP32 pop values of offsets j0 .. j0 + kPopR - 1 of a candidate at sp:
+// v[r] = sum_k e[sp + j0 + r - 127 + k] * q2f[k], e = +-1 / 0 inside [sp, L),
+// and mu[r] = the sum of |partial sums| (the running error bound's sum).
+__device__ __forceinline__ float seam_e(const __half* ef, int i, int sp, int L) {
+  return (i >= sp && i < L) ? __half2float(ef[i]) : 0.0f;
+}
+
+__device__ __forceinline__ void seam_screen(const __half* ef, const float* q2f, int L, int sp,
+                                            int j0, float (&v)[kPopR], float (&mu)[kPopR]) {
+  const int base = sp + j0 - 127;
+  float w[2 * kPopR - 1];
+#pragma unroll
+  for (int r = 0; r < kPopR; r++) {
+    v[r] = 0.0f;
+    mu[r] = 0.0f;
+  }
+#pragma unroll
+  for (int m = 0; m < kPopR - 1; m++) w[m] = seam_e(ef, base + m, sp, L);
+  for (int c = 0; c < kPopTaps / kPopR; c++) {
+    const int cb = base + c * kPopR;
+#pragma unroll
+    for (int t = 0; t < kPopR; t++) w[kPopR - 1 + t] = seam_e(ef, cb + kPopR - 1 + t, sp, L);
+#pragma unroll
+    for (int kk = 0; kk < kPopR; kk++) {
+      const float q = q2f[c * kPopR + kk];
+#pragma unroll
+      for (int r = 0; r < kPopR; r++) {
+        v[r] = fmaf(w[kk + r], q, v[r]);
+        mu[r] += fabsf(v[r]);
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < kPopR - 1; m++) w[m] = w[m + kPopR];
+  }
+}
+
+// Error bound of one screened offset (rounded up): 2u * mu + c0.
+__device__ __forceinline__ float seam_err(float mu, float c0) {
+  return __fadd_ru(__fmul_ru(mu, 0x1p-23f), c0);
+}
+
 template <bool kGlobal>
-__global__ void __launch_bounds__(kSeamThreads)
+__global__ void __launch_bounds__(kSeamThreads, 3)
 das_seam_kernel(const SeamTask* __restrict__ tasks, int ntasks, const double* __restrict__ qfir2,
                 int* __restrict__ bp_out, unsigned char* __restrict__ gscr, size_t gstride) {
   const int ti = blockIdx.x;
@@ -235,17 +413,34 @@ das_seam_kernel(const SeamTask* __restrict__ tasks, int ntasks, const double* __
   int8_t* dif = (int8_t*)base;                        // next - prev in {-1, 0, 1} (x2 later)
   int* dmap = (int*)(base + ((L + 15) & ~15));        // prefix sums, then the density map
   int* win = kGlobal ? dmap + ((L + 1 + 3) & ~3) : dmap;   // density map (global form)
+  unsigned char* scr = (unsigned char*)(kGlobal ? win + L : dmap + (L + 1));
+  const int W = (L + 31) >> 5;
+  unsigned* zb = (unsigned*)scr;                      // bit p: prev[p] == next[p]
+  unsigned* fb = zb + W;                              // bit p: density >= floor
+  int* runs = (int*)(fb + W);                         // run starts (then the pop scratch)
+  float* pop_blk = (float*)(fb + W);
+  int* pop_list = (int*)(pop_blk + (kMaxQ + 1) * kPopBlocks);
   __shared__ int red[32];
-  __shared__ int s_peak, s_pp, s_nq, s_best;
+  __shared__ int s_peak, s_pp, s_nq, s_best, s_nruns, s_first8, s_first4, s_last1, s_nlist,
+      s_overflow;
   __shared__ int qpos[kMaxQ + 1], qden[kMaxQ + 1];
   __shared__ double qmax[kMaxQ + 1];
+  __shared__ unsigned s_lb[kMaxQ + 1];
   __shared__ double s_q2[255];
+  __shared__ float s_q2f[kPopTaps];
+  __shared__ float s_abs;
 
   for (int k = threadIdx.x; k < 255; k += blockDim.x) s_q2[k] = qfir2[k];
   // match flags: prev = T.prev[0..L), next = T.next[0..L)
   for (int i = threadIdx.x; i < L; i += blockDim.x) {
     const int a = T.prev[i], b = T.next[i];
     dif[i] = (int8_t)(b - a);          // bits 0/1: diff of the +-1 samples is 2 * (b - a)
+  }
+  if (threadIdx.x == 0) {
+    s_first8 = s_first4 = 0x7fffffff;
+    s_last1 = -1;
+    s_nlist = 0;
+    s_overflow = 0;
   }
   __syncthreads();
 
@@ -261,25 +456,7 @@ das_seam_kernel(const SeamTask* __restrict__ tasks, int ntasks, const double* __
     const int b0 = threadIdx.x * per, b1 = min(L, b0 + per);
     int loc = 0;
     for (int i = b0; i < b1; i++) loc += (dif[i] == 0);
-    // exclusive scan of loc over threads
-    int v = loc;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int n = __shfl_up_sync(0xffffffffu, v, o);
-      if (lane >= o) v += n;
-    }
-    if (lane == 31) red[w] = v;
-    __syncthreads();
-    if (w == 0) {
-      int x = lane < (int)(blockDim.x >> 5) ? red[lane] : 0;
-      for (int o = 1; o < 32; o <<= 1) {
-        const int n = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += n;
-      }
-      red[lane] = x;
-    }
-    __syncthreads();
-    int run = v - loc + (w > 0 ? red[w - 1] : 0);
+    int run = block_excl_sum(loc, red, nullptr);
     if (threadIdx.x == 0) dmap[0] = 0;
     for (int i = b0; i < b1; i++) {
       run += (dif[i] == 0);
@@ -335,40 +512,80 @@ das_seam_kernel(const SeamTask* __restrict__ tasks, int ntasks, const double* __
     }
     __syncthreads();
   }
+  const int floor_d = s_peak * 9 / 10;
+  const int pp = s_pp;
 
-  // candidate scan and the peak-run candidate (serial, as the reference)
+  // match and floor bitmasks, one word per warp step
+  {
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int w = threadIdx.x >> 5; w < W; w += nw) {
+      const int p = (w << 5) + lane;
+      const bool z = p < L && dif[p] == 0;
+      const bool f = p < L && dmap[p] >= floor_d;
+      const unsigned zm = __ballot_sync(0xffffffffu, z);
+      const unsigned fm = __ballot_sync(0xffffffffu, f);
+      if (lane == 0) {
+        zb[w] = zm;
+        fb[w] = fm;
+      }
+    }
+  }
+  __syncthreads();
+
+  // run starts in order, and the scan-order hits around the peak
+  {
+    const int per = (W + blockDim.x - 1) / blockDim.x;
+    const int w0 = min(W, (int)threadIdx.x * per), w1 = min(W, w0 + per);
+    int lzf = -1, lnz = -1;
+    for (int w = w0; w < w1; w++) {
+      const unsigned zf = zb[w] & fb[w], nz = ~zb[w];
+      if (zf) lzf = (w << 5) + 31 - __clz(zf);
+      if (nz) lnz = (w << 5) + 31 - __clz(nz);
+    }
+    const int czf = block_excl_max(lzf, red);
+    const int cnz = block_excl_max(lnz, red);
+    int cnt = 0;
+    seam_runs(zb, fb, W, L, w0, w1, czf, cnz, [&](int) { cnt++; });
+    int total;
+    int off = block_excl_sum(cnt, red, &total);
+    seam_runs(zb, fb, W, L, w0, w1, czf, cnz, [&](int p) { runs[off++] = p; });
+    if (threadIdx.x == 0) s_nruns = total;
+    for (int o = threadIdx.x; o < 2 * (half_w + 1); o += blockDim.x) {
+      const int r = o >> 1;
+      const int tp = (o & 1) ? pp + r : pp - r;
+      if (seam_zrun(zb, W, L, tp, 8)) atomicMin(&s_first8, o);
+      if (seam_zrun(zb, W, L, tp, 4)) atomicMin(&s_first4, o);
+      if (seam_zrun(zb, W, L, tp, 1)) atomicMax(&s_last1, o);
+    }
+  }
+  __syncthreads();
+
+  // candidates: spacing rule over the run starts, then the peak-run pick
   if (threadIdx.x == 0) {
-    const int peak = s_peak;
-    const int floor_d = peak * 9 / 10;
     const int min_spacing = half_w;
-    int nq = 0;
-    for (int p = 0; p < L - 3 && nq < kMaxQ;) {
-      if (dif[p] != 0 || dmap[p] < floor_d) { p++; continue; }
-      const int rs = p;
-      int rl = 0;
-      while (p < L && dif[p] == 0) { rl++; p++; }
-      if (rl < 4) continue;
-      if (nq > 0 && rs - qpos[nq - 1] < min_spacing) continue;
+    const int nr = s_nruns;
+    int nq = 0, i = 0;
+    while (i < nr && nq < kMaxQ) {
+      const int rs = runs[i];
+      if (nq > 0 && rs - qpos[nq - 1] < min_spacing) {
+        const int target = qpos[nq - 1] + min_spacing;
+        int lo = i + 1, hi = nr;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (runs[mid] < target) lo = mid + 1;
+          else hi = mid;
+        }
+        i = lo;
+        continue;
+      }
       qpos[nq] = rs;
       qden[nq] = dmap[rs];
       nq++;
+      i++;
     }
-    const int pp = s_pp;
-    int prp = pp, prl = 1;
-    for (int mr = 8; mr >= 1 && prl < 4; mr >>= 1) {
-      for (int r = 0; r <= half_w && prl < 4; r++) {
-        for (int t = 0; t < 2 && prl < 4; t++) {
-          const int tp = t == 0 ? pp - r : pp + r;
-          if (tp < 0 || tp + mr > L) continue;
-          int rl = 0;
-          for (int k = 0; k < mr; k++) {
-            if (dif[tp + k] == 0) rl++;
-            else break;
-          }
-          if (rl >= mr) { prp = tp; prl = mr; }
-        }
-      }
-    }
+    int prp = pp;
+    const int o = s_first8 != 0x7fffffff ? s_first8 : (s_first4 != 0x7fffffff ? s_first4 : s_last1);
+    if (o >= 0) prp = (o & 1) ? pp + (o >> 1) : pp - (o >> 1);
     int dup = 0;
     for (int ci = 0; ci < nq; ci++)
       if (abs(qpos[ci] - prp) < min_spacing) { dup = 1; break; }
@@ -378,21 +595,74 @@ das_seam_kernel(const SeamTask* __restrict__ tasks, int ntasks, const double* __
       nq++;
     }
     if (nq == 0) { qpos[0] = 0; qden[0] = 0; nq = 1; }
-    for (int ci = 0; ci < nq; ci++) qmax[ci] = 0.0;
+    for (int ci = 0; ci < nq; ci++) {
+      qmax[ci] = 0.0;
+      s_lb[ci] = 0u;
+    }
     s_nq = nq;
   }
   __syncthreads();
   const int nq = s_nq;
 
   // pop metric: |255-tap FIR of the stitched-minus-unstitched difference| over
-  // j in [-512, 512); terms with idx < sp (before the stitch) or with equal
-  // bits are zero and are skipped (adding +-0 leaves the magnitude unchanged)
+  // j in [-127, 512) (offsets below -127 see no term: value 0); terms with
+  // idx < sp (before the stitch) or with equal bits are zero and are skipped
+  // (adding +-0 leaves the magnitude unchanged)
   if (nq > 1) {
-    // offsets j < -127 see no term at all (k >= 127 - j > 254): value 0
-    const int jlo = -127, jhi = 512, nj = jhi - jlo;
-    for (int it = threadIdx.x; it < nq * nj; it += blockDim.x) {
-      const int ci = it / nj;
-      const int j = jlo + it % nj;
+    __half* ef = reinterpret_cast<__half*>(dmap);   // the density map is no longer read
+    for (int i = threadIdx.x; i < L; i += blockDim.x) ef[i] = __int2half_rn((int)dif[i]);
+    for (int k = threadIdx.x; k < kPopTaps; k += blockDim.x)
+      s_q2f[k] = k < 255 ? __double2float_rn(s_q2[k]) : 0.0f;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      float a = 0.0f;
+      for (int k = threadIdx.x; k < kPopTaps; k += 32) a += fabsf(s_q2f[k]);
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+      if (threadIdx.x == 0) s_abs = a;
+    }
+    __syncthreads();
+    // u * sum|q2| (the taps' rounding to FP32, with margin) + 2^-40, rounded up
+    const float c0 = __fmaf_ru(s_abs, 0x1.04p-24f, 0x1p-40f);
+    const int items = nq * kPopBlocks;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+      const int ci = it / kPopBlocks;
+      const int j0 = kPopJlo + (it - ci * kPopBlocks) * kPopR;
+      float v[kPopR], mu[kPopR];
+      seam_screen(ef, s_q2f, L, qpos[ci], j0, v, mu);
+      float hi = 0.0f, lo = 0.0f;
+#pragma unroll
+      for (int r = 0; r < kPopR; r++) {
+        if (j0 + r >= kPopJhi) continue;
+        const float e = seam_err(mu[r], c0);
+        hi = fmaxf(hi, __fadd_ru(fabsf(v[r]), e));
+        lo = fmaxf(lo, __fsub_rd(fabsf(v[r]), e));
+      }
+      pop_blk[it] = hi;
+      atomicMax(&s_lb[ci], __float_as_uint(lo));   // lo >= 0: bit order is value order
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+      const int ci = it / kPopBlocks;
+      const float lb = __uint_as_float(s_lb[ci]);
+      if (pop_blk[it] < lb) continue;
+      const int j0 = kPopJlo + (it - ci * kPopBlocks) * kPopR;
+      float v[kPopR], mu[kPopR];
+      seam_screen(ef, s_q2f, L, qpos[ci], j0, v, mu);
+#pragma unroll
+      for (int r = 0; r < kPopR; r++) {
+        if (j0 + r >= kPopJhi || __fadd_ru(fabsf(v[r]), seam_err(mu[r], c0)) < lb) continue;
+        const int slot = atomicAdd(&s_nlist, 1);
+        if (slot < kPopList) pop_list[slot] = ci * kPopJ + (j0 + r - kPopJlo);
+        else s_overflow = 1;
+      }
+    }
+    __syncthreads();
+    const bool all = s_overflow != 0;
+    const int n = all ? nq * kPopJ : s_nlist;
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+      const int item = all ? e : pop_list[e];
+      const int ci = item / kPopJ;
+      const int j = kPopJlo + (item - ci * kPopJ);
       const int sp = qpos[ci];
       double val = 0.0;
       int k0 = 127 - j;
@@ -489,19 +759,24 @@ int launch_das_rms(const double* x, const long long* d_centers, int n, double* d
 }
 
 size_t das_seam_smem(int max_ovl) {
-  return ((size_t)(max_ovl + 15) & ~(size_t)15) + sizeof(int) * (size_t)(max_ovl + 1) + 64;
+  return ((size_t)(max_ovl + 15) & ~(size_t)15) + sizeof(int) * (size_t)(max_ovl + 1) +
+         seam_scratch_bytes(max_ovl) + 64;
 }
 
 size_t das_seam_global_bytes(int max_ovl) {
   if (max_ovl <= kMaxSeamOverlap) return 0;
   const size_t L = (size_t)max_ovl;
-  return (((L + 15) & ~(size_t)15) + sizeof(int) * (((L + 1 + 3) & ~(size_t)3) + L) + 255) &
-         ~(size_t)255;
+  return (((L + 15) & ~(size_t)15) + sizeof(int) * (((L + 1 + 3) & ~(size_t)3) + L) +
+          seam_scratch_bytes(max_ovl) + 255) & ~(size_t)255;
 }
 
 int das_seam_prepare(int max_ovl) {
   if (max_ovl > kMaxSeamOverlap) return 0;
   const size_t smem = das_seam_smem(max_ovl);
+  // the largest carveout: three CTAs per SM hold ~70 KB each at overlap 8,192
+  if (cudaFuncSetAttribute(das_seam_kernel<false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           100) != cudaSuccess)
+    return -1;
   if (smem <= 48 * 1024) return 0;
   return cudaFuncSetAttribute(das_seam_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)smem) == cudaSuccess ? 0 : -1;
@@ -620,6 +895,10 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
     else return c->fail(DSDGPU_ERR_STATE, "persistent contexts: call dsdgpu_sdm_setup with num_contexts >= channels");
   }
   if (count > 0 && (!d_fir || !d_out)) return c->fail(DSDGPU_ERR_ARG, "null buffer");
+  if (count == 0) {   // an empty chunk: no decisions, the contexts unchanged
+    if (out_count) *out_count = 0;
+    return DSDGPU_OK;
+  }
   cudaSetDevice(c->device);
   const int lat = c->sdm.lat;
   const size_t overlap = 64 * (size_t)lat;

@@ -71,27 +71,38 @@ int das_reposition_apply(std::vector<long long>& start, std::vector<long long>& 
   long long max_shift = (long long)(base * 2 / 5);
   if (max_shift > 200000) max_shift = 200000;
   const long long step = win / 2;
+  // Candidate windows of every quiet boundary, evaluated in one call.  A
+  // boundary's candidates depend only on its own nominal start (each boundary
+  // appears once in `which`, and only its own turn moves it), so they can all
+  // be taken before the first move; the neighbour constraints, which do see
+  // earlier moves, are applied in the scan below.  The RMS values are pure, so
+  // evaluating offsets past the reference's early exit changes nothing.
+  std::vector<long long> cand;
+  std::vector<size_t> first(which.size() + 1, 0);
   for (size_t wi = 0; wi < which.size(); wi++) {
+    first[wi] = cand.size();
     if (cur[wi] > 0.005) continue;
-    const int s = which[wi];
-    // RMS at every offset this boundary could try; the constraints below
-    // depend on the neighbours' (possibly moved) starts, the RMS does not
-    std::vector<long long> cand;
-    const long long b = start[s];
+    const long long b = start[which[wi]];
     for (long long off = step; off <= max_shift; off += step)
       for (int dir = -1; dir <= 1; dir += 2) {
         const long long cc = dir < 0 ? (b > off ? b - off : 0) : b + off;
         if (cc < win / 2 || cc + win / 2 >= (long long)count) continue;
         cand.push_back(cc);
       }
-    std::vector<double> rms(cand.size());
-    if (!cand.empty()) {
-      const int rc = rms_eval(cand, rms);
-      if (rc) return rc;
-    }
+  }
+  first[which.size()] = cand.size();
+  std::vector<double> rms(cand.size());
+  if (!cand.empty()) {
+    const int rc = rms_eval(cand, rms);
+    if (rc) return rc;
+  }
+  for (size_t wi = 0; wi < which.size(); wi++) {
+    if (cur[wi] > 0.005) continue;
+    const int s = which[wi];
+    const long long b = start[s];
     long long best_pos = b;
     double best_rms = cur[wi];
-    size_t ci = 0;
+    size_t ci = first[wi];
     for (long long off = step; off <= max_shift; off += step) {
       for (int dir = -1; dir <= 1; dir += 2) {
         const long long cc = dir < 0 ? (b > off ? b - off : 0) : b + off;

@@ -37,8 +37,8 @@ void das_reposition_centers(const std::vector<long long>& start, size_t count,
 // Reposition of quiet boundaries (src/dsp_plugin.c:1959-2024): a boundary
 // whose window RMS `cur[i]` is <= 0.005 moves to the loudest offset found by
 // the reference's outward scan (steps of win/2 up to min(40 %, 200,000)),
-// subject to keeping 2 * overlap from its neighbours.  `rms` evaluates the
-// candidate windows of one boundary.  Returns 0 or the callback's error.
+// subject to keeping 2 * overlap from its neighbours.  `rms` is called once,
+// with the candidate windows of every quiet boundary.  Returns 0 or the callback's error.
 int das_reposition_apply(std::vector<long long>& start, std::vector<long long>& size, size_t count,
                          size_t overlap, const std::vector<int>& which,
                          const std::vector<double>& cur, const RmsEval& rms);

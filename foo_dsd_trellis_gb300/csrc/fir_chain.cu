@@ -25,14 +25,18 @@
 // products are below FP32 resolution of any output.
 #include "api_context.h"
 #include "fir_internal.h"
+#include "fp_convert.h"
 
 #include <cmath>
 #include <cstring>
 
 namespace dsdgpu {
 
-// floor division for possibly negative numerators
+// floor division for possibly negative numerators.  Stage ratios are powers
+// of two (2 or 4): an arithmetic shift, since a 64-bit integer division runs
+// through the FP64 pipe's reciprocal on this part.
 __device__ __forceinline__ long long fdiv(long long a, int b) {
+  if (b > 0 && (b & (b - 1)) == 0) return a >> (__ffs(b) - 1);
   return a >= 0 ? a / b : -((-a + b - 1) / b);
 }
 
@@ -112,21 +116,7 @@ __device__ __forceinline__ void generic_stage(const FirChainConst& F, int k, con
 // The engine's epilogue of one output (src/engine.c:646-651, 704-717): gain
 // ramp and the soft clip's threshold test in FP32 (within the chain's 1e-6
 // contract), the tanh knee in FP64 on the rare samples above the threshold,
-// one widening per output.
-// float -> double without the FP64 pipe: a normal binary32 value is the
-// binary64 value with the exponent rebiased (127 -> 1023) and the significand
-// shifted up by 29 bits, exactly; zeros, subnormals, infinities and NaNs take
-// the hardware conversion.
-__device__ __forceinline__ double widen_exact(float f) {
-  const unsigned u = __float_as_uint(f);
-  const unsigned e = (u >> 23) & 0xffu;
-  if (e == 0u || e == 0xffu) return (double)f;
-  const unsigned long long bits = ((unsigned long long)(u >> 31) << 63) |
-                                  ((unsigned long long)(e + 896u) << 52) |
-                                  ((unsigned long long)(u & 0x7fffffu) << 29);
-  return __longlong_as_double((long long)bits);
-}
-
+// one widening per output (widen_exact, on the integer pipe).
 __device__ __forceinline__ double fir_epilogue(float v, long long m, float gs, float gstep,
                                                int apply_gain, int soft_clip) {
   const float y = apply_gain ? v * fmaf(gstep, (float)m, gs) : v;

@@ -126,6 +126,11 @@ int dsdgpu_pipeline_process(dsdgpu_context_t* c, const float* d_pcm, size_t pcm_
   if (!c) return DSDGPU_ERR_ARG;
   if (!c->pipe_ready) return c->fail(DSDGPU_ERR_STATE, "pipeline not set up");
   if (frames > 0 && (!d_pcm || !d_out)) return c->fail(DSDGPU_ERR_ARG, "null buffer");
+  if (frames == 0) {   // an empty block: no output, no state change
+    if (out_samples) *out_samples = 0;
+    if (out_bytes) *out_bytes = 0;
+    return DSDGPU_OK;
+  }
   cudaSetDevice(c->device);
   const int nch = c->pipe_nch;
   if (c->pipe_pcm_out) {
@@ -273,6 +278,11 @@ int dsdgpu_pipeline_process_host(dsdgpu_context_t* c, const float* h_pcm, size_t
   if (!c) return DSDGPU_ERR_ARG;
   if (!c->pipe_ready) return c->fail(DSDGPU_ERR_STATE, "pipeline not set up");
   if (frames > 0 && (!h_pcm || !h_out)) return c->fail(DSDGPU_ERR_ARG, "null buffer");
+  if (frames == 0) {
+    if (out_samples) *out_samples = 0;
+    if (out_bytes) *out_bytes = 0;
+    return DSDGPU_OK;
+  }
   cudaSetDevice(c->device);
   const int nch = c->pipe_nch;
   size_t n_fir = frames * (c->pipe_same_rate || c->pipe_pcm_out ? (size_t)16 : (size_t)c->fir.ratio);

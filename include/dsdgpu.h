@@ -11,7 +11,10 @@
  *     it is not thread-safe: drive one context from one thread;
  *   - setup calls are separate from per-block calls;
  *   - buffers named d_* are device pointers owned by the caller; buffers named
- *     h_* are host pointers (pinned or pageable).
+ *     h_* are host pointers (pinned or pageable);
+ *   - a per-block call with zero samples or frames returns DSDGPU_OK with no
+ *     output, changes no stream state, and accepts null buffers;
+ *   - dsdgpu_destroy(NULL) does nothing.
  * Decisions are exchanged as one byte per DSD sample (1 = +1.0, 0 = -1.0)
  * unless a function says otherwise.
  */
@@ -355,6 +358,14 @@ int dsdgpu_sdm_process_noalloc(const dsdgpu_sdm_params_t *p, int nch, int keep_s
 /* Measured FP64 add/multiply issue rate of the device in Gop/s (separate
  * DADD and DMUL, the operations the trellis SDM is made of). */
 int dsdgpu_probe_fp64(dsdgpu_context_t *ctx, double *gops);
+
+/* Self-check of the library's float -> double widening on the integer pipe
+ * (the FIR chain's output conversion) against the hardware conversion, on the
+ * binary32 patterns seed + i * 0x9E3779B1 (mod 2^32) for i < n: n = 2^32
+ * checks every pattern.  *mismatches counts differing results (0 expected).
+ * No counterpart in the reference. */
+int dsdgpu_selftest_convert(dsdgpu_context_t *ctx, uint64_t n, uint64_t seed,
+                            uint64_t *mismatches);
 
 /* Best candidate's integrator state (sdm_state_distance's input,
  * src/trellis.c:1094-1109) and the counters conv_fail, cands_collapse,

@@ -71,6 +71,24 @@ def test_das_quiet_boundary_reposition(oracle):
     assert np.array_equal(got, want)
 
 
+def test_das_several_quiet_boundaries(oracle):
+    """Four neighbouring boundaries inside one near-silent stretch: all their
+    candidate windows are evaluated in one RMS launch, and each move sees the
+    neighbour constraints of the moves made before it, as in the reference's
+    boundary-by-boundary scan."""
+    f = _ntf("clans-5", 2822400)
+    n = 160000
+    x = multitone(n, 13) * 2.0
+    x[35000:105000] = uniform_noise(70000, 6, 1e-4)   # boundaries at 40k, 60k, 80k, 100k
+    want, ws, got, gs = _run(oracle, f, 16, 4, 16, x[None, :], nsegs=8, seed_mode=1)
+    _, _, starts = oracle.das_run(f.order, np.array(f.a), np.array(f.g), 16, 4, 16, 0.0,
+                                  x[None, :], nsegs=8, seed_mode=1)
+    nominal = [s * (n // 8) for s in range(8)]
+    assert sum(a != b for a, b in zip(starts, nominal)) >= 3
+    assert list(gs) == list(ws)
+    assert np.array_equal(got, want)
+
+
 def test_das_single_segment_is_plain_sdm(oracle):
     f = _ntf("clans-6", 5644800)
     x = multitone(30000, 21)[None, :]

@@ -84,3 +84,18 @@ def test_fir_multichannel(oracle):
         want = oracle.engine_fir(44100, 2822400, xs[c], boxcar_taps=8, soft_clip=True)
         err = np.abs(got[c] - want).max() / np.abs(want).max()
         assert err <= TOL
+
+
+def test_integer_pipe_widening_equals_hardware():
+    """The chain's epilogue widens every FP32 output to FP64 on the integer
+    pipe: every one of the 2^32 binary32 patterns gives the hardware
+    conversion's bits (NaNs as NaN)."""
+    import ctypes as C
+    from foo_dsd_trellis_gb300 import _lib
+    L = _lib.load()
+    h = C.c_void_p()
+    assert L.dsdgpu_create(0, C.byref(h)) == _lib.OK
+    bad = C.c_uint64(123)
+    _lib.check(h, L.dsdgpu_selftest_convert(h, 1 << 32, 0, C.byref(bad)))
+    assert bad.value == 0
+    L.dsdgpu_destroy(h)
