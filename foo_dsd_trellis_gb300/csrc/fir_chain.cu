@@ -113,13 +113,21 @@ __device__ __forceinline__ void generic_stage(const FirChainConst& F, int k, con
   }
 }
 
+// 0 <= p < 2^23 as a float, exactly, without a conversion instruction: the
+// integer placed in the significand of 2^23, minus 2^23.
+__device__ __forceinline__ float small_to_float(int p) {
+  return __fsub_rn(__int_as_float(0x4B000000 | p), 8388608.0f);
+}
+
 // The engine's epilogue of one output (src/engine.c:646-651, 704-717): gain
 // ramp and the soft clip's threshold test in FP32 (within the chain's 1e-6
 // contract), the tanh knee in FP64 on the rare samples above the threshold,
-// one widening per output (widen_exact, on the integer pipe).
-__device__ __forceinline__ double fir_epilogue(float v, long long m, float gs, float gstep,
+// one widening per output (widen_exact, integer operations).  The ramp is
+// gb + step * p, with gb = g_start + step * (tile start) formed once per
+// thread and p the output's offset in the tile: no per-output conversion.
+__device__ __forceinline__ double fir_epilogue(float v, int p, float gb, float gstep,
                                                int apply_gain, int soft_clip) {
-  const float y = apply_gain ? v * fmaf(gstep, (float)m, gs) : v;
+  const float y = apply_gain ? v * fmaf(gstep, small_to_float(p), gb) : v;
   if (soft_clip && fabsf(y) > 0.95f) return soft_clip_095((double)y);
   return widen_exact(y);
 }
@@ -197,22 +205,22 @@ fir_chain_kernel(const __grid_constant__ FirChainConst F, const float* __restric
   // the final tile to HBM: consecutive threads write consecutive outputs,
   // two per 16-byte store where the row allows it
   const float* fin = buf[F.S];
-  const long long n = o_hi - o_lo;
+  const int n = (int)(o_hi - o_lo);   // <= tile < 2^23
   double* dst = out + (size_t)ch * out_stride + o_lo;
+  const float gb = fmaf(g_step, (float)o_lo, g_start);
   if (vec2) {
-    for (long long p = 2 * (long long)threadIdx.x; p < n; p += 2 * (long long)blockDim.x) {
-      const double y0 = fir_epilogue(fin[p], o_lo + p, g_start, g_step, apply_gain, soft_clip);
+    for (int p = 2 * (int)threadIdx.x; p < n; p += 2 * (int)blockDim.x) {
+      const double y0 = fir_epilogue(fin[p], p, gb, g_step, apply_gain, soft_clip);
       if (p + 1 < n) {
-        const double y1 =
-            fir_epilogue(fin[p + 1], o_lo + p + 1, g_start, g_step, apply_gain, soft_clip);
+        const double y1 = fir_epilogue(fin[p + 1], p + 1, gb, g_step, apply_gain, soft_clip);
         *reinterpret_cast<double2*>(dst + p) = make_double2(y0, y1);
       } else {
         dst[p] = y0;
       }
     }
   } else {
-    for (long long p = threadIdx.x; p < n; p += blockDim.x)
-      dst[p] = fir_epilogue(fin[p], o_lo + p, g_start, g_step, apply_gain, soft_clip);
+    for (int p = threadIdx.x; p < n; p += blockDim.x)
+      dst[p] = fir_epilogue(fin[p], p, gb, g_step, apply_gain, soft_clip);
   }
 }
 

@@ -159,9 +159,9 @@ struct PcWalk {
   unsigned hist;   // last 8 output bits
   unsigned code;   // decision code of this step's cell
 
-  // one sample with prev_y = +-1; `row` = codes of the next step's phase;
-  // x is the input already narrowed to FP32
-  __device__ __forceinline__ unsigned step(const uint8_t* row, float x) {
+  // one sample with prev_y = +-1; `row` = codes of the next step's phase
+  __device__ __forceinline__ unsigned step(const uint8_t* row, double xd) {
+    const float x = __double2float_rn(xd);
     const unsigned pair = row[hist];
     float d[10];
     const float t0 = __fadd_rn(__fsub_rn(s[0], __fmul_rn(C.g[0], s[1])), x);
@@ -244,36 +244,27 @@ __device__ void pc_run(const PcCoef& Cg, const uint8_t* codes, PcState& st,
 #pragma unroll
   for (int r = 0; r < kPcPhases; r++) rows[r] = codes + ((ph0 + r + 1) & 7) * kPcHist;
   const bool vec_out = ((uintptr_t)out & 15u) == 0;
-  // Inputs run two chunks ahead: chunk c + 2 is loaded while chunk c is
-  // walked, and chunk c + 1 (loaded a chunk earlier) is narrowed to FP32 one
-  // sample per step, so neither the load latency nor the conversion (an
-  // FP64-class instruction on this part) sits on the walk's chain.
-  auto load = [&](double (&d)[kPcAhead], long long at) {
-    if (at + kPcAhead <= count) {
+  double xa[kPcAhead];
 #pragma unroll
-      for (int j = 0; j < kPcAhead; j++) d[j] = x[at + j];
+  for (int j = 0; j < kPcAhead; j++) xa[j] = j < count ? x[j] : 0.0;
+  long long base = 0;
+  // whole chunks: straight-line code over kPcAhead samples, the next chunk's
+  // inputs in flight meanwhile (converted when used)
+  for (; base + kPcAhead <= count; base += kPcAhead) {
+    double xb[kPcAhead];
+    if (base + 2 * kPcAhead <= count) {
+#pragma unroll
+      for (int j = 0; j < kPcAhead; j++) xb[j] = x[base + kPcAhead + j];
     } else {
 #pragma unroll
-      for (int j = 0; j < kPcAhead; j++) d[j] = at + j < count ? x[at + j] : 0.0;
+      for (int j = 0; j < kPcAhead; j++) {
+        const long long i = base + kPcAhead + j;
+        xb[j] = i < count ? x[i] : 0.0;
+      }
     }
-  };
-  float xf[kPcAhead];
-  double xd[kPcAhead];
-  load(xd, 0);
-#pragma unroll
-  for (int j = 0; j < kPcAhead; j++) xf[j] = __double2float_rn(xd[j]);
-  load(xd, kPcAhead);
-  long long base = 0;
-  for (; base + kPcAhead <= count; base += kPcAhead) {
-    double xn[kPcAhead];
-    load(xn, base + 2 * kPcAhead);
-    float xfn[kPcAhead];
     unsigned w[kPcAhead / 4] = {0u, 0u, 0u, 0u};
 #pragma unroll
-    for (int j = 0; j < kPcAhead; j++) {
-      xfn[j] = __double2float_rn(xd[j]);
-      w[j >> 2] |= W.step(rows[j & 7], xf[j]) << (8 * (j & 3));
-    }
+    for (int j = 0; j < kPcAhead; j++) w[j >> 2] |= W.step(rows[j & 7], xa[j]) << (8 * (j & 3));
     if (vec_out) {
       *reinterpret_cast<uint4*>(out + base) = make_uint4(w[0], w[1], w[2], w[3]);
     } else {
@@ -281,16 +272,13 @@ __device__ void pc_run(const PcCoef& Cg, const uint8_t* codes, PcState& st,
       for (int j = 0; j < kPcAhead; j++) out[base + j] = (uint8_t)((w[j >> 2] >> (8 * (j & 3))) & 1u);
     }
 #pragma unroll
-    for (int j = 0; j < kPcAhead; j++) {
-      xf[j] = xfn[j];
-      xd[j] = xn[j];
-    }
+    for (int j = 0; j < kPcAhead; j++) xa[j] = xb[j];
   }
   // the ragged tail
   const int m = (int)(count - base);
 #pragma unroll
   for (int j = 0; j < kPcAhead; j++)
-    if (j < m) out[base + j] = (uint8_t)W.step(rows[j & 7], xf[j]);
+    if (j < m) out[base + j] = (uint8_t)W.step(rows[j & 7], xa[j]);
 #pragma unroll
   for (int k = 0; k < 10; k++) st.s[k] = W.s[k];
   if (any) st.prev_y = W.pbit ? 1.0f : -1.0f;
