@@ -29,6 +29,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 namespace dsdgpu {
 
@@ -84,6 +85,68 @@ __device__ __forceinline__ void halfband_stage(const FirChainConst& F, const flo
       const int m = 2 * (ib + q) + moff;
       if ((unsigned)m < (unsigned)n_out) out[m] = a0 + a1;
       if ((unsigned)(m + 1) < (unsigned)n_out) out[m + 1] = F.hb_center * w[q + kHbTaps - 16];
+    }
+  }
+}
+
+// A merged stage (factor U = 8 or 16, kPolyTaps taps per branch; always stage
+// 0, its branch r at taps[r * kPolyTaps]): out[U*i + r] = sum_j hm[U*j + r]
+// x[i - j].  A work item is (branch group g, input index i): the inputs
+// x[i - j], streamed through registers kPolyChunk at a time, feed the
+// group's kPolyGroup branches.  Items run i fastest, so a warp's lanes share
+// the group, whose taps are compile-time constant operands (one instance per
+// group), and read consecutive inputs.
+constexpr int kPolyChunk = 12;
+static_assert(kPolyTaps % kPolyChunk == 0 && kPolyChunk % 2 == 0, "chunked taps");
+
+template <int G>
+__device__ __forceinline__ void poly_item(const FirChainConst& F, const float* in, int base,
+                                          float (&a)[kPolyGroup]) {
+  float a0[kPolyGroup], a1[kPolyGroup];
+#pragma unroll
+  for (int rr = 0; rr < kPolyGroup; rr++) a0[rr] = a1[rr] = 0.0f;
+#pragma unroll
+  for (int c = 0; c < kPolyTaps; c += kPolyChunk) {
+    float w[kPolyChunk];
+#pragma unroll
+    for (int jj = 0; jj < kPolyChunk; jj++) w[jj] = in[base - c - jj];
+#pragma unroll
+    for (int rr = 0; rr < kPolyGroup; rr++) {
+      constexpr int kRow = G * kPolyGroup * kPolyTaps;
+#pragma unroll
+      for (int jj = 0; jj < kPolyChunk; jj += 2) {
+        a0[rr] = fmaf(F.taps[kRow + rr * kPolyTaps + c + jj], w[jj], a0[rr]);
+        a1[rr] = fmaf(F.taps[kRow + rr * kPolyTaps + c + jj + 1], w[jj + 1], a1[rr]);
+      }
+    }
+  }
+#pragma unroll
+  for (int rr = 0; rr < kPolyGroup; rr++) a[rr] = a0[rr] + a1[rr];
+}
+
+__device__ __forceinline__ void poly_stage(const FirChainConst& F, int k, const float* in,
+                                           long long ilo, float* out, long long mlo,
+                                           long long mhi) {
+  const int U = F.U[k];
+  const long long i0 = fdiv(mlo, U), i1 = fdiv(mhi - 1, U) + 1;
+  const int ni = (int)(i1 - i0);
+  const int groups = U / kPolyGroup;
+  for (int it = threadIdx.x; it < groups * ni; it += blockDim.x) {
+    const int g = it / ni;
+    const int il = it - g * ni;
+    const int base = (int)(i0 + il - ilo);   // >= kPolyTaps - 1: the stage's halo
+    float a[kPolyGroup];
+    switch (g) {
+      case 0: poly_item<0>(F, in, base, a); break;
+      case 1: poly_item<1>(F, in, base, a); break;
+      case 2: poly_item<2>(F, in, base, a); break;
+      default: poly_item<3>(F, in, base, a); break;
+    }
+    const long long mb = (long long)U * (i0 + il) + g * kPolyGroup;
+#pragma unroll
+    for (int rr = 0; rr < kPolyGroup; rr++) {
+      const long long m = mb + rr;
+      if (m >= mlo && m < mhi) out[m - mlo] = a[rr];
     }
   }
 }
@@ -195,7 +258,9 @@ fir_chain_kernel(const __grid_constant__ FirChainConst F, const float* __restric
   __syncthreads();
 
   for (int k = 0; k < F.S; k++) {
-    if (F.hb_stage[k])
+    if (F.poly_stage[k])
+      poly_stage(F, k, buf[k], lo[k], buf[k + 1], lo[k + 1], hi[k + 1]);
+    else if (F.hb_stage[k])
       halfband_stage(F, buf[k], lo[k], hi[k], buf[k + 1], lo[k + 1], hi[k + 1]);
     else
       generic_stage(F, k, buf[k], lo[k], buf[k + 1], lo[k + 1], hi[k + 1]);
@@ -290,18 +355,72 @@ int plan_chain(unsigned fs_in, unsigned fs_out, int* U, int* L) {
   return S;
 }
 
+// The leading stages a chain merges into one polyphase stage: all but the
+// last three, at most four (U <= 16), at least three (a shorter run leaves
+// too much zero padding), and only 63-tap half-band 2x stages.  Their
+// cascade is one LTI filter: stage k maps y_k = h'_k * (up2 y_{k-1}), so the
+// first M stages are hm * (up 2^M x) with hm = h'_{M-1} * up2(h'_{M-2} *
+// up2(... h'_0)), of length 1 + 62 (2^M - 1).  Its FP32 form differs from the
+// stage-by-stage FP32 cascade only in rounding (both within the chain's 1e-6
+// of the FP64 restatement), and its branches keep every thread busy where
+// the early stages, 1/16 to 1/2 of a tile's width, left most of them idle.
+int merged_stages(int S, const int* U, const int* L) {
+  int M = S - 3;
+  if (M > 4) M = 4;
+  if (M < 3) return 0;
+  for (int k = 0; k < M; k++)
+    if (U[k] != 2 || L[k] != 63) return 0;
+  return M;
+}
+
 int build_chain_const(unsigned fs_in, unsigned fs_out, int boxcar, FirChainConst* F) {
   memset(F, 0, sizeof *F);
   int U[kMaxStages], L[kMaxStages];
-  const int S = plan_chain(fs_in, fs_out, U, L);
-  if (S < 0) return -1;
-  F->S = S;
+  const int S0 = plan_chain(fs_in, fs_out, U, L);
+  if (S0 < 0) return -1;
+  const int M = merged_stages(S0, U, L);
+  F->S = M ? S0 - M + 1 : S0;
   F->ratio = (int)(fs_out / fs_in);
   F->boxcar = boxcar;
   F->inv_boxcar = boxcar > 0 ? (float)(1.0 / boxcar) : 1.0f;
   int toff = 0;
   int rows = 1;
-  for (int k = 0; k < S; k++) {
+  if (M) {
+    std::vector<double> g(63), t;
+    design_taps(63, false, g.data());
+    for (double& v : g) v *= 2.0;                   // h'_0
+    for (int k = 1; k < M; k++) {
+      double h[63];
+      design_taps(63, false, h);
+      const size_t n = 2 * (g.size() - 1) + 1;     // up2(g)
+      t.assign(n + 62, 0.0);
+      for (size_t a = 0; a < g.size(); a++)
+        for (int b = 0; b < 63; b++) t[2 * a + (size_t)b] += g[a] * (2.0 * h[b]);
+      g.swap(t);
+    }
+    const int Um = 1 << M;
+    if ((int)g.size() > Um * kPolyTaps || toff + Um * kPolyTaps > kMaxChainTaps) return -1;
+    F->U[0] = Um;
+    F->L[0] = Um * kPolyTaps;
+    F->poly_stage[0] = 1;
+    for (int r = 0; r < Um; r++) {
+      F->phase_off[0][r] = toff + r * kPolyTaps;
+      F->nphase[0][r] = kPolyTaps;
+      for (int j = 0; j < kPolyTaps; j++) {
+        const size_t tap = (size_t)Um * j + r;
+        F->taps[toff + r * kPolyTaps + j] = tap < g.size() ? (float)g[tap] : 0.0f;
+        F->lag[toff + r * kPolyTaps + j] = j;
+      }
+    }
+    toff += Um * kPolyTaps;
+    rows = Um;
+    for (int k = M; k < S0; k++) {
+      U[k - M + 1] = U[k];
+      L[k - M + 1] = L[k];
+    }
+  }
+  const int S = F->S;
+  for (int k = M ? 1 : 0; k < S; k++) {
     F->U[k] = U[k];
     F->L[k] = L[k];
     double h[255];

@@ -6,7 +6,10 @@
 namespace dsdgpu {
 
 constexpr int kMaxStages = 9;         // FIR_MAX_STAGES (reference include/fir.h:14)
-constexpr int kMaxChainTaps = 1024;   // non-zero polyphase taps over all stages
+constexpr int kMaxChainTaps = 2048;   // polyphase taps over all stages
+constexpr int kMaxPhases = 16;        // polyphase branches of one stage (a merged stage: 8 or 16)
+constexpr int kPolyTaps = 60;         // taps per branch of a merged stage (zero-padded)
+constexpr int kPolyGroup = 4;         // branches per work item of a merged stage
 constexpr int kHistory = 256;         // PCM samples kept between blocks per channel
 constexpr int kFirThreads = 256;
 constexpr int kFirMaxSmem = 200 * 1024;   // dynamic shared memory cap of one FIR tile
@@ -30,12 +33,16 @@ struct FirChainConst {
   int boxcar;                          // boxcar taps, 0 = off
   float inv_boxcar;
   int tile;                            // final output samples per CTA
-  int U[kMaxStages];                   // stage factors (2 or 4)
-  int L[kMaxStages];                   // stage tap counts (63 or 127)
-  int nphase[kMaxStages][4];           // non-zero taps per polyphase branch
-  int phase_off[kMaxStages][4];        // offset into taps[] / lag[]
+  int U[kMaxStages];                   // stage factors (2 or 4; 8 or 16 for a merged stage)
+  int L[kMaxStages];                   // stage tap counts (63 or 127; U * kPolyTaps merged)
+  int nphase[kMaxStages][kMaxPhases];  // non-zero taps per polyphase branch
+  int phase_off[kMaxStages][kMaxPhases];   // offset into taps[] / lag[]
   float taps[kMaxChainTaps];           // h'[U*j + r] = U * h[U*j + r]
   int lag[kMaxChainTaps];              // j
+  // a merged stage: the leading 63-tap half-band stages of a long chain as
+  // one polyphase stage of factor U = 2^M, branch r holding the kPolyTaps
+  // taps hm[U*j + r] (lag j, zero-padded) of the stages' combined response
+  int poly_stage[kMaxStages];
   // the 63-tap half-band 2x stage (every stage but a 127-tap first stage and
   // the 4x quarter-band one): its 32 even-phase taps and the centre tap, at
   // fixed offsets so that the unrolled kernel reads them as constant operands

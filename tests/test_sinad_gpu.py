@@ -11,6 +11,9 @@ standard deviation s differ by more than 3 * sqrt(2) * s with probability
 below 0.3 %.
 
   DSD64 one segment, 997 Hz sine, 8 channels x 2 s     s = 0.015 dB
+    (the test runs 16 channels: the mean of independent channels has
+    s / sqrt(2) = 0.011 dB, so 0.05 dB is 3.3 standard deviations of the
+    difference of two realisations)
   DSD128 DAS, 997 Hz sine, 8 channels x 1 s: interior  s = 0.34 dB
                                                whole   s = 0.26 dB
   DSD128 DAS, the headline's 10 s multitone + pink,
@@ -65,14 +68,14 @@ def test_sinad_dsd64_single_segment(oracle):
     """The small plain case's signal and trellis: 997 Hz at -6 dBFS + TPDF
     dither at -110 dBFS, 44.1 kHz -> DSD64 (six 63-tap stages, boxcar 8,
     engine gain and soft clip), CLANS-5, K = 16, depth 32, lat 32, one segment
-    per channel; 8 channels of 2 s."""
+    per channel; 16 channels of 2 s."""
     from foo_dsd_trellis_gb300 import ntf, signals
     from foo_dsd_trellis_gb300.fir import FirChain
     from foo_dsd_trellis_gb300.pipeline import PCM_FIR_GAIN
     from foo_dsd_trellis_gb300.sdm import TrellisSdm
     fs_in, fs_out, K, depth, lat = 44100, 2822400, 16, 32, 32
     f = ntf.get_filter("clans-5", fs_out)
-    nch = 8
+    nch = 16
     pcm = signals.sine_tpdf(2.0, fs_in, nch, seed=1000)
     gain = float(PCM_FIR_GAIN)
     fc = FirChain(fs_in, fs_out, boxcar_taps=8, soft_clip=True, num_channels=nch)
