@@ -89,9 +89,9 @@ __device__ __forceinline__ void halfband_stage(const FirChainConst& F, const flo
   }
 }
 
-// A merged stage (factor U = 8 or 16, kPolyTaps taps per branch; always stage
-// 0, its branch r at taps[r * kPolyTaps]): out[U*i + r] = sum_j hm[U*j + r]
-// x[i - j].  A work item is (branch group g, input index i): the inputs
+// A merged stage (factor U = 8 or 16, kPolyTaps taps per branch, its branch r
+// at taps[r * kPolyTaps] whatever its place in the chain): out[U*i + r] =
+// sum_j hm[U*j + r] x[i - j].  A work item is (branch group g, input index i): the inputs
 // x[i - j], streamed through registers kPolyChunk at a time, feed the
 // group's kPolyGroup branches.  Items run i fastest, so a warp's lanes share
 // the group, whose taps are compile-time constant operands (one instance per
@@ -355,20 +355,22 @@ int plan_chain(unsigned fs_in, unsigned fs_out, int* U, int* L) {
   return S;
 }
 
-// The leading stages a chain merges into one polyphase stage: all but the
-// last three, at most four (U <= 16), at least three (a shorter run leaves
-// too much zero padding), and only 63-tap half-band 2x stages.  Their
-// cascade is one LTI filter: stage k maps y_k = h'_k * (up2 y_{k-1}), so the
-// first M stages are hm * (up 2^M x) with hm = h'_{M-1} * up2(h'_{M-2} *
-// up2(... h'_0)), of length 1 + 62 (2^M - 1).  Its FP32 form differs from the
-// stage-by-stage FP32 cascade only in rounding (both within the chain's 1e-6
-// of the FP64 restatement), and its branches keep every thread busy where
-// the early stages, 1/16 to 1/2 of a tile's width, left most of them idle.
-int merged_stages(int S, const int* U, const int* L) {
-  int M = S - 3;
+// The run of stages a chain merges into one polyphase stage: the 63-tap
+// half-band 2x stages from k0 (0, or 1 behind the 127-tap first stage of the
+// chains into DSD512), all but the last three, at most four (U <= 16) and at
+// least three (a shorter run leaves too much zero padding).  Their cascade is
+// one LTI filter: stage k maps y_k = h'_k * (up2 y_{k-1}), so the run is
+// hm * (up 2^M y) with hm = h'_{M-1} * up2(h'_{M-2} * up2(... h'_0)), of length
+// 1 + 62 (2^M - 1).  Its FP32 form differs from the stage-by-stage FP32
+// cascade only in rounding (both within the chain's 1e-6 of the FP64
+// restatement), and its branches keep every thread busy where those stages,
+// 1/16 to 1/2 of a tile's width, left most of them idle at the barrier.
+int merged_stages(int S, const int* U, const int* L, int* k0) {
+  *k0 = (S > 0 && (U[0] != 2 || L[0] != 63)) ? 1 : 0;
+  int M = S - *k0 - 3;
   if (M > 4) M = 4;
   if (M < 3) return 0;
-  for (int k = 0; k < M; k++)
+  for (int k = *k0; k < *k0 + M; k++)
     if (U[k] != 2 || L[k] != 63) return 0;
   return M;
 }
@@ -378,7 +380,8 @@ int build_chain_const(unsigned fs_in, unsigned fs_out, int boxcar, FirChainConst
   int U[kMaxStages], L[kMaxStages];
   const int S0 = plan_chain(fs_in, fs_out, U, L);
   if (S0 < 0) return -1;
-  const int M = merged_stages(S0, U, L);
+  int k0 = 0;
+  const int M = merged_stages(S0, U, L, &k0);
   F->S = M ? S0 - M + 1 : S0;
   F->ratio = (int)(fs_out / fs_in);
   F->boxcar = boxcar;
@@ -386,9 +389,11 @@ int build_chain_const(unsigned fs_in, unsigned fs_out, int boxcar, FirChainConst
   int toff = 0;
   int rows = 1;
   if (M) {
+    // the merged stage's taps first (offset 0: the kernel addresses them
+    // as constants), branch r at r * kPolyTaps
     std::vector<double> g(63), t;
     design_taps(63, false, g.data());
-    for (double& v : g) v *= 2.0;                   // h'_0
+    for (double& v : g) v *= 2.0;                   // h'
     for (int k = 1; k < M; k++) {
       double h[63];
       design_taps(63, false, h);
@@ -399,28 +404,32 @@ int build_chain_const(unsigned fs_in, unsigned fs_out, int boxcar, FirChainConst
       g.swap(t);
     }
     const int Um = 1 << M;
-    if ((int)g.size() > Um * kPolyTaps || toff + Um * kPolyTaps > kMaxChainTaps) return -1;
-    F->U[0] = Um;
-    F->L[0] = Um * kPolyTaps;
-    F->poly_stage[0] = 1;
+    if ((int)g.size() > Um * kPolyTaps || Um * kPolyTaps > kMaxChainTaps) return -1;
+    F->U[k0] = Um;
+    F->L[k0] = Um * kPolyTaps;
+    F->poly_stage[k0] = 1;
     for (int r = 0; r < Um; r++) {
-      F->phase_off[0][r] = toff + r * kPolyTaps;
-      F->nphase[0][r] = kPolyTaps;
+      F->phase_off[k0][r] = r * kPolyTaps;
+      F->nphase[k0][r] = kPolyTaps;
       for (int j = 0; j < kPolyTaps; j++) {
         const size_t tap = (size_t)Um * j + r;
-        F->taps[toff + r * kPolyTaps + j] = tap < g.size() ? (float)g[tap] : 0.0f;
-        F->lag[toff + r * kPolyTaps + j] = j;
+        F->taps[r * kPolyTaps + j] = tap < g.size() ? (float)g[tap] : 0.0f;
+        F->lag[r * kPolyTaps + j] = j;
       }
     }
-    toff += Um * kPolyTaps;
-    rows = Um;
-    for (int k = M; k < S0; k++) {
+    toff = Um * kPolyTaps;
+    // the stages behind the run move up to follow the merged one
+    for (int k = k0 + M; k < S0; k++) {
       U[k - M + 1] = U[k];
       L[k - M + 1] = L[k];
     }
   }
   const int S = F->S;
-  for (int k = M ? 1 : 0; k < S; k++) {
+  for (int k = 0; k < S; k++) {
+    if (F->poly_stage[k]) {
+      rows *= F->U[k];
+      continue;
+    }
     F->U[k] = U[k];
     F->L[k] = L[k];
     double h[255];
