@@ -387,7 +387,6 @@ int build_chain_const(unsigned fs_in, unsigned fs_out, int boxcar, FirChainConst
   F->boxcar = boxcar;
   F->inv_boxcar = boxcar > 0 ? (float)(1.0 / boxcar) : 1.0f;
   int toff = 0;
-  int rows = 1;
   if (M) {
     // the merged stage's taps first (offset 0: the kernel addresses them
     // as constants), branch r at r * kPolyTaps
@@ -426,10 +425,7 @@ int build_chain_const(unsigned fs_in, unsigned fs_out, int boxcar, FirChainConst
   }
   const int S = F->S;
   for (int k = 0; k < S; k++) {
-    if (F->poly_stage[k]) {
-      rows *= F->U[k];
-      continue;
-    }
+    if (F->poly_stage[k]) continue;
     F->U[k] = U[k];
     F->L[k] = L[k];
     double h[255];
@@ -454,7 +450,6 @@ int build_chain_const(unsigned fs_in, unsigned fs_out, int boxcar, FirChainConst
       for (int t = 0; t < 32; t++) F->hb[t] = F->taps[F->phase_off[k][0] + t];
       F->hb_center = F->taps[F->phase_off[k][1]];
     }
-    rows *= U[k];
   }
   // output tile: 8,192 final samples per CTA (measured on the 10 s DSD128 stereo
   // chain: 4,096 / 6,144 / 8,192 / 12,288 / 16,384 ran 1.03 / 0.83 / 0.75 / 0.84 / 1.26 ms;
