@@ -185,14 +185,14 @@ __device__ __forceinline__ float small_to_float(int p) {
 // The engine's epilogue of one output (src/engine.c:646-651, 704-717): gain
 // ramp and the soft clip's threshold test in FP32 (within the chain's 1e-6
 // contract), the tanh knee in FP64 on the rare samples above the threshold,
-// one widening per output (widen_exact, integer operations).  The ramp is
+// one widening per output (integer operations).  The ramp is
 // gb + step * p, with gb = g_start + step * (tile start) formed once per
 // thread and p the output's offset in the tile: no per-output conversion.
 __device__ __forceinline__ double fir_epilogue(float v, int p, float gb, float gstep,
                                                int apply_gain, int soft_clip) {
   const float y = apply_gain ? v * fmaf(gstep, small_to_float(p), gb) : v;
   if (soft_clip && fabsf(y) > 0.95f) return soft_clip_095((double)y);
-  return widen_exact(y);
+  return widen_normal_fast(y);
 }
 
 // The chain description is a by-value kernel parameter (constant bank, about

@@ -33,4 +33,20 @@ __device__ __forceinline__ double widen_exact(float f) {
   return __longlong_as_double((long long)(sign | mag));
 }
 
+// The same for an output that is almost always a normal number: the normal
+// case from the high and low words (high = sign | ((|u| >> 3) + (896 << 20)),
+// low = u << 29: the rebiased exponent and the significand's top 20 bits, and
+// its last 3 bits), everything else through widen_exact out of line, so that
+// the common path is a handful of integer instructions and a uniform branch.
+static __device__ __noinline__ double widen_exact_rare(float f) { return widen_exact(f); }
+
+__device__ __forceinline__ double widen_normal_fast(float f) {
+  const unsigned u = __float_as_uint(f);
+  if (((u >> 23) & 0xffu) - 1u < 254u) {
+    const unsigned hi = (((u & 0x7fffffffu) >> 3) + 0x38000000u) | (u & 0x80000000u);
+    return __hiloint2double((int)hi, (int)(u << 29));
+  }
+  return widen_exact_rare(f);
+}
+
 }  // namespace dsdgpu

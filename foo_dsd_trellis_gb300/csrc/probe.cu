@@ -31,15 +31,17 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
 
 // Conversion self-check: binary32 pattern (seed + i * 0x9E3779B1) mod 2^32
 // for i < n (an odd multiplier: n = 2^32 visits every pattern once), widened
-// by widen_exact and by the hardware; NaNs compare as NaN.
+// by widen_exact, by widen_normal_fast and by the hardware; NaNs compare as NaN.
 __global__ void convert_check_kernel(unsigned long long n, unsigned seed,
                                      unsigned long long* bad) {
   unsigned long long local = 0;
   for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
        i += (unsigned long long)gridDim.x * blockDim.x) {
     const float f = __uint_as_float(seed + (unsigned)i * 0x9E3779B1u);
-    const double a = widen_exact(f), b = (double)f;
-    const bool same = (f != f) ? (a != a) : (__double_as_longlong(a) == __double_as_longlong(b));
+    const double a = widen_exact(f), a2 = widen_normal_fast(f), b = (double)f;
+    const bool same = (f != f) ? (a != a && a2 != a2)
+                               : (__double_as_longlong(a) == __double_as_longlong(b) &&
+                                  __double_as_longlong(a2) == __double_as_longlong(b));
     local += same ? 0 : 1;
   }
   if (local) atomicAdd(bad, local);
