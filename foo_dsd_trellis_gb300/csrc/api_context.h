@@ -45,9 +45,17 @@ void lowpass_free(dsdgpu_lowpass_state* s);
 struct dsdgpu_precorr_state;  // PreCorr greedy SDM (precorr.cu)
 void precorr_free(dsdgpu_precorr_state* s);
 struct dsdgpu_context;
-// PreCorr decisions for channels [first, first + nch) of the context's state.
+// PreCorr decisions for channels [first, first + nch) of the context's state
+// (FP64 input, narrowed per sample as the reference's float walk reads it, or
+// input already in FP32).
 int precorr_run(dsdgpu_context* c, int first, int nch, const double* d_in, size_t in_stride,
                 size_t count, uint8_t* d_bits, size_t bits_stride);
+int precorr_run(dsdgpu_context* c, int first, int nch, const float* d_in, size_t in_stride,
+                size_t count, uint8_t* d_bits, size_t bits_stride);
+// The FIR chain of channels [0, nch) writing FP32 outputs (for PreCorr).
+int fir_process_async_f32(dsdgpu_context* c, int nch, const float* d_in, size_t in_stride,
+                          size_t count, float* d_out, size_t out_stride, double gain_start,
+                          double gain_end, size_t* out_count);
 // Convolve a chunk of `nch` channels with the context's IRs (history carried).
 int conv_run(dsdgpu_context* c, int nch, const double* d_in, size_t in_stride, size_t count,
              double* d_out, size_t out_stride);

@@ -195,13 +195,42 @@ __device__ __forceinline__ double fir_epilogue(float v, int p, float gb, float g
   return widen_normal_fast(y);
 }
 
+// The same output for a consumer that reads FP32 (the PreCorr walk narrows
+// its input to FP32): y itself, which equals narrowing its exact widening;
+// the rare knee value narrowed as that consumer would.
+__device__ __forceinline__ float fir_epilogue_f32(float v, int p, float gb, float gstep,
+                                                  int apply_gain, int soft_clip) {
+  const float y = apply_gain ? v * fmaf(gstep, small_to_float(p), gb) : v;
+  if (soft_clip && fabsf(y) > 0.95f) return __double2float_rn(soft_clip_095((double)y));
+  return y;
+}
+
+template <typename OutT>
+__device__ __forceinline__ OutT fir_out(float v, int p, float gb, float gstep, int apply_gain,
+                                        int soft_clip);
+template <>
+__device__ __forceinline__ double fir_out<double>(float v, int p, float gb, float gstep,
+                                                  int apply_gain, int soft_clip) {
+  return fir_epilogue(v, p, gb, gstep, apply_gain, soft_clip);
+}
+template <>
+__device__ __forceinline__ float fir_out<float>(float v, int p, float gb, float gstep,
+                                                int apply_gain, int soft_clip) {
+  return fir_epilogue_f32(v, p, gb, gstep, apply_gain, soft_clip);
+}
+
+template <typename T> struct Pair2;
+template <> struct Pair2<double> { using type = double2; };
+template <> struct Pair2<float> { using type = float2; };
+
 // The chain description is a by-value kernel parameter (constant bank, about
 // 8.7 KB): every launch carries its own chain, so contexts and batch streams
 // with different rate pairs never share mutable device constants.
+template <typename OutT>
 __global__ void __launch_bounds__(kFirThreads, 2)
 fir_chain_kernel(const __grid_constant__ FirChainConst F, const float* __restrict__ pcm,
                  size_t pcm_stride, long long count, const float* __restrict__ hist,
-                 double* __restrict__ out, size_t out_stride, float g_start, float g_step,
+                 OutT* __restrict__ out, size_t out_stride, float g_start, float g_step,
                  int apply_gain, int soft_clip, int vec2) {
   extern __shared__ float sm[];
   const int ch = blockIdx.y;
@@ -271,21 +300,25 @@ fir_chain_kernel(const __grid_constant__ FirChainConst F, const float* __restric
   // two per 16-byte store where the row allows it
   const float* fin = buf[F.S];
   const int n = (int)(o_hi - o_lo);   // <= tile < 2^23
-  double* dst = out + (size_t)ch * out_stride + o_lo;
+  OutT* dst = out + (size_t)ch * out_stride + o_lo;
   const float gb = fmaf(g_step, (float)o_lo, g_start);
   if (vec2) {
+    using P2 = typename Pair2<OutT>::type;
     for (int p = 2 * (int)threadIdx.x; p < n; p += 2 * (int)blockDim.x) {
-      const double y0 = fir_epilogue(fin[p], p, gb, g_step, apply_gain, soft_clip);
+      const OutT y0 = fir_out<OutT>(fin[p], p, gb, g_step, apply_gain, soft_clip);
       if (p + 1 < n) {
-        const double y1 = fir_epilogue(fin[p + 1], p + 1, gb, g_step, apply_gain, soft_clip);
-        *reinterpret_cast<double2*>(dst + p) = make_double2(y0, y1);
+        const OutT y1 = fir_out<OutT>(fin[p + 1], p + 1, gb, g_step, apply_gain, soft_clip);
+        P2 v;
+        v.x = y0;
+        v.y = y1;
+        *reinterpret_cast<P2*>(dst + p) = v;
       } else {
         dst[p] = y0;
       }
     }
   } else {
     for (int p = threadIdx.x; p < n; p += blockDim.x)
-      dst[p] = fir_epilogue(fin[p], p, gb, g_step, apply_gain, soft_clip);
+      dst[p] = fir_out<OutT>(fin[p], p, gb, g_step, apply_gain, soft_clip);
   }
 }
 
@@ -485,33 +518,55 @@ int fir_chain_prepare() {
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return -1;
   if (!attr_set[dev]) {
-    if (cudaFuncSetAttribute(fir_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kFirMaxSmem) != cudaSuccess ||
-        cudaFuncSetAttribute(fir_chain_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                             100) != cudaSuccess)
+    if (cudaFuncSetAttribute(fir_chain_kernel<double>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, kFirMaxSmem) != cudaSuccess ||
+        cudaFuncSetAttribute(fir_chain_kernel<double>,
+                             cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess ||
+        cudaFuncSetAttribute(fir_chain_kernel<float>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, kFirMaxSmem) != cudaSuccess ||
+        cudaFuncSetAttribute(fir_chain_kernel<float>,
+                             cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
       return -1;
     attr_set[dev] = true;
   }
   return 0;
 }
 
-int launch_fir_chain(const FirChainConst& F, size_t smem, const float* pcm, size_t pcm_stride,
-                     long long count, const float* hist, double* out, size_t out_stride,
-                     double g_start, double g_step, int apply_gain, int soft_clip, int nch,
-                     cudaStream_t stream) {
+template <typename OutT>
+static int launch_fir_chain_t(const FirChainConst& F, size_t smem, const float* pcm,
+                              size_t pcm_stride, long long count, const float* hist, OutT* out,
+                              size_t out_stride, double g_start, double g_step, int apply_gain,
+                              int soft_clip, int nch, cudaStream_t stream) {
   const long long n_out = count * (long long)F.ratio;
   if (n_out <= 0) return 0;
   if (fir_chain_prepare() != 0) return -1;
   if (smem > (size_t)kFirMaxSmem) return -1;
   const dim3 grid((unsigned)((n_out + F.tile - 1) / F.tile), (unsigned)nch);
-  // 16-byte stores of output pairs: tiles start at even outputs, so the rows
-  // and the base have to be 16-byte aligned
-  const int vec2 = ((reinterpret_cast<uintptr_t>(out) & 15) == 0 && (out_stride & 1) == 0 &&
-                    (F.tile & 1) == 0) ? 1 : 0;
-  fir_chain_kernel<<<grid, kFirThreads, smem, stream>>>(F, pcm, pcm_stride, count, hist, out,
-                                                        out_stride, (float)g_start, (float)g_step,
-                                                        apply_gain, soft_clip, vec2);
+  // pair stores (16 bytes of doubles, 8 of floats): tiles start at even
+  // outputs, so the rows and the base have to be aligned to a pair
+  const int vec2 = ((reinterpret_cast<uintptr_t>(out) & (2 * sizeof(OutT) - 1)) == 0 &&
+                    (out_stride & 1) == 0 && (F.tile & 1) == 0) ? 1 : 0;
+  fir_chain_kernel<OutT><<<grid, kFirThreads, smem, stream>>>(F, pcm, pcm_stride, count, hist,
+                                                              out, out_stride, (float)g_start,
+                                                              (float)g_step, apply_gain,
+                                                              soft_clip, vec2);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_fir_chain(const FirChainConst& F, size_t smem, const float* pcm, size_t pcm_stride,
+                     long long count, const float* hist, double* out, size_t out_stride,
+                     double g_start, double g_step, int apply_gain, int soft_clip, int nch,
+                     cudaStream_t stream) {
+  return launch_fir_chain_t(F, smem, pcm, pcm_stride, count, hist, out, out_stride, g_start,
+                            g_step, apply_gain, soft_clip, nch, stream);
+}
+
+int launch_fir_chain(const FirChainConst& F, size_t smem, const float* pcm, size_t pcm_stride,
+                     long long count, const float* hist, float* out, size_t out_stride,
+                     double g_start, double g_step, int apply_gain, int soft_clip, int nch,
+                     cudaStream_t stream) {
+  return launch_fir_chain_t(F, smem, pcm, pcm_stride, count, hist, out, out_stride, g_start,
+                            g_step, apply_gain, soft_clip, nch, stream);
 }
 
 int launch_fir_history(const float* pcm, size_t pcm_stride, long long count, float* hist, int nch,
@@ -555,9 +610,16 @@ int dsdgpu_fir_reset(dsdgpu_context_t* c) {
   return c->check_status();
 }
 
-int dsdgpu_fir_process_async(dsdgpu_context_t* c, int first, int nch, const float* d_in,
-                             size_t in_stride, size_t count, double* d_out, size_t out_stride,
-                             double gain_start, double gain_end, size_t* out_count) {
+}  // extern "C"
+
+namespace dsdgpu {
+
+// dsdgpu_fir_process_async for either output type (FP64 for the trellis SDM,
+// FP32 for the pipeline's PreCorr mode)
+template <typename OutT>
+int fir_process_async_t(dsdgpu_context_t* c, int first, int nch, const float* d_in,
+                        size_t in_stride, size_t count, OutT* d_out, size_t out_stride,
+                        double gain_start, double gain_end, size_t* out_count) {
   if (!c) return DSDGPU_ERR_ARG;
   if (!c->fir_ready) return c->fail(DSDGPU_ERR_STATE, "fir not set up");
   if (first < 0 || nch < 1 || first + nch > c->fir_channels) return c->fail(DSDGPU_ERR_ARG, "bad channel range");
@@ -581,6 +643,24 @@ int dsdgpu_fir_process_async(dsdgpu_context_t* c, int first, int nch, const floa
     return c->cuda_fail(cudaGetLastError(), "fir history launch");
   c->launches++;
   return DSDGPU_OK;
+}
+
+}  // namespace dsdgpu
+
+int fir_process_async_f32(dsdgpu_context* c, int nch, const float* d_in, size_t in_stride,
+                          size_t count, float* d_out, size_t out_stride, double gain_start,
+                          double gain_end, size_t* out_count) {
+  return dsdgpu::fir_process_async_t(c, 0, nch, d_in, in_stride, count, d_out, out_stride,
+                                     gain_start, gain_end, out_count);
+}
+
+extern "C" {
+
+int dsdgpu_fir_process_async(dsdgpu_context_t* c, int first, int nch, const float* d_in,
+                             size_t in_stride, size_t count, double* d_out, size_t out_stride,
+                             double gain_start, double gain_end, size_t* out_count) {
+  return dsdgpu::fir_process_async_t(c, first, nch, d_in, in_stride, count, d_out, out_stride,
+                                     gain_start, gain_end, out_count);
 }
 
 int dsdgpu_fir_process(dsdgpu_context_t* c, int first, int nch, const float* d_in,

@@ -63,6 +63,11 @@ int launch_fir_chain(const FirChainConst& F, size_t smem, const float* pcm, size
                      long long count, const float* hist, double* out, size_t out_stride,
                      double g_start, double g_step, int apply_gain, int soft_clip, int nch,
                      cudaStream_t stream);
+// the same chain writing FP32 outputs (for a consumer that reads FP32)
+int launch_fir_chain(const FirChainConst& F, size_t smem, const float* pcm, size_t pcm_stride,
+                     long long count, const float* hist, float* out, size_t out_stride,
+                     double g_start, double g_step, int apply_gain, int soft_clip, int nch,
+                     cudaStream_t stream);
 int launch_fir_history(const float* pcm, size_t pcm_stride, long long count, float* hist, int nch,
                        cudaStream_t stream);
 

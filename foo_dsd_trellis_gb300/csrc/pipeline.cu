@@ -182,6 +182,12 @@ int dsdgpu_pipeline_process(dsdgpu_context_t* c, const float* d_pcm, size_t pcm_
   uint8_t* d_extra = d_bits + bit_row * (size_t)nch;
   const size_t fir_stride = fir_bytes / sizeof(double);
 
+  // PCM into PreCorr without a convolution: the chain writes FP32, the
+  // values the walk would narrow its FP64 input to (the FP32 chain's outputs
+  // widen exactly, and PreCorr has no soft clip ahead of it), so the walk
+  // reads them as they are; the rows keep their FP64 stride in elements
+  const bool f32_precorr = c->pipe_precorr && !c->conv && !c->pipe_same_rate &&
+                           !c->pipe_dsd_up && !c->pipe_dsd_down;
   cudaEventRecord(c->ev[0], c->stream);
   size_t fo = 0;
   if (c->pipe_same_rate) {
@@ -214,6 +220,9 @@ int dsdgpu_pipeline_process(dsdgpu_context_t* c, const float* d_pcm, size_t pcm_
     if (rc) return rc;
     rc = dsdgpu_decim_process_f64_async(c, nch, d_box, box_stride, n_in, d_fir, fir_stride,
                                         gain_start, gain_end, c->pipe.fir.soft_clip, &fo);
+  } else if (f32_precorr) {
+    rc = fir_process_async_f32(c, nch, d_pcm, pcm_stride, frames, (float*)d_fir,
+                               fir_stride, gain_start, gain_end, &fo);
   } else {
     rc = dsdgpu_fir_process_async(c, 0, nch, d_pcm, pcm_stride, frames, d_fir, fir_stride,
                                   gain_start, gain_end, &fo);
@@ -229,7 +238,8 @@ int dsdgpu_pipeline_process(dsdgpu_context_t* c, const float* d_pcm, size_t pcm_
   if (c->pipe_precorr) {
     // PreCorr: sequential per channel, no latency (src/engine.c:557-559, 723-726)
     cudaEventRecord(c->ev[2], c->stream);
-    rc = precorr_run(c, 0, nch, d_fir, fir_stride, fo, d_bits, bit_row);
+    rc = f32_precorr ? precorr_run(c, 0, nch, (const float*)d_fir, fir_stride, fo, d_bits, bit_row)
+                     : precorr_run(c, 0, nch, d_fir, fir_stride, fo, d_bits, bit_row);
     cudaEventRecord(c->ev[3], c->stream);
     n = fo;
   } else {
