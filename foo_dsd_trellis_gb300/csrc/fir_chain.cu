@@ -27,6 +27,7 @@
 #include "fir_internal.h"
 #include "fp_convert.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -219,6 +220,19 @@ __device__ __forceinline__ float fir_out<float>(float v, int p, float gb, float 
   return fir_epilogue_f32(v, p, gb, gstep, apply_gain, soft_clip);
 }
 
+// The epilogue's last part for an output whose gain is applied: the knee or
+// the widening (or, for FP32 consumers, the value itself).
+template <typename OutT>
+__device__ __forceinline__ OutT fir_finish(float y, bool knee);
+template <>
+__device__ __forceinline__ double fir_finish<double>(float y, bool knee) {
+  return knee ? soft_clip_095((double)y) : widen_normal_fast(y);
+}
+template <>
+__device__ __forceinline__ float fir_finish<float>(float y, bool knee) {
+  return knee ? __double2float_rn(soft_clip_095((double)y)) : y;
+}
+
 template <typename T> struct Pair2;
 template <> struct Pair2<double> { using type = double2; };
 template <> struct Pair2<float> { using type = float2; };
@@ -322,6 +336,186 @@ fir_chain_kernel(const __grid_constant__ FirChainConst F, const float* __restric
   }
 }
 
+// The whole chain as one polyphase stage (chains of five to seven 63-tap
+// half-band stages: factor U = 32, 64 or 128): out[U*i + r] = sum_k
+// h_r[k] b[i - k], b the boxcar output, h_r[k] = hm[U*k + r] the chain's
+// combined response (length 62 (U - 1) + 1, at most 62 taps per branch,
+// zero-padded to kPolyK).  For fixed k this is an outer product of a column
+// of inputs and a row of taps, so each thread holds an 8 x 8 block of outputs
+// (8 consecutive input indices x 8 branches, in pairs spread so that a row's
+// pair stores from neighbouring lanes are contiguous) in registers and per
+// tap row does 64 FMAs from 8 inputs (a register window sliding along k) and
+// 8 taps (four broadcast 8-byte shared loads).  No intermediate signal,
+// no stage barrier; the combined filter's FP32 result differs from the
+// stage-by-stage cascade only in rounding.  A warp holds (32 / RT) x 8 input
+// indices and RT x 8 branches; a CTA covers kPolyOut outputs.
+template <int RT, typename OutT>
+__global__ void __launch_bounds__(kFirThreads, 2)
+fir_poly_kernel(const __grid_constant__ FirChainConst F, const float* __restrict__ taps,
+                const float* __restrict__ pcm, size_t pcm_stride, long long count,
+                const float* __restrict__ hist, OutT* __restrict__ out, size_t out_stride,
+                float g_start, float g_step, int apply_gain, int soft_clip, int vec2, int nch) {
+  constexpr int IT = 32 / RT;
+  constexpr int halo = kPolyK - 1;
+  extern __shared__ __align__(16) float smp[];
+  const int U = F.poly_U;
+  const int rows = kPolyOut / U;           // input indices per tile
+  const int bt = F.boxcar;
+  // shared: taps [kPolyK][U] (k-major, loaded once: the CTAs are persistent
+  // and take tiles in turn), b[i0 - halo + t] for t < rows + halo, then the
+  // PCM window behind it
+  float* ts = smp;
+  float* bw = ts + kPolyK * U;
+  const int nb = rows + halo;
+  float* pw = bw + nb;
+  const int np = nb + (bt > 0 ? bt - 1 : 0);
+  for (int t = threadIdx.x; t < kPolyK * U; t += blockDim.x) ts[t] = taps[t];
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int per_rb = U / (8 * RT);        // warps across the branches of a row block
+  const int rb = warp / per_rb, pb = warp - rb * per_rb;
+  const int it = lane / RT, rt = lane - it * RT;
+  const int row0 = rb * (8 * IT) + it * 8;   // local input index of q = 0
+  // the thread's 8 branches: rb0 + 2 RT j + {0, 1}, j < 4, rb0 = block + 2 rt,
+  // so that for each j the RT lanes of a row write one contiguous run
+  const int rbase = pb * (8 * RT) + 2 * rt;
+  const long long tiles = (count + rows - 1) / rows;
+
+  for (long long wi = blockIdx.x; wi < tiles * nch; wi += gridDim.x) {
+    const int ch = (int)(wi / tiles);
+    const long long i0 = (wi - (long long)ch * tiles) * rows;
+    const float* x = pcm + (size_t)ch * pcm_stride;
+    const float* hx = hist + (size_t)ch * kHistory;
+    const long long p0 = i0 - halo - (bt > 0 ? bt - 1 : 0);
+    __syncthreads();                       // the previous tile's window is read
+    for (int t = threadIdx.x; t < np; t += blockDim.x) {
+      const long long i = p0 + t;
+      float v = 0.0f;                      // beyond the block: read by no kept output
+      if (i >= 0 && i < count) v = x[i];
+      else if (i < 0 && i >= -kHistory) v = hx[kHistory + i];
+      pw[t] = v;
+    }
+    __syncthreads();
+    // boxcar: mean of the last `bt` samples, newest first
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+      float v;
+      if (bt > 0) {
+        float sum = 0.0f;
+        for (int j = 0; j < bt; j++) sum += pw[t + bt - 1 - j];
+        v = sum * F.inv_boxcar;
+      } else {
+        v = pw[t];
+      }
+      bw[t] = v;
+    }
+    __syncthreads();
+
+    float acc[8][8];
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+#pragma unroll
+      for (int rr = 0; rr < 8; rr++) acc[q][rr] = 0.0f;
+    // b[row0 + q - k] = bb[q - k]; for the tap rows k0 .. k0 + 7 the window
+    // w[m] = bb[m - 7 - k0] (m < 15) holds every input they need:
+    // b[row0 + q - (k0 + kk)] = w[7 + q - kk]
+    const float* bb = bw + halo + row0;
+    float w[15];
+#pragma unroll
+    for (int m = 0; m < 15; m++) w[m] = bb[m - 7];
+#pragma unroll 1
+    for (int k0 = 0; k0 < kPolyK; k0 += 8) {
+      if (k0 > 0) {
+#pragma unroll
+        for (int m = 14; m >= 8; m--) w[m] = w[m - 8];
+#pragma unroll
+        for (int m = 0; m < 8; m++) w[m] = bb[m - 7 - k0];
+      }
+#pragma unroll
+      for (int kk = 0; kk < 8; kk++) {
+        const float* tr = ts + (k0 + kk) * U + rbase;
+        float hv[8];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const float2 h = *reinterpret_cast<const float2*>(tr + 2 * RT * j);
+          hv[2 * j] = h.x;
+          hv[2 * j + 1] = h.y;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const float xv = w[7 + q - kk];
+#pragma unroll
+          for (int rr = 0; rr < 8; rr++) acc[q][rr] = fmaf(hv[rr], xv, acc[q][rr]);
+        }
+      }
+    }
+
+    // epilogue: the gain ramp in place, then the knee test: a tile whose
+    // outputs all stay within the threshold (the usual case) takes the short
+    // path, and the unrolled code with the inlined FP64 tanh runs only for a
+    // warp where some output needs it
+    const float gb = fmaf(g_step, (float)(i0 * U), g_start);
+    bool over = false;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int pq = (row0 + q) * U + rbase;   // offset from the tile's first output (< 2^23)
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+          float& y = acc[q][2 * j + e];
+          if (apply_gain) y *= fmaf(g_step, small_to_float(pq + 2 * RT * j + e), gb);
+          over |= fabsf(y) > 0.95f;
+        }
+    }
+    over = soft_clip && __any_sync(0xffffffffu, over);
+    OutT* dst = out + (size_t)ch * out_stride;
+    if (!over) {
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const long long i = i0 + row0 + q;
+        if (i >= count) break;
+        OutT* d = dst + (size_t)i * U + rbase;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const OutT y0 = fir_finish<OutT>(acc[q][2 * j], false);
+          const OutT y1 = fir_finish<OutT>(acc[q][2 * j + 1], false);
+          if (vec2) {
+            typename Pair2<OutT>::type v;
+            v.x = y0;
+            v.y = y1;
+            *reinterpret_cast<typename Pair2<OutT>::type*>(d + 2 * RT * j) = v;
+          } else {
+            d[2 * RT * j] = y0;
+            d[2 * RT * j + 1] = y1;
+          }
+        }
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const long long i = i0 + row0 + q;
+        if (i >= count) break;
+        OutT* d = dst + (size_t)i * U + rbase;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const float a = acc[q][2 * j], b = acc[q][2 * j + 1];
+          const OutT y0 = fir_finish<OutT>(a, fabsf(a) > 0.95f);
+          const OutT y1 = fir_finish<OutT>(b, fabsf(b) > 0.95f);
+          if (vec2) {
+            typename Pair2<OutT>::type v;
+            v.x = y0;
+            v.y = y1;
+            *reinterpret_cast<typename Pair2<OutT>::type*>(d + 2 * RT * j) = v;
+          } else {
+            d[2 * RT * j] = y0;
+            d[2 * RT * j + 1] = y1;
+          }
+        }
+      }
+    }
+  }
+}
+
 // Keep the last kHistory PCM samples of this block (for the next one).
 __global__ void fir_history_kernel(const float* __restrict__ pcm, size_t pcm_stride,
                                    long long count, float* __restrict__ hist) {
@@ -408,11 +602,58 @@ int merged_stages(int S, const int* U, const int* L, int* k0) {
   return M;
 }
 
+// The combined impulse response of M cascaded 63-tap half-band 2x stages
+// (h'_k = 2 h_k): hm = h'_{M-1} * up2(h'_{M-2} * up2(... h'_0)), in FP64.
+static std::vector<double> cascade_response(int M) {
+  std::vector<double> g(63), t;
+  design_taps(63, false, g.data());
+  for (double& v : g) v *= 2.0;
+  double h[63];
+  design_taps(63, false, h);
+  for (int k = 1; k < M; k++) {
+    const size_t n = 2 * (g.size() - 1) + 1;     // up2(g)
+    t.assign(n + 62, 0.0);
+    for (size_t a = 0; a < g.size(); a++)
+      for (int b = 0; b < 63; b++) t[2 * a + (size_t)b] += g[a] * (2.0 * h[b]);
+    g.swap(t);
+  }
+  return g;
+}
+
+// The chains run whole as one polyphase stage: five to seven 63-tap
+// half-band 2x stages (factor 32 to 128, at most 62 taps per branch).
+static int whole_chain_factor(int S, const int* U, const int* L) {
+  if (S < 5 || S > 7) return 0;
+  for (int k = 0; k < S; k++)
+    if (U[k] != 2 || L[k] != 63) return 0;
+  return 1 << S;
+}
+
+// Branch taps of the whole-chain stage of factor U, k-major: t[k * U + r] =
+// hm[U * k + r] as FP32 (zero past the response).
+static std::vector<float> whole_chain_taps(int U) {
+  int S = 0;
+  for (int u = U; u > 1; u >>= 1) S++;
+  const std::vector<double> g = cascade_response(S);
+  std::vector<float> t((size_t)kPolyK * U, 0.0f);
+  for (int k = 0; k < kPolyK; k++)
+    for (int r = 0; r < U; r++) {
+      const size_t tap = (size_t)U * k + r;
+      if (tap < g.size()) t[(size_t)k * U + r] = (float)g[tap];
+    }
+  return t;
+}
+
 int build_chain_const(unsigned fs_in, unsigned fs_out, int boxcar, FirChainConst* F) {
   memset(F, 0, sizeof *F);
   int U[kMaxStages], L[kMaxStages];
   const int S0 = plan_chain(fs_in, fs_out, U, L);
   if (S0 < 0) return -1;
+  int U0[kMaxStages], L0[kMaxStages];
+  for (int k = 0; k < S0; k++) {
+    U0[k] = U[k];
+    L0[k] = L[k];
+  }
   int k0 = 0;
   const int M = merged_stages(S0, U, L, &k0);
   F->S = M ? S0 - M + 1 : S0;
@@ -423,18 +664,7 @@ int build_chain_const(unsigned fs_in, unsigned fs_out, int boxcar, FirChainConst
   if (M) {
     // the merged stage's taps first (offset 0: the kernel addresses them
     // as constants), branch r at r * kPolyTaps
-    std::vector<double> g(63), t;
-    design_taps(63, false, g.data());
-    for (double& v : g) v *= 2.0;                   // h'
-    for (int k = 1; k < M; k++) {
-      double h[63];
-      design_taps(63, false, h);
-      const size_t n = 2 * (g.size() - 1) + 1;     // up2(g)
-      t.assign(n + 62, 0.0);
-      for (size_t a = 0; a < g.size(); a++)
-        for (int b = 0; b < 63; b++) t[2 * a + (size_t)b] += g[a] * (2.0 * h[b]);
-      g.swap(t);
-    }
+    const std::vector<double> g = cascade_response(M);
     const int Um = 1 << M;
     if ((int)g.size() > Um * kPolyTaps || Um * kPolyTaps > kMaxChainTaps) return -1;
     F->U[k0] = Um;
@@ -488,10 +718,19 @@ int build_chain_const(unsigned fs_in, unsigned fs_out, int boxcar, FirChainConst
   // chain: 4,096 / 6,144 / 8,192 / 12,288 / 16,384 ran 1.03 / 0.83 / 0.75 / 0.84 / 1.26 ms;
   // 256 threads with at least 2 CTAs per SM; 3 fit by registers and shared memory)
   F->tile = 8192;
+  F->poly_U = whole_chain_factor(S0, U0, L0);
+  if (F->poly_U) F->tile = kPolyOut;
   return 0;
 }
 
 size_t chain_smem_bytes(const FirChainConst& F) {
+  if (F.poly_U) {
+    // taps [kPolyK][U], the boxcar output with its halo, the PCM window
+    const size_t rows = (size_t)(kPolyOut / F.poly_U);
+    const size_t nb = rows + kPolyK - 1;
+    return ((size_t)kPolyK * F.poly_U + nb + nb + (F.boxcar > 0 ? F.boxcar - 1 : 0) + 16) *
+           sizeof(float);
+  }
   // worst-case extents of every signal for a tile, plus the PCM window
   long long lo[kMaxStages + 1], hi[kMaxStages + 1];
   size_t best = 0;
@@ -511,12 +750,34 @@ size_t chain_smem_bytes(const FirChainConst& F) {
   return (best + 16) * sizeof(float);
 }
 
+// Device copies of the whole-chain taps (factor 32, 64, 128), per device,
+// made by fir_chain_prepare (outside any stream capture).
+static float* g_whole_taps[64][3] = {};
+
+static const float* whole_taps_device(int dev, int U) {
+  const int slot = U == 32 ? 0 : (U == 64 ? 1 : (U == 128 ? 2 : -1));
+  return (slot < 0 || dev < 0 || dev >= 64) ? nullptr : g_whole_taps[dev][slot];
+}
+
 int fir_chain_prepare() {
   // the shared-memory opt-in is a per-device function attribute
   static bool attr_set[64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return -1;
+  if (!g_whole_taps[dev][0]) {
+    for (int slot = 0; slot < 3; slot++) {
+      const int U = 32 << slot;
+      const std::vector<float> t = whole_chain_taps(U);
+      float* d = nullptr;
+      if (cudaMalloc(&d, sizeof(float) * t.size()) != cudaSuccess) return -1;
+      if (cudaMemcpy(d, t.data(), sizeof(float) * t.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(d);
+        return -1;
+      }
+      g_whole_taps[dev][slot] = d;
+    }
+  }
   if (!attr_set[dev]) {
     if (cudaFuncSetAttribute(fir_chain_kernel<double>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, kFirMaxSmem) != cudaSuccess ||
@@ -546,6 +807,25 @@ static int launch_fir_chain_t(const FirChainConst& F, size_t smem, const float* 
   // outputs, so the rows and the base have to be aligned to a pair
   const int vec2 = ((reinterpret_cast<uintptr_t>(out) & (2 * sizeof(OutT) - 1)) == 0 &&
                     (out_stride & 1) == 0 && (F.tile & 1) == 0) ? 1 : 0;
+  if (F.poly_U) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const float* taps = whole_taps_device(dev, F.poly_U);
+    if (!taps) return -1;
+    // persistent CTAs, two per SM (the register bound), taking tiles in turn
+    const long long work = (long long)grid.x * nch;
+    const unsigned ctas = (unsigned)std::min<long long>(work, 2ll * (sms > 0 ? sms : 148));
+    if (F.poly_U == 32)
+      fir_poly_kernel<4, OutT><<<ctas, kFirThreads, smem, stream>>>(
+          F, taps, pcm, pcm_stride, count, hist, out, out_stride, (float)g_start, (float)g_step,
+          apply_gain, soft_clip, vec2, nch);
+    else
+      fir_poly_kernel<8, OutT><<<ctas, kFirThreads, smem, stream>>>(
+          F, taps, pcm, pcm_stride, count, hist, out, out_stride, (float)g_start, (float)g_step,
+          apply_gain, soft_clip, vec2, nch);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+  }
   fir_chain_kernel<OutT><<<grid, kFirThreads, smem, stream>>>(F, pcm, pcm_stride, count, hist,
                                                               out, out_stride, (float)g_start,
                                                               (float)g_step, apply_gain,

@@ -10,6 +10,8 @@ constexpr int kMaxChainTaps = 2048;   // polyphase taps over all stages
 constexpr int kMaxPhases = 16;        // polyphase branches of one stage (a merged stage: 8 or 16)
 constexpr int kPolyTaps = 60;         // taps per branch of a merged stage (zero-padded)
 constexpr int kPolyGroup = 4;         // branches per work item of a merged stage
+constexpr int kPolyK = 64;            // taps per branch of a whole-chain stage (zero-padded)
+constexpr int kPolyOut = 16384;       // outputs per CTA of a whole-chain stage
 constexpr int kHistory = 256;         // PCM samples kept between blocks per channel
 constexpr int kFirThreads = 256;
 constexpr int kFirMaxSmem = 200 * 1024;   // dynamic shared memory cap of one FIR tile
@@ -43,6 +45,9 @@ struct FirChainConst {
   // one polyphase stage of factor U = 2^M, branch r holding the kPolyTaps
   // taps hm[U*j + r] (lag j, zero-padded) of the stages' combined response
   int poly_stage[kMaxStages];
+  // > 0: the whole chain (only 63-tap half-band 2x stages, factor 32 to 128)
+  // as one polyphase stage of this factor, run by fir_poly_kernel
+  int poly_U;
   // the 63-tap half-band 2x stage (every stage but a 127-tap first stage and
   // the 4x quarter-band one): its 32 even-phase taps and the centre tap, at
   // fixed offsets so that the unrolled kernel reads them as constant operands
