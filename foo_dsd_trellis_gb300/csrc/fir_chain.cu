@@ -345,7 +345,7 @@ fir_chain_kernel(const __grid_constant__ FirChainConst F, const float* __restric
 // (8 consecutive input indices x 8 branches, in pairs spread so that a row's
 // pair stores from neighbouring lanes are contiguous) in registers and per
 // tap row does 64 FMAs from 8 inputs (a register window sliding along k) and
-// 8 taps (four broadcast 8-byte shared loads).  No intermediate signal,
+// 8 taps (four broadcast 8-byte shared loads), as 32 packed FMAs.  No intermediate signal,
 // no stage barrier; the combined filter's FP32 result differs from the
 // stage-by-stage cascade only in rounding.  A warp holds (32 / RT) x 8 input
 // indices and RT x 8 branches; a CTA covers kPolyOut outputs.
@@ -410,41 +410,46 @@ fir_poly_kernel(const __grid_constant__ FirChainConst F, const float* __restrict
     }
     __syncthreads();
 
-    float acc[8][8];
+    // acc[q][j] = outputs (row0 + q, branches rbase + 2 RT j + {0, 1}) as a
+    // pair, accumulated with packed FP32 FMAs (two FMAs per instruction, each
+    // rounded as a scalar fmaf)
+    float2 acc[8][4];
 #pragma unroll
     for (int q = 0; q < 8; q++)
 #pragma unroll
-      for (int rr = 0; rr < 8; rr++) acc[q][rr] = 0.0f;
+      for (int j = 0; j < 4; j++) acc[q][j] = make_float2(0.0f, 0.0f);
     // b[row0 + q - k] = bb[q - k]; for the tap rows k0 .. k0 + 7 the window
     // w[m] = bb[m - 7 - k0] (m < 15) holds every input they need:
-    // b[row0 + q - (k0 + kk)] = w[7 + q - kk]
+    // b[row0 + q - (k0 + kk)] = w[7 + q - kk] (each held twice, as a pair)
     const float* bb = bw + halo + row0;
-    float w[15];
+    float2 w[15];
 #pragma unroll
-    for (int m = 0; m < 15; m++) w[m] = bb[m - 7];
+    for (int m = 0; m < 15; m++) {
+      const float v = bb[m - 7];
+      w[m] = make_float2(v, v);
+    }
 #pragma unroll 1
     for (int k0 = 0; k0 < kPolyK; k0 += 8) {
       if (k0 > 0) {
 #pragma unroll
         for (int m = 14; m >= 8; m--) w[m] = w[m - 8];
 #pragma unroll
-        for (int m = 0; m < 8; m++) w[m] = bb[m - 7 - k0];
+        for (int m = 0; m < 8; m++) {
+          const float v = bb[m - 7 - k0];
+          w[m] = make_float2(v, v);
+        }
       }
 #pragma unroll
       for (int kk = 0; kk < 8; kk++) {
         const float* tr = ts + (k0 + kk) * U + rbase;
-        float hv[8];
+        float2 h[4];
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-          const float2 h = *reinterpret_cast<const float2*>(tr + 2 * RT * j);
-          hv[2 * j] = h.x;
-          hv[2 * j + 1] = h.y;
-        }
+        for (int j = 0; j < 4; j++) h[j] = *reinterpret_cast<const float2*>(tr + 2 * RT * j);
 #pragma unroll
         for (int q = 0; q < 8; q++) {
-          const float xv = w[7 + q - kk];
+          const float2 xv = w[7 + q - kk];
 #pragma unroll
-          for (int rr = 0; rr < 8; rr++) acc[q][rr] = fmaf(hv[rr], xv, acc[q][rr]);
+          for (int j = 0; j < 4; j++) acc[q][j] = __ffma2_rn(h[j], xv, acc[q][j]);
         }
       }
     }
@@ -462,7 +467,7 @@ fir_poly_kernel(const __grid_constant__ FirChainConst F, const float* __restrict
       for (int j = 0; j < 4; j++)
 #pragma unroll
         for (int e = 0; e < 2; e++) {
-          float& y = acc[q][2 * j + e];
+          float& y = e ? acc[q][j].y : acc[q][j].x;
           if (apply_gain) y *= fmaf(g_step, small_to_float(pq + 2 * RT * j + e), gb);
           over |= fabsf(y) > 0.95f;
         }
@@ -477,8 +482,8 @@ fir_poly_kernel(const __grid_constant__ FirChainConst F, const float* __restrict
         OutT* d = dst + (size_t)i * U + rbase;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-          const OutT y0 = fir_finish<OutT>(acc[q][2 * j], false);
-          const OutT y1 = fir_finish<OutT>(acc[q][2 * j + 1], false);
+          const OutT y0 = fir_finish<OutT>(acc[q][j].x, false);
+          const OutT y1 = fir_finish<OutT>(acc[q][j].y, false);
           if (vec2) {
             typename Pair2<OutT>::type v;
             v.x = y0;
@@ -498,7 +503,7 @@ fir_poly_kernel(const __grid_constant__ FirChainConst F, const float* __restrict
         OutT* d = dst + (size_t)i * U + rbase;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-          const float a = acc[q][2 * j], b = acc[q][2 * j + 1];
+          const float a = acc[q][j].x, b = acc[q][j].y;
           const OutT y0 = fir_finish<OutT>(a, fabsf(a) > 0.95f);
           const OutT y1 = fir_finish<OutT>(b, fabsf(b) > 0.95f);
           if (vec2) {
