@@ -8,12 +8,18 @@
 //                 test in FP32, the tanh knee above +-0.95 in FP64 (optional)
 //              -> double output for the trellis SDM
 //
-// One CTA produces a tile of final output samples for one channel.  It walks
-// the chain backwards to find the input range each stage needs, stages the
-// PCM window (with its history halo) and every intermediate signal in shared
-// memory, and writes only the final double tile to HBM, two outputs per
-// 16-byte store: the chain's HBM traffic is one read of the PCM input and one
-// write of the output.
+// Two kernels, either way one read of the PCM input and one write of the
+// output in HBM:
+//   fir_poly_kernel   chains of five to seven 63-tap half-band stages (factor
+//                     32 to 128: the PCM rates into DSD64 / DSD128 / DSD256)
+//                     as one polyphase stage of the chain's combined response,
+//                     register-tiled (below);
+//   fir_chain_kernel  every other chain as a cascade: one CTA produces a tile
+//                     of final outputs for one channel, walks the chain
+//                     backwards to find the input range each stage needs,
+//                     stages the PCM window (with its history halo) and every
+//                     intermediate signal in shared memory, and writes only
+//                     the final tile, two outputs per 16-byte store.
 //
 // Stream continuity: a call may be one block of a longer stream.  The last
 // kHistory PCM samples of the previous block are kept per channel and stand in
