@@ -10,8 +10,8 @@
 //
 // Two kernels, either way one read of the PCM input and one write of the
 // output in HBM:
-//   fir_poly_kernel   chains of five to seven 63-tap half-band stages (factor
-//                     32 to 128: the PCM rates into DSD64 / DSD128 / DSD256)
+//   fir_poly_kernel   chains of five to eight 63-tap half-band stages (factor
+//                     32 to 256: the PCM rates into DSD64 / DSD128 / DSD256)
 //                     as one polyphase stage of the chain's combined response,
 //                     register-tiled (below);
 //   fir_chain_kernel  every other chain as a cascade: one CTA produces a tile
@@ -342,8 +342,8 @@ fir_chain_kernel(const __grid_constant__ FirChainConst F, const float* __restric
   }
 }
 
-// The whole chain as one polyphase stage (chains of five to seven 63-tap
-// half-band stages: factor U = 32, 64 or 128): out[U*i + r] = sum_k
+// The whole chain as one polyphase stage (chains of five to eight 63-tap
+// half-band stages: factor U = 32, 64, 128 or 256): out[U*i + r] = sum_k
 // h_r[k] b[i - k], b the boxcar output, h_r[k] = hm[U*k + r] the chain's
 // combined response (length 62 (U - 1) + 1, at most 62 taps per branch,
 // zero-padded to kPolyK).  For fixed k this is an outer product of a column
@@ -631,10 +631,10 @@ static std::vector<double> cascade_response(int M) {
   return g;
 }
 
-// The chains run whole as one polyphase stage: five to seven 63-tap
-// half-band 2x stages (factor 32 to 128, at most 62 taps per branch).
+// The chains run whole as one polyphase stage: five to eight 63-tap
+// half-band 2x stages (factor 32 to 256, at most 62 taps per branch).
 static int whole_chain_factor(int S, const int* U, const int* L) {
-  if (S < 5 || S > 7) return 0;
+  if (S < 5 || S > 8) return 0;
   for (int k = 0; k < S; k++)
     if (U[k] != 2 || L[k] != 63) return 0;
   return 1 << S;
@@ -761,12 +761,13 @@ size_t chain_smem_bytes(const FirChainConst& F) {
   return (best + 16) * sizeof(float);
 }
 
-// Device copies of the whole-chain taps (factor 32, 64, 128), per device,
-// made by fir_chain_prepare (outside any stream capture).
-static float* g_whole_taps[64][3] = {};
+// Device copies of the whole-chain taps (factor 32, 64, 128, 256), per
+// device, made by fir_chain_prepare (outside any stream capture).
+constexpr int kWholeFactors = 4;
+static float* g_whole_taps[64][kWholeFactors] = {};
 
 static const float* whole_taps_device(int dev, int U) {
-  const int slot = U == 32 ? 0 : (U == 64 ? 1 : (U == 128 ? 2 : -1));
+  const int slot = U == 32 ? 0 : (U == 64 ? 1 : (U == 128 ? 2 : (U == 256 ? 3 : -1)));
   return (slot < 0 || dev < 0 || dev >= 64) ? nullptr : g_whole_taps[dev][slot];
 }
 
@@ -777,7 +778,7 @@ int fir_chain_prepare() {
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return -1;
   if (!g_whole_taps[dev][0]) {
-    for (int slot = 0; slot < 3; slot++) {
+    for (int slot = 0; slot < kWholeFactors; slot++) {
       const int U = 32 << slot;
       const std::vector<float> t = whole_chain_taps(U);
       float* d = nullptr;
@@ -797,7 +798,15 @@ int fir_chain_prepare() {
         cudaFuncSetAttribute(fir_chain_kernel<float>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, kFirMaxSmem) != cudaSuccess ||
         cudaFuncSetAttribute(fir_chain_kernel<float>,
-                             cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
+                             cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess ||
+        cudaFuncSetAttribute(fir_poly_kernel<8, double>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, kFirMaxSmem) != cudaSuccess ||
+        cudaFuncSetAttribute(fir_poly_kernel<8, float>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, kFirMaxSmem) != cudaSuccess ||
+        cudaFuncSetAttribute(fir_poly_kernel<4, double>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, kFirMaxSmem) != cudaSuccess ||
+        cudaFuncSetAttribute(fir_poly_kernel<4, float>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, kFirMaxSmem) != cudaSuccess)
       return -1;
     attr_set[dev] = true;
   }

@@ -45,7 +45,7 @@ struct FirChainConst {
   // one polyphase stage of factor U = 2^M, branch r holding the kPolyTaps
   // taps hm[U*j + r] (lag j, zero-padded) of the stages' combined response
   int poly_stage[kMaxStages];
-  // > 0: the whole chain (only 63-tap half-band 2x stages, factor 32 to 128)
+  // > 0: the whole chain (only 63-tap half-band 2x stages, factor 32 to 256)
   // as one polyphase stage of this factor, run by fir_poly_kernel
   int poly_U;
   // the 63-tap half-band 2x stage (every stage but a 127-tap first stage and

@@ -23,6 +23,7 @@ def _pcm(n, seed, amp=0.5):
 RATES = [
     (44100, 2822400),      # 6 stages to DSD64
     (48000, 6144000),      # 7 stages to DSD128/48
+    (44100, 11289600),     # 8 stages to DSD256 (the whole-chain kernel's largest factor)
     (88200, 11289600),     # 7 stages to DSD256
     (192000, 24576000),    # 7 stages, 127-tap first stage (to DSD512/48)
     (2822400, 22579200),   # ratio 8 to DSD512: 4x quarter-band + 2x
