@@ -114,6 +114,8 @@ struct dsdgpu_context {
   double* d_das_qfir = nullptr;    size_t das_qfir_cap = 0;
   unsigned char* d_das_seam_scr = nullptr;  size_t das_seam_scr_cap = 0;   // overlaps > 16,384
   bool das_qfir_ready = false;
+  cudaStream_t das_side = nullptr;      // seg0-first: the estimator beside seg1's trellis run
+  cudaEvent_t das_side_ev[2] = {};
 
   // whole-path pipeline
   bool pipe_ready = false;
@@ -189,6 +191,11 @@ struct dsdgpu_context {
     if (ev_ready)
       for (int i = 0; i < kEvents; i++) cudaEventDestroy(ev[i]);
     ev_ready = false;
+    for (cudaEvent_t& e : das_side_ev)
+      if (e) cudaEventDestroy(e);
+    das_side_ev[0] = das_side_ev[1] = nullptr;
+    if (das_side) cudaStreamDestroy(das_side);
+    das_side = nullptr;
     void* das[] = {d_das_bits, d_das_est, d_das_i64, d_das_f64, d_das_bp, d_das_tasks,
                    d_das_pieces, d_das_segbuf, d_das_qfir, d_das_seam_scr};
     for (void* p : das)

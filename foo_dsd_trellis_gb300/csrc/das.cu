@@ -52,136 +52,242 @@ __global__ void das_rms_kernel(const double* __restrict__ x, const long long* __
 // One sample of sdm_estimate_state_multibit: the NTF advance with y = 0, the
 // quantiser (levels <= 2: the sign of v * a0; else v / a0 rounded to the
 // nearest of `levels` values in [-1, 1]), y subtracted from state 0, clamp.
-// The estimate is one serial chain per channel, so its cost is the latency of
-// that chain.  The state is held in registers (the step is instantiated per
-// NTF order), and the quantiser's index
-//     idx = trunc((v / a0 + 1) / step + 0.5), clamped to [0, levels - 1]
-// is first taken with the two divisions replaced by products with their
-// rounded reciprocals (within ~1e-14 of the exact value for |w| < 2^20): the
-// integer is the same wherever that value is more than 1e-9 from an integer
-// in [1, levels - 1], and the correctly rounded divisions decide the rest
-// (and NaN or huge values).  y = -1 + idx * step comes from a table of the
-// same products.
+//
+// The estimate is one serial chain per channel.  Every FP64 warp instruction
+// holds its sub-partition's FP64 pipe for ~64 cycles however many lanes it
+// runs, so the chain costs its count of FP64 instructions, and the step is
+// written in warp form: lane i (< order) holds state[i], and the state update
+// is four warp instructions
+//     p  = g[i] * state[i+1]
+//     r  = state[i] + (i == 0 ? -p : state[i-1])
+//     ns = r + (i == 0 ? x : i == order-1 ? -0.0 : -p)
+//     q  = a[i] * ns
+// that are the reference's expressions operand for operand (a - b == a + (-b)
+// and r + (-0.0) == r in IEEE arithmetic, signed zeros included); the sum
+// v = x + q[0] + q[1] + ... keeps the reference's order on broadcast q.
+//
+// The quantiser's index idx = trunc((v / a0 + 1) / step + 0.5), clamped to
+// [0, levels - 1], comes from u = fma(v, 1/(a0 step), 1/step) and integer
+// work on u's bits.  While |u| < 1024, u is within 1e-12 of the reference's
+// rounded (v / a0 + 1) / step (three roundings in the two constants and the
+// fma against three in the reference's divisions and sum), so floor(u + 0.5)
+// is the index unless u + 0.5 lies within 1e-9 of an integer; those samples,
+// |u| >= 1024 and non-finite u take the reference's divisions.  The 1-bit
+// sign test and the limiter compare bit patterns as integers.  A step is
+// order + 6 FP64 instructions (order + 8 above 32 levels).
+constexpr unsigned kFullMask = 0xffffffffu;
+constexpr unsigned kNearHalf = 1100;   // 1e-9 in units of 2^-40, rounded up
+
 struct EstConst {
-  double ra0;       // 1 / a0, rounded
-  double rstep;     // 1 / step, rounded
-  double step;
-  double ylev[64];  // -1 + k * step for k < min(levels, 64)
+  double c1;                 // (1 / a0) * (1 / step), rounded
+  double rstep;              // 1 / step, rounded
+  double step;               // 2 / (levels - 1)
+  double lim;                // state_limit
+  unsigned long long lim_bits;  // bits of state_limit when it is > 0, else 0 (limiter off)
   int levels;
 };
 
-__device__ __forceinline__ int quant_index(double v, double a0, const EstConst& E) {
-  const double w = __dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(v, E.ra0), 1.0), E.rstep), 0.5);
-  const int L = E.levels;
-  if (w < 1.0 - 1e-9) return 0;                        // trunc < 1 or negative: clamped to 0
-  if (w >= (double)(L - 1) + 1e-9 && w < 1048576.0) return L - 1;
-  if (w < 1048576.0 && L <= 1024) {
-    const double r = rint(w);
-    if (fabs(w - r) > 1e-9) return (int)w;             // w > 0: trunc == floor
-  }
-  // near a level boundary (or not finite): the reference's expression
+// Per-lane constants of the warp form.
+struct EstLane {
+  double g, a;   // g[lane], a[lane]; 0 for lanes >= order
+  double a0;
+  double ylev;   // -1 + lane * step (the level table, one level per lane)
+  int lane;
+};
+
+template <int N>
+__device__ __forceinline__ EstLane est_lane(const SdmParams& P, const EstConst& E) {
+  EstLane W;
+  W.lane = threadIdx.x & 31;
+  W.g = 0.0;
+  W.a = 0.0;
+#pragma unroll
+  for (int i = 0; i < N; i++)
+    if (W.lane == i) {
+      W.g = P.g[i];
+      W.a = P.a[i];
+    }
+  W.a0 = P.a[0];
+  W.ylev = __dadd_rn(-1.0, __dmul_rn((double)W.lane, E.step));
+  return W;
+}
+
+// The reference's quantiser expression, for the blocks the product form
+// leaves undecided.
+__device__ __forceinline__ int quant_exact(double v, double a0, double step, int levels) {
   const double yi = __ddiv_rn(v, a0);
-  int idx = __double2int_rz(__dadd_rn(__ddiv_rn(__dadd_rn(yi, 1.0), E.step), 0.5));
+  int idx = __double2int_rz(__dadd_rn(__ddiv_rn(__dadd_rn(yi, 1.0), step), 0.5));
   if (idx < 0) idx = 0;
-  if (idx > L - 1) idx = L - 1;
+  if (idx > levels - 1) idx = levels - 1;
   return idx;
 }
 
-template <int N>
-__device__ __forceinline__ void estimate_step_n(const SdmParams& P, const EstConst& E, double* st,
-                                                double xv) {
-  double ns[N];
-  ns[0] = __dadd_rn(__dsub_rn(st[0], __dmul_rn(P.g[0], st[1])), xv);
-  double v = __dadd_rn(xv, __dmul_rn(P.a[0], ns[0]));
-#pragma unroll
-  for (int i = 1; i < N - 1; i++) {
-    ns[i] = __dsub_rn(__dadd_rn(st[i], st[i - 1]), __dmul_rn(P.g[i], st[i + 1]));
-    v = __dadd_rn(v, __dmul_rn(P.a[i], ns[i]));
-  }
-  ns[N - 1] = __dadd_rn(st[N - 1], st[N - 2]);
-  v = __dadd_rn(v, __dmul_rn(P.a[N - 1], ns[N - 1]));
-  double y;
-  if (E.levels <= 2) y = __dmul_rn(v, P.a[0]) > 0.0 ? 1.0 : -1.0;
-  else {
-    const int idx = quant_index(v, P.a[0], E);
-    y = idx < 64 ? E.ylev[idx] : __dadd_rn(-1.0, __dmul_rn((double)idx, E.step));
-  }
-  ns[0] = __dsub_rn(ns[0], y);
-  if (P.state_limit > 0.0) {
-#pragma unroll
-    for (int i = 0; i < N; i++) {
-      if (ns[i] > P.state_limit) ns[i] = P.state_limit;
-      else if (ns[i] < -P.state_limit) ns[i] = -P.state_limit;
-    }
-  }
-#pragma unroll
-  for (int i = 0; i < N; i++) st[i] = ns[i];
+// floor(u + 0.5) clamped to [0, levels - 1] from u's bits, without branches;
+// `bad` is set where the reference's divisions must decide (|u| >= 1024, inf,
+// NaN, or u + 0.5 within 1e-9 of an integer).
+__device__ __forceinline__ int quant_fast(double u, int levels, bool& bad) {
+  const unsigned hi = (unsigned)__double2hiint(u);
+  const unsigned lo = (unsigned)__double2loint(u);
+  const unsigned ex = (hi >> 20) & 0x7ffu;             // biased exponent
+  const unsigned sh = 1035u - min(max(ex, 1021u), 1032u);  // 3..14: F = floor(u * 2^40) = fh:fl
+  const unsigned mh = (hi & 0xfffffu) | 0x100000u;
+  const unsigned fl = __funnelshift_r(lo, mh, sh);
+  const unsigned fh = mh >> sh;
+  const unsigned f8 = fh & 0xffu;                      // fraction bits 39..32
+  const bool near = (f8 == 0x80u && fl <= kNearHalf) || (f8 == 0x7fu && fl >= 0u - kNearHalf);
+  const bool low = (hi >> 31) != 0u || ex < 1021u;     // u < 0.25: w < 1 however it rounds
+  bad |= ex >= 1033u || (!low && near);
+  const int k = min((int)((fh + 0x80u) >> 8), levels - 1);  // (F + 2^39) >> 40
+  return low ? 0 : k;
 }
 
-EstConst make_est_const(double a0, int levels) {
+__device__ __forceinline__ double neg(double p) {
+  return __longlong_as_double(__double_as_longlong(p) ^ (long long)0x8000000000000000ull);
+}
+
+// One estimator step in warp form; s is this lane's state.  Q: 0 = the 1-bit
+// sign rule, 1 = 3..32 levels (the level comes from the lane holding it),
+// 2 = more levels (y = -1 + idx * step as the reference forms it).  EXACT
+// takes the reference's divisions for the index; otherwise the product form,
+// which sets `bad` for a sample it cannot decide.
+template <int N, int Q, bool LIM, bool EXACT>
+__device__ __forceinline__ double est_step(double s, double x, const EstLane& W, const EstConst& E,
+                                           bool& bad) {
+  const double sn = __shfl_down_sync(kFullMask, s, 1);
+  const double sp = __shfl_up_sync(kFullMask, s, 1);
+  const double np = neg(__dmul_rn(W.g, sn));
+  const double r = __dadd_rn(s, W.lane == 0 ? np : sp);
+  double ns = __dadd_rn(r, W.lane == 0 ? x : (W.lane == N - 1 ? -0.0 : np));
+  const double q = __dmul_rn(W.a, ns);
+  double v = __dadd_rn(x, __shfl_sync(kFullMask, q, 0));
+#pragma unroll
+  for (int i = 1; i < N; i++) v = __dadd_rn(v, __shfl_sync(kFullMask, q, i));
+  double y;
+  if (Q == 0) {
+    const long long b = __double_as_longlong(__dmul_rn(v, W.a0));
+    y = (b > 0 && b <= 0x7ff0000000000000LL) ? 1.0 : -1.0;   // v * a0 > 0
+  } else {
+    const int idx = EXACT ? quant_exact(v, W.a0, E.step, E.levels)
+                          : quant_fast(__fma_rn(v, E.c1, E.rstep), E.levels, bad);
+    y = Q == 1 ? __shfl_sync(kFullMask, W.ylev, idx)
+               : __dadd_rn(-1.0, __dmul_rn((double)idx, E.step));
+  }
+  ns = __dsub_rn(ns, W.lane == 0 ? y : 0.0);
+  if (LIM) {   // ns > lim -> lim; ns < -lim -> -lim; NaN stays
+    const long long b = __double_as_longlong(ns);
+    const unsigned long long ab = (unsigned long long)b & 0x7fffffffffffffffull;
+    if (ab > E.lim_bits && ab <= 0x7ff0000000000000ull) ns = b < 0 ? -E.lim : E.lim;
+  }
+  return W.lane < N ? ns : 0.0;
+}
+
+// n samples of x (any 8-byte alignment) through the estimator: 32 inputs per
+// coalesced load, the next block's load in flight while this block runs.  A
+// block with a sample the product form could not decide runs again from its
+// starting state with the reference's divisions.
+template <int N, int Q, bool LIM>
+__device__ double est_walk(double s, const EstLane& W, const EstConst& E,
+                           const double* __restrict__ x, long long n) {
+  if (n <= 0) return s;
+  double xl = W.lane < n ? __ldg(x + W.lane) : 0.0;
+  for (long long b = 0; b < n; b += 32) {
+    const long long nx = b + 32 + W.lane;
+    const double xn = nx < n ? __ldg(x + nx) : 0.0;
+    const int m = (int)min(32LL, n - b);
+    const double s0 = s;
+    bool bad = false;
+    if (m == 32) {
+#pragma unroll 4
+      for (int j = 0; j < 32; j++)
+        s = est_step<N, Q, LIM, false>(s, __shfl_sync(kFullMask, xl, j), W, E, bad);
+    } else {
+      for (int j = 0; j < m; j++)
+        s = est_step<N, Q, LIM, false>(s, __shfl_sync(kFullMask, xl, j), W, E, bad);
+    }
+    if (Q != 0 && __any_sync(kFullMask, bad)) {
+      s = s0;
+      for (int j = 0; j < m; j++)
+        s = est_step<N, Q, LIM, true>(s, __shfl_sync(kFullMask, xl, j), W, E, bad);
+    }
+    xl = xn;
+  }
+  return s;
+}
+
+EstConst make_est_const(const SdmParams& P, int levels) {
   EstConst E;
   memset(&E, 0, sizeof E);
   E.levels = levels;
   E.step = 2.0 / (double)(levels - 1);
-  E.ra0 = 1.0 / a0;
   E.rstep = 1.0 / E.step;
-  for (int k = 0; k < levels && k < 64; k++) E.ylev[k] = -1.0 + (double)k * E.step;
+  E.c1 = (1.0 / P.a[0]) * E.rstep;
+  E.lim = P.state_limit;
+  if (P.state_limit > 0.0) memcpy(&E.lim_bits, &P.state_limit, sizeof E.lim_bits);
   return E;
 }
 
-// One thread per estimate (sdm_estimate_state(_multibit) on its own input).
-template <int N>
-__global__ void estimate_kernel(SdmParams P, EstConst E, const dsdgpu_estimate_t* __restrict__ items,
-                                int n, double* __restrict__ out /* [n][kMaxOrder] */) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+int est_kind(int levels) { return levels <= 2 ? 0 : levels <= 32 ? 1 : 2; }
+
+// One warp per estimate (sdm_estimate_state(_multibit) on its own input).
+constexpr int kEstWarps = 4;
+template <int N, int Q, bool LIM>
+__global__ void __launch_bounds__(32 * kEstWarps)
+estimate_kernel(SdmParams P, EstConst E, const dsdgpu_estimate_t* __restrict__ items, int n,
+                double* __restrict__ out /* [n][kMaxOrder] */) {
+  const int j = blockIdx.x * kEstWarps + (int)(threadIdx.x >> 5);
   if (j >= n) return;
-  double st[N];
-#pragma unroll
-  for (int k = 0; k < N; k++) st[k] = items[j].init_state[k];
-  const double* x = items[j].d_in;
-  const long long count = items[j].count;
-  for (long long t = 0; t < count; t++) estimate_step_n<N>(P, E, st, x[t]);
-  for (int k = 0; k < kMaxOrder; k++) out[(size_t)j * kMaxOrder + k] = 0.0;
-#pragma unroll
-  for (int k = 0; k < N; k++) out[(size_t)j * kMaxOrder + k] = st[k];
+  const EstLane W = est_lane<N>(P, E);
+  double s = W.lane < N ? items[j].init_state[W.lane] : 0.0;
+  s = est_walk<N, Q, LIM>(s, W, E, items[j].d_in, items[j].count);
+  if (W.lane < kMaxOrder) out[(size_t)j * kMaxOrder + W.lane] = W.lane < N ? s : 0.0;
 }
 
-// DAS seeding: one thread per channel walks the chunk from seg1's start with
+// DAS seeding: one warp per channel walks the chunk from seg1's start with
 // the 16-level estimator and records the state at every later segment start.
-template <int N>
-__global__ void das_estimate_kernel(SdmParams P, EstConst E, const double* __restrict__ fir,
-                                    size_t fir_stride, const SdmCtx* __restrict__ pers,
-                                    int pers_first, const long long* __restrict__ starts, int S,
-                                    long long count, double* __restrict__ est /* [nch][S][kMaxOrder] */,
-                                    int nch) {
-  const int ch = blockIdx.x * blockDim.x + threadIdx.x;
+template <int N, bool LIM>
+__global__ void __launch_bounds__(32)
+das_estimate_kernel(SdmParams P, EstConst E, const double* __restrict__ fir, size_t fir_stride,
+                    const SdmCtx* __restrict__ pers, int pers_first,
+                    const long long* __restrict__ starts, int S, long long count,
+                    double* __restrict__ est /* [nch][S][kMaxOrder] */, int nch) {
+  const int ch = blockIdx.x;
   if (ch >= nch) return;
-  double st[N];
-  const SdmCtx* c = &pers[pers_first + ch];
-#pragma unroll
-  for (int k = 0; k < N; k++) st[k] = c->s[0][k];
+  const EstLane W = est_lane<N>(P, E);
+  double s = W.lane < N ? pers[pers_first + ch].s[0][W.lane] : 0.0;
   const double* x = fir + (size_t)ch * fir_stride;
   const long long est_start = starts[1];
   long long pos = 0;
-  for (int s = 1; s < S; s++) {
-    const long long bnd = s >= 2 ? starts[s] - est_start : 0;
+  for (int sg = 1; sg < S; sg++) {
+    const long long bnd = sg >= 2 ? starts[sg] - est_start : 0;
     if (bnd > pos && bnd <= count - est_start) {
-      for (long long t = pos; t < bnd; t++) estimate_step_n<N>(P, E, st, x[est_start + t]);
+      s = est_walk<N, 1, LIM>(s, W, E, x + est_start + pos, bnd - pos);
       pos = bnd;
     }
-    double* o = est + ((size_t)ch * S + s) * kMaxOrder;
-    for (int k = 0; k < kMaxOrder; k++) o[k] = 0.0;
-#pragma unroll
-    for (int k = 0; k < N; k++) o[k] = st[k];
+    double* o = est + ((size_t)ch * S + sg) * kMaxOrder;
+    if (W.lane < kMaxOrder) o[W.lane] = W.lane < N ? s : 0.0;
   }
+}
+
+template <int N, bool LIM>
+void launch_estimate_n(const SdmParams& P, const EstConst& E, int kind,
+                       const dsdgpu_estimate_t* d_items, int n, double* d_out, cudaStream_t stream) {
+  const int blocks = (n + kEstWarps - 1) / kEstWarps;
+  const int threads = 32 * kEstWarps;
+  if (kind == 0) estimate_kernel<N, 0, LIM><<<blocks, threads, 0, stream>>>(P, E, d_items, n, d_out);
+  else if (kind == 1) estimate_kernel<N, 1, LIM><<<blocks, threads, 0, stream>>>(P, E, d_items, n, d_out);
+  else estimate_kernel<N, 2, LIM><<<blocks, threads, 0, stream>>>(P, E, d_items, n, d_out);
 }
 
 int launch_estimate(const SdmParams& P, int levels, const dsdgpu_estimate_t* d_items, int n,
                     double* d_out, cudaStream_t stream) {
-  const EstConst E = make_est_const(P.a[0], levels);
+  const EstConst E = make_est_const(P, levels);
+  const int kind = est_kind(levels);
   switch (P.order) {
 #define DSD_CASE(NN) \
-  case NN: estimate_kernel<NN><<<(n + 31) / 32, 32, 0, stream>>>(P, E, d_items, n, d_out); break;
+  case NN:                                                                    \
+    if (E.lim_bits) launch_estimate_n<NN, true>(P, E, kind, d_items, n, d_out, stream); \
+    else launch_estimate_n<NN, false>(P, E, kind, d_items, n, d_out, stream);           \
+    break;
     DSD_CASE(2) DSD_CASE(3) DSD_CASE(4) DSD_CASE(5) DSD_CASE(6)
     DSD_CASE(7) DSD_CASE(8) DSD_CASE(9) DSD_CASE(10)
 #undef DSD_CASE
@@ -193,13 +299,18 @@ int launch_estimate(const SdmParams& P, int levels, const dsdgpu_estimate_t* d_i
 int launch_das_estimate(const SdmParams& P, const double* fir, size_t fir_stride, const SdmCtx* pers,
                         int pers_first, const long long* starts, int S, long long count, double* est,
                         int nch, cudaStream_t stream) {
-  const EstConst E = make_est_const(P.a[0], 16);
+  const EstConst E = make_est_const(P, 16);
   switch (P.order) {
-#define DSD_CASE(NN)                                                                          \
-  case NN:                                                                                    \
-    das_estimate_kernel<NN><<<(nch + 31) / 32, 32, 0, stream>>>(P, E, fir, fir_stride, pers,  \
-                                                               pers_first, starts, S, count, \
-                                                               est, nch);                    \
+#define DSD_CASE(NN)                                                                 \
+  case NN:                                                                           \
+    if (E.lim_bits)                                                                  \
+      das_estimate_kernel<NN, true><<<nch, 32, 0, stream>>>(P, E, fir, fir_stride, pers, \
+                                                            pers_first, starts, S,   \
+                                                            count, est, nch);        \
+    else                                                                             \
+      das_estimate_kernel<NN, false><<<nch, 32, 0, stream>>>(P, E, fir, fir_stride,  \
+                                                             pers, pers_first, starts, \
+                                                             S, count, est, nch);    \
     break;
     DSD_CASE(2) DSD_CASE(3) DSD_CASE(4) DSD_CASE(5) DSD_CASE(6)
     DSD_CASE(7) DSD_CASE(8) DSD_CASE(9) DSD_CASE(10)
@@ -825,6 +936,16 @@ int ensure_dev(dsdgpu_context* c, T** p, size_t* cap, size_t n, const char* what
   return DSDGPU_OK;
 }
 
+// The side stream and events of the seg0-first estimator, made on first use.
+int ensure_das_side(dsdgpu_context* c) {
+  if (c->das_side) return DSDGPU_OK;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->das_side, cudaStreamNonBlocking);
+  for (int i = 0; i < 2 && e == cudaSuccess; i++)
+    e = cudaEventCreateWithFlags(&c->das_side_ev[i], cudaEventDisableTiming);
+  if (e != cudaSuccess) return c->cuda_fail(e, "estimator stream");
+  return DSDGPU_OK;
+}
+
 // Grow the SDM context bank to `need` contexts, keeping the existing ones.
 int ensure_ctx_capacity(dsdgpu_context* c, int need) {
   if (c->nctx >= need) return DSDGPU_OK;
@@ -987,22 +1108,34 @@ int dsdgpu_das_process(dsdgpu_context_t* c, const dsdgpu_das_params_t* dp, int n
     for (int ch = 0; ch < nch; ch++) add_job(j0, ch, 0, ch, -1, false, ch);
     rc = c->run_jobs(j0);
     if (rc) return rc;
+    // seg1 and the estimator both start from seg0's final state and neither
+    // writes what the other reads: the estimator walks on a side stream
+    // while seg1's trellis runs, and the segment launch waits for it
+    if (S > 2) {
+      rc = ensure_das_side(c);
+      if (rc) return rc;
+      std::vector<long long> st(start.begin(), start.end());
+      rc = ensure_dev(c, &c->d_das_i64, &c->das_i64_cap, (size_t)S, "starts");
+      if (rc) return rc;
+      cudaEventRecord(c->das_side_ev[0], c->stream);
+      cudaStreamWaitEvent(c->das_side, c->das_side_ev[0], 0);
+      cudaMemcpyAsync(c->d_das_i64, st.data(), sizeof(long long) * S, cudaMemcpyHostToDevice, c->das_side);
+      if (launch_das_estimate(c->sdm, d_fir, fir_stride, c->d_ctx, 0, c->d_das_i64, S,
+                              (long long)count, c->d_das_est, nch, c->das_side) != 0)
+        return c->cuda_fail(cudaGetLastError(), "estimate launch");
+      c->launches++;
+      cudaEventRecord(c->das_side_ev[1], c->das_side);
+    }
     if (S > 1) {
       std::vector<SdmJob> j1;
       for (int ch = 0; ch < nch; ch++) add_job(j1, ch, 1, temp0 + ch * S + 1, ch, false, ch);
       rc = c->run_jobs(j1);
-      if (rc) return rc;
+      if (rc) {
+        if (S > 2) cudaStreamSynchronize(c->das_side);
+        return rc;
+      }
     }
-    if (S > 2) {
-      std::vector<long long> st(start.begin(), start.end());
-      rc = ensure_dev(c, &c->d_das_i64, &c->das_i64_cap, (size_t)S, "starts");
-      if (rc) return rc;
-      cudaMemcpyAsync(c->d_das_i64, st.data(), sizeof(long long) * S, cudaMemcpyHostToDevice, c->stream);
-      if (launch_das_estimate(c->sdm, d_fir, fir_stride, c->d_ctx, 0, c->d_das_i64, S,
-                              (long long)count, c->d_das_est, nch, c->stream) != 0)
-        return c->cuda_fail(cudaGetLastError(), "estimate launch");
-      c->launches++;
-    }
+    if (S > 2) cudaStreamWaitEvent(c->stream, c->das_side_ev[1], 0);
     // seg2+ copy the persistent context after seg0: snapshot it so the
     // parallel launch reads a context nothing writes
     for (int ch = 0; ch < nch; ch++) {

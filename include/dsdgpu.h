@@ -378,7 +378,7 @@ int dsdgpu_sdm_query(dsdgpu_context_t *ctx, int channel, double *best_state, uin
 int dsdgpu_sdm_state_distance(dsdgpu_context_t *ctx, int a, int b, double *dist);
 
 /* sdm_estimate_state / sdm_estimate_state_multibit (src/trellis.c:1118-1187),
- * many at once (one GPU thread each): the NTF loop of `p` (order, a, g,
+ * many at once (one GPU warp each): the NTF loop of `p` (order, a, g,
  * state_limit; K, depth and lat are not used) run greedily from init_state
  * over `count` samples of d_in (device) with a num_levels quantiser (2 = the
  * 1-bit sign rule, 16 = sdm_estimate_state's default); out_state receives the

@@ -358,6 +358,57 @@ def test_estimate_state_batch(oracle):
     L.dsdgpu_destroy(h)
 
 
+def test_estimate_state_level_boundaries(oracle):
+    """The estimator's quantiser at its level boundaries: from a zero state
+    the first output is v = x + a0 * x, so first inputs placed on, and one or
+    a few ulps and 1e-12 .. 1e-9 either side of, every boundary
+    (v / a0 + 1) / step + 0.5 = k (and x = 0, where u = 7.5 exactly at 16
+    levels) reach the samples the warp form hands to the reference's
+    divisions; the next 40 inputs continue from the state they leave.  Equal
+    to the oracle for 3, 16 and 32 levels, with and without the limiter."""
+    import ctypes as C
+    from foo_dsd_trellis_gb300 import _lib, ntf
+    L = _lib.load()
+    h = C.c_void_p()
+    assert L.dsdgpu_create(0, C.byref(h)) == 0
+    f = ntf.get_filter("clans-7", 5644800)
+    a0 = float(f.a[0])
+    rng = np.random.default_rng(5)
+    for levels in (3, 16, 32):
+        step = 2.0 / (levels - 1)
+        firsts = [0.0]
+        for k in range(levels + 1):
+            yi = (k - 0.5) * step - 1.0
+            x0 = yi * a0 / (1.0 + a0)
+            firsts.append(x0)
+            for d in (1, 2, 4):
+                firsts.append(float(np.nextafter(x0, np.inf) if d == 1 else x0 + d * np.spacing(x0)))
+                firsts.append(float(np.nextafter(x0, -np.inf) if d == 1 else x0 - d * np.spacing(x0)))
+            for rel in (1e-12, 3e-10, 1e-9, 2e-9):
+                firsts.extend([x0 * (1 + rel) + rel, x0 * (1 - rel) - rel])
+        for lim in (0.0, 1.5):
+            p = _lib.SdmParams()
+            p.order = f.order
+            for i in range(f.order):
+                p.a[i], p.g[i] = f.a[i], f.g[i]
+            p.state_limit = lim
+            xs = [np.concatenate([[x0], 0.3 * rng.standard_normal(40)]) for x0 in firsts
+                  for _ in range(2)]
+            d_x = [torch.from_numpy(x).cuda() for x in xs]
+            items = (_lib.EstimateItem * len(xs))()
+            for j, x in enumerate(xs):
+                items[j].d_in = d_x[j].data_ptr()
+                items[j].count = len(x) if j % 2 else 1
+            _lib.check(h, L.dsdgpu_sdm_estimate_state(h, C.byref(p), levels, items, len(xs)))
+            for j, x in enumerate(xs):
+                n = items[j].count
+                want = oracle.estimate_state(f.order, np.array(f.a), np.array(f.g),
+                                             np.zeros(f.order), x[:n], lim, levels)
+                got = np.array(items[j].out_state[: f.order])
+                assert np.array_equal(got, want), (levels, lim, j, x[0])
+    L.dsdgpu_destroy(h)
+
+
 def test_state_distance(oracle):
     """dsdgpu_sdm_state_distance (src/trellis.c:1094-1109) of two contexts run on
     different inputs equals the sum of squared differences of the oracle's best
