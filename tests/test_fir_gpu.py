@@ -21,6 +21,7 @@ def _pcm(n, seed, amp=0.5):
 
 
 RATES = [
+    (88200, 2822400),      # 5 stages to DSD64 (the whole-chain kernel's smallest factor)
     (44100, 2822400),      # 6 stages to DSD64
     (48000, 6144000),      # 7 stages to DSD128/48
     (44100, 11289600),     # 8 stages to DSD256 (the whole-chain kernel's largest factor)
