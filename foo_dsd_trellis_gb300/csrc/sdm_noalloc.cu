@@ -14,8 +14,7 @@
 //
 // The array's name is only a host-side stand-in in host code, not a device
 // address, so the first call on each device looks its address up with
-// cudaGetSymbolAddress (with that device current) and caches it; that first
-// call should therefore come before any stream capture.  The cached address
+// cudaGetSymbolAddress (with that device current) and caches it.  The cached address
 // belongs to the device's primary context: after cudaDeviceReset the module
 // is loaded again elsewhere and this entry point must not be used in that
 // process any more.

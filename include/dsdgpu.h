@@ -340,9 +340,8 @@ int dsdgpu_get_stream(const dsdgpu_context_t *ctx, void **stream);
  * checked as for dsdgpu_sdm_setup (lat up to 2048).  With more than one
  * channel, in_stride must be at least count and out_stride at least the
  * decisions a channel writes (DSDGPU_ERR_ARG otherwise).
- * The first call on a device looks up the array's device address (make it
- * before any stream capture); the address is not valid across
- * cudaDeviceReset.  CUDA loads kernels lazily, so make one warm-up call with
+ * The first call on a device looks up the array's device address; the
+ * address is not valid across cudaDeviceReset.  CUDA loads kernels lazily, so make one warm-up call with
  * the same parameters and channel count outside the real-time path (or set
  * CUDA_MODULE_LOADING=EAGER): the first use of a kernel variant can allocate
  * inside the driver.  Calls share the array: two calls whose work overlaps on
