@@ -17,7 +17,8 @@ from source only where its tree is present, and never on an aarch64 GPU host)
 on a bounded slice of the same workload.
 
 Other workloads (`--workload`, one JSON line each): multistream64 (64 streams
-in one batched plan), diff16 (the adjoint of the differentiable path),
+in one batched plan), multistream64_precorr (the same streams through the
+PreCorr SDM in one plan), diff16 (the adjoint of the differentiable path),
 dsd512conv6 (DSD512 5.1 with UPOLS room convolution), samerate128 (DoP DSD128
 re-encode on the engine's path-table parameters), samerate128lp (the same with
 the engine's 127-tap FIR lowpass instead of the boxcar), dsd2pcm128 (DSD128 ->
@@ -114,7 +115,8 @@ def parse():
     ap.add_argument("--das-seg-len", type=int, default=WL["das_seg_len"],
                     help="nominal DAS segment length (profiling of small cases only)")
     ap.add_argument("--workload", default="dsd128_das",
-                    choices=["dsd128_das", "multistream64", "diff16", "dsd512conv6",
+                    choices=["dsd128_das", "multistream64", "multistream64_precorr", "diff16",
+                             "dsd512conv6",
                              "samerate128", "samerate128lp", "precorr128", "dsd2pcm128",
                              "dsd256to128", "dsd128_seg0first"],
                     help="multistream64: the batched 64-stream form; diff16: the adjoint; "
@@ -128,7 +130,7 @@ def parse():
     ap.add_argument("--fd-dirs", type=int, default=32,
                     help="diff16: random unit directions of the finite-difference check")
     ap.add_argument("--ms-scale", type=float, default=1.0,
-                    help="multistream64: stream lengths scale (1.0 = 0.5-30 s)")
+                    help="multistream64(_precorr): stream lengths scale (1.0 = 0.5-30 s)")
     ap.add_argument("--ms-seg-len", type=int, default=0,
                     help="multistream64: DAS segment length (0 = autotuned)")
     return ap.parse_args()
@@ -644,6 +646,128 @@ def run_multistream(args):
                              "kernel": "sdm_jobs_kernel<6,32>, sdm_jobs_kernel<8,32> (concurrent)"},
                 "cpu_baseline": None, "clocks": clk, "gpu_launches": int(launches),
                 "plan": info, "stages_ms": plan.times_ms()}
+        print(json.dumps(line), flush=True)
+    plan.close()
+
+
+MSP_METRIC = ("PreCorr greedy SDM DSD Msamples/s, batched 64-stream form (one launch per PreCorr "
+              "parameter set, one thread per channel row)")
+
+
+def run_multistream_precorr(args):
+    """The 64-stream layout of multistream64 in PreCorr mode (src/precorr.c:20-287):
+    the same streams, lengths and signals, the PreCorr NTF per rate
+    (ntf_auto_select_precorr), state limit 12, FIR chain without the soft clip,
+    DoP output.  One step converts every stream once; the walk is one thread
+    per channel row, so the step is as long as the longest stream's walk.  The
+    CPU leg runs the oracle's PreCorr (pinned to src/precorr.c) on the eight
+    shortest streams' chain outputs on every host core and checks their DoP
+    bytes against the GPU's."""
+    import concurrent.futures as cf
+
+    import numpy as np
+    import torch
+    from foo_dsd_trellis_gb300 import ntf, signals
+    from foo_dsd_trellis_gb300.batch import OUT_DOP, BatchPlan, StreamSpec
+    from foo_dsd_trellis_gb300.fir import FirChain
+    from foo_dsd_trellis_gb300.pipeline import PCM_FIR_GAIN
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    layout = signals.multistream_layout(seed=1003 + 17 * rank, scale=args.ms_scale)
+    specs = [StreamSpec(e["fs_in"], e["fs_out"], e["channels"], e["frames"],
+                        ntf.auto_select_precorr(e["fs_out"]), state_limit=12.0,
+                        gain=PCM_FIR_GAIN, boxcar_taps=8, soft_clip=False, reposition=False,
+                        precorr=True) for e in layout]
+    pcms = [signals.multistream_pcm(e) for e in layout]
+    plan = BatchPlan(specs, seg_len=0, output_format=OUT_DOP, device=local,
+                     max_device_bytes=int(240e9))
+    info = plan.info()
+    plan.load([torch.from_numpy(x).cuda() for x in pcms])
+    for _ in range(args.warmup):
+        plan.run()
+    clocks = ClockSampler(local)
+    l0 = plan.launches()
+    tot_ms = []
+    clocks.start()
+    for _ in range(args.steps):
+        plan.run()
+        tot_ms.append(plan.times_ms()["total"])
+    clk = clocks.stop()
+    launches = (plan.launches() - l0) // max(1, args.steps)
+    total_s = max_over_ranks(sum(tot_ms) / 1000.0)
+    out_samples = int(info["out_samples"])
+    value = job_throughput(out_samples, args.steps, world, total_s)
+    rows = sum(s.channels for s in specs)
+    longest = max(s.frames * (s.fs_out // s.fs_in) for s in specs)
+    h_in = [torch.from_numpy(x).pin_memory().numpy() for x in pcms]
+    h_out = [torch.empty(plan.out_bytes(i), dtype=torch.uint8).pin_memory().numpy()
+             for i in range(len(specs))]
+    t0 = time.perf_counter()
+    plan.run_host(h_in, h_out)
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+        short = sorted(range(len(specs)), key=lambda i: specs[i].frames)[:8]
+        firs = {}
+        for i in short:
+            s = specs[i]
+            fc = FirChain(s.fs_in, s.fs_out, boxcar_taps=s.boxcar_taps, soft_clip=False,
+                          num_channels=s.channels, device=local)
+            firs[i] = fc.process(torch.from_numpy(pcms[i]).cuda(), PCM_FIR_GAIN, PCM_FIR_GAIN).cpu().numpy()
+            fc.close()
+        work = [(i, c) for i in short for c in range(specs[i].channels)]
+
+        def walk(ic):
+            i, c = ic
+            s = specs[i]
+            return O.PreCorr(s.ntf.order, np.array(s.ntf.a), np.array(s.ntf.g), 12.0).process(firs[i][c])
+
+        nthreads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(nthreads) as ex:
+            bits = list(ex.map(walk, work))
+        t_cpu = time.perf_counter() - t0
+        same = True
+        k = 0
+        for i in short:
+            s = specs[i]
+            per = []
+            for c in range(s.channels):
+                per.append(O.dop_pack_bits(bits[k], 0)[0].reshape(-1, 3))
+                k += 1
+            want = np.stack(per, axis=1).reshape(-1)
+            got = plan.out_view(i).cpu().numpy()
+            same = same and got.shape == want.shape and bool(np.array_equal(got, want))
+        n_cpu = sum(len(b) for b in bits)
+        cpu = {"value": n_cpu / t_cpu / 1e6, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": f"the 8 shortest streams ({len(work)} channel rows, {n_cpu} samples): "
+                         "the oracle's PreCorr on the GPU's chain output, one row per thread",
+               "bit_exact_with_gpu": same}
+    if rank == 0:
+        line = {"metric": MSP_METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1000 * total_s / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "multistream64_precorr", "streams": len(specs),
+                           "channel_rows": rows, "lengths_s": "U(0.5, 30) x %g" % args.ms_scale,
+                           "rates": [44100, 48000, 88200, 96000, 176400, 192000],
+                           "targets": "DSD128/DSD256 of the input's family",
+                           "ntf": "auto_select_precorr per rate", "state_limit": 12.0,
+                           "precorr_classes": "one per NTF", "output": "dop",
+                           "l2": "inputs far larger than L2"},
+                "xrt": sum(plan.out_samples(i) / s.fs_out for i, s in enumerate(specs)) *
+                       args.steps / total_s,
+                "e2e": {"value": out_samples * world / e2e_s / 1e6, "unit": UNIT,
+                        "h2d_bytes_per_step": int(sum(x.nbytes for x in pcms)),
+                        "d2h_bytes_per_step": int(sum(plan.out_bytes(i) for i in range(len(specs))))},
+                "walk": {"longest_row_samples": longest,
+                         "longest_row_msamples_per_s": longest * args.steps / total_s / 1e6,
+                         "note": "one thread per channel row: the step lasts as long as the "
+                                 "longest row's walk (the FP32 recurrence through the previous "
+                                 "output)"},
+                "roofline": None, "cpu_baseline": cpu, "clocks": clk,
+                "gpu_launches": int(launches), "plan": info, "stages_ms": plan.times_ms()}
         print(json.dumps(line), flush=True)
     plan.close()
 
@@ -1290,6 +1414,8 @@ def main():
         run_next(args)
     elif args.workload == "multistream64":
         run_multistream(args)
+    elif args.workload == "multistream64_precorr":
+        run_multistream_precorr(args)
     elif args.workload == "diff16":
         run_diff(args)
     elif args.workload == "dsd512conv6":

@@ -3,7 +3,9 @@
 `BatchPlan` converts many whole PCM streams (uneven lengths, mixed rates,
 mixed NTFs) in one pass: per-stream FIR chains, one persistent SDM launch per
 trellis parameter set over every DAS segment of every stream, one seam-search
-launch, per-stream assembly and packing, replayed from CUDA graphs.  Each
+launch, per-stream assembly and packing, replayed from CUDA graphs.  Streams
+marked `precorr` run the PreCorr greedy SDM instead (one launch per PreCorr
+parameter set over all such channels, one thread each).  Each
 stream's output equals the single-stream pipeline (dsdgpu_pipeline_process,
 the reference's plugin PCM path src/dsp_plugin.c:2990-3216 with full-parallel
 DAS) run on a fresh context with the same parameters.
@@ -37,6 +39,7 @@ class StreamSpec:
     boxcar_taps: int = 8
     soft_clip: bool = True
     reposition: bool = True
+    precorr: bool = False      # PreCorr greedy SDM instead of the DAS trellis
 
     def desc(self) -> _lib.StreamDesc:
         d = _lib.StreamDesc()
@@ -49,6 +52,7 @@ class StreamSpec:
             d.sdm.g[i] = float(self.ntf.g[i])
         d.sdm.depth, d.sdm.cands, d.sdm.lat = self.depth, self.cands, self.lat
         d.sdm.state_limit = float(self.state_limit)
+        d.sdm_mode = _lib.SDM_PRECORR if self.precorr else _lib.SDM_TRELLIS
         return d
 
 

@@ -43,6 +43,18 @@ void decim_free(dsdgpu_decim_state* s);
 struct dsdgpu_lowpass_state;  // same-rate FIR lowpass (lowpass.cu)
 void lowpass_free(dsdgpu_lowpass_state* s);
 struct dsdgpu_precorr_state;  // PreCorr greedy SDM (precorr.cu)
+// PreCorr rows of the batch plan: one channel of a stream, walked from fresh state
+struct PcBatchRow {
+  const float* in;
+  long long count;
+  uint8_t* out;
+};
+size_t precorr_table_floats();
+int precorr_batch_train(int order, const double* a, const double* g, double limit, float* d_table,
+                        cudaStream_t stream);
+int launch_precorr_batch(int order, const double* a, const double* g, double limit,
+                         const float* d_table, const PcBatchRow* d_rows, int nrows,
+                         cudaStream_t stream);
 void precorr_free(dsdgpu_precorr_state* s);
 struct dsdgpu_context;
 // PreCorr decisions for channels [first, first + nch) of the context's state

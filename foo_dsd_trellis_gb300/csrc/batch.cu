@@ -67,7 +67,10 @@ struct StreamPlan {
   std::vector<size_t> seg_off;          // per segment, within a channel's row
   size_t bits_off = 0, bits_stride = 0; // stitched decision rows
   size_t out_off = 0, out_stride = 0, out_bytes = 0;
-  int cls = 0;
+  int cls = 0;                          // trellis parameter class (-1: a PreCorr stream)
+  bool precorr = false;
+  int pc_cls = -1;                      // PreCorr parameter class
+  size_t f32_off = 0, f32_stride = 0;   // FP32 chain output of a PreCorr stream (floats)
   int lat = 0;
   size_t overlap = 0;
   int S = 0;
@@ -95,6 +98,17 @@ struct SdmClass {
   int scratch_first = 0;                // its CTAs' scratch contexts
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+// Streams in PreCorr mode with one NTF and limit: one table, one launch.
+struct PcClass {
+  int order = 0;
+  double a[kMaxOrder] = {}, g[kMaxOrder] = {};
+  double limit = 0.0;
+  int row_first = 0, nrows = 0;
+  long long samples = 0;
+  cudaStream_t side = nullptr;
+  cudaEvent_t join = nullptr;
 };
 
 // Layout of one stream for a given segment length: the segment inputs and the
@@ -129,6 +143,9 @@ struct dsdgpu_plan {
   double predicted_ms = 0;
   std::vector<StreamPlan> st;
   std::vector<SdmClass> cls;
+  std::vector<PcClass> pcls;
+  std::vector<PcBatchRow> pcrows;
+  long long pc_samples = 0;
   std::vector<SdmJob> jobs;
   std::vector<SeamTask> tasks;
   std::vector<AssemblePiece> pieces;
@@ -143,6 +160,10 @@ struct dsdgpu_plan {
   size_t arena_bytes = 0;
   float* d_pcm = nullptr;
   double* d_fir = nullptr;
+  float* d_f32 = nullptr;              // FP32 chain outputs of the PreCorr streams
+  float* d_pctab = nullptr;            // PreCorr tables, one per class
+  PcBatchRow* d_pcrows = nullptr;
+  cudaEvent_t fork = nullptr;          // graph 2's fork point (several launches)
   uint8_t* d_seg = nullptr;
   uint8_t* d_bits = nullptr;
   uint8_t* d_out = nullptr;
@@ -182,6 +203,11 @@ dsdgpu_plan::~dsdgpu_plan() {
     if (k.fork) cudaEventDestroy(k.fork);
     if (k.join) cudaEventDestroy(k.join);
   }
+  for (auto& k : pcls) {
+    if (k.side) cudaStreamDestroy(k.side);
+    if (k.join) cudaEventDestroy(k.join);
+  }
+  if (fork) cudaEventDestroy(fork);
   for (cudaEvent_t e : ev)
     if (e) cudaEventDestroy(e);
   if (h_rms) cudaFreeHost(h_rms);
@@ -309,6 +335,7 @@ double model_seconds(const std::vector<StreamPlan>& st, const std::vector<SdmCla
   std::vector<double> W(nc, 0.0), Lmax(nc, 0.0);
   long long J = 0;
   for (const StreamPlan& s0 : st) {
+    if (s0.precorr) continue;
     StreamPlan s = s0;
     layout_stream(s, seg_len);
     segment_io(s);
@@ -334,7 +361,6 @@ double model_seconds(const std::vector<StreamPlan>& st, const std::vector<SdmCla
 
 // ---- plan construction -----------------------------------------------------
 
-int build_tables(dsdgpu_plan* pl);
 int upload_stream_rows(dsdgpu_plan* pl, StreamPlan& s, cudaStream_t stream);
 
 int capture_graphs(dsdgpu_plan* pl) {
@@ -348,9 +374,17 @@ int capture_graphs(dsdgpu_plan* pl) {
   for (StreamPlan& s : pl->st) {
     const double gain = s.d.gain;
     const int apply = gain != 1.0 ? 1 : 0;
-    if (launch_fir_chain(s.F, s.fir_smem, pl->d_pcm + s.pcm_off, s.pcm_stride, s.d.frames,
-                         pl->d_hist, pl->d_fir + s.fir_off, s.fir_stride, gain, 0.0, apply,
-                         s.d.soft_clip, s.d.channels, m) != 0) {
+    // PreCorr streams: FP32 out (the values the walk reads), no soft clip
+    // ahead of PreCorr (the pipeline in that mode, src/engine.c:557-559)
+    const int r = s.precorr
+                      ? launch_fir_chain(s.F, s.fir_smem, pl->d_pcm + s.pcm_off, s.pcm_stride,
+                                         s.d.frames, pl->d_hist, pl->d_f32 + s.f32_off,
+                                         s.f32_stride, gain, 0.0, apply, 0, s.d.channels, m)
+                      : launch_fir_chain(s.F, s.fir_smem, pl->d_pcm + s.pcm_off, s.pcm_stride,
+                                         s.d.frames, pl->d_hist, pl->d_fir + s.fir_off,
+                                         s.fir_stride, gain, 0.0, apply, s.d.soft_clip,
+                                         s.d.channels, m);
+    if (r != 0) {
       rc = DSDGPU_ERR_CUDA;
       break;
     }
@@ -376,10 +410,11 @@ int capture_graphs(dsdgpu_plan* pl) {
   // waits on one fork point; the main stream joins them all at the end)
   if (cudaStreamBeginCapture(m, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
     return c->cuda_fail(cudaGetLastError(), "graph capture");
-  const bool forked = pl->cls.size() > 1;
+  const bool forked = pl->cls.size() + pl->pcls.size() > 1;
   if (forked) {
-    cudaEventRecord(pl->cls[0].fork, m);
-    for (SdmClass& K : pl->cls) cudaStreamWaitEvent(K.side, pl->cls[0].fork, 0);
+    cudaEventRecord(pl->fork, m);
+    for (SdmClass& K : pl->cls) cudaStreamWaitEvent(K.side, pl->fork, 0);
+    for (PcClass& Q : pl->pcls) cudaStreamWaitEvent(Q.side, pl->fork, 0);
   }
   for (size_t k = 0; k < pl->cls.size() && !rc; k++) {
     SdmClass& K = pl->cls[k];
@@ -390,11 +425,22 @@ int capture_graphs(dsdgpu_plan* pl) {
                         c->d_status, K.grid, forked ? K.side : m) != 0)
       rc = DSDGPU_ERR_CUDA;
   }
-  if (forked)
+  for (size_t q = 0; q < pl->pcls.size() && !rc; q++) {
+    PcClass& Q = pl->pcls[q];
+    if (launch_precorr_batch(Q.order, Q.a, Q.g, Q.limit, pl->d_pctab + q * precorr_table_floats(),
+                             pl->d_pcrows + Q.row_first, Q.nrows, forked ? Q.side : m) != 0)
+      rc = DSDGPU_ERR_CUDA;
+  }
+  if (forked) {
     for (SdmClass& K : pl->cls) {
       cudaEventRecord(K.join, K.side);
       cudaStreamWaitEvent(m, K.join, 0);
     }
+    for (PcClass& Q : pl->pcls) {
+      cudaEventRecord(Q.join, Q.side);
+      cudaStreamWaitEvent(m, Q.join, 0);
+    }
+  }
   e = cudaStreamEndCapture(m, &g);
   if (rc || e != cudaSuccess) {
     if (g) cudaGraphDestroy(g);
@@ -416,7 +462,9 @@ int capture_graphs(dsdgpu_plan* pl) {
   for (StreamPlan& s : pl->st) {
     if (rc) break;
     const int nch = s.d.channels;
-    if (launch_das_assemble(pl->d_pieces + s.piece_first, s.npieces, pl->d_bp + s.bp_base,
+    // PreCorr streams wrote their decision rows directly
+    if (!s.precorr &&
+        launch_das_assemble(pl->d_pieces + s.piece_first, s.npieces, pl->d_bp + s.bp_base,
                             pl->d_bits + s.bits_off, s.bits_stride, nch, s.S,
                             pl->d_segbuf + s.segbuf_first, m) != 0) {
       rc = DSDGPU_ERR_CUDA;
@@ -475,6 +523,7 @@ bool rows_in_bounds(const dsdgpu_plan* pl, const StreamPlan& s) {
 // layout (the rows' positions in the tables are fixed at plan creation).
 // Returns false when a row would reach outside the stream's buffers.
 bool fill_stream_rows(dsdgpu_plan* pl, StreamPlan& s) {
+  if (s.precorr) return true;   // no segments: its rows are the PreCorr rows
   segment_io(s);
   const int nch = s.d.channels;
   s.seg_off.assign(s.S, 0);
@@ -562,12 +611,43 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
     s.fir_smem = chain_smem_bytes(s.F);
     if (s.fir_smem > (size_t)kFirMaxSmem)
       return bail(c->fail(DSDGPU_ERR_UNSUPPORTED, "fir tile does not fit shared memory"));
+    if (d.sdm_mode != DSDGPU_SDM_TRELLIS && d.sdm_mode != DSDGPU_SDM_PRECORR)
+      return bail(c->fail(DSDGPU_ERR_ARG, "bad sdm mode"));
+    s.precorr = d.sdm_mode == DSDGPU_SDM_PRECORR;
+    s.n_fir = (size_t)d.frames * (size_t)s.F.ratio;
+    if (s.precorr) {
+      // the checks of dsdgpu_precorr_setup; K, depth and lat are not used
+      const dsdgpu_sdm_params_t& q = d.sdm;
+      if (q.order < 2 || q.order > kMaxOrder)
+        return bail(c->fail(DSDGPU_ERR_ARG, "NTF order out of range (2..10)"));
+      if (!(q.state_limit >= 0.0)) return bail(c->fail(DSDGPU_ERR_ARG, "state limit must be >= 0"));
+      s.cls = -1;
+      int k = -1;
+      for (size_t j = 0; j < pl->pcls.size() && k < 0; j++) {
+        const PcClass& Q = pl->pcls[j];
+        bool same = Q.order == q.order && Q.limit == q.state_limit;
+        for (int i = 0; same && i < q.order; i++) same = Q.a[i] == q.a[i] && Q.g[i] == q.g[i];
+        if (same) k = (int)j;
+      }
+      if (k < 0) {
+        PcClass Q;
+        Q.order = q.order;
+        for (int i = 0; i < q.order; i++) {
+          Q.a[i] = q.a[i];
+          Q.g[i] = q.g[i];
+        }
+        Q.limit = q.state_limit;
+        pl->pcls.push_back(Q);
+        k = (int)pl->pcls.size() - 1;
+      }
+      s.pc_cls = k;
+      continue;
+    }
     SdmParams P;
     const char* err = nullptr;
     const int prc = sdm_params_from_abi(&d.sdm, &P, &err);
     if (prc) return bail(c->fail(prc, err));
     P.lanes = c->sdm_lanes;   // part of the class: the plan's job slots depend on it
-    s.n_fir = (size_t)d.frames * (size_t)s.F.ratio;
     s.lat = P.lat;
     s.overlap = 64 * (size_t)P.lat;
     int k = -1;
@@ -616,33 +696,45 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
 
   // ---- layouts, sizes, table positions ----
   size_t pcm_total = 0, fir_total = 0, seg_total = 0, bits_total = 0, out_total = 0;
+  size_t f32_total = 0;
   for (StreamPlan& s : pl->st) {
-    layout_stream(s, pl->seg_len);
-    segment_io(s);
     const int nch = s.d.channels;
     s.pcm_stride = align_up((size_t)s.d.frames, 64);
     s.pcm_off = pcm_total;
     pcm_total += s.pcm_stride * nch;
-    s.fir_stride = align_up(s.n_fir, 32);
-    s.fir_off = fir_total;
-    fir_total += s.fir_stride * nch;
-    // a reposition moves samples between neighbouring segments but keeps their
-    // sum: 256 bytes of slack per segment cover the per-segment alignment
-    size_t row = 0;
-    for (int k = 0; k < s.S; k++) row += align_up((size_t)s.in_cnt[k], 256);
-    s.seg_row = row + 256 * (size_t)s.S;
-    s.seg_off0 = seg_total;
-    seg_total += s.seg_row * nch;
-    s.bits_stride = align_up(s.n_fir, 256);
-    s.bits_off = bits_total;
-    bits_total += s.bits_stride * nch;
-    // final count does not depend on the seams or on the reposition
     std::vector<SeamPlan> sp;
     std::vector<AssemblePiece> pc;
-    const char* err = nullptr;
-    if (das_stream_plan(s.S, s.seg_out.data(), s.size, s.overlap, false, sp, pc, &s.final_count,
-                        &err) != 0)
-      return bail(c->fail(DSDGPU_ERR_UNSUPPORTED, err));
+    if (s.precorr) {
+      s.S = 0;
+      s.f32_stride = align_up(s.n_fir, 64);
+      s.f32_off = f32_total;
+      f32_total += s.f32_stride * nch;
+      s.bits_stride = align_up(s.n_fir, 256);
+      s.bits_off = bits_total;
+      bits_total += s.bits_stride * nch;
+      s.final_count = (long long)s.n_fir;   // one decision per input, no latency
+    } else {
+      layout_stream(s, pl->seg_len);
+      segment_io(s);
+      s.fir_stride = align_up(s.n_fir, 32);
+      s.fir_off = fir_total;
+      fir_total += s.fir_stride * nch;
+      // a reposition moves samples between neighbouring segments but keeps their
+      // sum: 256 bytes of slack per segment cover the per-segment alignment
+      size_t row = 0;
+      for (int k = 0; k < s.S; k++) row += align_up((size_t)s.in_cnt[k], 256);
+      s.seg_row = row + 256 * (size_t)s.S;
+      s.seg_off0 = seg_total;
+      seg_total += s.seg_row * nch;
+      s.bits_stride = align_up(s.n_fir, 256);
+      s.bits_off = bits_total;
+      bits_total += s.bits_stride * nch;
+      // final count does not depend on the seams or on the reposition
+      const char* err = nullptr;
+      if (das_stream_plan(s.S, s.seg_out.data(), s.size, s.overlap, false, sp, pc, &s.final_count,
+                          &err) != 0)
+        return bail(c->fail(DSDGPU_ERR_UNSUPPORTED, err));
+    }
     const size_t n = (size_t)s.final_count;
     if (pl->fmt == DSDGPU_OUT_DOP) {
       s.out_stride = (n / 16) * 3 * (size_t)nch;
@@ -662,7 +754,20 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
     s.npieces = (int)pc.size();
     for (const SeamPlan& t : sp) pl->max_ovl = std::max(pl->max_ovl, t.ovl_len);
     pl->out_samples += (long long)n * nch;
-    if (s.d.reposition && s.S > 2) das_reposition_centers(s.nom_start, s.n_fir, s.centers, s.which);
+    if (!s.precorr && s.d.reposition && s.S > 2)
+      das_reposition_centers(s.nom_start, s.n_fir, s.centers, s.which);
+  }
+  // PreCorr rows: class-major, then stream, channel (pointers set with the arena)
+  for (size_t q = 0; q < pl->pcls.size(); q++) {
+    PcClass& Q = pl->pcls[q];
+    Q.row_first = (int)pl->pcrows.size();
+    for (StreamPlan& s : pl->st) {
+      if (!s.precorr || s.pc_cls != (int)q) continue;
+      for (int ch = 0; ch < s.d.channels; ch++) pl->pcrows.push_back(PcBatchRow{nullptr, 0, nullptr});
+      Q.samples += (long long)s.n_fir * s.d.channels;
+    }
+    Q.nrows = (int)pl->pcrows.size() - Q.row_first;
+    pl->pc_samples += Q.samples;
   }
   // jobs: class-major, then stream, segment, channel
   int njobs = 0;
@@ -720,6 +825,9 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
   std::vector<Part> parts = {
       {(void**)&pl->d_pcm, sizeof(float) * pcm_total},
       {(void**)&pl->d_fir, sizeof(double) * fir_total},
+      {(void**)&pl->d_f32, sizeof(float) * f32_total},
+      {(void**)&pl->d_pctab, sizeof(float) * precorr_table_floats() * pl->pcls.size()},
+      {(void**)&pl->d_pcrows, sizeof(PcBatchRow) * pl->pcrows.size()},
       {(void**)&pl->d_seg, seg_total},
       {(void**)&pl->d_bits, bits_total},
       {(void**)&pl->d_out, out_total},
@@ -785,12 +893,38 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
   if (init_contexts(pl->d_ctx, 0, 1, 0, m) != 0)
     return bail(c->cuda_fail(cudaGetLastError(), "context init"));
   c->launches++;
-  for (SdmClass& K : pl->cls)
-    if (pl->cls.size() > 1 &&
-        (cudaStreamCreateWithFlags(&K.side, cudaStreamNonBlocking) != cudaSuccess ||
-         cudaEventCreateWithFlags(&K.fork, cudaEventDisableTiming) != cudaSuccess ||
-         cudaEventCreateWithFlags(&K.join, cudaEventDisableTiming) != cudaSuccess))
-      return bail(c->cuda_fail(cudaGetLastError(), "class streams"));
+  {
+    size_t r = 0;
+    for (size_t q = 0; q < pl->pcls.size(); q++)
+      for (StreamPlan& s : pl->st) {
+        if (!s.precorr || s.pc_cls != (int)q) continue;
+        for (int ch = 0; ch < s.d.channels; ch++)
+          pl->pcrows[r++] = PcBatchRow{pl->d_f32 + s.f32_off + (size_t)ch * s.f32_stride,
+                                       (long long)s.n_fir,
+                                       pl->d_bits + s.bits_off + (size_t)ch * s.bits_stride};
+      }
+    if (!pl->pcrows.empty())
+      cudaMemcpyAsync(pl->d_pcrows, pl->pcrows.data(), sizeof(PcBatchRow) * pl->pcrows.size(),
+                      cudaMemcpyHostToDevice, m);
+    for (size_t q = 0; q < pl->pcls.size(); q++) {
+      const PcClass& Q = pl->pcls[q];
+      if (precorr_batch_train(Q.order, Q.a, Q.g, Q.limit, pl->d_pctab + q * precorr_table_floats(),
+                              m) != 0)
+        return bail(c->cuda_fail(cudaGetLastError(), "precorr table"));
+      c->launches++;
+    }
+  }
+  if (pl->cls.size() + pl->pcls.size() > 1) {
+    // graph 2 forks one side stream per launch
+    bool ok = cudaEventCreateWithFlags(&pl->fork, cudaEventDisableTiming) == cudaSuccess;
+    for (SdmClass& K : pl->cls)
+      ok = ok && cudaStreamCreateWithFlags(&K.side, cudaStreamNonBlocking) == cudaSuccess &&
+           cudaEventCreateWithFlags(&K.join, cudaEventDisableTiming) == cudaSuccess;
+    for (PcClass& Q : pl->pcls)
+      ok = ok && cudaStreamCreateWithFlags(&Q.side, cudaStreamNonBlocking) == cudaSuccess &&
+           cudaEventCreateWithFlags(&Q.join, cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) return bail(c->cuda_fail(cudaGetLastError(), "class streams"));
+  }
   for (cudaEvent_t& ev : pl->ev)
     if (cudaEventCreate(&ev) != cudaSuccess) return bail(c->cuda_fail(cudaGetLastError(), "events"));
   // function attributes are set outside the capture
@@ -913,8 +1047,11 @@ int dsdgpu_plan_run(dsdgpu_plan_t* pl) {
   e = cudaGraphLaunch(pl->g3, m);
   if (e != cudaSuccess) return c->cuda_fail(e, "graph 3 launch");
   cudaEventRecord(pl->ev[4], m);
-  c->launches += pl->cls.size() + (pl->tasks.empty() ? 0 : 1) +
-                 pl->st.size() * (pl->fmt == DSDGPU_OUT_BITS ? 1 : 2);
+  size_t npc = 0;
+  for (const StreamPlan& s : pl->st) npc += s.precorr ? 1 : 0;
+  // per stream: assembly (trellis streams) and packing (unless BITS)
+  c->launches += pl->cls.size() + pl->pcls.size() + (pl->tasks.empty() ? 0 : 1) +
+                 (pl->st.size() - npc) + (pl->fmt == DSDGPU_OUT_BITS ? 0 : pl->st.size());
   c->sdm_samples += (unsigned long long)pl->sdm_samples;
   c->sdm_last_samples = (unsigned long long)pl->sdm_samples;
   rc = c->check_status();

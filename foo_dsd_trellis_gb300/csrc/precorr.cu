@@ -343,6 +343,42 @@ __global__ void precorr_reset_kernel(PcState* states, int nch) {
   states[c] = st;
 }
 
+// The batch plan's PreCorr streams: one thread per row (a channel of a
+// stream), each from fresh state (precorr_context_init) over its own count,
+// rows of one class (NTF and limit) per launch.
+__global__ void __launch_bounds__(32) precorr_batch_kernel(const __grid_constant__ PcCoef C,
+                                                           const float* __restrict__ table,
+                                                           const PcBatchRow* __restrict__ rows,
+                                                           int nrows) {
+  __shared__ uint8_t codes[kPcPhases * kPcHist];
+  for (int i = threadIdx.x; i < kPcPhases * kPcHist; i += blockDim.x) {
+    const int ph = i / kPcHist, h2 = (2 * (i % kPcHist)) & 0xFF;
+    codes[i] = (uint8_t)(pc_code(table[h2 * kPcPhases + ph]) |
+                         (pc_code(table[(h2 + 1) * kPcPhases + ph]) << 2));
+  }
+  __syncthreads();
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const PcBatchRow row = rows[r];
+  PcState st;
+  for (int k = 0; k < 10; k++) st.s[k] = 0.0f;
+  st.prev_y = 0.0f;
+  st.history = kPcHistInit;
+  st.phase = 0;
+  st.pad = 0;
+  switch (C.order) {
+    case 2: pc_run_lim<2>(C, codes, st, row.in, row.count, row.out); break;
+    case 3: pc_run_lim<3>(C, codes, st, row.in, row.count, row.out); break;
+    case 4: pc_run_lim<4>(C, codes, st, row.in, row.count, row.out); break;
+    case 5: pc_run_lim<5>(C, codes, st, row.in, row.count, row.out); break;
+    case 6: pc_run_lim<6>(C, codes, st, row.in, row.count, row.out); break;
+    case 7: pc_run_lim<7>(C, codes, st, row.in, row.count, row.out); break;
+    case 8: pc_run_lim<8>(C, codes, st, row.in, row.count, row.out); break;
+    case 9: pc_run_lim<9>(C, codes, st, row.in, row.count, row.out); break;
+    default: pc_run_lim<10>(C, codes, st, row.in, row.count, row.out); break;
+  }
+}
+
 // FP64 rows narrowed to FP32 in one wide pass (all lanes of every warp
 // busy), so the walk's loop carries no conversion: out[ch][j] =
 // float(in[ch][j]), rounded to nearest as the walk would round them.
@@ -373,6 +409,35 @@ struct dsdgpu_precorr_state {
 };
 
 void precorr_free(dsdgpu_precorr_state* s) { delete s; }
+
+// precorr_context_init's float copies of the coefficients (src/precorr.c:198-220).
+static PcCoef pc_coef(int order, const double* a, const double* g, double limit) {
+  PcCoef C{};
+  C.order = order;
+  for (int i = 0; i < 10; i++) {
+    C.a[i] = i < order ? (float)a[i] : 0.0f;
+    C.g[i] = i < order ? (float)g[i] : 0.0f;
+  }
+  C.limit = (float)limit;
+  return C;
+}
+
+size_t precorr_table_floats() { return (size_t)kPcTable; }
+
+int precorr_batch_train(int order, const double* a, const double* g, double limit, float* d_table,
+                        cudaStream_t stream) {
+  precorr_train_kernel<<<1, 256, 0, stream>>>(pc_coef(order, a, g, limit), d_table);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_precorr_batch(int order, const double* a, const double* g, double limit,
+                         const float* d_table, const PcBatchRow* d_rows, int nrows,
+                         cudaStream_t stream) {
+  if (nrows <= 0) return 0;
+  precorr_batch_kernel<<<(nrows + 31) / 32, 32, 0, stream>>>(pc_coef(order, a, g, limit), d_table,
+                                                            d_rows, nrows);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
 
 // The pipeline's SDM stage in PreCorr mode (src/engine.c:557-559, 723-726):
 // FP32 input (the reference's walk reads floats).
@@ -423,13 +488,7 @@ int dsdgpu_precorr_setup(dsdgpu_context_t* c, int order, const double* a, const 
   cudaSetDevice(c->device);
   dsdgpu_precorr_state* s = new (std::nothrow) dsdgpu_precorr_state();
   if (!s) return DSDGPU_ERR_NOMEM;
-  // precorr_context_init keeps float copies of the coefficients (src/precorr.c:198-220)
-  s->coef.order = order;
-  for (int i = 0; i < 10; i++) {
-    s->coef.a[i] = i < order ? (float)a[i] : 0.0f;
-    s->coef.g[i] = i < order ? (float)g[i] : 0.0f;
-  }
-  s->coef.limit = (float)state_limit;
+  s->coef = pc_coef(order, a, g, state_limit);
   s->nch = nch;
   if (cudaMalloc(&s->d_table, sizeof(float) * kPcTable) != cudaSuccess ||
       cudaMalloc(&s->d_states, sizeof(PcState) * (size_t)nch) != cudaSuccess) {

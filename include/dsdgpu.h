@@ -402,6 +402,11 @@ int dsdgpu_sdm_estimate_state(dsdgpu_context_t *ctx, const dsdgpu_sdm_params_t *
  * converts one stream per plugin instance; each stream's output equals
  * dsdgpu_pipeline_process on a fresh context with the same parameters
  * (constant gain, full-parallel DAS seeding, src/dsp_plugin.c:2185-2283).
+ * A stream with sdm_mode DSDGPU_SDM_PRECORR runs the PreCorr greedy SDM
+ * instead (src/precorr.c:20-287; K, depth and lat unused, no soft clip
+ * ahead of it, as the pipeline in that mode): its chain writes FP32 and one
+ * launch per PreCorr parameter set walks every such channel of every stream,
+ * one thread each, beside the trellis launches.
  * Each run converts whole streams from fresh state. */
 typedef struct {
     int32_t fs_in;             /* PCM rate, Hz */
@@ -413,6 +418,7 @@ typedef struct {
     int32_t soft_clip;         /* tanh soft clip above +-0.95 */
     int32_t reposition;        /* RMS reposition of quiet DAS boundaries */
     dsdgpu_sdm_params_t sdm;   /* NTF, K, depth, lat, state limit */
+    int32_t sdm_mode;          /* DSDGPU_SDM_TRELLIS (DAS trellis) or DSDGPU_SDM_PRECORR */
 } dsdgpu_stream_desc_t;
 
 typedef struct {

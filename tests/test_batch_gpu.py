@@ -8,6 +8,8 @@ rates of both families, DSD128 and DSD256 targets (CLANS-6 and CLANS-8, two
 SDM parameter sets in one plan), uneven lengths, and one stream with a quiet
 stretch over a DAS boundary (the host reposition path between the graphs).
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -153,6 +155,92 @@ def test_batch_rejects_bad_streams():
     with pytest.raises(_lib.DsdGpuError) as e:
         BatchPlan([StreamSpec(44100, 5644800, 2, 100000, f)], seg_len=32768, max_device_bytes=1 << 20)
     assert e.value.code == _lib.ERR_TOO_LARGE
+    # an unknown SDM mode, and a PreCorr stream with an NTF order out of range
+    L = _lib.load()
+    h = C.c_void_p()
+    assert L.dsdgpu_create(0, C.byref(h)) == 0
+    p = C.c_void_p()
+    d = StreamSpec(44100, 5644800, 2, 1000, f).desc()
+    d.sdm_mode = 7
+    assert L.dsdgpu_plan_create(h, C.byref(d), 1, 32768, _lib.OUT_BITS, 0, C.byref(p)) == _lib.ERR_ARG
+    d = StreamSpec(44100, 5644800, 2, 1000, f, precorr=True).desc()
+    d.sdm.order = 11
+    assert L.dsdgpu_plan_create(h, C.byref(d), 1, 32768, _lib.OUT_BITS, 0, C.byref(p)) == _lib.ERR_ARG
+    L.dsdgpu_destroy(h)
+
+
+def _precorr_want(oracle, s, x, fmt):
+    """A PreCorr stream from fresh state: its FIR chain without the soft clip
+    (the engine does not clip ahead of PreCorr), then the oracle's PreCorr per
+    channel (pinned to src/precorr.c), packed as the plan packs."""
+    from foo_dsd_trellis_gb300.batch import OUT_BITS
+    from foo_dsd_trellis_gb300.fir import FirChain
+    fc = FirChain(s.fs_in, s.fs_out, boxcar_taps=s.boxcar_taps, soft_clip=False,
+                  num_channels=s.channels)
+    fir = fc.process(torch.from_numpy(x).cuda(), GAIN, GAIN).cpu().numpy()
+    fc.close()
+    bits = np.stack([oracle.PreCorr(s.ntf.order, np.array(s.ntf.a), np.array(s.ntf.g),
+                                    s.state_limit).process(fir[c]) for c in range(s.channels)])
+    if fmt == OUT_BITS:
+        return bits
+    per = [oracle.dop_pack_bits(bits[c], 0)[0].reshape(-1, 3) for c in range(s.channels)]
+    return np.stack(per, axis=1).reshape(-1)
+
+
+@pytest.mark.parametrize("fmt", [0, 1], ids=["bits", "dop"])
+def test_batch_precorr_streams(oracle, fmt):
+    """PreCorr streams in a batch beside trellis streams: two PreCorr parameter
+    sets (DSD64 without the limiter; DSD128 at 44.1 and 48 kHz with limit 12,
+    sharing one table when their NTFs agree), uneven lengths, a mono stream.
+    Each PreCorr stream equals its chain followed by the oracle's PreCorr from
+    fresh state; each trellis stream still equals the single-stream path."""
+    from foo_dsd_trellis_gb300 import ntf
+    from foo_dsd_trellis_gb300.batch import BatchPlan, StreamSpec
+    specs = _specs()[:2]
+    for (fi, fo, frames, lim, ch) in [(44100, 2822400, 3000, 0.0, 2), (48000, 6144000, 1500, 12.0, 2),
+                                      (44100, 5644800, 2200, 12.0, 1)]:
+        specs.append(StreamSpec(fi, fo, ch, frames, ntf.auto_select_precorr(fo), gain=GAIN,
+                                boxcar_taps=8, soft_clip=True, state_limit=lim, precorr=True))
+    xs = _inputs(specs)
+    plan = BatchPlan(specs, seg_len=32768, output_format=fmt)
+    assert plan.info()["classes"] == 2
+    plan.load([torch.from_numpy(x).cuda() for x in xs])
+    plan.run()
+    for i, s in enumerate(specs):
+        if s.precorr:
+            want = _precorr_want(oracle, s, xs[i], fmt)
+            assert plan.out_samples(i) == s.frames * (s.fs_out // s.fs_in)
+        else:
+            want, _ = _oracle_stream(oracle, s, xs[i], 32768, fmt)
+        got = plan.out_view(i).cpu().numpy()
+        assert got.shape == want.shape, (i, got.shape, want.shape)
+        assert np.array_equal(got, want), f"stream {i}"
+    plan.close()
+
+
+def test_batch_precorr_only():
+    """A plan of PreCorr streams alone (no trellis launch, no seams), run twice:
+    the second run equals the first (every run starts from fresh state), and
+    the host-buffer form equals the device form."""
+    from foo_dsd_trellis_gb300 import ntf
+    from foo_dsd_trellis_gb300.batch import OUT_DOP, BatchPlan, StreamSpec
+    specs = [StreamSpec(44100, 2822400, 2, 4000, ntf.auto_select_precorr(2822400), gain=GAIN,
+                        precorr=True),
+             StreamSpec(96000, 12288000, 2, 1000, ntf.auto_select_precorr(12288000), gain=GAIN,
+                        state_limit=12.0, precorr=True)]
+    xs = [_noise(s.frames, s.channels, 71 + i) for i, s in enumerate(specs)]
+    plan = BatchPlan(specs, seg_len=0, output_format=OUT_DOP)
+    assert plan.info()["classes"] == 0 and plan.info()["jobs"] == 0
+    plan.load([torch.from_numpy(x).cuda() for x in xs])
+    plan.run()
+    first = [plan.out_view(i).cpu().numpy().copy() for i in range(len(specs))]
+    plan.run()
+    for i in range(len(specs)):
+        assert np.array_equal(plan.out_view(i).cpu().numpy(), first[i])
+    outs = plan.run_host(xs)
+    for i in range(len(specs)):
+        assert np.array_equal(outs[i], first[i])
+    plan.close()
 
 
 def test_batch_small_k_path_table_parameters(oracle):
