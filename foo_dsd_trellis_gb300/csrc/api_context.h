@@ -73,6 +73,15 @@ int conv_run(dsdgpu_context* c, int nch, const double* d_in, size_t in_stride, s
              double* d_out, size_t out_stride);
 void conv_free(dsdgpu_conv_state* s);
 int samerate_boxcar_taps(unsigned fs);   // engine_init's same-rate boxcar length
+// context-free launchers of the DSD-input kernels (dsd_in.cu), fresh state
+size_t boxcar_hist_bytes(int nch);
+int launch_dop_unpack(const float* dop, size_t dop_stride, long long frames, int nch,
+                      uint8_t* bits, size_t bits_stride, cudaStream_t stream);
+int launch_dop_unpack_f32(const float* dop, size_t dop_stride, long long frames, int nch,
+                          float* out, size_t out_stride, cudaStream_t stream);
+int launch_boxcar_fresh(const uint8_t* bits, size_t bits_stride, long long count,
+                        const int8_t* zero_hist, int taps, int nch, double g_start, double g_step,
+                        double* out, size_t out_stride, cudaStream_t stream);
 
 struct dsdgpu_context {
   int device = 0;

@@ -53,6 +53,7 @@ constexpr long long kTuneSegLens[] = {32768, 49152, 65536, 98304, 131072};
 constexpr int kTuneBps[] = {8, 12, 16};  // resident SDM warps per SM (16 = register limit)
 constexpr int kTuneWarpLevels[] = {1, 4, 8, 12, 16};
 constexpr long long kTuneSamples = 1024;
+constexpr int kDsd64Rate = 2822400;   // input at this rate or above is DoP (DSD)
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
@@ -70,7 +71,12 @@ struct StreamPlan {
   int cls = 0;                          // trellis parameter class (-1: a PreCorr stream)
   bool precorr = false;
   int pc_cls = -1;                      // PreCorr parameter class
-  size_t f32_off = 0, f32_stride = 0;   // FP32 chain output of a PreCorr stream (floats)
+  // DoP input (fs_in a DSD rate): 1 = same rate (unpack, boxcar of box_taps),
+  // 2 = to a higher DSD rate (unpack to +-1 floats, the FIR chain); 0 = PCM
+  int dsd_mode = 0;
+  int box_taps = 0;
+  size_t f32_off = 0, f32_stride = 0;   // FP32 rows: a PreCorr stream's chain output, or a
+                                        // DSD-up stream's unpacked +-1 input (floats)
   int lat = 0;
   size_t overlap = 0;
   int S = 0;
@@ -163,6 +169,7 @@ struct dsdgpu_plan {
   float* d_f32 = nullptr;              // FP32 chain outputs of the PreCorr streams
   float* d_pctab = nullptr;            // PreCorr tables, one per class
   PcBatchRow* d_pcrows = nullptr;
+  int8_t* d_boxhist = nullptr;         // zero boxcar history of the same-rate DSD streams
   cudaEvent_t fork = nullptr;          // graph 2's fork point (several launches)
   uint8_t* d_seg = nullptr;
   uint8_t* d_bits = nullptr;
@@ -374,16 +381,36 @@ int capture_graphs(dsdgpu_plan* pl) {
   for (StreamPlan& s : pl->st) {
     const double gain = s.d.gain;
     const int apply = gain != 1.0 ? 1 : 0;
-    // PreCorr streams: FP32 out (the values the walk reads), no soft clip
-    // ahead of PreCorr (the pipeline in that mode, src/engine.c:557-559)
-    const int r = s.precorr
-                      ? launch_fir_chain(s.F, s.fir_smem, pl->d_pcm + s.pcm_off, s.pcm_stride,
-                                         s.d.frames, pl->d_hist, pl->d_f32 + s.f32_off,
-                                         s.f32_stride, gain, 0.0, apply, 0, s.d.channels, m)
-                      : launch_fir_chain(s.F, s.fir_smem, pl->d_pcm + s.pcm_off, s.pcm_stride,
-                                         s.d.frames, pl->d_hist, pl->d_fir + s.fir_off,
-                                         s.fir_stride, gain, 0.0, apply, s.d.soft_clip,
-                                         s.d.channels, m);
+    const int nch = s.d.channels;
+    int r = 0;
+    if (s.dsd_mode == 1) {
+      // same-rate DSD: DoP unpack into the decision rows (free until the
+      // assembly writes them), the boxcar with the constant gain
+      r = launch_dop_unpack(pl->d_pcm + s.pcm_off, s.pcm_stride, s.d.frames, nch,
+                            pl->d_bits + s.bits_off, s.bits_stride, m);
+      if (!r)
+        r = launch_boxcar_fresh(pl->d_bits + s.bits_off, s.bits_stride, (long long)s.n_fir,
+                                pl->d_boxhist, s.box_taps, nch, gain, 0.0, pl->d_fir + s.fir_off,
+                                s.fir_stride, m);
+    } else if (s.dsd_mode == 2) {
+      // DSD up: +-1 floats at the input rate through the FIR chain
+      r = launch_dop_unpack_f32(pl->d_pcm + s.pcm_off, s.pcm_stride, s.d.frames, nch,
+                                pl->d_f32 + s.f32_off, s.f32_stride, m);
+      if (!r)
+        r = launch_fir_chain(s.F, s.fir_smem, pl->d_f32 + s.f32_off, s.f32_stride,
+                             16 * s.d.frames, pl->d_hist, pl->d_fir + s.fir_off, s.fir_stride,
+                             gain, 0.0, apply, s.d.soft_clip, nch, m);
+    } else if (s.precorr) {
+      // PreCorr streams: FP32 out (the values the walk reads), no soft clip
+      // ahead of PreCorr (the pipeline in that mode, src/engine.c:557-559)
+      r = launch_fir_chain(s.F, s.fir_smem, pl->d_pcm + s.pcm_off, s.pcm_stride, s.d.frames,
+                           pl->d_hist, pl->d_f32 + s.f32_off, s.f32_stride, gain, 0.0, apply, 0,
+                           nch, m);
+    } else {
+      r = launch_fir_chain(s.F, s.fir_smem, pl->d_pcm + s.pcm_off, s.pcm_stride, s.d.frames,
+                           pl->d_hist, pl->d_fir + s.fir_off, s.fir_stride, gain, 0.0, apply,
+                           s.d.soft_clip, nch, m);
+    }
     if (r != 0) {
       rc = DSDGPU_ERR_CUDA;
       break;
@@ -603,18 +630,35 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
     if (d.channels < 1 || d.channels > kBatchMaxChannels)
       return bail(c->fail(DSDGPU_ERR_ARG, "stream channels out of range (1..8)"));
     if (d.frames < 1) return bail(c->fail(DSDGPU_ERR_ARG, "stream without frames"));
-    if (d.boxcar_taps < 0 || d.boxcar_taps > 64)
-      return bail(c->fail(DSDGPU_ERR_ARG, "boxcar taps out of range"));
-    if (d.fs_in <= 0 || d.fs_out <= 0 ||
-        build_chain_const((unsigned)d.fs_in, (unsigned)d.fs_out, d.boxcar_taps, &s.F) != 0)
-      return bail(c->fail(DSDGPU_ERR_ARG, "unsupported rate pair (upsampling by a power of two only)"));
-    s.fir_smem = chain_smem_bytes(s.F);
-    if (s.fir_smem > (size_t)kFirMaxSmem)
-      return bail(c->fail(DSDGPU_ERR_UNSUPPORTED, "fir tile does not fit shared memory"));
     if (d.sdm_mode != DSDGPU_SDM_TRELLIS && d.sdm_mode != DSDGPU_SDM_PRECORR)
       return bail(c->fail(DSDGPU_ERR_ARG, "bad sdm mode"));
     s.precorr = d.sdm_mode == DSDGPU_SDM_PRECORR;
-    s.n_fir = (size_t)d.frames * (size_t)s.F.ratio;
+    if (d.fs_in <= 0 || d.fs_out <= 0) return bail(c->fail(DSDGPU_ERR_ARG, "bad rate"));
+    // DoP input at a DSD rate (the pipeline's rule): the same-rate re-encode
+    // or the FIR chain on +-1 floats to a higher DSD rate
+    if (d.fs_in >= kDsd64Rate) {
+      if (d.fs_out < d.fs_in)
+        return bail(c->fail(DSDGPU_ERR_UNSUPPORTED, "DSD input to a lower rate is not in the batch plan"));
+      if (s.precorr)
+        return bail(c->fail(DSDGPU_ERR_UNSUPPORTED, "PreCorr on DSD input is not in the batch plan"));
+      s.dsd_mode = d.fs_out == d.fs_in ? 1 : 2;
+    }
+    if (s.dsd_mode == 1) {
+      // engine_init's same-rate boxcar (src/engine.c:130-147), 0 = the rate's default
+      s.box_taps = d.boxcar_taps > 0 ? d.boxcar_taps : samerate_boxcar_taps((unsigned)d.fs_in);
+      if (d.boxcar_taps < 0 || s.box_taps > 256)
+        return bail(c->fail(DSDGPU_ERR_ARG, "boxcar taps out of range (1..256)"));
+      s.n_fir = 16 * (size_t)d.frames;
+    } else {
+      if (d.boxcar_taps < 0 || d.boxcar_taps > 64)
+        return bail(c->fail(DSDGPU_ERR_ARG, "boxcar taps out of range"));
+      if (build_chain_const((unsigned)d.fs_in, (unsigned)d.fs_out, d.boxcar_taps, &s.F) != 0)
+        return bail(c->fail(DSDGPU_ERR_ARG, "unsupported rate pair (upsampling by a power of two only)"));
+      s.fir_smem = chain_smem_bytes(s.F);
+      if (s.fir_smem > (size_t)kFirMaxSmem)
+        return bail(c->fail(DSDGPU_ERR_UNSUPPORTED, "fir tile does not fit shared memory"));
+      s.n_fir = (size_t)d.frames * (s.dsd_mode == 2 ? 16 : 1) * (size_t)s.F.ratio;
+    }
     if (s.precorr) {
       // the checks of dsdgpu_precorr_setup; K, depth and lat are not used
       const dsdgpu_sdm_params_t& q = d.sdm;
@@ -714,6 +758,11 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
       bits_total += s.bits_stride * nch;
       s.final_count = (long long)s.n_fir;   // one decision per input, no latency
     } else {
+      if (s.dsd_mode == 2) {
+        s.f32_stride = align_up(16 * (size_t)s.d.frames, 64);
+        s.f32_off = f32_total;
+        f32_total += s.f32_stride * nch;
+      }
       layout_stream(s, pl->seg_len);
       segment_io(s);
       s.fir_stride = align_up(s.n_fir, 32);
@@ -828,6 +877,7 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
       {(void**)&pl->d_f32, sizeof(float) * f32_total},
       {(void**)&pl->d_pctab, sizeof(float) * precorr_table_floats() * pl->pcls.size()},
       {(void**)&pl->d_pcrows, sizeof(PcBatchRow) * pl->pcrows.size()},
+      {(void**)&pl->d_boxhist, boxcar_hist_bytes(kBatchMaxChannels)},
       {(void**)&pl->d_seg, seg_total},
       {(void**)&pl->d_bits, bits_total},
       {(void**)&pl->d_out, out_total},
@@ -874,6 +924,7 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
   cudaMemcpyAsync(pl->d_qfir, q2, sizeof q2, cudaMemcpyHostToDevice, m);
   cudaMemsetAsync(pl->d_seed, 0, sizeof(double) * kMaxOrder, m);
   cudaMemsetAsync(pl->d_hist, 0, sizeof(float) * kHistory * kBatchMaxChannels, m);
+  cudaMemsetAsync(pl->d_boxhist, 0, boxcar_hist_bytes(kBatchMaxChannels), m);
   cudaMemsetAsync(pl->d_bp, 0, sizeof(int) * (size_t)nbp, m);
   cudaMemsetAsync(pl->d_pcm, 0, sizeof(float) * pcm_total, m);
   if (!pl->jobs.empty())
@@ -984,7 +1035,8 @@ int dsdgpu_plan_run(dsdgpu_plan_t* pl) {
   cudaError_t e = cudaGraphLaunch(pl->g1, m);
   if (e != cudaSuccess) return c->cuda_fail(e, "graph 1 launch");
   cudaEventRecord(pl->ev[3], m);
-  c->launches += pl->st.size() + (pl->centers.empty() ? 0 : 1);
+  for (const StreamPlan& s : pl->st) c->launches += s.dsd_mode ? 2 : 1;
+  c->launches += pl->centers.empty() ? 0 : 1;
   int rc = DSDGPU_OK;
   if (!pl->centers.empty()) {
     // the boundary RMS values are needed on the host

@@ -90,6 +90,37 @@ unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
 }  // namespace
 
+// Launchers without a context (the batch plan's DSD-input streams, fresh
+// state: `zero_hist` holds nch x (kMaxBoxcar - 1) zero bytes).
+size_t boxcar_hist_bytes(int nch) { return (size_t)nch * (kMaxBoxcar - 1); }
+
+int launch_dop_unpack(const float* dop, size_t dop_stride, long long frames, int nch,
+                      uint8_t* bits, size_t bits_stride, cudaStream_t stream) {
+  if (frames <= 0) return 0;
+  dop_unpack_kernel<<<nblk(frames * nch, 256), 256, 0, stream>>>(dop, dop_stride, frames, nch,
+                                                                  bits, bits_stride);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_dop_unpack_f32(const float* dop, size_t dop_stride, long long frames, int nch,
+                          float* out, size_t out_stride, cudaStream_t stream) {
+  if (frames <= 0) return 0;
+  dop_unpack_f32_kernel<<<nblk(frames * nch, 256), 256, 0, stream>>>(dop, dop_stride, frames,
+                                                                      nch, out, out_stride);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_boxcar_fresh(const uint8_t* bits, size_t bits_stride, long long count,
+                        const int8_t* zero_hist, int taps, int nch, double g_start, double g_step,
+                        double* out, size_t out_stride, cudaStream_t stream) {
+  if (count <= 0) return 0;
+  if (taps < 1 || taps > kMaxBoxcar) return -1;
+  boxcar_kernel<<<nblk(count * nch, 256), 256, 0, stream>>>(bits, bits_stride, count, zero_hist,
+                                                            taps, nch, g_start, g_step, out,
+                                                            out_stride);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 // Same-rate boxcar taps of engine_init (src/engine.c:130-147): DSD512 and up
 // 16, DSD128/256 64, DSD64 32.
 int samerate_boxcar_taps(unsigned fs) {

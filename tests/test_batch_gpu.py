@@ -278,3 +278,76 @@ def test_batch_long_latency_with_a_short_one(oracle):
         got = plan.out_view(i).cpu().numpy()
         assert got.shape == want.shape and np.array_equal(got, want), f"stream {i}"
     plan.close()
+
+
+def _dop_input(oracle, rate, frames, nch, seed):
+    """DoP floats [nch, frames] of a DSD bitstream at `rate` (a quick trellis
+    encode of a multitone, as the same-rate pipeline tests use)."""
+    from signals import multitone
+
+    from foo_dsd_trellis_gb300 import ntf
+    f = ntf.get_filter("clans-5", rate)
+    out = []
+    for c in range(nch):
+        ctx = oracle.sdm(f.order, np.array(f.a), np.array(f.g), 8, 4, 8)
+        x = multitone(16 * frames + 8, 7 + seed + c) * 1.5
+        out.append(oracle.dop_float_frames(oracle.sdm_bits(ctx, x)[: 16 * frames], 0))
+    return np.stack(out).astype(np.float32)
+
+
+@pytest.mark.parametrize("fmt", [1, 0], ids=["dop", "bits"])
+def test_batch_dsd_input_streams(oracle, fmt):
+    """DoP input in a batch, as the pipeline takes it: same-rate DSD64 (the
+    engine's default 32-tap boxcar) and DSD128 (64 taps given), DSD64 -> DSD128
+    through the FIR chain on the unpacked +-1 values, beside a PCM stream.
+    Each stream equals the single-stream pipeline on a fresh context with the
+    same parameters (itself checked against the oracle's unpack, boxcar, FIR
+    and DAS in test_dsd_gpu.py)."""
+    from foo_dsd_trellis_gb300 import ntf
+    from foo_dsd_trellis_gb300.batch import OUT_BITS, BatchPlan, StreamSpec
+    from foo_dsd_trellis_gb300.pipeline import FULL_PARALLEL, Encoder
+    pcm_spec = _specs()[0]
+    dsd = [(2822400, 2822400, 2, 12000, 0, False), (5644800, 5644800, 1, 9000, 64, False),
+           (2822400, 5644800, 2, 6000, 8, True)]
+    specs = [pcm_spec]
+    xs = [_inputs([pcm_spec])[0]]
+    for k, (fi, fo, ch, frames, box, clip) in enumerate(dsd):
+        specs.append(StreamSpec(fi, fo, ch, frames, ntf.auto_select(fo), cands=8, depth=16, lat=16,
+                                gain=0.9, boxcar_taps=box, soft_clip=clip, reposition=True))
+        xs.append(_dop_input(oracle, fi, frames, ch, 40 + k))
+    plan = BatchPlan(specs, seg_len=32768, output_format=fmt)
+    plan.load([torch.from_numpy(x).cuda() for x in xs])
+    plan.run()
+    for i, s in enumerate(specs):
+        got = plan.out_view(i).cpu().numpy()
+        if i == 0:
+            want, _ = _oracle_stream(oracle, s, xs[0], 32768, fmt)
+        else:
+            enc = Encoder(s.fs_in, s.fs_out, s.channels, s.ntf, s.depth, s.cands, s.lat,
+                          seg_len=32768, seed_mode=FULL_PARALLEL, reposition=True,
+                          boxcar_taps=s.boxcar_taps, soft_clip=s.soft_clip, output_format=fmt)
+            n_out = 16 * s.frames * (s.fs_out // s.fs_in)
+            if fmt == OUT_BITS:
+                buf = torch.empty((s.channels, n_out + 256), dtype=torch.uint8, device="cuda")
+            else:
+                buf = torch.empty(enc.out_capacity(s.frames) + 64, dtype=torch.uint8, device="cuda")
+            ns, nb = enc.process(torch.from_numpy(xs[i]).cuda(), buf, 0.9, 0.9)
+            want = buf[:, :ns].cpu().numpy() if fmt == OUT_BITS else buf[:nb].cpu().numpy()
+            enc.close()
+            assert plan.out_samples(i) == ns
+        assert got.shape == want.shape, (i, got.shape, want.shape)
+        assert np.array_equal(got, want), f"stream {i}"
+    plan.close()
+
+
+def test_batch_rejects_unsupported_dsd_input():
+    """DSD input to a lower DSD rate and PreCorr on DSD input are not in the
+    batch plan: DSDGPU_ERR_UNSUPPORTED at plan creation."""
+    from foo_dsd_trellis_gb300 import _lib, ntf
+    from foo_dsd_trellis_gb300.batch import BatchPlan, StreamSpec
+    for spec in (StreamSpec(5644800, 2822400, 2, 1000, ntf.auto_select(2822400)),
+                 StreamSpec(2822400, 2822400, 2, 1000, ntf.auto_select_precorr(2822400),
+                            precorr=True)):
+        with pytest.raises(_lib.DsdGpuError) as e:
+            BatchPlan([spec])
+        assert e.value.code == _lib.ERR_UNSUPPORTED
