@@ -72,9 +72,12 @@ struct StreamPlan {
   bool precorr = false;
   int pc_cls = -1;                      // PreCorr parameter class
   // DoP input (fs_in a DSD rate): 1 = same rate (unpack, boxcar of box_taps),
-  // 2 = to a higher DSD rate (unpack to +-1 floats, the FIR chain); 0 = PCM
+  // 2 = to a higher DSD rate (unpack to +-1 floats, the FIR chain), 3 = to a
+  // lower one (unpack, boxcar of box_taps, down_stages FP64 half-band /2
+  // stages); 0 = PCM
   int dsd_mode = 0;
   int box_taps = 0;
+  int down_stages = 0;
   size_t f32_off = 0, f32_stride = 0;   // FP32 rows: a PreCorr stream's chain output, or a
                                         // DSD-up stream's unpacked +-1 input (floats)
   int lat = 0;
@@ -169,7 +172,14 @@ struct dsdgpu_plan {
   float* d_f32 = nullptr;              // FP32 chain outputs of the PreCorr streams
   float* d_pctab = nullptr;            // PreCorr tables, one per class
   PcBatchRow* d_pcrows = nullptr;
-  int8_t* d_boxhist = nullptr;         // zero boxcar history of the same-rate DSD streams
+  int8_t* d_boxhist = nullptr;         // zero boxcar history of the DSD streams
+  // scratch of the DSD streams to a lower rate, shared (graph 1 runs its
+  // streams in order): unpacked decisions, boxcar output, the chain's
+  // ping-pong rows, the chain's zero delay lines
+  uint8_t* d_dn_bits = nullptr;
+  double* d_dn_box = nullptr;
+  double* d_dn_pp = nullptr;
+  double* d_dn_dly = nullptr;
   cudaEvent_t fork = nullptr;          // graph 2's fork point (several launches)
   uint8_t* d_seg = nullptr;
   uint8_t* d_bits = nullptr;
@@ -400,6 +410,21 @@ int capture_graphs(dsdgpu_plan* pl) {
         r = launch_fir_chain(s.F, s.fir_smem, pl->d_f32 + s.f32_off, s.f32_stride,
                              16 * s.d.frames, pl->d_hist, pl->d_fir + s.fir_off, s.fir_stride,
                              gain, 0.0, apply, s.d.soft_clip, nch, m);
+    } else if (s.dsd_mode == 3) {
+      // DSD down (the pipeline's rate-conversion branch with DSD in): unpack,
+      // the boxcar at gain 1, the FP64 chain with the gain and the clip
+      const long long cnt = 16 * s.d.frames;
+      const size_t bs = align_up((size_t)cnt, 256), fs = align_up((size_t)cnt, 32);
+      const size_t row = align_up((size_t)cnt / 2 + 1, 32);
+      r = launch_dop_unpack(pl->d_pcm + s.pcm_off, s.pcm_stride, s.d.frames, nch, pl->d_dn_bits,
+                            bs, m);
+      if (!r)
+        r = launch_boxcar_fresh(pl->d_dn_bits, bs, cnt, pl->d_boxhist, s.box_taps, nch, 1.0, 0.0,
+                                pl->d_dn_box, fs, m);
+      if (!r)
+        r = launch_decim_f64_fresh(pl->d_dn_box, fs, cnt, s.down_stages, nch, pl->d_dn_pp, row,
+                                   pl->d_dn_dly, gain, 0.0, apply, s.d.soft_clip,
+                                   pl->d_fir + s.fir_off, s.fir_stride, m);
     } else if (s.precorr) {
       // PreCorr streams: FP32 out (the values the walk reads), no soft clip
       // ahead of PreCorr (the pipeline in that mode, src/engine.c:557-559)
@@ -637,13 +662,26 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
     // DoP input at a DSD rate (the pipeline's rule): the same-rate re-encode
     // or the FIR chain on +-1 floats to a higher DSD rate
     if (d.fs_in >= kDsd64Rate) {
-      if (d.fs_out < d.fs_in)
-        return bail(c->fail(DSDGPU_ERR_UNSUPPORTED, "DSD input to a lower rate is not in the batch plan"));
       if (s.precorr)
         return bail(c->fail(DSDGPU_ERR_UNSUPPORTED, "PreCorr on DSD input is not in the batch plan"));
-      s.dsd_mode = d.fs_out == d.fs_in ? 1 : 2;
+      s.dsd_mode = d.fs_out == d.fs_in ? 1 : (d.fs_out > d.fs_in ? 2 : 3);
     }
-    if (s.dsd_mode == 1) {
+    if (s.dsd_mode == 3) {
+      // the decimation chain's plan (dsdgpu_decim_setup); boxcar 0 = a one-tap
+      // mean, the identity on +-1 input (the plugin's DAS FIR phase has none)
+      unsigned r = (unsigned)d.fs_in / (unsigned)d.fs_out;
+      if ((unsigned)d.fs_in % (unsigned)d.fs_out || (r & (r - 1)))
+        return bail(c->fail(DSDGPU_ERR_ARG, "decimation needs fs_in = fs_out * 2^k"));
+      while (r > 1) {
+        s.down_stages++;
+        r >>= 1;
+      }
+      if (s.down_stages > kMaxStages) return bail(c->fail(DSDGPU_ERR_ARG, "too many stages"));
+      s.box_taps = d.boxcar_taps > 0 ? d.boxcar_taps : 1;
+      if (d.boxcar_taps < 0 || s.box_taps > 256)
+        return bail(c->fail(DSDGPU_ERR_ARG, "boxcar taps out of range (1..256)"));
+      s.n_fir = (16 * (size_t)d.frames) >> s.down_stages;
+    } else if (s.dsd_mode == 1) {
       // engine_init's same-rate boxcar (src/engine.c:130-147), 0 = the rate's default
       s.box_taps = d.boxcar_taps > 0 ? d.boxcar_taps : samerate_boxcar_taps((unsigned)d.fs_in);
       if (d.boxcar_taps < 0 || s.box_taps > 256)
@@ -868,6 +906,16 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
   pl->pieces.resize(npieces);
   pl->segbuf.resize(nseg);
 
+  // shared scratch of the DSD streams to a lower rate (the largest one's)
+  size_t dn_bits = 0, dn_box = 0, dn_pp = 0;
+  for (const StreamPlan& s : pl->st) {
+    if (s.dsd_mode != 3) continue;
+    const size_t cnt = 16 * (size_t)s.d.frames, nch = (size_t)s.d.channels;
+    dn_bits = std::max(dn_bits, align_up(cnt, 256) * nch);
+    dn_box = std::max(dn_box, align_up(cnt, 32) * nch);
+    dn_pp = std::max(dn_pp, 2 * align_up(cnt / 2 + 1, 32) * nch);
+  }
+
   // ---- device arena ----
   struct Part { void** p; size_t bytes; };
   const size_t nctx = 1 + (size_t)nscratch;
@@ -878,6 +926,10 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
       {(void**)&pl->d_pctab, sizeof(float) * precorr_table_floats() * pl->pcls.size()},
       {(void**)&pl->d_pcrows, sizeof(PcBatchRow) * pl->pcrows.size()},
       {(void**)&pl->d_boxhist, boxcar_hist_bytes(kBatchMaxChannels)},
+      {(void**)&pl->d_dn_bits, dn_bits},
+      {(void**)&pl->d_dn_box, sizeof(double) * dn_box},
+      {(void**)&pl->d_dn_pp, sizeof(double) * dn_pp},
+      {(void**)&pl->d_dn_dly, sizeof(double) * 62 * kBatchMaxChannels},
       {(void**)&pl->d_seg, seg_total},
       {(void**)&pl->d_bits, bits_total},
       {(void**)&pl->d_out, out_total},
@@ -925,6 +977,7 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
   cudaMemsetAsync(pl->d_seed, 0, sizeof(double) * kMaxOrder, m);
   cudaMemsetAsync(pl->d_hist, 0, sizeof(float) * kHistory * kBatchMaxChannels, m);
   cudaMemsetAsync(pl->d_boxhist, 0, boxcar_hist_bytes(kBatchMaxChannels), m);
+  cudaMemsetAsync(pl->d_dn_dly, 0, sizeof(double) * 62 * kBatchMaxChannels, m);
   cudaMemsetAsync(pl->d_bp, 0, sizeof(int) * (size_t)nbp, m);
   cudaMemsetAsync(pl->d_pcm, 0, sizeof(float) * pcm_total, m);
   if (!pl->jobs.empty())
@@ -1035,7 +1088,8 @@ int dsdgpu_plan_run(dsdgpu_plan_t* pl) {
   cudaError_t e = cudaGraphLaunch(pl->g1, m);
   if (e != cudaSuccess) return c->cuda_fail(e, "graph 1 launch");
   cudaEventRecord(pl->ev[3], m);
-  for (const StreamPlan& s : pl->st) c->launches += s.dsd_mode ? 2 : 1;
+  for (const StreamPlan& s : pl->st)
+    c->launches += s.dsd_mode == 3 ? 3 + s.down_stages : (s.dsd_mode ? 2 : 1);
   c->launches += pl->centers.empty() ? 0 : 1;
   int rc = DSDGPU_OK;
   if (!pl->centers.empty()) {

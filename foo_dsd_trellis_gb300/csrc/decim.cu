@@ -168,6 +168,42 @@ struct dsdgpu_decim_state {
 
 void decim_free(dsdgpu_decim_state* s) { delete s; }
 
+// The FP64 chain from fresh state without a context (the batch plan's DSD
+// input to a lower rate): `stages` 63-tap half-band /2 stages over `count`
+// inputs through the ping-pong rows of `buf` (2 x nch rows of `row` doubles,
+// row >= count / 2 + 1), with the zero delay lines `zero_dly` (nch x 62
+// zeros, read only: a fresh stream has nothing before its first sample), then
+// gain and the optional soft clip into `out`.  *out_count = count >> stages.
+int launch_decim_f64_fresh(const double* in, size_t in_stride, long long count, int stages,
+                           int nch, double* buf, size_t row, const double* zero_dly,
+                           double g_start, double g_step, int apply, int soft_clip, double* out,
+                           size_t out_stride, cudaStream_t st) {
+  if (count < 2 || stages < 1) return 0;
+  DecTaps taps{};
+  DecNz nz{};
+  design_taps(kDecTaps, false, taps.h);
+  for (int q = 0, k = 0; k < kDecTaps; k++)
+    if ((k & 1) == 0 || k == kDecTaps / 2) { nz.h[q] = taps.h[k]; nz.k[q] = k; q++; }
+  double* pp[2] = {buf, buf + row * (size_t)nch};
+  long long cur = count;
+  const double* x = in;
+  size_t xs = in_stride;
+  for (int k = 0; k < stages; k++) {
+    const long long m = cur / 2;
+    if (m > 0)
+      decim_stage_kernel<<<nb(m * nch, 256), 256, 0, st>>>(nz, x, xs, m, zero_dly, pp[k & 1], row,
+                                                           nch);
+    x = pp[k & 1];
+    xs = row;
+    cur = m;
+  }
+  if (cur > 0)
+    decim_gain_f64_kernel<<<nb(cur * nch, 256), 256, 0, st>>>(x, xs, cur, nch, g_start, g_step,
+                                                              apply, soft_clip ? 1 : 0, out,
+                                                              out_stride);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 extern "C" {
 
 int dsdgpu_decim_setup(dsdgpu_context_t* c, unsigned fs_in, unsigned fs_out, int nch) {

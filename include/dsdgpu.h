@@ -410,15 +410,15 @@ int dsdgpu_sdm_estimate_state(dsdgpu_context_t *ctx, const dsdgpu_sdm_params_t *
  * A stream whose fs_in is a DSD rate takes DoP floats (planar, 16 DSD samples
  * per frame) as the pipeline does: at fs_out == fs_in the same-rate
  * re-encode (unpack, boxcar, DAS trellis), above it the FIR chain on the
- * unpacked +-1 values; DSD input to a lower rate, and PreCorr on DSD input,
- * are DSDGPU_ERR_UNSUPPORTED here.
+ * unpacked +-1 values, below it the boxcar and the FP64 half-band /2 chain;
+ * PreCorr on DSD input is DSDGPU_ERR_UNSUPPORTED here.
  * Each run converts whole streams from fresh state. */
 typedef struct {
     int32_t fs_in;             /* PCM rate, Hz; a DSD rate (2,822,400 and up): DoP input */
     int32_t fs_out;            /* DSD rate, Hz: fs_in times a power of two */
     int32_t channels;          /* 1..8 */
     int32_t boxcar_taps;       /* 0 = off (engine default 8); same-rate DSD: 0 = the rate's
-                                  default (32 / 64 / 16), up to 256 */
+                                  default (32 / 64 / 16), up to 256; DSD down: up to 256 */
     int64_t frames;            /* PCM frames per channel (DoP frames for DSD input) */
     double gain;               /* FIR output gain, constant over the stream */
     int32_t soft_clip;         /* tanh soft clip above +-0.95 */

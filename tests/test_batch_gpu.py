@@ -299,7 +299,9 @@ def _dop_input(oracle, rate, frames, nch, seed):
 def test_batch_dsd_input_streams(oracle, fmt):
     """DoP input in a batch, as the pipeline takes it: same-rate DSD64 (the
     engine's default 32-tap boxcar) and DSD128 (64 taps given), DSD64 -> DSD128
-    through the FIR chain on the unpacked +-1 values, beside a PCM stream.
+    through the FIR chain on the unpacked +-1 values, DSD128 -> DSD64 (boxcar 8,
+    one FP64 half-band /2 stage, soft clip) and DSD256 -> DSD64 (no boxcar, two
+    stages), beside a PCM stream.
     Each stream equals the single-stream pipeline on a fresh context with the
     same parameters (itself checked against the oracle's unpack, boxcar, FIR
     and DAS in test_dsd_gpu.py)."""
@@ -308,7 +310,8 @@ def test_batch_dsd_input_streams(oracle, fmt):
     from foo_dsd_trellis_gb300.pipeline import FULL_PARALLEL, Encoder
     pcm_spec = _specs()[0]
     dsd = [(2822400, 2822400, 2, 12000, 0, False), (5644800, 5644800, 1, 9000, 64, False),
-           (2822400, 5644800, 2, 6000, 8, True)]
+           (2822400, 5644800, 2, 6000, 8, True), (5644800, 2822400, 2, 12000, 8, True),
+           (11289600, 2822400, 1, 16000, 0, False)]
     specs = [pcm_spec]
     xs = [_inputs([pcm_spec])[0]]
     for k, (fi, fo, ch, frames, box, clip) in enumerate(dsd):
@@ -326,7 +329,7 @@ def test_batch_dsd_input_streams(oracle, fmt):
             enc = Encoder(s.fs_in, s.fs_out, s.channels, s.ntf, s.depth, s.cands, s.lat,
                           seg_len=32768, seed_mode=FULL_PARALLEL, reposition=True,
                           boxcar_taps=s.boxcar_taps, soft_clip=s.soft_clip, output_format=fmt)
-            n_out = 16 * s.frames * (s.fs_out // s.fs_in)
+            n_out = 16 * s.frames * s.fs_out // s.fs_in
             if fmt == OUT_BITS:
                 buf = torch.empty((s.channels, n_out + 256), dtype=torch.uint8, device="cuda")
             else:
@@ -341,13 +344,12 @@ def test_batch_dsd_input_streams(oracle, fmt):
 
 
 def test_batch_rejects_unsupported_dsd_input():
-    """DSD input to a lower DSD rate and PreCorr on DSD input are not in the
-    batch plan: DSDGPU_ERR_UNSUPPORTED at plan creation."""
+    """PreCorr on DSD input is not in the batch plan: DSDGPU_ERR_UNSUPPORTED at
+    plan creation."""
     from foo_dsd_trellis_gb300 import _lib, ntf
     from foo_dsd_trellis_gb300.batch import BatchPlan, StreamSpec
-    for spec in (StreamSpec(5644800, 2822400, 2, 1000, ntf.auto_select(2822400)),
-                 StreamSpec(2822400, 2822400, 2, 1000, ntf.auto_select_precorr(2822400),
-                            precorr=True)):
+    for fo in (2822400, 5644800):
+        spec = StreamSpec(2822400, fo, 2, 1000, ntf.auto_select_precorr(fo), precorr=True)
         with pytest.raises(_lib.DsdGpuError) as e:
             BatchPlan([spec])
         assert e.value.code == _lib.ERR_UNSUPPORTED
