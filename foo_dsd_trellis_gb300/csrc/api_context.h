@@ -82,11 +82,15 @@ int launch_dop_unpack_f32(const float* dop, size_t dop_stride, long long frames,
 int launch_boxcar_fresh(const uint8_t* bits, size_t bits_stride, long long count,
                         const int8_t* zero_hist, int taps, int nch, double g_start, double g_step,
                         double* out, size_t out_stride, cudaStream_t stream);
-// the FP64 decimation chain from fresh state without a context (decim.cu)
+int launch_boxcar_fresh_f32(const uint8_t* bits, size_t bits_stride, long long count,
+                            const int8_t* zero_hist, int taps, int nch, double g_start,
+                            double g_step, float* out, size_t out_stride, cudaStream_t stream);
+// the FP64 decimation chain from fresh state without a context (decim.cu);
+// out32 non-null: FP32 output (gain, no clip) there instead of `out`
 int launch_decim_f64_fresh(const double* in, size_t in_stride, long long count, int stages,
                            int nch, double* buf, size_t row, const double* zero_dly,
                            double g_start, double g_step, int apply, int soft_clip, double* out,
-                           size_t out_stride, cudaStream_t st);
+                           size_t out_stride, cudaStream_t st, float* out32 = nullptr);
 
 struct dsdgpu_context {
   int device = 0;

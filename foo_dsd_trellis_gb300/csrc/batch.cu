@@ -78,8 +78,10 @@ struct StreamPlan {
   int dsd_mode = 0;
   int box_taps = 0;
   int down_stages = 0;
-  size_t f32_off = 0, f32_stride = 0;   // FP32 rows: a PreCorr stream's chain output, or a
-                                        // DSD-up stream's unpacked +-1 input (floats)
+  size_t f32_off = 0, f32_stride = 0;   // FP32 rows: a PreCorr stream's walk input, or a
+                                        // DSD-up trellis stream's unpacked +-1 input (floats)
+  size_t f32in_off = 0;                 // a DSD-up PreCorr stream's unpacked input (f32_stride
+                                        // is its walk rows'; these rows are 16 x frames long)
   int lat = 0;
   size_t overlap = 0;
   int S = 0;
@@ -393,7 +395,39 @@ int capture_graphs(dsdgpu_plan* pl) {
     const int apply = gain != 1.0 ? 1 : 0;
     const int nch = s.d.channels;
     int r = 0;
-    if (s.dsd_mode == 1) {
+    if (s.precorr && s.dsd_mode) {
+      // PreCorr on DoP input: the same stages with FP32 output, no clip
+      // (the pipeline narrows their FP64 output ahead of the walk)
+      float* w = pl->d_f32 + s.f32_off;
+      const long long cnt = 16 * s.d.frames;
+      if (s.dsd_mode == 1) {
+        r = launch_dop_unpack(pl->d_pcm + s.pcm_off, s.pcm_stride, s.d.frames, nch,
+                              pl->d_bits + s.bits_off, s.bits_stride, m);
+        if (!r)
+          r = launch_boxcar_fresh_f32(pl->d_bits + s.bits_off, s.bits_stride, (long long)s.n_fir,
+                                      pl->d_boxhist, s.box_taps, nch, gain, 0.0, w, s.f32_stride,
+                                      m);
+      } else if (s.dsd_mode == 2) {
+        const size_t in_stride = align_up((size_t)cnt, 64);
+        r = launch_dop_unpack_f32(pl->d_pcm + s.pcm_off, s.pcm_stride, s.d.frames, nch,
+                                  pl->d_f32 + s.f32in_off, in_stride, m);
+        if (!r)
+          r = launch_fir_chain(s.F, s.fir_smem, pl->d_f32 + s.f32in_off, in_stride, cnt,
+                               pl->d_hist, w, s.f32_stride, gain, 0.0, apply, 0, nch, m);
+      } else {
+        const size_t bs = align_up((size_t)cnt, 256), fs = align_up((size_t)cnt, 32);
+        const size_t row = align_up((size_t)cnt / 2 + 1, 32);
+        r = launch_dop_unpack(pl->d_pcm + s.pcm_off, s.pcm_stride, s.d.frames, nch,
+                              pl->d_dn_bits, bs, m);
+        if (!r)
+          r = launch_boxcar_fresh(pl->d_dn_bits, bs, cnt, pl->d_boxhist, s.box_taps, nch, 1.0,
+                                  0.0, pl->d_dn_box, fs, m);
+        if (!r)
+          r = launch_decim_f64_fresh(pl->d_dn_box, fs, cnt, s.down_stages, nch, pl->d_dn_pp, row,
+                                     pl->d_dn_dly, gain, 0.0, apply, 0, nullptr, s.f32_stride, m,
+                                     w);
+      }
+    } else if (s.dsd_mode == 1) {
       // same-rate DSD: DoP unpack into the decision rows (free until the
       // assembly writes them), the boxcar with the constant gain
       r = launch_dop_unpack(pl->d_pcm + s.pcm_off, s.pcm_stride, s.d.frames, nch,
@@ -662,8 +696,6 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
     // DoP input at a DSD rate (the pipeline's rule): the same-rate re-encode
     // or the FIR chain on +-1 floats to a higher DSD rate
     if (d.fs_in >= kDsd64Rate) {
-      if (s.precorr)
-        return bail(c->fail(DSDGPU_ERR_UNSUPPORTED, "PreCorr on DSD input is not in the batch plan"));
       s.dsd_mode = d.fs_out == d.fs_in ? 1 : (d.fs_out > d.fs_in ? 2 : 3);
     }
     if (s.dsd_mode == 3) {
@@ -791,6 +823,10 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
       s.f32_stride = align_up(s.n_fir, 64);
       s.f32_off = f32_total;
       f32_total += s.f32_stride * nch;
+      if (s.dsd_mode == 2) {
+        s.f32in_off = f32_total;
+        f32_total += align_up(16 * (size_t)s.d.frames, 64) * nch;
+      }
       s.bits_stride = align_up(s.n_fir, 256);
       s.bits_off = bits_total;
       bits_total += s.bits_stride * nch;

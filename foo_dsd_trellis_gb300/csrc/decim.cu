@@ -174,10 +174,12 @@ void decim_free(dsdgpu_decim_state* s) { delete s; }
 // row >= count / 2 + 1), with the zero delay lines `zero_dly` (nch x 62
 // zeros, read only: a fresh stream has nothing before its first sample), then
 // gain and the optional soft clip into `out`.  *out_count = count >> stages.
+// out32 non-null: FP32 output instead (the gain, no clip, narrowed to
+// nearest: the PreCorr walk's input), `out` unused.
 int launch_decim_f64_fresh(const double* in, size_t in_stride, long long count, int stages,
                            int nch, double* buf, size_t row, const double* zero_dly,
                            double g_start, double g_step, int apply, int soft_clip, double* out,
-                           size_t out_stride, cudaStream_t st) {
+                           size_t out_stride, cudaStream_t st, float* out32) {
   if (count < 2 || stages < 1) return 0;
   DecTaps taps{};
   DecNz nz{};
@@ -197,7 +199,10 @@ int launch_decim_f64_fresh(const double* in, size_t in_stride, long long count, 
     xs = row;
     cur = m;
   }
-  if (cur > 0)
+  if (cur > 0 && out32)
+    decim_gain_kernel<<<nb(cur * nch, 256), 256, 0, st>>>(x, xs, cur, nch, g_start, g_step, apply,
+                                                          out32, out_stride);
+  else if (cur > 0)
     decim_gain_f64_kernel<<<nb(cur * nch, 256), 256, 0, st>>>(x, xs, cur, nch, g_start, g_step,
                                                               apply, soft_clip ? 1 : 0, out,
                                                               out_stride);

@@ -51,9 +51,11 @@ __global__ void dop_unpack_f32_kernel(const float* __restrict__ dop, size_t dop_
   for (int b = 0; b < 16; b++) o[b] = ((w >> (15 - b)) & 1u) ? 1.0f : -1.0f;
 }
 
+// OutT = float: the FP64 value narrowed to nearest (the PreCorr walk's input)
+template <typename OutT>
 __global__ void boxcar_kernel(const uint8_t* __restrict__ bits, size_t bits_stride, long long count,
                               const int8_t* __restrict__ hist, int taps, int nch,
-                              double g_start, double g_step, double* __restrict__ out,
+                              double g_start, double g_step, OutT* __restrict__ out,
                               size_t out_stride) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count * nch) return;
@@ -66,7 +68,7 @@ __global__ void boxcar_kernel(const uint8_t* __restrict__ bits, size_t bits_stri
     sum += j >= 0 ? (x[j] ? 1 : -1) : h[kMaxBoxcar - 1 + j];
   }
   const double inv_n = 1.0 / (double)taps;
-  out[(size_t)c * out_stride + t] =
+  out[(size_t)c * out_stride + t] = (OutT)
       __dmul_rn(__dmul_rn((double)sum, inv_n), __dadd_rn(g_start, __dmul_rn(g_step, (double)t)));
 }
 
@@ -115,9 +117,18 @@ int launch_boxcar_fresh(const uint8_t* bits, size_t bits_stride, long long count
                         double* out, size_t out_stride, cudaStream_t stream) {
   if (count <= 0) return 0;
   if (taps < 1 || taps > kMaxBoxcar) return -1;
-  boxcar_kernel<<<nblk(count * nch, 256), 256, 0, stream>>>(bits, bits_stride, count, zero_hist,
-                                                            taps, nch, g_start, g_step, out,
-                                                            out_stride);
+  boxcar_kernel<double><<<nblk(count * nch, 256), 256, 0, stream>>>(
+      bits, bits_stride, count, zero_hist, taps, nch, g_start, g_step, out, out_stride);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_boxcar_fresh_f32(const uint8_t* bits, size_t bits_stride, long long count,
+                            const int8_t* zero_hist, int taps, int nch, double g_start,
+                            double g_step, float* out, size_t out_stride, cudaStream_t stream) {
+  if (count <= 0) return 0;
+  if (taps < 1 || taps > kMaxBoxcar) return -1;
+  boxcar_kernel<float><<<nblk(count * nch, 256), 256, 0, stream>>>(
+      bits, bits_stride, count, zero_hist, taps, nch, g_start, g_step, out, out_stride);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -194,7 +205,7 @@ int dsdgpu_boxcar_process_async(dsdgpu_context_t* c, int first, int nch, const u
   if (gs == 0.0) gs = gain_end;
   const double step = count > 1 ? (gain_end - gs) / (double)(count - 1) : 0.0;
   int8_t* hist = c->d_box_hist + (size_t)first * (kMaxBoxcar - 1);
-  boxcar_kernel<<<nblk((long long)count * nch, 256), 256, 0, c->stream>>>(
+  boxcar_kernel<double><<<nblk((long long)count * nch, 256), 256, 0, c->stream>>>(
       d_bits, bits_stride, (long long)count, hist, c->box_taps, nch, gs, step, d_out, out_stride);
   boxcar_hist_kernel<<<nch, 256, 0, c->stream>>>(d_bits, bits_stride, (long long)count, hist, nch);
   c->launches += 2;

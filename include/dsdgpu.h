@@ -410,8 +410,8 @@ int dsdgpu_sdm_estimate_state(dsdgpu_context_t *ctx, const dsdgpu_sdm_params_t *
  * A stream whose fs_in is a DSD rate takes DoP floats (planar, 16 DSD samples
  * per frame) as the pipeline does: at fs_out == fs_in the same-rate
  * re-encode (unpack, boxcar, DAS trellis), above it the FIR chain on the
- * unpacked +-1 values, below it the boxcar and the FP64 half-band /2 chain;
- * PreCorr on DSD input is DSDGPU_ERR_UNSUPPORTED here.
+ * unpacked +-1 values, below it the boxcar and the FP64 half-band /2 chain
+ * (in PreCorr mode each with FP32 output and no clip).
  * Each run converts whole streams from fresh state. */
 typedef struct {
     int32_t fs_in;             /* PCM rate, Hz; a DSD rate (2,822,400 and up): DoP input */

@@ -343,13 +343,40 @@ def test_batch_dsd_input_streams(oracle, fmt):
     plan.close()
 
 
-def test_batch_rejects_unsupported_dsd_input():
-    """PreCorr on DSD input is not in the batch plan: DSDGPU_ERR_UNSUPPORTED at
-    plan creation."""
+@pytest.mark.parametrize("fmt", [0, 1], ids=["bits", "dop"])
+def test_batch_precorr_dsd_input(oracle, fmt):
+    """PreCorr on DoP input in a batch: same-rate DSD64 (default boxcar), DSD64 ->
+    DSD128 (FIR chain, FP32 out), DSD128 -> DSD64 (decimation chain, FP32 out),
+    limiter on and off, beside a PreCorr PCM stream.  Each equals the
+    single-stream pipeline in PreCorr mode (which narrows its FP64 stage output
+    ahead of the walk; checked against the oracle in test_dsd_gpu.py)."""
     from foo_dsd_trellis_gb300 import _lib, ntf
-    from foo_dsd_trellis_gb300.batch import BatchPlan, StreamSpec
-    for fo in (2822400, 5644800):
-        spec = StreamSpec(2822400, fo, 2, 1000, ntf.auto_select_precorr(fo), precorr=True)
-        with pytest.raises(_lib.DsdGpuError) as e:
-            BatchPlan([spec])
-        assert e.value.code == _lib.ERR_UNSUPPORTED
+    from foo_dsd_trellis_gb300.batch import OUT_BITS, BatchPlan, StreamSpec
+    from foo_dsd_trellis_gb300.pipeline import FULL_PARALLEL, Encoder
+    cases = [(44100, 2822400, 2, 3000, 8, 12.0), (2822400, 2822400, 2, 8000, 0, 0.0),
+             (2822400, 5644800, 1, 5000, 8, 12.0), (5644800, 2822400, 2, 10000, 8, 0.0)]
+    specs, xs = [], []
+    for k, (fi, fo, ch, frames, box, lim) in enumerate(cases):
+        specs.append(StreamSpec(fi, fo, ch, frames, ntf.auto_select_precorr(fo), gain=0.8,
+                                boxcar_taps=box, soft_clip=True, state_limit=lim, precorr=True))
+        xs.append(_noise(frames, ch, 90) if fi < 2822400 else _dop_input(oracle, fi, frames, ch, 60 + k))
+    plan = BatchPlan(specs, seg_len=32768, output_format=fmt)
+    plan.load([torch.from_numpy(x).cuda() for x in xs])
+    plan.run()
+    for i, s in enumerate(specs):
+        enc = Encoder(s.fs_in, s.fs_out, s.channels, s.ntf, 16, 8, 16, state_limit=s.state_limit,
+                      seg_len=32768, seed_mode=FULL_PARALLEL, boxcar_taps=s.boxcar_taps,
+                      soft_clip=True, output_format=fmt, sdm_mode=_lib.SDM_PRECORR)
+        n_out = (16 if s.fs_in >= 2822400 else 1) * s.frames * s.fs_out // s.fs_in
+        if fmt == OUT_BITS:
+            buf = torch.empty((s.channels, n_out + 256), dtype=torch.uint8, device="cuda")
+        else:
+            buf = torch.empty(enc.out_capacity(s.frames) + 64, dtype=torch.uint8, device="cuda")
+        ns, nb = enc.process(torch.from_numpy(xs[i]).cuda(), buf, 0.8, 0.8)
+        want = buf[:, :ns].cpu().numpy() if fmt == OUT_BITS else buf[:nb].cpu().numpy()
+        enc.close()
+        got = plan.out_view(i).cpu().numpy()
+        assert plan.out_samples(i) == ns == n_out
+        assert got.shape == want.shape, (i, got.shape, want.shape)
+        assert np.array_equal(got, want), f"stream {i}"
+    plan.close()
