@@ -67,7 +67,7 @@ class StreamDesc(C.Structure):
     _fields_ = [("fs_in", C.c_int32), ("fs_out", C.c_int32), ("channels", C.c_int32),
                 ("boxcar_taps", C.c_int32), ("frames", C.c_int64), ("gain", C.c_double),
                 ("soft_clip", C.c_int32), ("reposition", C.c_int32), ("sdm", SdmParams),
-                ("sdm_mode", C.c_int32)]
+                ("sdm_mode", C.c_int32), ("samerate_filter", C.c_int32)]
 
 
 class PlanInfo(C.Structure):

@@ -40,6 +40,7 @@ class StreamSpec:
     soft_clip: bool = True
     reposition: bool = True
     precorr: bool = False      # PreCorr greedy SDM instead of the DAS trellis
+    lowpass: bool = False      # same-rate DSD input: the 127-tap FIR lowpass, not the boxcar
 
     def desc(self) -> _lib.StreamDesc:
         d = _lib.StreamDesc()
@@ -53,6 +54,7 @@ class StreamSpec:
         d.sdm.depth, d.sdm.cands, d.sdm.lat = self.depth, self.cands, self.lat
         d.sdm.state_limit = float(self.state_limit)
         d.sdm_mode = _lib.SDM_PRECORR if self.precorr else _lib.SDM_TRELLIS
+        d.samerate_filter = _lib.SAMERATE_LOWPASS if self.lowpass else _lib.SAMERATE_BOXCAR
         return d
 
 

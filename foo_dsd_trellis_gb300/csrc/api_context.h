@@ -85,6 +85,20 @@ int launch_boxcar_fresh(const uint8_t* bits, size_t bits_stride, long long count
 int launch_boxcar_fresh_f32(const uint8_t* bits, size_t bits_stride, long long count,
                             const int8_t* zero_hist, int taps, int nch, double g_start,
                             double g_step, float* out, size_t out_stride, cudaStream_t stream);
+// the same-rate FIR lowpass without a context (lowpass.cu): host tables,
+// the shared-memory attribute (outside capture), fresh-state launches
+int lowpass_tables(unsigned fs, double cutoff_hz, int ntaps_req, std::vector<double>& lut,
+                   std::vector<double>& taps, int* W);
+size_t lowpass_hist_bytes(int nch);
+int lowpass_prepare(int W);
+int launch_lowpass_fresh(const double* lut, const double* taps, int ntaps, int W,
+                         const uint8_t* bits, size_t bits_stride, long long count,
+                         const void* zero_hist, int nch, double g_start, double g_step,
+                         double* out, size_t out_stride, int num_sms, cudaStream_t stream);
+int launch_lowpass_fresh(const double* lut, const double* taps, int ntaps, int W,
+                         const uint8_t* bits, size_t bits_stride, long long count,
+                         const void* zero_hist, int nch, double g_start, double g_step,
+                         float* out, size_t out_stride, int num_sms, cudaStream_t stream);
 // the FP64 decimation chain from fresh state without a context (decim.cu);
 // out32 non-null: FP32 output (gain, no clip) there instead of `out`
 int launch_decim_f64_fresh(const double* in, size_t in_stride, long long count, int stages,

@@ -78,6 +78,7 @@ struct StreamPlan {
   int dsd_mode = 0;
   int box_taps = 0;
   int down_stages = 0;
+  int lp = -1;                          // same-rate DSD through the FIR lowpass: its table set
   size_t f32_off = 0, f32_stride = 0;   // FP32 rows: a PreCorr stream's walk input, or a
                                         // DSD-up trellis stream's unpacked +-1 input (floats)
   size_t f32in_off = 0;                 // a DSD-up PreCorr stream's unpacked input (f32_stride
@@ -109,6 +110,15 @@ struct SdmClass {
   int scratch_first = 0;                // its CTAs' scratch contexts
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+// The same-rate FIR lowpass of one input rate (fir_lowpass_init: 127 taps at
+// 50 kHz): taps and group tables in the arena.
+struct LpSet {
+  unsigned fs = 0;
+  int ntaps = 0, W = 0;
+  std::vector<double> lut, taps;
+  size_t lut_off = 0, taps_off = 0;     // doubles into d_lp
 };
 
 // Streams in PreCorr mode with one NTF and limit: one table, one launch.
@@ -155,6 +165,7 @@ struct dsdgpu_plan {
   std::vector<StreamPlan> st;
   std::vector<SdmClass> cls;
   std::vector<PcClass> pcls;
+  std::vector<LpSet> lps;
   std::vector<PcBatchRow> pcrows;
   long long pc_samples = 0;
   std::vector<SdmJob> jobs;
@@ -175,6 +186,8 @@ struct dsdgpu_plan {
   float* d_pctab = nullptr;            // PreCorr tables, one per class
   PcBatchRow* d_pcrows = nullptr;
   int8_t* d_boxhist = nullptr;         // zero boxcar history of the DSD streams
+  double* d_lp = nullptr;              // lowpass taps and tables
+  void* d_lphist = nullptr;            // zero lowpass history (fresh streams)
   // scratch of the DSD streams to a lower rate, shared (graph 1 runs its
   // streams in order): unpacked decisions, boxcar output, the chain's
   // ping-pong rows, the chain's zero delay lines
@@ -403,10 +416,16 @@ int capture_graphs(dsdgpu_plan* pl) {
       if (s.dsd_mode == 1) {
         r = launch_dop_unpack(pl->d_pcm + s.pcm_off, s.pcm_stride, s.d.frames, nch,
                               pl->d_bits + s.bits_off, s.bits_stride, m);
-        if (!r)
+        if (!r && s.lp >= 0) {
+          const LpSet& L = pl->lps[s.lp];
+          r = launch_lowpass_fresh(pl->d_lp + L.lut_off, pl->d_lp + L.taps_off, L.ntaps, L.W,
+                                   pl->d_bits + s.bits_off, s.bits_stride, (long long)s.n_fir,
+                                   pl->d_lphist, nch, gain, 0.0, w, s.f32_stride, c->num_sms, m);
+        } else if (!r) {
           r = launch_boxcar_fresh_f32(pl->d_bits + s.bits_off, s.bits_stride, (long long)s.n_fir,
                                       pl->d_boxhist, s.box_taps, nch, gain, 0.0, w, s.f32_stride,
                                       m);
+        }
       } else if (s.dsd_mode == 2) {
         const size_t in_stride = align_up((size_t)cnt, 64);
         r = launch_dop_unpack_f32(pl->d_pcm + s.pcm_off, s.pcm_stride, s.d.frames, nch,
@@ -432,10 +451,17 @@ int capture_graphs(dsdgpu_plan* pl) {
       // assembly writes them), the boxcar with the constant gain
       r = launch_dop_unpack(pl->d_pcm + s.pcm_off, s.pcm_stride, s.d.frames, nch,
                             pl->d_bits + s.bits_off, s.bits_stride, m);
-      if (!r)
+      if (!r && s.lp >= 0) {
+        const LpSet& L = pl->lps[s.lp];
+        r = launch_lowpass_fresh(pl->d_lp + L.lut_off, pl->d_lp + L.taps_off, L.ntaps, L.W,
+                                 pl->d_bits + s.bits_off, s.bits_stride, (long long)s.n_fir,
+                                 pl->d_lphist, nch, gain, 0.0, pl->d_fir + s.fir_off,
+                                 s.fir_stride, c->num_sms, m);
+      } else if (!r) {
         r = launch_boxcar_fresh(pl->d_bits + s.bits_off, s.bits_stride, (long long)s.n_fir,
                                 pl->d_boxhist, s.box_taps, nch, gain, 0.0, pl->d_fir + s.fir_off,
                                 s.fir_stride, m);
+      }
     } else if (s.dsd_mode == 2) {
       // DSD up: +-1 floats at the input rate through the FIR chain
       r = launch_dop_unpack_f32(pl->d_pcm + s.pcm_off, s.pcm_stride, s.d.frames, nch,
@@ -698,6 +724,22 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
     if (d.fs_in >= kDsd64Rate) {
       s.dsd_mode = d.fs_out == d.fs_in ? 1 : (d.fs_out > d.fs_in ? 2 : 3);
     }
+    if (d.samerate_filter != DSDGPU_SAMERATE_BOXCAR && d.samerate_filter != DSDGPU_SAMERATE_LOWPASS)
+      return bail(c->fail(DSDGPU_ERR_ARG, "bad same-rate filter"));
+    if (s.dsd_mode == 1 && d.samerate_filter == DSDGPU_SAMERATE_LOWPASS) {
+      // the pipeline's same-rate FIR mode (src/engine.c:168-181, 505-523)
+      int k = -1;
+      for (size_t j = 0; j < pl->lps.size() && k < 0; j++)
+        if (pl->lps[j].fs == (unsigned)d.fs_in) k = (int)j;
+      if (k < 0) {
+        LpSet L;
+        L.fs = (unsigned)d.fs_in;
+        L.ntaps = lowpass_tables(L.fs, 50000.0, 127, L.lut, L.taps, &L.W);
+        pl->lps.push_back(std::move(L));
+        k = (int)pl->lps.size() - 1;
+      }
+      s.lp = k;
+    }
     if (s.dsd_mode == 3) {
       // the decimation chain's plan (dsdgpu_decim_setup); boxcar 0 = a one-tap
       // mean, the identity on +-1 input (the plugin's DAS FIR phase has none)
@@ -952,6 +994,14 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
     dn_pp = std::max(dn_pp, 2 * align_up(cnt / 2 + 1, 32) * nch);
   }
 
+  size_t lp_total = 0;
+  for (LpSet& L : pl->lps) {
+    L.lut_off = lp_total;
+    lp_total += L.lut.size();
+    L.taps_off = lp_total;
+    lp_total += L.taps.size();
+  }
+
   // ---- device arena ----
   struct Part { void** p; size_t bytes; };
   const size_t nctx = 1 + (size_t)nscratch;
@@ -966,6 +1016,8 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
       {(void**)&pl->d_dn_box, sizeof(double) * dn_box},
       {(void**)&pl->d_dn_pp, sizeof(double) * dn_pp},
       {(void**)&pl->d_dn_dly, sizeof(double) * 62 * kBatchMaxChannels},
+      {(void**)&pl->d_lp, sizeof(double) * lp_total},
+      {(void**)&pl->d_lphist, lowpass_hist_bytes(kBatchMaxChannels)},
       {(void**)&pl->d_seg, seg_total},
       {(void**)&pl->d_bits, bits_total},
       {(void**)&pl->d_out, out_total},
@@ -1014,6 +1066,14 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
   cudaMemsetAsync(pl->d_hist, 0, sizeof(float) * kHistory * kBatchMaxChannels, m);
   cudaMemsetAsync(pl->d_boxhist, 0, boxcar_hist_bytes(kBatchMaxChannels), m);
   cudaMemsetAsync(pl->d_dn_dly, 0, sizeof(double) * 62 * kBatchMaxChannels, m);
+  cudaMemsetAsync(pl->d_lphist, 0, lowpass_hist_bytes(kBatchMaxChannels), m);
+  for (const LpSet& L : pl->lps) {
+    cudaMemcpyAsync(pl->d_lp + L.lut_off, L.lut.data(), sizeof(double) * L.lut.size(),
+                    cudaMemcpyHostToDevice, m);
+    cudaMemcpyAsync(pl->d_lp + L.taps_off, L.taps.data(), sizeof(double) * L.taps.size(),
+                    cudaMemcpyHostToDevice, m);
+    if (lowpass_prepare(L.W) != 0) return bail(c->cuda_fail(cudaGetLastError(), "lowpass attributes"));
+  }
   cudaMemsetAsync(pl->d_bp, 0, sizeof(int) * (size_t)nbp, m);
   cudaMemsetAsync(pl->d_pcm, 0, sizeof(float) * pcm_total, m);
   if (!pl->jobs.empty())

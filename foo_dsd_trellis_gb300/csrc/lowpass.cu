@@ -93,11 +93,13 @@ __device__ __forceinline__ uint32_t window_bit(const uint8_t* x, const uint32_t*
   return hw[q >> 5] >> (q & 31) & 1u;
 }
 
+// OutT = float: the FP64 output narrowed to nearest (the PreCorr walk's input)
+template <typename OutT>
 __global__ void __launch_bounds__(kLpTile) lowpass_kernel(
     const double* __restrict__ lut, const double* __restrict__ taps, int ntaps, int W,
     const uint8_t* __restrict__ bits, size_t bits_stride, long long count,
     const LpHist* __restrict__ hist, int nch, double g_start, double g_step,
-    double* __restrict__ out, size_t out_stride) {
+    OutT* __restrict__ out, size_t out_stride) {
   extern __shared__ double smem[];
   double* tab = smem;
   uint32_t* words = reinterpret_cast<uint32_t*>(smem + (W / 8) * 256);
@@ -149,7 +151,7 @@ __global__ void __launch_bounds__(kLpTile) lowpass_kernel(
       }
     }
     out[(size_t)c * out_stride + i] =
-        __dmul_rn(acc, __dadd_rn(g_start, __dmul_rn(g_step, (double)i)));
+        (OutT)__dmul_rn(acc, __dadd_rn(g_start, __dmul_rn(g_step, (double)i)));
   }
 }
 
@@ -174,6 +176,67 @@ __global__ void lowpass_hist_kernel(const uint8_t* __restrict__ bits, size_t bit
 }
 
 }  // namespace
+
+// Context-free form (the batch plan's same-rate DSD streams, fresh state):
+// the design and group tables on the host, the kernel with a zeroed history
+// (valid = 0: every window starts at the stream's first sample).
+int lowpass_tables(unsigned fs, double cutoff_hz, int ntaps_req, std::vector<double>& lut,
+                   std::vector<double>& taps, int* W) {
+  double h[kLpMaxTaps + 1];
+  const int n = design_lowpass(fs, cutoff_hz, ntaps_req, h);
+  *W = 32 * ((n + 31) / 32);
+  taps.assign(h, h + n);
+  lut.assign((size_t)(*W / 8) * 256, 0.0);
+  build_tables(h, n, *W, lut.data());
+  return n;
+}
+
+size_t lowpass_hist_bytes(int nch) { return (size_t)nch * sizeof(LpHist); }
+
+static size_t lowpass_smem(int W) {
+  return (size_t)(W / 8) * 256 * sizeof(double) + kLpWords * sizeof(uint32_t);
+}
+
+int lowpass_prepare(int W) {
+  const int smem = (int)lowpass_smem(W);
+  if (cudaFuncSetAttribute(lowpass_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           smem) != cudaSuccess ||
+      cudaFuncSetAttribute(lowpass_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           smem) != cudaSuccess)
+    return -1;
+  return 0;
+}
+
+template <typename OutT>
+static int launch_lowpass_fresh_t(const double* lut, const double* taps, int ntaps, int W,
+                                  const uint8_t* bits, size_t bits_stride, long long count,
+                                  const void* zero_hist, int nch, double g_start, double g_step,
+                                  OutT* out, size_t out_stride, int num_sms, cudaStream_t stream) {
+  if (count <= 0) return 0;
+  const size_t smem = lowpass_smem(W);
+  const long long tiles = (count + kLpTile - 1) / kLpTile * nch;
+  const long long cap = (long long)(num_sms > 0 ? num_sms : 152) * (smem > 50 * 1024 ? 3 : 4);
+  lowpass_kernel<OutT><<<(unsigned)(tiles < cap ? tiles : cap), kLpTile, smem, stream>>>(
+      lut, taps, ntaps, W, bits, bits_stride, count, (const LpHist*)zero_hist, nch, g_start,
+      g_step, out, out_stride);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_lowpass_fresh(const double* lut, const double* taps, int ntaps, int W,
+                         const uint8_t* bits, size_t bits_stride, long long count,
+                         const void* zero_hist, int nch, double g_start, double g_step,
+                         double* out, size_t out_stride, int num_sms, cudaStream_t stream) {
+  return launch_lowpass_fresh_t(lut, taps, ntaps, W, bits, bits_stride, count, zero_hist, nch,
+                                g_start, g_step, out, out_stride, num_sms, stream);
+}
+
+int launch_lowpass_fresh(const double* lut, const double* taps, int ntaps, int W,
+                         const uint8_t* bits, size_t bits_stride, long long count,
+                         const void* zero_hist, int nch, double g_start, double g_step,
+                         float* out, size_t out_stride, int num_sms, cudaStream_t stream) {
+  return launch_lowpass_fresh_t(lut, taps, ntaps, W, bits, bits_stride, count, zero_hist, nch,
+                                g_start, g_step, out, out_stride, num_sms, stream);
+}
 
 struct dsdgpu_lowpass_state {
   int ntaps = 0;
@@ -220,7 +283,7 @@ int dsdgpu_lowpass_setup(dsdgpu_context_t* c, unsigned fs, double cutoff_hz, int
   cudaMemcpyAsync(s->d_taps, h, (size_t)s->ntaps * sizeof(double), cudaMemcpyHostToDevice, c->stream);
   cudaMemsetAsync(s->d_hist, 0, (size_t)nch * sizeof(LpHist), c->stream);
   const size_t smem = (size_t)(s->W / 8) * 256 * sizeof(double) + kLpWords * sizeof(uint32_t);
-  e = cudaFuncSetAttribute(lowpass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  e = cudaFuncSetAttribute(lowpass_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) {
     lowpass_free(s);
     return c->cuda_fail(e, "lowpass shared memory");
@@ -281,7 +344,7 @@ int dsdgpu_lowpass_process_async(dsdgpu_context_t* c, int first, int nch, const 
   const long long cap = (long long)(c->num_sms > 0 ? c->num_sms : 152) * per_sm;
   const unsigned grid = (unsigned)(tiles < cap ? tiles : cap);
   LpHist* hist = s->d_hist + first;
-  lowpass_kernel<<<grid, kLpTile, smem, c->stream>>>(s->d_lut, s->d_taps, s->ntaps, s->W, d_bits,
+  lowpass_kernel<double><<<grid, kLpTile, smem, c->stream>>>(s->d_lut, s->d_taps, s->ntaps, s->W, d_bits,
                                                      bits_stride, (long long)count, hist, nch, gs,
                                                      step, d_out, out_stride);
   lowpass_hist_kernel<<<nch, 256, 0, c->stream>>>(d_bits, bits_stride, (long long)count, hist, nch);

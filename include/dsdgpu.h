@@ -409,7 +409,7 @@ int dsdgpu_sdm_estimate_state(dsdgpu_context_t *ctx, const dsdgpu_sdm_params_t *
  * one thread each, beside the trellis launches.
  * A stream whose fs_in is a DSD rate takes DoP floats (planar, 16 DSD samples
  * per frame) as the pipeline does: at fs_out == fs_in the same-rate
- * re-encode (unpack, boxcar, DAS trellis), above it the FIR chain on the
+ * re-encode (unpack, boxcar or the 127-tap FIR lowpass, DAS trellis), above it the FIR chain on the
  * unpacked +-1 values, below it the boxcar and the FP64 half-band /2 chain
  * (in PreCorr mode each with FP32 output and no clip).
  * Each run converts whole streams from fresh state. */
@@ -425,6 +425,7 @@ typedef struct {
     int32_t reposition;        /* RMS reposition of quiet DAS boundaries */
     dsdgpu_sdm_params_t sdm;   /* NTF, K, depth, lat, state limit */
     int32_t sdm_mode;          /* DSDGPU_SDM_TRELLIS (DAS trellis) or DSDGPU_SDM_PRECORR */
+    int32_t samerate_filter;   /* DSDGPU_SAMERATE_*: same-rate DSD input only */
 } dsdgpu_stream_desc_t;
 
 typedef struct {

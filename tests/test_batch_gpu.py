@@ -300,23 +300,25 @@ def test_batch_dsd_input_streams(oracle, fmt):
     """DoP input in a batch, as the pipeline takes it: same-rate DSD64 (the
     engine's default 32-tap boxcar) and DSD128 (64 taps given), DSD64 -> DSD128
     through the FIR chain on the unpacked +-1 values, DSD128 -> DSD64 (boxcar 8,
-    one FP64 half-band /2 stage, soft clip) and DSD256 -> DSD64 (no boxcar, two
-    stages), beside a PCM stream.
+    one FP64 half-band /2 stage, soft clip), DSD256 -> DSD64 (no boxcar, two
+    stages) and same-rate DSD128 through the 127-tap FIR lowpass, beside a PCM
+    stream.
     Each stream equals the single-stream pipeline on a fresh context with the
     same parameters (itself checked against the oracle's unpack, boxcar, FIR
     and DAS in test_dsd_gpu.py)."""
-    from foo_dsd_trellis_gb300 import ntf
+    from foo_dsd_trellis_gb300 import _lib, ntf
     from foo_dsd_trellis_gb300.batch import OUT_BITS, BatchPlan, StreamSpec
     from foo_dsd_trellis_gb300.pipeline import FULL_PARALLEL, Encoder
     pcm_spec = _specs()[0]
-    dsd = [(2822400, 2822400, 2, 12000, 0, False), (5644800, 5644800, 1, 9000, 64, False),
-           (2822400, 5644800, 2, 6000, 8, True), (5644800, 2822400, 2, 12000, 8, True),
-           (11289600, 2822400, 1, 16000, 0, False)]
+    dsd = [(2822400, 2822400, 2, 12000, 0, False, False), (5644800, 5644800, 1, 9000, 64, False, False),
+           (2822400, 5644800, 2, 6000, 8, True, False), (5644800, 2822400, 2, 12000, 8, True, False),
+           (11289600, 2822400, 1, 16000, 0, False, False), (5644800, 5644800, 2, 9000, 0, False, True)]
     specs = [pcm_spec]
     xs = [_inputs([pcm_spec])[0]]
-    for k, (fi, fo, ch, frames, box, clip) in enumerate(dsd):
+    for k, (fi, fo, ch, frames, box, clip, lp) in enumerate(dsd):
         specs.append(StreamSpec(fi, fo, ch, frames, ntf.auto_select(fo), cands=8, depth=16, lat=16,
-                                gain=0.9, boxcar_taps=box, soft_clip=clip, reposition=True))
+                                gain=0.9, boxcar_taps=box, soft_clip=clip, reposition=True,
+                                lowpass=lp))
         xs.append(_dop_input(oracle, fi, frames, ch, 40 + k))
     plan = BatchPlan(specs, seg_len=32768, output_format=fmt)
     plan.load([torch.from_numpy(x).cuda() for x in xs])
@@ -328,7 +330,8 @@ def test_batch_dsd_input_streams(oracle, fmt):
         else:
             enc = Encoder(s.fs_in, s.fs_out, s.channels, s.ntf, s.depth, s.cands, s.lat,
                           seg_len=32768, seed_mode=FULL_PARALLEL, reposition=True,
-                          boxcar_taps=s.boxcar_taps, soft_clip=s.soft_clip, output_format=fmt)
+                          boxcar_taps=s.boxcar_taps, soft_clip=s.soft_clip, output_format=fmt,
+                          samerate_filter=_lib.SAMERATE_LOWPASS if s.lowpass else _lib.SAMERATE_BOXCAR)
             n_out = 16 * s.frames * s.fs_out // s.fs_in
             if fmt == OUT_BITS:
                 buf = torch.empty((s.channels, n_out + 256), dtype=torch.uint8, device="cuda")
@@ -345,7 +348,8 @@ def test_batch_dsd_input_streams(oracle, fmt):
 
 @pytest.mark.parametrize("fmt", [0, 1], ids=["bits", "dop"])
 def test_batch_precorr_dsd_input(oracle, fmt):
-    """PreCorr on DoP input in a batch: same-rate DSD64 (default boxcar), DSD64 ->
+    """PreCorr on DoP input in a batch: same-rate DSD64 (default boxcar, and the
+    FIR lowpass), DSD64 ->
     DSD128 (FIR chain, FP32 out), DSD128 -> DSD64 (decimation chain, FP32 out),
     limiter on and off, beside a PreCorr PCM stream.  Each equals the
     single-stream pipeline in PreCorr mode (which narrows its FP64 stage output
@@ -353,12 +357,14 @@ def test_batch_precorr_dsd_input(oracle, fmt):
     from foo_dsd_trellis_gb300 import _lib, ntf
     from foo_dsd_trellis_gb300.batch import OUT_BITS, BatchPlan, StreamSpec
     from foo_dsd_trellis_gb300.pipeline import FULL_PARALLEL, Encoder
-    cases = [(44100, 2822400, 2, 3000, 8, 12.0), (2822400, 2822400, 2, 8000, 0, 0.0),
-             (2822400, 5644800, 1, 5000, 8, 12.0), (5644800, 2822400, 2, 10000, 8, 0.0)]
+    cases = [(44100, 2822400, 2, 3000, 8, 12.0, False), (2822400, 2822400, 2, 8000, 0, 0.0, False),
+             (2822400, 5644800, 1, 5000, 8, 12.0, False), (5644800, 2822400, 2, 10000, 8, 0.0, False),
+             (2822400, 2822400, 1, 8000, 0, 12.0, True)]
     specs, xs = [], []
-    for k, (fi, fo, ch, frames, box, lim) in enumerate(cases):
+    for k, (fi, fo, ch, frames, box, lim, lp) in enumerate(cases):
         specs.append(StreamSpec(fi, fo, ch, frames, ntf.auto_select_precorr(fo), gain=0.8,
-                                boxcar_taps=box, soft_clip=True, state_limit=lim, precorr=True))
+                                boxcar_taps=box, soft_clip=True, state_limit=lim, precorr=True,
+                                lowpass=lp))
         xs.append(_noise(frames, ch, 90) if fi < 2822400 else _dop_input(oracle, fi, frames, ch, 60 + k))
     plan = BatchPlan(specs, seg_len=32768, output_format=fmt)
     plan.load([torch.from_numpy(x).cuda() for x in xs])
@@ -366,7 +372,8 @@ def test_batch_precorr_dsd_input(oracle, fmt):
     for i, s in enumerate(specs):
         enc = Encoder(s.fs_in, s.fs_out, s.channels, s.ntf, 16, 8, 16, state_limit=s.state_limit,
                       seg_len=32768, seed_mode=FULL_PARALLEL, boxcar_taps=s.boxcar_taps,
-                      soft_clip=True, output_format=fmt, sdm_mode=_lib.SDM_PRECORR)
+                      soft_clip=True, output_format=fmt, sdm_mode=_lib.SDM_PRECORR,
+                      samerate_filter=_lib.SAMERATE_LOWPASS if s.lowpass else _lib.SAMERATE_BOXCAR)
         n_out = (16 if s.fs_in >= 2822400 else 1) * s.frames * s.fs_out // s.fs_in
         if fmt == OUT_BITS:
             buf = torch.empty((s.channels, n_out + 256), dtype=torch.uint8, device="cuda")
