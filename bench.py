@@ -26,9 +26,9 @@ the engine's 127-tap FIR lowpass instead of the boxcar), dsd2pcm128 (DSD128 ->
 (DoP DSD256 -> DSD128 through the FP64 decimation chain and the DAS trellis) and
 dsd128_seg0first (the headline's signal and trellis with the reference's own
 seeding rule below DSD512, seg0-first, on 1 s chunks of one stream).  The
-default run (N = 1) also runs the quick ones after the headline's timed steps,
-each in its own process, and summarises them under "also" (`--also none` skips
-them).
+default run (N = 1) also runs the quick ones after the headline's timed steps
+(and multistream64 at an eighth of its stream lengths), each in its own
+process, and summarises them under "also" (`--also none` skips them).
 """
 from __future__ import annotations
 
@@ -65,7 +65,7 @@ SDM_PARTS_DRAM_BYTES_PER_SAMPLE = 9.15                # the balanced launch's (p
 # PreCorr, the DSD512 5.1 UPOLS configuration and the adjoint.  The 64-stream
 # batched form (about a minute per step) runs only on request.
 ALSO_DEFAULT = ["samerate128", "samerate128lp", "dsd256to128", "dsd2pcm128", "precorr128",
-                "dsd512conv6", "diff16"]
+                "dsd512conv6", "diff16", "multistream64@0.125"]
 
 
 def run_also(names: list[str]) -> dict:
@@ -73,8 +73,10 @@ def run_also(names: list[str]) -> dict:
     headline's numbers are final by then.  Returns name -> summary."""
     out = {}
     for w in names:
-        cmd = [sys.executable, os.path.abspath(__file__), "--workload", w, "--steps", "3",
-               "--warmup", "3"]
+        # name@scale: a multistream workload at that fraction of its stream lengths
+        name, _, scale = w.partition("@")
+        cmd = [sys.executable, os.path.abspath(__file__), "--workload", name, "--steps", "3",
+               "--warmup", "3"] + (["--ms-scale", scale] if scale else [])
         try:
             r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
             lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
@@ -96,6 +98,7 @@ def run_also(names: list[str]) -> dict:
                   "cpu_baseline": {k: cb.get(k) for k in ("value", "cores", "kind", "sample")}
                   if cb else None,
                   "workload": (d.get("config") or {}).get("workload"),
+                  "lengths_s": (d.get("config") or {}).get("lengths_s"),
                   "clocks": d.get("clocks"), "gpu_launches": d.get("gpu_launches")}
         for k in ("forward_ms", "exact_sdm_ms", "fd_check", "stages_ms", "parity"):
             if k in d:
@@ -126,7 +129,8 @@ def parse():
     ap.add_argument("--also", default=",".join(ALSO_DEFAULT),
                     help="dsd128_das at N=1: other workloads run after the headline, one "
                          "subprocess each (3 warm-up + 3 timed steps), summarised under "
-                         "'also' in the headline's JSON line; 'none' skips them")
+                         "'also' in the headline's JSON line; name@f runs a multistream "
+                         "workload at f times its stream lengths; 'none' skips them")
     ap.add_argument("--fd-dirs", type=int, default=32,
                     help="diff16: random unit directions of the finite-difference check")
     ap.add_argument("--ms-scale", type=float, default=1.0,
