@@ -387,3 +387,42 @@ def test_batch_precorr_dsd_input(oracle, fmt):
         assert got.shape == want.shape, (i, got.shape, want.shape)
         assert np.array_equal(got, want), f"stream {i}"
     plan.close()
+
+
+def test_batch_tiny_streams_every_mode(oracle):
+    """One-frame and few-frame streams in every mode of the plan (PCM trellis,
+    PCM PreCorr, same-rate DSD by boxcar and by lowpass, DSD up, DSD down by
+    one and two stages, PreCorr on DoP input): no error, and each equals the
+    single-stream pipeline on a fresh context (decision bytes)."""
+    from foo_dsd_trellis_gb300 import _lib, ntf
+    from foo_dsd_trellis_gb300.batch import OUT_BITS, BatchPlan, StreamSpec
+    from foo_dsd_trellis_gb300.pipeline import FULL_PARALLEL, Encoder
+    cases = [(44100, 2822400, 1, 1, False, False), (48000, 6144000, 2, 3, True, False),
+             (2822400, 2822400, 1, 1, False, False), (5644800, 5644800, 2, 2, False, True),
+             (2822400, 5644800, 1, 1, False, False), (5644800, 2822400, 2, 1, False, False),
+             (11289600, 2822400, 1, 3, False, False), (2822400, 2822400, 1, 2, True, False)]
+    specs, xs = [], []
+    for k, (fi, fo, ch, frames, pc, lp) in enumerate(cases):
+        f = ntf.auto_select_precorr(fo) if pc else ntf.auto_select(fo)
+        specs.append(StreamSpec(fi, fo, ch, frames, f, cands=8, depth=16, lat=16, gain=0.7,
+                                boxcar_taps=0 if fi == fo else 8, precorr=pc, lowpass=lp))
+        xs.append(_noise(frames, ch, 200 + k) if fi < 2822400
+                  else _dop_input(oracle, fi, frames, ch, 300 + k))
+    plan = BatchPlan(specs, seg_len=32768, output_format=OUT_BITS)
+    plan.load([torch.from_numpy(x).cuda() for x in xs])
+    plan.run()
+    for i, s in enumerate(specs):
+        enc = Encoder(s.fs_in, s.fs_out, s.channels, s.ntf, 16, 8, 16, seg_len=32768,
+                      seed_mode=FULL_PARALLEL, boxcar_taps=s.boxcar_taps, soft_clip=True,
+                      output_format=OUT_BITS,
+                      sdm_mode=_lib.SDM_PRECORR if s.precorr else _lib.SDM_TRELLIS,
+                      samerate_filter=_lib.SAMERATE_LOWPASS if s.lowpass else _lib.SAMERATE_BOXCAR)
+        n_out = (16 if s.fs_in >= 2822400 else 1) * s.frames * s.fs_out // s.fs_in
+        buf = torch.zeros((s.channels, n_out + 256), dtype=torch.uint8, device="cuda")
+        ns, _ = enc.process(torch.from_numpy(xs[i]).cuda(), buf, 0.7, 0.7)
+        enc.close()
+        want = buf[:, :ns].cpu().numpy()
+        got = plan.out_view(i).cpu().numpy()
+        assert plan.out_samples(i) == ns, (i, plan.out_samples(i), ns)
+        assert got.shape == want.shape and np.array_equal(got, want), f"stream {i}"
+    plan.close()
