@@ -109,7 +109,7 @@ struct SdmClass {
   int grid = 0;
   int scratch_first = 0;                // its CTAs' scratch contexts
   cudaStream_t side = nullptr;
-  cudaEvent_t fork = nullptr, join = nullptr;
+  cudaEvent_t join = nullptr;
 };
 
 // The same-rate FIR lowpass of one input rate (fir_lowpass_init: 127 taps at
@@ -232,7 +232,6 @@ dsdgpu_plan::~dsdgpu_plan() {
   if (g3) cudaGraphExecDestroy(g3);
   for (auto& k : cls) {
     if (k.side) cudaStreamDestroy(k.side);
-    if (k.fork) cudaEventDestroy(k.fork);
     if (k.join) cudaEventDestroy(k.join);
   }
   for (auto& k : pcls) {
