@@ -68,15 +68,20 @@ ALSO_DEFAULT = ["samerate128", "samerate128lp", "dsd256to128", "dsd2pcm128", "pr
                 "dsd512conv6", "diff16", "multistream64@0.125"]
 
 
+def also_command(w: str) -> list[str]:
+    """The subprocess command of one `also` entry: 3 warm-up and 3 timed steps;
+    name@f runs a multistream workload at f times its stream lengths."""
+    name, _, scale = w.partition("@")
+    return [sys.executable, os.path.abspath(__file__), "--workload", name, "--steps", "3",
+            "--warmup", "3"] + (["--ms-scale", scale] if scale else [])
+
+
 def run_also(names: list[str]) -> dict:
     """Each workload in its own process after the headline's timed steps; the
     headline's numbers are final by then.  Returns name -> summary."""
     out = {}
     for w in names:
-        # name@scale: a multistream workload at that fraction of its stream lengths
-        name, _, scale = w.partition("@")
-        cmd = [sys.executable, os.path.abspath(__file__), "--workload", name, "--steps", "3",
-               "--warmup", "3"] + (["--ms-scale", scale] if scale else [])
+        cmd = also_command(w)
         try:
             r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
             lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]

@@ -1,4 +1,5 @@
-"""World-size-2 gloo tests of the bench's multi-rank host logic (CPU only).
+"""World-size-2 gloo tests of the bench's multi-rank host logic, and its
+side-run commands (CPU only).
 
 Every rank converts its own stream (replicas, weak scaling): no data-path
 collective exists; the only cross-rank step is the MAX of the ranks' timed
@@ -64,3 +65,18 @@ def test_reference_arm_nonzero_rank_is_silent(monkeypatch, capsys):
                                       "--warmup", "1"])
     bench.run_reference(bench.parse())
     assert capsys.readouterr().out == ""
+
+
+def test_also_commands():
+    """The default run's side workloads: each a subprocess with 3 warm-up and 3
+    timed steps; name@f adds the multistream length scale."""
+    import bench
+    cmd = bench.also_command("samerate128")
+    assert cmd[2:] == ["--workload", "samerate128", "--steps", "3", "--warmup", "3"]
+    cmd = bench.also_command("multistream64@0.125")
+    assert cmd[2:] == ["--workload", "multistream64", "--steps", "3", "--warmup", "3",
+                       "--ms-scale", "0.125"]
+    for w in bench.ALSO_DEFAULT:
+        name = w.partition("@")[0]
+        assert name in ("samerate128", "samerate128lp", "dsd256to128", "dsd2pcm128", "precorr128",
+                        "dsd512conv6", "diff16", "multistream64")
