@@ -18,7 +18,8 @@ on a bounded slice of the same workload.
 
 Other workloads (`--workload`, one JSON line each): multistream64 (64 streams
 in one batched plan), multistream64_precorr (the same streams through the
-PreCorr SDM in one plan), diff16 (the adjoint of the differentiable path),
+PreCorr SDM in one plan), multistream64_dsd (the same streams as DoP input,
+re-encoded at their DSD rate in one plan), diff16 (the adjoint of the differentiable path),
 dsd512conv6 (DSD512 5.1 with UPOLS room convolution), samerate128 (DoP DSD128
 re-encode on the engine's path-table parameters), samerate128lp (the same with
 the engine's 127-tap FIR lowpass instead of the boxcar), dsd2pcm128 (DSD128 ->
@@ -123,7 +124,8 @@ def parse():
     ap.add_argument("--das-seg-len", type=int, default=WL["das_seg_len"],
                     help="nominal DAS segment length (profiling of small cases only)")
     ap.add_argument("--workload", default="dsd128_das",
-                    choices=["dsd128_das", "multistream64", "multistream64_precorr", "diff16",
+                    choices=["dsd128_das", "multistream64", "multistream64_precorr",
+                             "multistream64_dsd", "diff16",
                              "dsd512conv6",
                              "samerate128", "samerate128lp", "precorr128", "dsd2pcm128",
                              "dsd256to128", "dsd128_seg0first"],
@@ -140,6 +142,9 @@ def parse():
                     help="diff16: random unit directions of the finite-difference check")
     ap.add_argument("--ms-scale", type=float, default=1.0,
                     help="multistream64(_precorr): stream lengths scale (1.0 = 0.5-30 s)")
+    ap.add_argument("--ms-lanes", type=int, default=2,
+                    help="multistream64_dsd: lanes of a warp per trellis job (K = 2: 2 packs "
+                         "16 jobs a warp; 0 = the plan's default half-warp)")
     ap.add_argument("--ms-seg-len", type=int, default=0,
                     help="multistream64: DAS segment length (0 = autotuned)")
     return ap.parse_args()
@@ -776,6 +781,107 @@ def run_multistream_precorr(args):
                                  "longest row's walk (the FP32 recurrence through the previous "
                                  "output)"},
                 "roofline": None, "cpu_baseline": cpu, "clocks": clk,
+                "gpu_launches": int(launches), "plan": info, "stages_ms": plan.times_ms()}
+        print(json.dumps(line), flush=True)
+    plan.close()
+
+
+MSD_METRIC = ("same-rate DSD re-encode DSD Msamples/s, batched 64-stream form (DoP in -> unpack -> "
+              "boxcar -> DAS trellis SDM -> DoP, one persistent launch per parameter set)")
+
+
+def run_multistream_dsd(args):
+    """The 64-stream layout of multistream64 with DoP input at each stream's
+    DSD rate (DSD128 / DSD256): the same-rate re-encode of the engine's path
+    table (CLANS-6 or the rate's NTF, K = 2, depth 4, lat 128, the rate's
+    default 64-tap boxcar, path gain float32(0.708), DAS, DoP out) for every
+    stream in one plan.  The DSD input is each stream's PCM encoded by this
+    library's batched PCM path (set-up, untimed).  Parity: the four shortest
+    streams against the single-stream pipeline on fresh contexts."""
+    import numpy as np
+    import torch
+    from foo_dsd_trellis_gb300 import ntf, signals
+    from foo_dsd_trellis_gb300.batch import OUT_BITS, OUT_DOP, BatchPlan, StreamSpec
+    from foo_dsd_trellis_gb300.pipeline import FULL_PARALLEL, PCM_FIR_GAIN, Encoder
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    layout = signals.multistream_layout(seed=1003 + 17 * rank, scale=args.ms_scale)
+    # the DSD sources: the PCM streams through the batched PCM path (decision bytes)
+    src = BatchPlan([StreamSpec(e["fs_in"], e["fs_out"], e["channels"], e["frames"],
+                                ntf.auto_select(e["fs_out"]), cands=2, depth=4,
+                                lat=ntf.auto_latency(e["fs_in"], e["fs_out"]), gain=PCM_FIR_GAIN)
+                     for e in layout], seg_len=65536, output_format=OUT_BITS, device=local,
+                    max_device_bytes=int(240e9))
+    src.load([torch.from_numpy(signals.multistream_pcm(e)).cuda() for e in layout])
+    src.run()
+    dops = []
+    for i, e in enumerate(layout):
+        b = src.out_view(i).cpu().numpy()
+        n = b.shape[1] - b.shape[1] % 16
+        dops.append(np.stack([signals.dop_floats(b[c, :n], 0) for c in range(e["channels"])]))
+    src.close()
+    gain = float(np.float32(PATH_GAIN))
+    specs = [StreamSpec(e["fs_out"], e["fs_out"], e["channels"], dops[i].shape[1],
+                        ntf.get_filter("clans-6", e["fs_out"]), cands=2, depth=4, lat=128,
+                        gain=gain, boxcar_taps=0, soft_clip=False, reposition=True)
+             for i, e in enumerate(layout)]
+    plan = BatchPlan(specs, seg_len=65536, output_format=OUT_DOP, device=local,
+                     max_device_bytes=int(240e9), lanes=args.ms_lanes or None)
+    info = plan.info()
+    plan.load([torch.from_numpy(x).cuda() for x in dops])
+    for _ in range(args.warmup):
+        plan.run()
+    clocks = ClockSampler(local)
+    l0 = plan.launches()
+    tot_ms = []
+    clocks.start()
+    for _ in range(args.steps):
+        plan.run()
+        tot_ms.append(plan.times_ms()["total"])
+    clk = clocks.stop()
+    launches = (plan.launches() - l0) // max(1, args.steps)
+    total_s = max_over_ranks(sum(tot_ms) / 1000.0)
+    out_samples = int(info["out_samples"])
+    value = job_throughput(out_samples, args.steps, world, total_s)
+    h_in = [torch.from_numpy(x).pin_memory().numpy() for x in dops]
+    h_out = [torch.empty(plan.out_bytes(i), dtype=torch.uint8).pin_memory().numpy()
+             for i in range(len(specs))]
+    t0 = time.perf_counter()
+    plan.run_host(h_in, h_out)
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    same = True
+    for i in sorted(range(len(specs)), key=lambda i: specs[i].frames)[:4]:
+        s = specs[i]
+        enc = Encoder(s.fs_in, s.fs_out, s.channels, s.ntf, s.depth, s.cands, s.lat,
+                      seg_len=65536, seed_mode=FULL_PARALLEL, reposition=True, boxcar_taps=0,
+                      soft_clip=False, output_format=OUT_DOP, device=local)
+        buf = torch.empty(enc.out_capacity(s.frames) + 64, dtype=torch.uint8, device="cuda")
+        _, nb = enc.process(torch.from_numpy(dops[i]).cuda(), buf, gain, gain)
+        enc.close()
+        same = same and bool(np.array_equal(buf[:nb].cpu().numpy(), plan.out_view(i).cpu().numpy()))
+    if rank == 0:
+        line = {"metric": MSD_METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1000 * total_s / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "multistream64_dsd_samerate", "streams": len(specs),
+                           "lengths_s": "U(0.5, 30) x %g" % args.ms_scale,
+                           "rates": "DSD128 / DSD256 (each stream's multistream64 target)",
+                           "ntf": "clans-6", "cands": 2, "depth": 4, "lat": 128,
+                           "lanes_per_job": args.ms_lanes or "default (16)",
+                           "boxcar": "the rate's default (64)", "gain": "float32(0.708)",
+                           "seed_mode": "full_parallel", "output": "dop",
+                           "input": "DoP floats of the streams' PCM encoded by the batched PCM "
+                                    "path (untimed)", "l2": "inputs larger than L2"},
+                "xrt": sum(plan.out_samples(i) / s.fs_out for i, s in enumerate(specs)) *
+                       args.steps / total_s,
+                "e2e": {"value": out_samples * world / e2e_s / 1e6, "unit": UNIT,
+                        "h2d_bytes_per_step": int(sum(x.nbytes for x in dops)),
+                        "d2h_bytes_per_step": int(sum(plan.out_bytes(i) for i in range(len(specs))))},
+                "parity": {"bit_exact_with_pipeline": same,
+                           "sample": "the four shortest streams against the single-stream "
+                                     "pipeline on fresh contexts"},
+                "roofline": None, "cpu_baseline": None, "clocks": clk,
                 "gpu_launches": int(launches), "plan": info, "stages_ms": plan.times_ms()}
         print(json.dumps(line), flush=True)
     plan.close()
@@ -1425,6 +1531,8 @@ def main():
         run_multistream(args)
     elif args.workload == "multistream64_precorr":
         run_multistream_precorr(args)
+    elif args.workload == "multistream64_dsd":
+        run_multistream_dsd(args)
     elif args.workload == "diff16":
         run_diff(args)
     elif args.workload == "dsd512conv6":

@@ -69,7 +69,8 @@ class _Cai:
 
 class BatchPlan:
     def __init__(self, specs: list[StreamSpec], seg_len: int = 0, output_format: int = OUT_DOP,
-                 device: int = 0, max_device_bytes: int = 0, select: int | None = None):
+                 device: int = 0, max_device_bytes: int = 0, select: int | None = None,
+                 lanes: int | None = None):
         self.L = _lib.load()
         self.device = device
         self.specs = list(specs)
@@ -82,6 +83,8 @@ class BatchPlan:
         self.plan = None
         if select is not None:
             _lib.check(self.h, self.L.dsdgpu_set_option(self.h, _lib.OPT_SDM_SELECT, select))
+        if lanes is not None:   # lanes of a warp per trellis job (a power of two >= K)
+            _lib.check(self.h, self.L.dsdgpu_set_option(self.h, _lib.OPT_SDM_LANES, lanes))
         arr = (_lib.StreamDesc * len(specs))(*[s.desc() for s in specs])
         p = C.c_void_p()
         _lib.check(self.h, self.L.dsdgpu_plan_create(self.h, arr, len(specs), seg_len,
