@@ -142,9 +142,9 @@ def parse():
                     help="diff16: random unit directions of the finite-difference check")
     ap.add_argument("--ms-scale", type=float, default=1.0,
                     help="multistream64(_precorr): stream lengths scale (1.0 = 0.5-30 s)")
-    ap.add_argument("--ms-lanes", type=int, default=2,
-                    help="multistream64_dsd: lanes of a warp per trellis job (K = 2: 2 packs "
-                         "16 jobs a warp; 0 = the plan's default half-warp)")
+    ap.add_argument("--ms-lanes", type=int, default=0,
+                    help="multistream64_dsd: lanes of a warp per trellis job (0 = the plan's "
+                         "choice: beyond one wave of jobs the widest width that fits, here 2)")
     ap.add_argument("--ms-seg-len", type=int, default=0,
                     help="multistream64: DAS segment length (0 = autotuned)")
     return ap.parse_args()
@@ -868,7 +868,7 @@ def run_multistream_dsd(args):
                            "lengths_s": "U(0.5, 30) x %g" % args.ms_scale,
                            "rates": "DSD128 / DSD256 (each stream's multistream64 target)",
                            "ntf": "clans-6", "cands": 2, "depth": 4, "lat": 128,
-                           "lanes_per_job": args.ms_lanes or "default (16)",
+                           "lanes_per_job": args.ms_lanes or "the plan's choice",
                            "boxcar": "the rate's default (64)", "gain": "float32(0.708)",
                            "seed_mode": "full_parallel", "output": "dop",
                            "input": "DoP floats of the streams' PCM encoded by the batched PCM "

@@ -529,9 +529,8 @@ int capture_graphs(dsdgpu_plan* pl) {
   }
   for (size_t k = 0; k < pl->cls.size() && !rc; k++) {
     SdmClass& K = pl->cls[k];
-    SdmParams P = K.P;
+    SdmParams P = K.P;   // its lanes: the option's, or the width chosen with the job slots
     P.mode = c->sdm_mode;
-    P.lanes = c->sdm_lanes;
     if (launch_sdm_jobs(P, pl->d_jobs + K.job_first, K.njobs, pl->d_counters + k, pl->d_ctx,
                         c->d_status, K.grid, forked ? K.side : m) != 0)
       rc = DSDGPU_ERR_CUDA;
@@ -955,9 +954,29 @@ int dsdgpu_plan_create(dsdgpu_context_t* c, const dsdgpu_stream_desc_t* streams,
   const int slots = pl->bps * sms;
   int nscratch = 0;
   for (SdmClass& K : pl->cls) {
-    const int jpc = sdm_jobs_per_cta(K.P);
     int gsz = (int)std::llround((double)slots * (double)K.samples / (double)std::max(1LL, pl->sdm_samples));
-    gsz = std::max(1, std::min(gsz, (K.njobs + jpc - 1) / jpc));
+    gsz = std::max(1, gsz);
+    // lanes per job (unless the option fixes them): the default half-warp
+    // while the class's jobs fit one wave of its warps (a small trellis's
+    // step is a chain of dependent operations, and an FP64 warp instruction
+    // costs the same with 2 lanes active as with 32, so the fewest jobs a
+    // warp that still fit win); beyond one wave the widest width that fits,
+    // else the narrowest (K = 2 over 30,058 jobs: 569 -> 1,510 DSD Msamples/s
+    // at 2 lanes)
+    if (K.P.lanes == 0 && (long long)K.njobs > (long long)gsz * sdm_jobs_per_cta(K.P)) {
+      int best = 0;
+      for (int l = 16; l >= 2; l /= 2) {
+        SdmParams Q = K.P;
+        Q.lanes = l;
+        const int jpc = sdm_jobs_per_cta(Q);
+        if (32 / jpc != l) continue;            // below the trellis's own width
+        best = l;
+        if ((long long)K.njobs <= (long long)gsz * jpc) break;
+      }
+      if (best) K.P.lanes = best;
+    }
+    const int jpc = sdm_jobs_per_cta(K.P);
+    gsz = std::min(gsz, (K.njobs + jpc - 1) / jpc);
     K.grid = gsz;
     K.scratch_first = 1 + nscratch;
     nscratch += gsz * jpc;       // one scratch context per job slot of the launch
@@ -1322,9 +1341,8 @@ int dsdgpu_plan_time_plain(dsdgpu_plan_t* pl, int njobs, int64_t* samples, doubl
   cudaStreamSynchronize(m);
   const auto t0 = std::chrono::steady_clock::now();
   for (int j = 0; j < njobs; j++) {
-    SdmParams P = pl->cls[cls_of[j]].P;
+    SdmParams P = pl->cls[cls_of[j]].P;   // the class's width, as the batched launch
     P.mode = c->sdm_mode;
-    P.lanes = c->sdm_lanes;
     if (launch_sdm_jobs(P, pl->d_jobs + j, 1, pl->d_counters, pl->d_ctx, c->d_status, 1, m) != 0)
       return c->cuda_fail(cudaGetLastError(), "plain launch");
     c->launches++;
