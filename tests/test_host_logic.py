@@ -112,3 +112,56 @@ def test_reference_citations_resolve():
         pytest.skip("reference tree not present")
     bad = check_citations.bad_citations()
     assert not bad, bad[:10]
+
+
+def _quant_fast(u: float, levels: int):
+    """The estimator's quantiser shortcut, restated on the bits of u (as the
+    CUDA step forms them): floor(u + 0.5) clamped to [0, levels - 1], or None
+    where the reference's divisions must decide."""
+    import struct
+    b = struct.unpack("<Q", struct.pack("<d", u))[0]
+    hi, lo = b >> 32, b & 0xFFFFFFFF
+    ex = (hi >> 20) & 0x7FF
+    sh = 1035 - min(max(ex, 1021), 1032)
+    mh = (hi & 0xFFFFF) | 0x100000
+    fl = (((mh << 32) | lo) >> sh) & 0xFFFFFFFF
+    fh = mh >> sh
+    f8 = fh & 0xFF
+    near = (f8 == 0x80 and fl <= 1100) or (f8 == 0x7F and fl >= 2**32 - 1100)
+    low = (hi >> 31) != 0 or ex < 1021
+    if ex >= 1033 or (not low and near):
+        return None
+    return 0 if low else min((fh + 0x80) >> 8, levels - 1)
+
+
+def test_estimator_quantiser_shortcut():
+    """sdm_estimate_state_multibit's index trunc((v / a0 + 1) / step + 0.5)
+    (src/trellis.c:1162-1166, FP64) equals the shortcut floor(u + 0.5) with
+    u = fma(v, 1/(a0 step), 1/step) wherever the shortcut decides: random v,
+    and v placed a few ulps and 1e-12 .. 2e-9 from every level boundary, for
+    3, 16, 32 and 97 levels and four a0."""
+    from fractions import Fraction as Fr
+    rng = np.random.default_rng(7)
+    for levels in (3, 16, 32, 97):
+        step = 2.0 / (levels - 1)
+        rstep = 1.0 / step
+        for a0 in (0.51234, 1.7, 0.0923, 3.3e-3):
+            c1 = (1.0 / a0) * rstep
+            vs = list(rng.standard_normal(300) * a0 * 1.5)
+            for k in range(levels + 1):
+                v0 = ((k - 0.5) * step - 1.0) * a0
+                sp = np.spacing(v0) if v0 != 0.0 else 5e-324
+                vs += [v0 + d * sp for d in range(-4, 5)]
+                for rel in (1e-12, 1e-9, 2e-9):
+                    vs += [v0 * (1 + rel) + rel * a0, v0 * (1 - rel) - rel * a0]
+            decided = 0
+            for i, v in enumerate(vs):
+                v = float(v)
+                u = float(Fr(v) * Fr(c1) + Fr(rstep))          # one rounding: the fma
+                q = _quant_fast(u, levels)
+                w = (v / a0 + 1.0) / step + 0.5
+                ref = max(0, min(int(w), levels - 1))
+                if q is not None:
+                    decided += i < 300
+                    assert q == ref, (levels, a0, v)
+            assert decided >= 290   # random inputs: the shortcut decides nearly all
